@@ -1,0 +1,273 @@
+"""Benchmark of the GB300 WCSPH step on the 3-D dam break with mDBC and the box
+obstacle at dp=0.0025 m (~5.2M fluid + ~1.5M boundary particles).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference] [--dp DP]
+
+A step is one Symplectic step (predictor + corrector interaction passes, two
+cell divisions, mDBC correction, dt reduction) of the whole particle set.
+
+* ``value``: steps/s with the state resident in HBM, timed with CUDA events on
+  the context stream around K steps replayed from one captured CUDA graph.
+* ``e2e``: steps/s through the C ABI as a caller drives it (gbsph_upload from
+  host arrays, K x (gbsph_step + dt read-back, as the reference's Run loop
+  reads TimeStep every step), gbsph_download of the final state), wall clock.
+* ``roofline``: the fluid Interaction_Forces kernel (the dominant one): each
+  launch is bracketed by CUDA events inside the timed region; algorithmic bytes
+  per launch = 32 B (neighbour position + velocity/density) per checked
+  neighbour of the fluid rows.  ``roofline_fp32`` states the same launches
+  against the FP32 FLOP model (80 FLOP per real fluid-row pair).
+* ``cpu_baseline``: the oracle (CPU restatement of the reference step, OpenMP
+  on all host cores) timed on a bounded sample of the same state.
+* ``--impl reference``: the oracle port on the host cores as the reference arm.
+Inputs (~1.5 GB of particle arrays) are larger than L2 (129 MB).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s & particle-interactions/s on 1 GB300"
+FLOP_PER_FLUID_PAIR = 80.0  # Wendland + artificial visc + DDT2 + precomputed EOS
+BYTES_PER_CHECKED = 32.0    # pscell (16 B) + velrho (16 B) per checked neighbour
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.rows.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and "Active" in r[3 + i]
+                          and "Not" not in r[3 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_case(dp: float):
+    from dualsphysics_gb300 import casegen as cg
+    from dualsphysics_gb300.case import load_case
+    tmp = tempfile.mkdtemp(prefix="gbbench_")
+    spec = cg.spec_c2(dp=dp, name="DamC2")
+    cg.write_case(cg.make_dam_break(spec), tmp)
+    return load_case(tmp, "DamC2")
+
+
+def cpu_baseline(cd, stride: int, steps: int = 1):
+    """Oracle (OpenMP on all host cores) on a bounded sample: every step runs
+    the divides, mDBC and updates in full and the interaction rows p with
+    p % stride == phase; the full-step time is extrapolated as
+    t_step + (stride-1) * t_interaction."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    po.build()
+    ct = po.config(po.params_from(cd.params))
+    sim = po.Sim(ct, cd.pos, cd.velrho, cd.idp, cd.code, cd.npb, cd.boundnor)
+    ts = []
+    for k in range(steps):
+        po.lib().orc_set_sampling(stride, k % stride)
+        sim.step()
+        t_inter, t_step = sim.times()
+        ts.append(t_step + (stride - 1) * t_inter)
+    po.lib().orc_set_sampling(1, 0)
+    return float(np.mean(ts)), os.cpu_count()
+
+
+def run_reference(args, cd, rank):
+    stride = args.ref_stride
+    t_warm = [cpu_baseline(cd, stride, 1)[0] for _ in range(min(args.warmup, 1))]
+    del t_warm
+    t, cores = cpu_baseline(cd, stride, args.steps)
+    v = 1.0 / t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 positions)", "data": "synthetic",
+            "config": {"workload": f"3-D dam break, mDBC + box obstacle, dp={args.dp}", "particles": cd.np,
+                       "fluid": cd.nfluid, "boundary": cd.npb, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
+                             "sample": f"oracle step with 1/{stride} of the interaction rows per step, "
+                                       f"full step time extrapolated, {args.steps} steps"},
+            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
+    ap.add_argument("--dp", type=float, default=0.0025)
+    ap.add_argument("--ref-stride", type=int, default=16)
+    ap.add_argument("--cpu-stride", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo", init_method="env://")
+        dist = dist_mod
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, make_case(args.dp), rank)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    from dualsphysics_gb300 import _lib
+    from dualsphysics_gb300.sph import GbSphSingle
+
+    cd = make_case(args.dp)
+    K, W = args.steps, args.warmup
+    s = GbSphSingle(local)
+    s.setup(cd)
+    pi = s.pips()
+    s.RunSteps(W, use_graph=True)
+    s.sync()
+    # timed region: K steps from one captured graph, fluid forces bracketed by events
+    s.profile(2 * K)
+    s.graph_prepare(K)
+    l0 = s.launch_count()
+    if dist:
+        dist.barrier()
+    s.sync()
+    with ClockSampler(local) as clk:
+        s.mark(0)
+        s.RunSteps(K, use_graph=2)
+        s.mark(1)
+        ms = s.elapsed(0, 1)
+    s.sync()
+    launches = s.launch_count() - l0
+    kms = s.profile_read()
+    s.profile(0)
+    t_max = ms
+    if dist:
+        import torch
+        tt = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    steps_per_s = world * K / (t_max / 1e3)
+    pis_per_step = 2.0 * (pi["real_fluid"] + pi["real_bound"])
+    info = s.divinfo()
+    # roofline of the fluid Interaction_Forces kernel
+    peaks, src = _peaks()
+    kavg = float(np.mean(kms)) if len(kms) else float("nan")
+    bytes_launch = BYTES_PER_CHECKED * pi["checked_fluid"]
+    ach = bytes_launch / (kavg / 1e3) / 1e9
+    flops_launch = FLOP_PER_FLUID_PAIR * pi["real_fluid"]
+    # e2e through the C ABI with host buffers
+    s.close()
+    e2e = None
+    if rank == 0 or world > 1:
+        t0 = time.perf_counter()
+        e = GbSphSingle(local)
+        e.setup(cd)
+        for _ in range(K):
+            e.ComputeStep()
+            e.step_dt()
+        st = e.download()
+        e.sync()
+        te = time.perf_counter() - t0
+        h2d = cd.pos.nbytes + cd.velrho.nbytes + cd.idp.nbytes + cd.code.nbytes + \
+            (cd.boundnor.nbytes if cd.boundnor is not None else 0)
+        d2h = sum(v.nbytes for v in st.values()) + K * 24
+        e2e = {"value": world * K / te, "unit": "steps/s", "h2d_bytes_per_step": int(h2d / K),
+               "d2h_bytes_per_step": int(d2h / K)}
+        e.close()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t_cpu, cores = cpu_baseline(cd, args.cpu_stride, 1)
+        cpu = {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": cores, "kind": "port",
+               "sample": f"one oracle step of the same state with 1/{args.cpu_stride} of the interaction rows, "
+                         f"full step time extrapolated"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": t_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64 positions and integration)", "data": "synthetic",
+            "config": {"workload": f"3-D dam break (tank 1.6x0.67x0.4 m, column 0.4x0.67x0.3 m), mDBC + "
+                                   f"0.12x0.12x0.45 m box obstacle, dp={args.dp}, Symplectic, Wendland, "
+                                   f"artificial visc 0.01, DDT2 0.1",
+                       "particles": cd.np, "fluid": cd.nfluid, "boundary": cd.npb,
+                       "parallelism": "replicas only" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (no flush)"},
+            "particle_interactions_per_s": steps_per_s * pis_per_step,
+            "particle_interactions_per_step": pis_per_step,
+            "np_after": info["np"],
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": ach / peaks["hbm_gbs"], "traffic": None,
+                         "kernel": "k_forces_fluid", "model": "gather: 32 B per checked fluid-row neighbour",
+                         "peak_source": src, "launch_ms": kavg, "launches_timed": int(len(kms))},
+            "roofline_fp32": {"achieved_tflops": flops_launch / (kavg / 1e3) / 1e12,
+                              "model": "80 FLOP per real fluid-row pair"},
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

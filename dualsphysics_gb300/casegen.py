@@ -1,0 +1,270 @@
+"""Synthetic case generator for the 3-D dam-break workloads.
+
+The reference's pre-processor (GenCase) is not part of the reference source
+tree, so cases are generated here and written in the reference's own run
+formats: the run XML read by JSph::LoadCaseConfig (JSph.cpp:1003-1100;
+``case.execution.{constants,parameters,particles}``, JCaseCtes.cpp:208-222,
+JCaseParts.cpp:540-577, JCaseEParms.cpp:444-478) and the particle file read by
+JPartsLoad4::LoadParticles (JPartsLoad4.cpp:164-290).
+
+Geometry (all sizes in metres):
+
+* tank interior ``[0,Lx]x[0,Ly]x[0,Lz]``, fluid column against the x=0 wall on
+  the lattice ``(i,j,k)*dp``;
+* 3-layer DBC walls and floor outside the interior, open top, up to z=Lz;
+* optional box obstacle (solid lattice block) standing on the floor;
+* hydrostatic initial density of the fluid, rho = rho0*(1+rho0*g*(H-z)/B)^(1/gamma)
+  with H the top of the fluid column (the "water column" density gradient);
+  boundary particles start at rho0;
+* mDBC normals (``BoundNor``): vector from each boundary particle to the
+  nearest point of the boundary surface, which lies dp/2 outside the outer
+  particle layer of each solid; the solver doubles it to reach the ghost node
+  (JSph.cpp:1411-1418).
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import bi4
+
+CODE_TYPE_FLUID = 0x1800
+
+
+@dataclass
+class CaseSpec:
+    name: str = "Dam"
+    tank: tuple = (1.6, 0.67, 0.4)
+    column: tuple = (0.4, 0.67, 0.3)
+    dp: float = 0.01
+    obstacle: tuple | None = None           # (x0, y0, sx, sy, sz)
+    boundary: str = "dbc"                   # dbc | mdbc
+    jitter: float = 0.0                     # fraction of dp, uniform in [-j,j]^3
+    init_vel: float = 0.0                   # seeded uniform fluid velocity in [-v,v]^3 (m/s)
+    seed: int = 0
+    coefh: float = 1.2
+    coefsound: float = 20.0
+    hswl: float | None = None               # defaults to the column height
+    rhop0: float = 1000.0
+    gamma: float = 7.0
+    gravity: tuple = (0.0, 0.0, -9.81)
+    cflnumber: float = 0.2
+    visco_treatment: int = 1                # 1 artificial, 2 laminar+sps, 3 laminar
+    visco: float = 0.01
+    viscoboundfactor: float = 1.0
+    density_dt: int = 2
+    density_dt_value: float = 0.1
+    step_algorithm: int = 2                 # 1 verlet, 2 symplectic
+    verlet_steps: int = 40
+    time_max: float = 0.5
+    time_out: float = 0.01
+    posmax_z: str = "default + 50%"
+    extra_params: dict = field(default_factory=dict)
+
+
+@dataclass
+class Case:
+    spec: CaseSpec
+    pos: np.ndarray        # (n,3) f64
+    vel: np.ndarray        # (n,3) f32
+    rhop: np.ndarray       # (n,) f32
+    idp: np.ndarray        # (n,) u32
+    code: np.ndarray       # (n,) u16
+    boundnor: np.ndarray   # (nbound,3) f32
+    blocks: list           # [(kind, mkbound/mkfluid, begin, count)]
+    npb: int
+    h: float
+    b: float
+    mass: float
+
+    @property
+    def np(self) -> int:
+        return int(self.pos.shape[0])
+
+
+def _lattice(n0, n1, n2):
+    i, j, k = np.meshgrid(np.arange(n0[0], n0[1] + 1), np.arange(n1[0], n1[1] + 1),
+                          np.arange(n2[0], n2[1] + 1), indexing="ij")
+    # z slowest, then y, then x (x fastest) for memory order close to cells
+    return np.stack([i.transpose(2, 1, 0).ravel(), j.transpose(2, 1, 0).ravel(),
+                     k.transpose(2, 1, 0).ravel()], axis=1)
+
+
+def _nsteps(length: float, dp: float) -> int:
+    return int(math.floor(length / dp + 1e-6))
+
+
+def make_dam_break(spec: CaseSpec) -> Case:
+    dp = spec.dp
+    nx, ny, nz = (_nsteps(v, dp) for v in spec.tank)
+    # --- walls: lattice i in [-3,nx+3], j in [-3,ny+3], k in [-3,nz] minus interior
+    wl = _lattice((-3, nx + 3), (-3, ny + 3), (-3, nz))
+    inside = ((wl[:, 0] >= 0) & (wl[:, 0] <= nx) & (wl[:, 1] >= 0) & (wl[:, 1] <= ny) & (wl[:, 2] >= 0))
+    wall = wl[~inside].astype(np.float64) * dp
+    # --- obstacle: solid lattice block on the floor
+    obst = np.zeros((0, 3))
+    if spec.obstacle is not None:
+        x0, y0, sx, sy, sz = spec.obstacle
+        i0, j0 = int(round(x0 / dp)), int(round(y0 / dp))
+        ob = _lattice((i0, i0 + _nsteps(sx, dp)), (j0, j0 + _nsteps(sy, dp)), (0, _nsteps(sz, dp)))
+        obst = ob.astype(np.float64) * dp
+    # --- fluid column
+    fx, fy, fz = (_nsteps(v, dp) for v in spec.column)
+    fl = _lattice((0, fx), (0, fy), (0, fz)).astype(np.float64) * dp
+    if spec.obstacle is not None and len(obst):
+        lo, hi = obst.min(axis=0) - 0.5 * dp, obst.max(axis=0) + 0.5 * dp
+        keep = ~np.all((fl > lo) & (fl < hi), axis=1)
+        fl = fl[keep]
+    if spec.jitter:
+        rng = np.random.default_rng(spec.seed)
+        fl = fl + rng.uniform(-spec.jitter * dp, spec.jitter * dp, size=fl.shape)
+    nbw, nbo, nf = len(wall), len(obst), len(fl)
+    npb = nbw + nbo
+    pos = np.concatenate([wall, obst, fl], axis=0)
+    n = len(pos)
+    # --- constants (GenCase conventions, CaseDambreak_Def.xml constantsdef)
+    g = abs(spec.gravity[2])
+    hswl = spec.hswl if spec.hswl is not None else spec.column[2]
+    cs0 = spec.coefsound * math.sqrt(g * hswl)
+    b = cs0 * cs0 * spec.rhop0 / spec.gamma
+    h = spec.coefh * math.sqrt(3.0 * dp * dp)
+    mass = spec.rhop0 * dp ** 3
+    # --- density: hydrostatic fluid, rho0 boundary
+    rhop = np.full(n, spec.rhop0, dtype=np.float64)
+    if nf:
+        htop = fl[:, 2].max()
+        depth = np.maximum(htop - fl[:, 2], 0.0)
+        rhop[npb:] = spec.rhop0 * (1.0 + spec.rhop0 * g * depth / b) ** (1.0 / spec.gamma)
+    # --- codes: fixed blocks 0 (tank), 1 (obstacle); fluid block 0
+    code = np.zeros(n, dtype=np.uint16)
+    code[nbw:npb] = 1
+    code[npb:] = CODE_TYPE_FLUID
+    blocks = [("fixed", 0, 0, nbw)]
+    if nbo:
+        blocks.append(("fixed", 1, nbw, nbo))
+    blocks.append(("fluid", 0, npb, nf))
+    # --- mDBC normals
+    boundnor = np.zeros((npb, 3), dtype=np.float32)
+    if spec.boundary == "mdbc":
+        half = 0.5 * dp
+        lo = np.array([-half, -half, -half])
+        hi = np.array([nx * dp + half, ny * dp + half, np.inf])
+        q = np.clip(wall, lo, hi)
+        boundnor[:nbw] = (q - wall).astype(np.float32)
+        if nbo:
+            olo, ohi = obst.min(axis=0) - half, obst.max(axis=0) + half
+            ohi[2] = ohi[2]  # top face is a boundary too
+            d = np.stack([obst[:, 0] - olo[0], ohi[0] - obst[:, 0], obst[:, 1] - olo[1],
+                          ohi[1] - obst[:, 1], np.full(nbo, np.inf), ohi[2] - obst[:, 2]], axis=1)
+            face = np.argmin(d, axis=1)
+            dist = d[np.arange(nbo), face]
+            nvec = np.zeros((nbo, 3))
+            sign = np.array([-1, 1, -1, 1, -1, 1], dtype=np.float64)
+            axis = face // 2
+            nvec[np.arange(nbo), axis] = sign[face] * dist
+            boundnor[nbw:npb] = nvec.astype(np.float32)
+    vel = np.zeros((n, 3), np.float32)
+    if spec.init_vel and nf:
+        rng = np.random.default_rng(spec.seed + 1)
+        vel[npb:] = rng.uniform(-spec.init_vel, spec.init_vel, size=(nf, 3)).astype(np.float32)
+    return Case(spec=spec, pos=pos, vel=vel, rhop=rhop.astype(np.float32),
+                idp=np.arange(n, dtype=np.uint32), code=code, boundnor=boundnor, blocks=blocks,
+                npb=npb, h=h, b=b, mass=mass)
+
+
+def _fmt(v: float) -> str:
+    return repr(float(v))
+
+
+def write_case(case: Case, dirpath: str) -> tuple[str, str]:
+    """Writes ``<name>.xml`` and ``<name>.bi4`` into ``dirpath``; returns their paths."""
+    s = case.spec
+    os.makedirs(dirpath, exist_ok=True)
+    nf = case.np - case.npb
+    params = {
+        "SavePosDouble": 1, "StepAlgorithm": s.step_algorithm, "VerletSteps": s.verlet_steps,
+        "Kernel": 2, "ViscoTreatment": s.visco_treatment, "Visco": s.visco,
+        "ViscoBoundFactor": s.viscoboundfactor, "Boundary": 2 if s.boundary == "mdbc" else 1,
+        "SlipMode": 1, "DensityDT": s.density_dt, "DensityDTvalue": s.density_dt_value,
+        "Shifting": 0, "RigidAlgorithm": 1, "CoefDtMin": 0.05, "DtIni": 0, "DtMin": 0,
+        "TimeMax": s.time_max, "TimeOut": s.time_out, "RhopOutMin": 700, "RhopOutMax": 1300,
+    }
+    if s.boundary != "mdbc":
+        params.pop("SlipMode")
+    params.update(s.extra_params)
+    lines = ['<?xml version="1.0" encoding="UTF-8" ?>',
+             '<case app="dualsphysics_gb300.casegen">',
+             '  <execution>',
+             '    <parameters>']
+    for k, v in params.items():
+        lines.append(f'      <parameter key="{k}" value="{v}" />')
+    lines += ['      <simulationdomain>',
+              '        <posmin x="default" y="default" z="default" />',
+              f'        <posmax x="default" y="default" z="{s.posmax_z}" />',
+              '      </simulationdomain>',
+              '    </parameters>',
+              '    <constants>',
+              '      <data2d value="false" />',
+              f'      <gravity x="{_fmt(s.gravity[0])}" y="{_fmt(s.gravity[1])}" z="{_fmt(s.gravity[2])}" />',
+              f'      <cflnumber value="{_fmt(s.cflnumber)}" />',
+              f'      <gamma value="{_fmt(s.gamma)}" />',
+              f'      <rhop0 value="{_fmt(s.rhop0)}" />',
+              f'      <dp value="{_fmt(s.dp)}" />',
+              f'      <h value="{_fmt(case.h)}" />',
+              f'      <b value="{_fmt(case.b)}" />',
+              f'      <massbound value="{_fmt(case.mass)}" />',
+              f'      <massfluid value="{_fmt(case.mass)}" />',
+              '    </constants>',
+              f'    <particles np="{case.np}" nb="{case.npb}" nbf="{case.npb}" mkboundfirst="11" mkfluidfirst="1">']
+    for kind, mk, begin, count in case.blocks:
+        if kind == "fixed":
+            lines.append(f'      <fixed mkbound="{mk}" mk="{11 + mk}" begin="{begin}" count="{count}" />')
+        else:
+            lines.append(f'      <fluid mkfluid="{mk}" mk="{1 + mk}" begin="{begin}" count="{count}" />')
+    lines += ['    </particles>', '  </execution>', '</case>', '']
+    xml_path = os.path.join(dirpath, s.name + ".xml")
+    with open(xml_path, "w") as f:
+        f.write("\n".join(lines))
+    root = bi4.make_partdata_root(
+        casename=s.name, appname="dualsphysics_gb300.casegen", data2d=False, casenp=case.np,
+        casenfixed=case.npb, casenmoving=0, casenfloat=0, casenfluid=nf,
+        caseposmin=case.pos.min(axis=0), caseposmax=case.pos.max(axis=0), dp=s.dp, h=case.h, b=case.b,
+        rhop0=s.rhop0, gamma=s.gamma, massbound=case.mass, massfluid=case.mass)
+    part = bi4.make_part(0, 0.0, case.np, 0, 0, case.pos.min(axis=0), case.pos.max(axis=0), case.idp, case.pos,
+                         case.vel, case.rhop, posdouble=True,
+                         boundnor=case.boundnor if s.boundary == "mdbc" else None)
+    root.items.append(part)
+    bi4_path = os.path.join(dirpath, s.name + ".bi4")
+    bi4.write(bi4_path, root)
+    return xml_path, bi4_path
+
+
+# ---------------------------------------------------------------------------
+# The dam-break workloads (geometry actually generated is recorded by
+# counting the particles; see the design doc for the counts).
+# ---------------------------------------------------------------------------
+OBSTACLE_C2 = (0.9, 0.24, 0.12, 0.12, 0.45)
+
+
+def spec_c1(dp: float = 0.01, **kw) -> CaseSpec:
+    """3-D dam break, plain WCSPH with DBC walls (tank 1.6x0.67x0.4, column 0.4x0.67x0.3)."""
+    return CaseSpec(name=kw.pop("name", "DamC1"), dp=dp, time_max=0.5, **kw)
+
+
+def spec_c2(dp: float = 0.0025, **kw) -> CaseSpec:
+    """Same dam break with mDBC boundaries and the 0.12x0.12x0.45 box obstacle at x=0.9 m."""
+    return CaseSpec(name=kw.pop("name", "DamC2"), dp=dp, obstacle=OBSTACLE_C2, boundary="mdbc", time_max=1.0, **kw)
+
+
+def spec_c3(dp: float = 0.004, column_height: float = 0.6, **kw) -> CaseSpec:
+    """Dam-break geometry scaled x4 (tank 6.4x2.68x1.6) with a 1.6x2.68xH column."""
+    return CaseSpec(name=kw.pop("name", "DamC3"), tank=(6.4, 2.68, 1.6), column=(1.6, 2.68, column_height),
+                    dp=dp, hswl=0.3, **kw)
+
+
+def spec_c5(dp: float = 0.02, **kw) -> CaseSpec:
+    """C2 geometry at coarse resolution (the learned-closure workload)."""
+    return spec_c2(dp=dp, name=kw.pop("name", "DamC5"), **kw)

@@ -1,0 +1,642 @@
+// gbsph_api.cu -- C ABI of the GB300 WCSPH step (include/gbsph.h).
+//
+// A context owns one CUDA stream and one device arena (a single allocation
+// carved into every array the step needs), so the step functions allocate
+// nothing.  The step sequence mirrors JSphGpuSingle::ComputeStep_Sym /
+// ComputeStep_Ver and the Run loop (JSphGpuSingle.cpp:785-826, 950-1010), but
+// the dt, the particle counts and the cell-division limits stay on the device:
+// no host round trip happens inside a step, and a whole step can be captured
+// into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbsph_common.cuh"
+
+struct gbsph_ctx {
+  gbsph_consts c;
+  unsigned cap = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  DevArrays a;
+  unsigned npasses = 1;
+  unsigned nctt_cap = 0;
+  bool uploaded = false;
+  int verletstep = 0;
+  unsigned long long launches = 0;
+  int forces_bsize = 128, forces_variant = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_parity = -1;  // pointer-swap parity the graph was captured with
+  unsigned long long graph_launches = 0;  // kernel launches recorded in the step graph
+  unsigned swaps = 0;     // number of reorders (each swaps the cur/alt pairs)
+  // multi-step graph (one graph holding `multi_steps` steps)
+  cudaGraphExec_t multi_exec = nullptr;
+  unsigned multi_steps = 0;
+  int multi_parity = -1;
+  unsigned long long multi_launches = 0;
+  // profiling: event pairs bracketing the fluid Interaction_Forces launches
+  std::vector<cudaEvent_t> prof_ev;
+  unsigned prof_cap = 0, prof_n = 0;
+  cudaEvent_t marks[16] = {};
+  std::string err;
+};
+
+namespace {
+
+int set_err(gbsph_ctx* ctx, int code, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+  }
+  return code;
+}
+
+int cuda_check(gbsph_ctx* ctx, cudaError_t e, const char* what) {
+  if (e != cudaSuccess) return set_err(ctx, GBSPH_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+  return GBSPH_OK;
+}
+
+#define CK(call, what)                                  \
+  do {                                                  \
+    int rc_ = cuda_check(ctx, (call), what);            \
+    if (rc_) return rc_;                                \
+  } while (0)
+
+// Reads the device error words; returns a status for the first error found.
+int check_device_errors(gbsph_ctx* ctx) {
+  unsigned derr = 0, serr = 0;
+  CK(cudaMemcpyAsync(&derr, &ctx->a.div->error, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream), "read error");
+  CK(cudaMemcpyAsync(&serr, &ctx->a.st->error, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream), "read error");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  if (derr & GB_ERR_BOUNDOUT) return set_err(ctx, GBSPH_EBOUND_OUT, "boundary particles left the domain");
+  if (derr & GB_ERR_CELLCAP) return set_err(ctx, GBSPH_ECAPACITY, "cell domain exceeds the allocated cells");
+  if (serr & GB_ERR_NANDT) return set_err(ctx, GBSPH_ENAN_DT, "the computed dt is NaN or infinity");
+  return GBSPH_OK;
+}
+
+struct Carver {
+  char* base;
+  size_t off = 0;
+  explicit Carver(void* b) : base((char*)b) {}
+  template <typename T>
+  T* take(size_t n) {
+    off = (off + 255) & ~(size_t)255;
+    T* p = base ? (T*)(base + off) : nullptr;
+    off += n * sizeof(T);
+    return p;
+  }
+};
+
+// Lays out every array of the context; with base==nullptr only measures.
+size_t layout(gbsph_ctx* ctx, void* base) {
+  Carver k(base);
+  DevArrays& a = ctx->a;
+  const size_t n = ctx->cap;
+  const bool sps = ctx->c.tvisco == GBSPH_VISCO_LAMINARSPS;
+  const bool nor = ctx->c.tboundary == GBSPH_BC_MDBC;
+  a.px = k.take<double>(n); a.py = k.take<double>(n); a.pz = k.take<double>(n);
+  a.px2 = k.take<double>(n); a.py2 = k.take<double>(n); a.pz2 = k.take<double>(n);
+  a.qx = k.take<double>(n); a.qy = k.take<double>(n); a.qz = k.take<double>(n);
+  a.qx2 = k.take<double>(n); a.qy2 = k.take<double>(n); a.qz2 = k.take<double>(n);
+  a.velrho = k.take<float4>(n); a.velrho2 = k.take<float4>(n);
+  a.velrhopre = k.take<float4>(n); a.velrhopre2 = k.take<float4>(n);
+  a.idp = k.take<unsigned>(n); a.idp2 = k.take<unsigned>(n);
+  a.dcell = k.take<unsigned>(n); a.dcell2 = k.take<unsigned>(n);
+  a.code = k.take<uint16_t>(n); a.code2 = k.take<uint16_t>(n);
+  a.boundnor = nor ? k.take<float4>(n) : nullptr;
+  a.boundnor2 = nor ? k.take<float4>(n) : nullptr;
+  a.taua = sps ? k.take<float4>(n) : nullptr; a.taua2 = sps ? k.take<float4>(n) : nullptr;
+  a.taub = sps ? k.take<float2>(n) : nullptr; a.taub2 = sps ? k.take<float2>(n) : nullptr;
+  a.straina = sps ? k.take<float4>(n) : nullptr;
+  a.strainb = sps ? k.take<float2>(n) : nullptr;
+  a.pscell = k.take<float4>(n);
+  a.acear = k.take<float4>(n);
+  a.keys = k.take<unsigned>(n); a.keys2 = k.take<unsigned>(n);
+  a.vals = k.take<unsigned>(n); a.vals2 = k.take<unsigned>(n);
+  const size_t ntiles = (n + 2047) / 2048;
+  a.hist = k.take<unsigned>(ntiles * 256 + 1);
+  a.begincell = k.take<unsigned>(ctx->nctt_cap + 1);
+  a.div = k.take<DivState>(1);
+  a.st = k.take<StepState>(1);
+  a.pips = k.take<unsigned long long>(4);
+  return k.off + 256;
+}
+
+void reset_graph(gbsph_ctx* ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->graph_exec = nullptr;
+  ctx->graph = nullptr;
+  ctx->graph_parity = -1;
+  if (ctx->multi_exec) cudaGraphExecDestroy(ctx->multi_exec);
+  ctx->multi_exec = nullptr;
+  ctx->multi_steps = 0;
+  ctx->multi_parity = -1;
+}
+
+int do_divide(gbsph_ctx* ctx) {
+  gbk::divide(ctx->c, ctx->a, ctx->cap, ctx->npasses, ctx->stream, &ctx->launches);
+  ctx->swaps++;
+  return cuda_check(ctx, cudaGetLastError(), "divide");
+}
+
+int do_forces(gbsph_ctx* ctx) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (ctx->prof_n < ctx->prof_cap) {
+    e0 = ctx->prof_ev[2 * ctx->prof_n];
+    e1 = ctx->prof_ev[2 * ctx->prof_n + 1];
+    ctx->prof_n++;
+  }
+  gbk::forces(ctx->c, ctx->a, ctx->cap, ctx->forces_bsize, ctx->forces_variant, ctx->stream, &ctx->launches, e0, e1);
+  if (ctx->c.tvisco == GBSPH_VISCO_LAMINARSPS) gbk::sps_tau(ctx->c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
+  return cuda_check(ctx, cudaGetLastError(), "forces");
+}
+
+// One step, enqueued: ComputeStep_Sym/_Ver + RunCellDivide.
+int enqueue_step(gbsph_ctx* ctx) {
+  const gbsph_consts& c = ctx->c;
+  double* dtpre = &ctx->a.st->dtpre;
+  if (c.tstep == GBSPH_STEP_SYMPLECTIC) {
+    if (c.tboundary == GBSPH_BC_MDBC) gbk::mdbc(c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
+    if (int rc = do_forces(ctx)) return rc;
+    gbk::dtvariable(c, ctx->a, 0, ctx->stream, &ctx->launches);
+    gbk::symplectic_pre(c, ctx->a, ctx->cap, dtpre, ctx->stream, &ctx->launches);
+    if (int rc = do_divide(ctx)) return rc;
+    if (int rc = do_forces(ctx)) return rc;
+    gbk::dtvariable(c, ctx->a, 1, ctx->stream, &ctx->launches);
+    gbk::symplectic_cor(c, ctx->a, ctx->cap, dtpre, ctx->stream, &ctx->launches);
+    gbk::step_end(ctx->a, 1, ctx->stream, &ctx->launches);
+  } else {
+    if (c.tboundary == GBSPH_BC_MDBC) gbk::mdbc(c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
+    if (int rc = do_forces(ctx)) return rc;
+    gbk::dtvariable(c, ctx->a, 2, ctx->stream, &ctx->launches);
+    ctx->verletstep++;
+    const int euler = !(ctx->verletstep < c.verletsteps);
+    if (euler) ctx->verletstep = 0;
+    gbk::verlet_step(c, ctx->a, ctx->cap, &ctx->a.st->dt_var, euler, ctx->stream, &ctx->launches);
+    gbk::step_end(ctx->a, 0, ctx->stream, &ctx->launches);
+  }
+  return do_divide(ctx);
+}
+
+double* device_scalar(gbsph_ctx* ctx) { return &ctx->a.st->dt_var; }
+
+}  // namespace
+
+extern "C" {
+
+int gbsph_create(const gbsph_consts* c, unsigned capacity, int device, gbsph_ctx** out) {
+  if (!c || !out || capacity == 0) return GBSPH_EINVAL;
+  *out = nullptr;
+  if (c->domcellcode == 0) return GBSPH_EINVAL;
+  if (c->tstep != GBSPH_STEP_SYMPLECTIC && c->tstep != GBSPH_STEP_VERLET) return GBSPH_EINVAL;
+  gbsph_ctx* ctx = new gbsph_ctx();
+  ctx->c = *c;
+  ctx->cap = capacity;
+  ctx->device = device;
+  const unsigned long long maxnct = (unsigned long long)c->domcells[0] * c->domcells[1] * c->domcells[2];
+  if (2ull * maxnct + 6 >= 0xffffffffull) {
+    delete ctx;
+    return GBSPH_ECAPACITY;
+  }
+  ctx->nctt_cap = (unsigned)(2ull * maxnct + 6);
+  unsigned bits = 1;
+  while ((1ull << bits) < ctx->nctt_cap) bits++;
+  ctx->npasses = (bits + 7) / 8;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete ctx;
+    return GBSPH_ECUDA;
+  }
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return GBSPH_ECUDA;
+  }
+  ctx->arena_bytes = layout(ctx, nullptr);
+  if (cudaMalloc(&ctx->arena, ctx->arena_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GBSPH_ENOMEM;
+  }
+  layout(ctx, ctx->arena);
+  *out = ctx;
+  return GBSPH_OK;
+}
+
+void gbsph_destroy(gbsph_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  reset_graph(ctx);
+  for (auto ev : ctx->prof_ev) cudaEventDestroy(ev);
+  for (auto ev : ctx->marks) if (ev) cudaEventDestroy(ev);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->arena) cudaFree(ctx->arena);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* gbsph_last_error(const gbsph_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+static int upload_common(gbsph_ctx* ctx, unsigned np, unsigned npb) {
+  const gbsph_consts& c = ctx->c;
+  DivState ds;
+  memset(&ds, 0, sizeof(ds));
+  ds.np = np;
+  ds.npb = npb;
+  ds.npbok = npb;
+  ds.boundchanged = 1;
+  ds.nctt_cap = ctx->nctt_cap;
+  StepState st;
+  memset(&st, 0, sizeof(st));
+  st.dtpre = c.dtini;
+  CK(cudaMemcpyAsync(ctx->a.div, &ds, sizeof(ds), cudaMemcpyHostToDevice, ctx->stream), "upload div");
+  CK(cudaMemcpyAsync(ctx->a.st, &st, sizeof(st), cudaMemcpyHostToDevice, ctx->stream), "upload st");
+  // InitRunCpu: VelrhoM1 = Velrho; SPS tau = 0 (JSphCpu.cpp:472-482)
+  CK(cudaMemcpyAsync(ctx->a.velrhopre, ctx->a.velrho, sizeof(float4) * np, cudaMemcpyDeviceToDevice, ctx->stream), "m1");
+  if (ctx->a.taua) {
+    CK(cudaMemsetAsync(ctx->a.taua, 0, sizeof(float4) * ctx->cap, ctx->stream), "tau");
+    CK(cudaMemsetAsync(ctx->a.taub, 0, sizeof(float2) * ctx->cap, ctx->stream), "tau");
+  }
+  CK(cudaMemsetAsync(ctx->a.acear, 0, sizeof(float4) * ctx->cap, ctx->stream), "acear");
+  gbk::load_dcell(c, ctx->a, np, ctx->stream);
+  ctx->launches++;
+  ctx->verletstep = 0;
+  reset_graph(ctx);
+  {
+    unsigned derr = 0;
+    CK(cudaMemcpyAsync(&derr, &ctx->a.div->error, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream), "upload");
+    CK(cudaStreamSynchronize(ctx->stream), "upload");
+    if (derr & GB_ERR_PARTOUT) return set_err(ctx, GBSPH_EINVAL, "found particles outside the domain in the initial state");
+  }
+  if (int rc = do_divide(ctx)) return rc;
+  ctx->uploaded = true;
+  return check_device_errors(ctx);
+}
+
+int gbsph_upload(gbsph_ctx* ctx, unsigned np, unsigned npb, const double* pos, const float* velrho,
+                 const unsigned* idp, const uint16_t* code, const float* boundnor) {
+  if (!ctx || !pos || !velrho || !idp || !code) return set_err(ctx, GBSPH_EINVAL, "null argument");
+  if (np > ctx->cap || npb > np) return set_err(ctx, GBSPH_ECAPACITY, "np=%u exceeds capacity %u", np, ctx->cap);
+  CK(cudaSetDevice(ctx->device), "set device");
+  std::vector<double> x(np), y(np), z(np);
+  for (unsigned p = 0; p < np; p++) { x[p] = pos[3 * (size_t)p]; y[p] = pos[3 * (size_t)p + 1]; z[p] = pos[3 * (size_t)p + 2]; }
+  CK(cudaMemcpyAsync(ctx->a.px, x.data(), sizeof(double) * np, cudaMemcpyHostToDevice, ctx->stream), "upload pos");
+  CK(cudaMemcpyAsync(ctx->a.py, y.data(), sizeof(double) * np, cudaMemcpyHostToDevice, ctx->stream), "upload pos");
+  CK(cudaMemcpyAsync(ctx->a.pz, z.data(), sizeof(double) * np, cudaMemcpyHostToDevice, ctx->stream), "upload pos");
+  CK(cudaMemcpyAsync(ctx->a.velrho, velrho, sizeof(float4) * np, cudaMemcpyHostToDevice, ctx->stream), "upload velrho");
+  CK(cudaMemcpyAsync(ctx->a.idp, idp, sizeof(unsigned) * np, cudaMemcpyHostToDevice, ctx->stream), "upload idp");
+  CK(cudaMemcpyAsync(ctx->a.code, code, sizeof(uint16_t) * np, cudaMemcpyHostToDevice, ctx->stream), "upload code");
+  std::vector<float4> bn;
+  if (ctx->a.boundnor) {
+    // JSph::ConfigBoundNormals: normals of boundary particles are doubled (JSph.cpp:1411-1418)
+    bn.assign(np, make_float4(0.f, 0.f, 0.f, 0.f));
+    if (boundnor)
+      for (unsigned p = 0; p < np; p++)
+        if (idp[p] < npb) bn[p] = make_float4(boundnor[3 * (size_t)p] * 2.f, boundnor[3 * (size_t)p + 1] * 2.f,
+                                              boundnor[3 * (size_t)p + 2] * 2.f, 0.f);
+    CK(cudaMemcpyAsync(ctx->a.boundnor, bn.data(), sizeof(float4) * np, cudaMemcpyHostToDevice, ctx->stream), "upload nor");
+  }
+  CK(cudaStreamSynchronize(ctx->stream), "upload sync");
+  return upload_common(ctx, np, npb);
+}
+
+int gbsph_upload_device(gbsph_ctx* ctx, unsigned np, unsigned npb, const double* d_pos, const float* d_velrho,
+                        const unsigned* d_idp, const uint16_t* d_code, const float* d_boundnor) {
+  if (!ctx || !d_pos || !d_velrho || !d_idp || !d_code) return set_err(ctx, GBSPH_EINVAL, "null argument");
+  if (np > ctx->cap || npb > np) return set_err(ctx, GBSPH_ECAPACITY, "np=%u exceeds capacity %u", np, ctx->cap);
+  CK(cudaSetDevice(ctx->device), "set device");
+  // de-interleave xyz with strided 2-D copies
+  CK(cudaMemcpy2DAsync(ctx->a.px, sizeof(double), d_pos, 3 * sizeof(double), sizeof(double), np, cudaMemcpyDeviceToDevice, ctx->stream), "pos");
+  CK(cudaMemcpy2DAsync(ctx->a.py, sizeof(double), d_pos + 1, 3 * sizeof(double), sizeof(double), np, cudaMemcpyDeviceToDevice, ctx->stream), "pos");
+  CK(cudaMemcpy2DAsync(ctx->a.pz, sizeof(double), d_pos + 2, 3 * sizeof(double), sizeof(double), np, cudaMemcpyDeviceToDevice, ctx->stream), "pos");
+  CK(cudaMemcpyAsync(ctx->a.velrho, d_velrho, sizeof(float4) * np, cudaMemcpyDeviceToDevice, ctx->stream), "velrho");
+  CK(cudaMemcpyAsync(ctx->a.idp, d_idp, sizeof(unsigned) * np, cudaMemcpyDeviceToDevice, ctx->stream), "idp");
+  CK(cudaMemcpyAsync(ctx->a.code, d_code, sizeof(uint16_t) * np, cudaMemcpyDeviceToDevice, ctx->stream), "code");
+  if (ctx->a.boundnor) {
+    CK(cudaMemsetAsync(ctx->a.boundnor, 0, sizeof(float4) * ctx->cap, ctx->stream), "nor");
+    if (d_boundnor) {
+      // boundary particles come first in case order; doubled as in gbsph_upload
+      std::vector<float> h(3 * (size_t)npb);
+      CK(cudaMemcpyAsync(h.data(), d_boundnor, sizeof(float) * 3 * npb, cudaMemcpyDeviceToHost, ctx->stream), "nor");
+      CK(cudaStreamSynchronize(ctx->stream), "nor");
+      std::vector<float4> bn(npb);
+      for (unsigned p = 0; p < npb; p++) bn[p] = make_float4(h[3 * p] * 2.f, h[3 * p + 1] * 2.f, h[3 * p + 2] * 2.f, 0.f);
+      CK(cudaMemcpyAsync(ctx->a.boundnor, bn.data(), sizeof(float4) * npb, cudaMemcpyHostToDevice, ctx->stream), "nor");
+      CK(cudaStreamSynchronize(ctx->stream), "nor");
+    }
+  }
+  return upload_common(ctx, np, npb);
+}
+
+int gbsph_divide(gbsph_ctx* ctx) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  return do_divide(ctx);
+}
+
+int gbsph_mdbc(gbsph_ctx* ctx, int interstep) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  // MdbcCorrector is false for SlipMode=vel0: only the predictor (and Verlet) correct.
+  if (ctx->c.tboundary != GBSPH_BC_MDBC || interstep == GBSPH_INTERSTEP_SYMCORRECTOR) return GBSPH_OK;
+  gbk::mdbc(ctx->c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
+  return cuda_check(ctx, cudaGetLastError(), "mdbc");
+}
+
+int gbsph_forces(gbsph_ctx* ctx, int interstep, gbsph_maxes* maxes) {
+  (void)interstep;
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (int rc = do_forces(ctx)) return rc;
+  if (maxes) return gbsph_get_maxes(ctx, maxes);
+  return GBSPH_OK;
+}
+
+int gbsph_get_maxes(gbsph_ctx* ctx, gbsph_maxes* m) {
+  if (!ctx || !m) return GBSPH_EINVAL;
+  unsigned v[3];
+  CK(cudaMemcpyAsync(v, &ctx->a.st->acemax2, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream), "maxes");
+  CK(cudaStreamSynchronize(ctx->stream), "maxes");
+  float f[3];
+  memcpy(f, v, sizeof(f));
+  m->acemax = sqrt((double)f[0]);
+  m->velmax = sqrtf(f[1]);
+  m->viscdtmax = f[2];
+  return GBSPH_OK;
+}
+
+int gbsph_dtvariable(gbsph_ctx* ctx, int final, double* dt) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  const int which = (ctx->c.tstep == GBSPH_STEP_VERLET) ? 2 : (final ? 1 : 0);
+  gbk::dtvariable(ctx->c, ctx->a, which, ctx->stream, &ctx->launches);
+  if (dt) {
+    CK(cudaMemcpyAsync(dt, &ctx->a.st->dt_var, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "dt");
+    CK(cudaStreamSynchronize(ctx->stream), "dt");
+    return check_device_errors(ctx);
+  }
+  return GBSPH_OK;
+}
+
+static int set_device_dt(gbsph_ctx* ctx, double dt) {
+  CK(cudaMemcpyAsync(device_scalar(ctx), &dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "dt");
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "dt");
+}
+
+int gbsph_symplectic_pre(gbsph_ctx* ctx, double dt) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (int rc = set_device_dt(ctx, dt)) return rc;
+  gbk::symplectic_pre(ctx->c, ctx->a, ctx->cap, device_scalar(ctx), ctx->stream, &ctx->launches);
+  return cuda_check(ctx, cudaGetLastError(), "symplectic_pre");
+}
+
+int gbsph_symplectic_cor(gbsph_ctx* ctx, double dt) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (int rc = set_device_dt(ctx, dt)) return rc;
+  gbk::symplectic_cor(ctx->c, ctx->a, ctx->cap, device_scalar(ctx), ctx->stream, &ctx->launches);
+  return cuda_check(ctx, cudaGetLastError(), "symplectic_cor");
+}
+
+int gbsph_verlet(gbsph_ctx* ctx, double dt) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (int rc = set_device_dt(ctx, dt)) return rc;
+  ctx->verletstep++;
+  const int euler = !(ctx->verletstep < ctx->c.verletsteps);
+  if (euler) ctx->verletstep = 0;
+  gbk::verlet_step(ctx->c, ctx->a, ctx->cap, device_scalar(ctx), euler, ctx->stream, &ctx->launches);
+  return cuda_check(ctx, cudaGetLastError(), "verlet");
+}
+
+int gbsph_step(gbsph_ctx* ctx) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  return enqueue_step(ctx);
+}
+
+int gbsph_run(gbsph_ctx* ctx, unsigned nsteps, int use_graph) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  // A step swaps the cur/alt array pairs once per divide: graphs are replayed
+  // only with the pointer parity they were captured with.  Verlet steps (one
+  // divide and a host-side Euler counter) run eagerly.
+  if (!use_graph || ctx->c.tstep != GBSPH_STEP_SYMPLECTIC) {
+    for (unsigned i = 0; i < nsteps; i++)
+      if (int rc = enqueue_step(ctx)) return rc;
+    return cuda_check(ctx, cudaGetLastError(), "run");
+  }
+  const int parity = (int)(ctx->swaps & 1u);
+  if (use_graph == 2) {
+    if (int rc = gbsph_graph_prepare(ctx, nsteps)) return rc;
+    CK(cudaGraphLaunch(ctx->multi_exec, ctx->stream), "graph launch");
+    ctx->swaps += 2 * nsteps;
+    ctx->launches += ctx->multi_launches;
+    return cuda_check(ctx, cudaGetLastError(), "run");
+  }
+  if (!ctx->graph_exec || ctx->graph_parity != parity) {
+    reset_graph(ctx);
+    const unsigned long long l0 = ctx->launches;
+    const unsigned s0 = ctx->swaps;
+    const DevArrays a0 = ctx->a;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "capture");
+    int rc = enqueue_step(ctx);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    // capture records the work; it did not run: restore the host-side pointer state
+    ctx->graph_launches = ctx->launches - l0;
+    ctx->a = a0;
+    ctx->swaps = s0;
+    ctx->launches = l0;
+    if (rc) return rc;
+    CK(e, "end capture");
+    ctx->graph = g;
+    CK(cudaGraphInstantiate(&ctx->graph_exec, g, 0), "instantiate");
+    ctx->graph_parity = parity;
+  }
+  for (unsigned i = 0; i < nsteps; i++) {
+    CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream), "graph launch");
+    // the captured step swapped every cur/alt pair twice: parity unchanged
+    ctx->swaps += 2;
+    ctx->launches += ctx->graph_launches;
+  }
+  return cuda_check(ctx, cudaGetLastError(), "run");
+}
+
+int gbsph_graph_prepare(gbsph_ctx* ctx, unsigned nsteps) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (ctx->c.tstep != GBSPH_STEP_SYMPLECTIC) return set_err(ctx, GBSPH_EINVAL, "multi-step graphs need Symplectic");
+  const int parity = (int)(ctx->swaps & 1u);
+  if (ctx->multi_exec && ctx->multi_steps == nsteps && ctx->multi_parity == parity && ctx->prof_n == 0 &&
+      ctx->prof_cap == 0)
+    return GBSPH_OK;
+  if (ctx->multi_exec) cudaGraphExecDestroy(ctx->multi_exec);
+  ctx->multi_exec = nullptr;
+  const unsigned long long l0 = ctx->launches;
+  const unsigned s0 = ctx->swaps;
+  const DevArrays a0 = ctx->a;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "capture");
+  int rc = GBSPH_OK;
+  for (unsigned i = 0; i < nsteps && !rc; i++) rc = enqueue_step(ctx);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->multi_launches = ctx->launches - l0;
+  ctx->a = a0;
+  ctx->swaps = s0;
+  ctx->launches = l0;
+  if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+  CK(e, "end capture");
+  cudaError_t ei = cudaGraphInstantiate(&ctx->multi_exec, g, 0);
+  cudaGraphDestroy(g);
+  CK(ei, "instantiate");
+  ctx->multi_steps = nsteps;
+  ctx->multi_parity = parity;
+  return GBSPH_OK;
+}
+
+int gbsph_profile(gbsph_ctx* ctx, unsigned max_launches) {
+  if (!ctx) return GBSPH_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  for (auto ev : ctx->prof_ev) cudaEventDestroy(ev);
+  ctx->prof_ev.clear();
+  ctx->prof_cap = 0;
+  ctx->prof_n = 0;
+  reset_graph(ctx);
+  if (!max_launches) return GBSPH_OK;
+  ctx->prof_ev.resize(2 * (size_t)max_launches);
+  for (auto& ev : ctx->prof_ev) CK(cudaEventCreate(&ev), "event");
+  ctx->prof_cap = max_launches;
+  return GBSPH_OK;
+}
+
+int gbsph_profile_read(gbsph_ctx* ctx, float* ms, unsigned cap, unsigned* n) {
+  if (!ctx || !n) return GBSPH_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  const unsigned cnt = ctx->prof_n < cap ? ctx->prof_n : cap;
+  for (unsigned i = 0; i < cnt; i++)
+    CK(cudaEventElapsedTime(&ms[i], ctx->prof_ev[2 * i], ctx->prof_ev[2 * i + 1]), "elapsed");
+  *n = cnt;
+  ctx->prof_n = 0;
+  return GBSPH_OK;
+}
+
+int gbsph_pips(gbsph_ctx* ctx, unsigned long long* out4) {
+  if (!ctx || !ctx->uploaded || !out4) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  gbk::pips(ctx->c, ctx->a, ctx->cap, ctx->stream);
+  CK(cudaGetLastError(), "pips");
+  CK(cudaMemcpyAsync(out4, ctx->a.pips, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream), "pips");
+  CK(cudaStreamSynchronize(ctx->stream), "pips");
+  return GBSPH_OK;
+}
+
+int gbsph_mark(gbsph_ctx* ctx, unsigned slot) {
+  if (!ctx || slot >= 16) return GBSPH_EINVAL;
+  if (!ctx->marks[slot]) CK(cudaEventCreate(&ctx->marks[slot]), "event");
+  CK(cudaEventRecord(ctx->marks[slot], ctx->stream), "record");
+  return GBSPH_OK;
+}
+
+int gbsph_elapsed(gbsph_ctx* ctx, unsigned a, unsigned b, float* ms) {
+  if (!ctx || a >= 16 || b >= 16 || !ctx->marks[a] || !ctx->marks[b] || !ms) return GBSPH_EINVAL;
+  CK(cudaEventSynchronize(ctx->marks[b]), "sync");
+  CK(cudaEventElapsedTime(ms, ctx->marks[a], ctx->marks[b]), "elapsed");
+  return GBSPH_OK;
+}
+
+int gbsph_step_dt(gbsph_ctx* ctx, double* dt_last, double* dt_next, double* time) {
+  if (!ctx) return GBSPH_EINVAL;
+  StepState st;
+  CK(cudaMemcpyAsync(&st, ctx->a.st, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream), "step state");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  if (dt_last) *dt_last = st.dt_last;
+  if (dt_next) *dt_next = st.dtpre;
+  if (time) *time = st.time;
+  return check_device_errors(ctx);
+}
+
+int gbsph_sync(gbsph_ctx* ctx) {
+  if (!ctx) return GBSPH_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  return check_device_errors(ctx);
+}
+
+static int read_div(gbsph_ctx* ctx, DivState* ds) {
+  CK(cudaMemcpyAsync(ds, ctx->a.div, sizeof(DivState), cudaMemcpyDeviceToHost, ctx->stream), "div");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  return GBSPH_OK;
+}
+
+int gbsph_download(gbsph_ctx* ctx, double* pos, float* velrho, unsigned* idp, uint16_t* code, unsigned* dcell) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  DivState ds;
+  if (int rc = read_div(ctx, &ds)) return rc;
+  const unsigned np = ds.np;
+  if (pos) {
+    std::vector<double> x(np), y(np), z(np);
+    CK(cudaMemcpyAsync(x.data(), ctx->a.px, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->stream), "pos");
+    CK(cudaMemcpyAsync(y.data(), ctx->a.py, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->stream), "pos");
+    CK(cudaMemcpyAsync(z.data(), ctx->a.pz, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->stream), "pos");
+    CK(cudaStreamSynchronize(ctx->stream), "sync");
+    for (unsigned p = 0; p < np; p++) { pos[3 * (size_t)p] = x[p]; pos[3 * (size_t)p + 1] = y[p]; pos[3 * (size_t)p + 2] = z[p]; }
+  }
+  if (velrho) CK(cudaMemcpyAsync(velrho, ctx->a.velrho, sizeof(float4) * np, cudaMemcpyDeviceToHost, ctx->stream), "velrho");
+  if (idp) CK(cudaMemcpyAsync(idp, ctx->a.idp, sizeof(unsigned) * np, cudaMemcpyDeviceToHost, ctx->stream), "idp");
+  if (code) CK(cudaMemcpyAsync(code, ctx->a.code, sizeof(uint16_t) * np, cudaMemcpyDeviceToHost, ctx->stream), "code");
+  if (dcell) CK(cudaMemcpyAsync(dcell, ctx->a.dcell, sizeof(unsigned) * np, cudaMemcpyDeviceToHost, ctx->stream), "dcell");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  return check_device_errors(ctx);
+}
+
+int gbsph_get_forces(gbsph_ctx* ctx, float* ace, float* ar) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  DivState ds;
+  if (int rc = read_div(ctx, &ds)) return rc;
+  std::vector<float4> h(ds.np);
+  CK(cudaMemcpyAsync(h.data(), ctx->a.acear, sizeof(float4) * ds.np, cudaMemcpyDeviceToHost, ctx->stream), "acear");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  for (unsigned p = 0; p < ds.np; p++) {
+    if (ace) { ace[3 * (size_t)p] = h[p].x; ace[3 * (size_t)p + 1] = h[p].y; ace[3 * (size_t)p + 2] = h[p].z; }
+    if (ar) ar[p] = h[p].w;
+  }
+  return GBSPH_OK;
+}
+
+int gbsph_get_divinfo(gbsph_ctx* ctx, gbsph_divinfo* info, unsigned* begincell, unsigned begincell_cap,
+                      unsigned* sortpart, unsigned* cellpart) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  DivState ds;
+  if (int rc = read_div(ctx, &ds)) return rc;
+  if (info) {
+    info->np = ds.np; info->npb = ds.npb; info->npbok = ds.npbok; info->nout_total = ds.nout_total;
+    for (int k = 0; k < 3; k++) info->cellmin[k] = ds.cellmin[k];
+    info->ncells[0] = ds.ncx; info->ncells[1] = ds.ncy; info->ncells[2] = ds.ncz;
+    info->nct = ds.nct; info->nctt = ds.nctt; info->dividefull = ds.dividefull;
+    info->npfout = ds.npfout; info->npbout = ds.npbout;
+  }
+  if (begincell) {
+    const unsigned n = begincell_cap < ds.nctt ? begincell_cap : ds.nctt;
+    CK(cudaMemcpyAsync(begincell, ctx->a.begincell, sizeof(unsigned) * n, cudaMemcpyDeviceToHost, ctx->stream), "bc");
+  }
+  if (sortpart) CK(cudaMemcpyAsync(sortpart, ctx->a.vals, sizeof(unsigned) * ds.nptot, cudaMemcpyDeviceToHost, ctx->stream), "sp");
+  if (cellpart) CK(cudaMemcpyAsync(cellpart, ctx->a.keys, sizeof(unsigned) * ds.nptot, cudaMemcpyDeviceToHost, ctx->stream), "cp");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  return GBSPH_OK;
+}
+
+unsigned long long gbsph_launch_count(const gbsph_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+void* gbsph_stream(gbsph_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int gbsph_set_option(gbsph_ctx* ctx, int key, int value) {
+  if (!ctx) return GBSPH_EINVAL;
+  if (key == 0) ctx->forces_bsize = value;
+  else if (key == 1) ctx->forces_variant = value;
+  else return set_err(ctx, GBSPH_EINVAL, "unknown option %d", key);
+  reset_graph(ctx);
+  return GBSPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,450 @@
+// gbsph_divide.cu -- cell-linked neighbour list on the device: domain fit,
+// box keys, stable LSD radix sort by box with the previous array index as
+// tie-break, BeginCell, and the reorder of the particle arrays.
+//
+// Restates JCellDivCpuSingle::Divide (JCellDivCpuSingle.cpp:45-350; GPU twin
+// JCellDivGpuSingle.cpp:152-230 with kernels in JCellDivGpuSingle_ker.cu:41-165
+// and JCellDivGpu_ker.cu:120-760) bit-exactly: the CPU's counting sort is
+// stable by array index, and an LSD radix sort whose values start as the array
+// indices is stable in the same way.  Everything stays on the device: counts
+// and limits are read by later kernels from DivState, so the whole divide can
+// be captured in a CUDA graph.
+#include <cuda_runtime.h>
+
+#include "gbsph_common.cuh"
+
+namespace {
+
+constexpr int kDivBlock = 256;
+constexpr int kSortBlock = 256;
+constexpr int kSortItems = 8;                       // items per thread per tile
+constexpr int kSortTile = kSortBlock * kSortItems;  // 2048 keys per tile
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+
+// LoadDcellParticles (JSph.cpp:1794-1817): cell of every particle.
+__global__ void k_load_dcell(gbsph_consts c, DevArrays a, unsigned n) {
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const unsigned code = a.code[p];
+  unsigned cell = 0xffffffffu;
+  if ((code & GB_CODE_MASKSPECIAL) < GB_CODE_OUTIGNORE) {
+    const double x = a.px[p], y = a.py[p], z = a.pz[p];
+    if (x >= c.domrealposmin[0] && y >= c.domrealposmin[1] && z >= c.domrealposmin[2] &&
+        x < c.domrealposmax[0] && y < c.domrealposmax[1] && z < c.domrealposmax[2]) {
+      const double sc = (double)c.scell;
+      const unsigned cx = (unsigned)(__ddiv_rn(__dsub_rn(x, c.domposmin[0]), sc));
+      const unsigned cy = (unsigned)(__ddiv_rn(__dsub_rn(y, c.domposmin[1]), sc));
+      const unsigned cz = (unsigned)(__ddiv_rn(__dsub_rn(z, c.domposmin[2]), sc));
+      cell = gb_cell(c.domcellcode, cx, cy, cz);
+    } else {
+      // JSph::LoadDcellParticles raises "Found new particles out." (JSph.cpp:1811)
+      atomicOr(&a.div->error, GB_ERR_PARTOUT);
+    }
+  }
+  a.dcell[p] = cell;
+}
+
+// Start of a divide: reset the limit reductions (JCellDivCpuSingle.cpp:284-305).
+__global__ void k_div_begin(DivState* d) {
+  d->nptot = d->np;
+  d->npb1 = d->npb;
+  d->npbout = d->npfout = d->npboutignore = d->npfoutignore = 0;
+  if (d->boundchanged) {
+    d->boundlimitok = d->bounddivideok = 0;
+    for (int k = 0; k < 3; k++) d->blmin[k] = d->blmax[k] = d->bdmin[k] = d->bdmax[k] = 0;
+  }
+  for (int k = 0; k < 3; k++) {
+    d->fmin[k] = 0xffffffffu; d->fmax[k] = 0;
+    d->bmin[k] = 0xffffffffu; d->bmax[k] = 0;
+  }
+}
+
+// LimitsCellBound/LimitsCellFluid (JCellDivCpu.cpp:256-345) as a block
+// reduction followed by one atomic per block and axis.
+__global__ void k_limits(unsigned dcc, DevArrays a) {
+  DivState* d = a.div;
+  const unsigned np = d->nptot, npb = d->npb1;
+  const bool dobound = !d->boundlimitok;
+  unsigned fmn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, fmx[3] = {0, 0, 0};
+  unsigned bmn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, bmx[3] = {0, 0, 0};
+  const unsigned pbeg = dobound ? 0 : npb;
+  for (unsigned p = pbeg + blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    if ((a.code[p] & GB_CODE_MASKSPECIAL) < GB_CODE_OUTIGNORE) {
+      const unsigned cel = a.dcell[p];
+      const unsigned v[3] = {gb_cx(dcc, cel), gb_cy(dcc, cel), gb_cz(dcc, cel)};
+      if (p >= npb) {
+        for (int k = 0; k < 3; k++) { fmn[k] = min(fmn[k], v[k]); fmx[k] = max(fmx[k], v[k]); }
+      } else {
+        for (int k = 0; k < 3; k++) { bmn[k] = min(bmn[k], v[k]); bmx[k] = max(bmx[k], v[k]); }
+      }
+    }
+  }
+  for (int k = 0; k < 3; k++) {
+    for (int o = 16; o; o >>= 1) {
+      fmn[k] = min(fmn[k], __shfl_xor_sync(0xffffffffu, fmn[k], o));
+      fmx[k] = max(fmx[k], __shfl_xor_sync(0xffffffffu, fmx[k], o));
+      bmn[k] = min(bmn[k], __shfl_xor_sync(0xffffffffu, bmn[k], o));
+      bmx[k] = max(bmx[k], __shfl_xor_sync(0xffffffffu, bmx[k], o));
+    }
+  }
+  __shared__ unsigned s[32][12];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0)
+    for (int k = 0; k < 3; k++) { s[w][k] = fmn[k]; s[w][3 + k] = fmx[k]; s[w][6 + k] = bmn[k]; s[w][9 + k] = bmx[k]; }
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    const int nw = blockDim.x >> 5;
+    const int k = threadIdx.x;
+    unsigned r = s[0][k];
+    for (int i = 1; i < nw; i++) r = ((k % 6) < 3) ? min(r, s[i][k]) : max(r, s[i][k]);
+    if (k < 3) { if (r != 0xffffffffu) atomicMin(&d->fmin[k], r); }
+    else if (k < 6) atomicMax(&d->fmax[k - 3], r);
+    else if (k < 9) { if (r != 0xffffffffu) atomicMin(&d->bmin[k - 6], r); }
+    else atomicMax(&d->bmax[k - 9], r);
+  }
+}
+
+// CalcCellDomain + MergeMapCellBoundFluid + PrepareNct + DivideFull decision
+// (JCellDivCpuSingle.cpp:45-126, 319-324).
+__global__ void k_div_setup(gbsph_consts c, DivState* d) {
+  unsigned cb0[3], cb1[3], cf0[3], cf1[3];
+  if (!d->boundlimitok) {
+    // CalcCellDomainBound: an empty set gives (DomCells,0) (JCellDivCpu.cpp:295-305)
+    const bool empty = d->bmin[0] > d->bmax[0];
+    for (int k = 0; k < 3; k++) {
+      cb0[k] = empty ? c.domcells[k] : d->bmin[k];
+      cb1[k] = empty ? 0 : d->bmax[k];
+      d->blmin[k] = cb0[k]; d->blmax[k] = cb1[k];
+    }
+    d->boundlimitok = 1;
+  } else {
+    for (int k = 0; k < 3; k++) { cb0[k] = d->blmin[k]; cb1[k] = d->blmax[k]; }
+  }
+  {
+    const bool empty = d->fmin[0] > d->fmax[0];
+    for (int k = 0; k < 3; k++) { cf0[k] = empty ? c.domcells[k] : d->fmin[k]; cf1[k] = empty ? 0 : d->fmax[k]; }
+  }
+  const unsigned sd = (unsigned)c.cellmode_div;
+  unsigned cmn[3], cmx[3];
+  for (int k = 0; k < 3; k++) {
+    const unsigned a0 = min(cb0[k], cf0[k]);
+    const unsigned b0 = cf0[k] >= sd ? cf0[k] - sd : 0;
+    cmn[k] = max(a0, b0);
+    cmx[k] = min(max(cb1[k], cf1[k]), cf1[k] + sd);
+    if (cmx[k] >= c.domcells[k]) cmx[k] = c.domcells[k] - 1;
+  }
+  if (cmn[0] > cmx[0] || cmn[1] > cmx[1] || cmn[2] > cmx[2])
+    for (int k = 0; k < 3; k++) cmn[k] = cmx[k] = 0;
+  for (int k = 0; k < 3; k++) { d->cellmin[k] = cmn[k]; d->cellmax[k] = cmx[k]; }
+  d->ncx = cmx[0] - cmn[0] + 1;
+  d->ncy = cmx[1] - cmn[1] + 1;
+  d->ncz = cmx[2] - cmn[2] + 1;
+  d->nsheet = d->ncx * d->ncy;
+  d->nct = d->nsheet * d->ncz;
+  d->nctt = d->nct * 2 + 6;
+  d->boxboundignore = d->nct;
+  d->boxfluid = d->nct + 1;
+  d->boxboundout = d->boxfluid + d->nct;
+  d->boxfluidout = d->boxboundout + 1;
+  d->boxboundoutignore = d->boxfluidout + 1;
+  d->boxfluidoutignore = d->boxboundoutignore + 1;
+  if (d->nctt > d->nctt_cap) d->error |= GB_ERR_CELLCAP;
+  bool same = d->bounddivideok;
+  for (int k = 0; k < 3; k++) same = same && d->bdmin[k] == cmn[k] && d->bdmax[k] == cmx[k];
+  if (!same) {
+    d->dividefull = 1;
+    d->bounddivideok = 1;
+    for (int k = 0; k < 3; k++) { d->bdmin[k] = cmn[k]; d->bdmax[k] = cmx[k]; }
+  } else d->dividefull = 0;
+  d->ini = d->dividefull ? 0 : d->npb1;
+}
+
+// PreSortFull / PreSortFluid (JCellDivCpuSingle.cpp:137-205): box key per
+// particle; the value is the current array index.
+__global__ void k_presort(unsigned dcc, DevArrays a) {
+  const DivState* d = a.div;
+  if (d->error & GB_ERR_CELLCAP) return;
+  const unsigned p = d->ini + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d->nptot) return;
+  const unsigned rcell = a.dcell[p];
+  const unsigned cx = gb_cx(dcc, rcell) - d->cellmin[0];
+  const unsigned cy = gb_cy(dcc, rcell) - d->cellmin[1];
+  const unsigned cz = gb_cz(dcc, rcell) - d->cellmin[2];
+  const unsigned cellsort = cx + cy * d->ncx + cz * d->nsheet;
+  const unsigned rcode = a.code[p];
+  const unsigned ctype = rcode & GB_CODE_MASKTYPE;
+  const unsigned cout = rcode & GB_CODE_MASKSPECIAL;
+  unsigned box;
+  if (d->dividefull && ctype < GB_CODE_TYPE_FLOATING) {
+    box = (cout < GB_CODE_OUTIGNORE ? ((cx < d->ncx && cy < d->ncy && cz < d->ncz) ? cellsort : d->boxboundignore)
+                                    : (cout == GB_CODE_OUTIGNORE ? d->boxboundoutignore : d->boxboundout));
+  } else {
+    box = (cout <= GB_CODE_OUTIGNORE ? (cout < GB_CODE_OUTIGNORE ? d->boxfluid + cellsort : d->boxfluidoutignore)
+                                     : (ctype == GB_CODE_TYPE_FLOATING ? d->boxboundout : d->boxfluidout));
+  }
+  a.keys[p] = box;
+  a.vals[p] = p;
+}
+
+// ---- stable LSD radix sort of (key,value) over [ini, nptot) ------------------
+// Tile histograms, stored digit-major: hist[digit*ntiles + tile].
+__global__ void k_rs_hist(const unsigned* __restrict__ keys, unsigned* __restrict__ hist, const DivState* d,
+                          unsigned ntiles_cap, int shift) {
+  __shared__ unsigned sh[kRadix];
+  const unsigned ini = d->ini, n = d->nptot - d->ini;
+  const unsigned ntiles = gb_div_up(n, kSortTile);
+  for (int i = threadIdx.x; i < kRadix; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const unsigned tile = blockIdx.x;
+  if (tile < ntiles) {
+    const unsigned base = tile * kSortTile;
+    for (int i = threadIdx.x; i < kSortTile; i += blockDim.x) {
+      const unsigned q = base + i;
+      if (q < n) atomicAdd(&sh[(keys[ini + q] >> shift) & (kRadix - 1)], 1u);
+    }
+  }
+  __syncthreads();
+  for (int dgt = threadIdx.x; dgt < kRadix; dgt += blockDim.x)
+    hist[dgt * ntiles_cap + tile] = (tile < ntiles) ? sh[dgt] : 0;
+}
+
+// Exclusive scan of the histogram in digit-major order (one block).
+__global__ void k_rs_scan(unsigned* __restrict__ hist, unsigned total) {
+  __shared__ unsigned sums[1024];
+  const unsigned t = threadIdx.x, nt = blockDim.x;
+  const unsigned chunk = gb_div_up(total, nt);
+  const unsigned b = t * chunk, e = min(total, b + chunk);
+  unsigned s = 0;
+  for (unsigned i = b; i < e; i++) s += hist[i];
+  sums[t] = s;
+  __syncthreads();
+  for (unsigned o = 1; o < nt; o <<= 1) {
+    const unsigned v = (t >= o) ? sums[t - o] : 0;
+    __syncthreads();
+    sums[t] += v;
+    __syncthreads();
+  }
+  unsigned run = sums[t] - s;
+  for (unsigned i = b; i < e; i++) {
+    const unsigned v = hist[i];
+    hist[i] = run;
+    run += v;
+  }
+}
+
+// Stable scatter: within a tile, items keep their index order per digit.
+// The tile is processed in rounds of blockDim.x consecutive items; in a round
+// each warp ranks its 32 items with __match_any_sync, per-digit warp counts are
+// prefixed across warps in warp order, and a running per-digit offset carries
+// the order from one round to the next.
+__global__ void __launch_bounds__(kSortBlock) k_rs_scatter(const unsigned* __restrict__ kin, const unsigned* __restrict__ vin,
+                                                           unsigned* __restrict__ kout, unsigned* __restrict__ vout,
+                                                           const unsigned* __restrict__ hist, const DivState* d,
+                                                           unsigned ntiles_cap, int shift) {
+  constexpr int kWarps = kSortBlock / 32;
+  __shared__ unsigned s_off[kRadix];          // running output offset of each digit for this tile
+  __shared__ unsigned s_tot[kRadix];          // per-digit count of the current round
+  __shared__ unsigned s_wc[kWarps][kRadix];   // per-warp counts, then exclusive prefix across warps
+  const unsigned ini = d->ini, n = d->nptot - d->ini;
+  const unsigned ntiles = gb_div_up(n, kSortTile);
+  const unsigned tile = blockIdx.x;
+  if (tile >= ntiles) return;
+  for (int i = threadIdx.x; i < kRadix; i += blockDim.x) s_off[i] = hist[i * ntiles_cap + tile];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned lanemask_lt = (1u << lane) - 1u;
+  const unsigned base = tile * kSortTile;
+  for (int r = 0; r < kSortItems; r++) {
+    for (int i = threadIdx.x; i < kWarps * kRadix; i += blockDim.x) (&s_wc[0][0])[i] = 0;
+    __syncthreads();
+    const unsigned q = base + r * kSortBlock + threadIdx.x;
+    const bool valid = q < n;
+    unsigned key = 0, val = 0, dgt = kRadix;  // kRadix marks an invalid item
+    if (valid) {
+      key = kin[ini + q];
+      val = vin[ini + q];
+      dgt = (key >> shift) & (kRadix - 1);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, dgt);
+    const unsigned rank = __popc(peers & lanemask_lt);
+    if (valid && rank == 0) s_wc[w][dgt] = __popc(peers);
+    __syncthreads();
+    for (int dg = threadIdx.x; dg < kRadix; dg += blockDim.x) {
+      unsigned run = 0;
+      for (int ww = 0; ww < kWarps; ww++) {
+        const unsigned v = s_wc[ww][dg];
+        s_wc[ww][dg] = run;
+        run += v;
+      }
+      s_tot[dg] = run;
+    }
+    __syncthreads();
+    if (valid) {
+      const unsigned dst = s_off[dgt] + s_wc[w][dgt] + rank;
+      kout[ini + dst] = key;
+      vout[ini + dst] = val;
+    }
+    __syncthreads();
+    for (int dg = threadIdx.x; dg < kRadix; dg += blockDim.x) s_off[dg] += s_tot[dg];
+    __syncthreads();
+  }
+}
+
+// BeginCell (JCellDivCpuSingle.cpp:207-247): begincell[b] = first sorted index
+// with key >= b, found by binary search; b ranges over every box in a full
+// divide and over the fluid boxes above BoxFluid in a fluid-only divide (the
+// boundary part of the previous full divide is kept, as the reference does).
+__global__ void k_begincell(const unsigned* __restrict__ keys, DevArrays a) {
+  const DivState* d = a.div;
+  if (d->error & GB_ERR_CELLCAP) return;
+  const unsigned nctt = d->nctt;
+  const unsigned b0 = d->dividefull ? 0 : d->boxfluid + 1;
+  const unsigned b = b0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nctt) return;
+  unsigned lo = d->ini, hi = d->nptot;
+  while (lo < hi) {
+    const unsigned mid = (lo + hi) >> 1;
+    if (keys[mid] < b) lo = mid + 1;
+    else hi = mid;
+  }
+  a.begincell[b] = lo;
+}
+
+// Counts and new particle numbers (JCellDivCpuSingle.cpp:327-345,
+// JSphCpuSingle.cpp:566-572).
+__global__ void k_div_counts(DevArrays a) {
+  DivState* d = a.div;
+  if (d->error & GB_ERR_CELLCAP) return;
+  const unsigned* bc = a.begincell;
+  d->npbignore = bc[d->boxboundignore + 1] - bc[d->boxboundignore];
+  d->npbout = bc[d->boxboundout + 1] - bc[d->boxboundout];
+  d->npfout = bc[d->boxfluidout + 1] - bc[d->boxfluidout];
+  d->npboutignore = bc[d->boxboundoutignore + 1] - bc[d->boxboundoutignore];
+  d->npfoutignore = bc[d->boxfluidoutignore + 1] - bc[d->boxfluidoutignore];
+  d->npfinal = d->nptot - d->npbout - d->npfout - d->npboutignore - d->npfoutignore;
+  d->npbfinal = d->npb1 - d->npboutignore;
+  if (d->npbout) d->error |= GB_ERR_BOUNDOUT;
+  d->np = d->npfinal;
+  d->npb = d->npbfinal;
+  d->npbok = d->npbfinal - d->npbignore;
+  d->nout_total += d->npfout;
+  d->boundchanged = 0;
+}
+
+// SortDataParticles + UpdatePosCell (JCellDivGpu_ker.cu:577-760,
+// JSphGpuSimple_ker.cu:41-62): gather every particle array in the new order and
+// rebuild the cell-relative float position and the pressure.
+template <bool withpre, bool withsps, bool withnor>
+__global__ void k_reorder(gbsph_consts c, DevArrays a) {
+  const DivState* d = a.div;
+  if (d->error & GB_ERR_CELLCAP) return;
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d->nptot) return;
+  const unsigned src = (p < d->ini) ? p : a.vals[p];
+  const double x = a.px[src], y = a.py[src], z = a.pz[src];
+  a.px2[p] = x; a.py2[p] = y; a.pz2[p] = z;
+  const float4 vr = a.velrho[src];
+  a.velrho2[p] = vr;
+  a.idp2[p] = a.idp[src];
+  a.code2[p] = a.code[src];
+  const unsigned cel = a.dcell[src];
+  a.dcell2[p] = cel;
+  if (withpre) {
+    a.qx2[p] = a.qx[src]; a.qy2[p] = a.qy[src]; a.qz2[p] = a.qz[src];
+    a.velrhopre2[p] = a.velrhopre[src];
+  }
+  if (withsps) {
+    a.taua2[p] = a.taua[src];
+    a.taub2[p] = a.taub[src];
+  }
+  if (withnor) a.boundnor2[p] = a.boundnor[src];
+  // position relative to the origin of the particle's cell
+  const unsigned dcc = c.domcellcode;
+  const double sc = (double)c.scell;
+  float4 ps;
+  if (cel != 0xffffffffu) {
+    ps.x = (float)__dsub_rn(__dsub_rn(x, c.domposmin[0]), __dmul_rn((double)gb_cx(dcc, cel), sc));
+    ps.y = (float)__dsub_rn(__dsub_rn(y, c.domposmin[1]), __dmul_rn((double)gb_cy(dcc, cel), sc));
+    ps.z = (float)__dsub_rn(__dsub_rn(z, c.domposmin[2]), __dmul_rn((double)gb_cz(dcc, cel), sc));
+  } else {
+    ps.x = ps.y = ps.z = 0.f;
+  }
+  ps.w = gb_press(vr.w, c.rhopzero, c.cteb, c.gamma);
+  a.pscell[p] = ps;
+}
+
+template <typename T>
+inline void swp(T*& x, T*& y) {
+  T* t = x;
+  x = y;
+  y = t;
+}
+
+}  // namespace
+
+namespace gbk {
+
+void load_dcell(const gbsph_consts& c, const DevArrays& a, unsigned n, cudaStream_t s) {
+  if (!n) return;
+  k_load_dcell<<<gb_div_up(n, kDivBlock), kDivBlock, 0, s>>>(c, a, n);
+}
+
+// JSphGpuSingle::RunCellDivide without periodic conditions.  `cap` is the
+// particle capacity (grids are sized by it; kernels read the live counts from
+// DivState).  The reorder swaps the cur/alt array pairs in `a`.
+void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses, cudaStream_t s,
+            unsigned long long* nlaunch) {
+  const unsigned dcc = c.domcellcode;
+  const unsigned grid_p = gb_div_up(cap, kDivBlock);
+  k_div_begin<<<1, 1, 0, s>>>(a.div);
+  k_limits<<<min(grid_p, 152u * 8u), kDivBlock, 0, s>>>(dcc, a);
+  k_div_setup<<<1, 1, 0, s>>>(c, a.div);
+  k_presort<<<grid_p, kDivBlock, 0, s>>>(dcc, a);
+  const unsigned ntiles_cap = gb_div_up(cap, kSortTile);
+  unsigned* kin = a.keys;
+  unsigned* vin = a.vals;
+  unsigned* kout = a.keys2;
+  unsigned* vout = a.vals2;
+  for (unsigned pass = 0; pass < npasses; pass++) {
+    const int shift = (int)(pass * kRadixBits);
+    k_rs_hist<<<ntiles_cap, kSortBlock, 0, s>>>(kin, a.hist, a.div, ntiles_cap, shift);
+    k_rs_scan<<<1, 1024, 0, s>>>(a.hist, ntiles_cap * kRadix);
+    k_rs_scatter<<<ntiles_cap, kSortBlock, 0, s>>>(kin, vin, kout, vout, a.hist, a.div, ntiles_cap, shift);
+    swp(kin, kout);
+    swp(vin, vout);
+  }
+  // sorted keys/vals are in kin/vin
+  a.keys = kin; a.keys2 = kout; a.vals = vin; a.vals2 = vout;
+  const unsigned long long maxboxes = 2ull * c.domcells[0] * c.domcells[1] * c.domcells[2] + 6;
+  k_begincell<<<(unsigned)((maxboxes + kDivBlock - 1) / kDivBlock), kDivBlock, 0, s>>>(kin, a);
+  k_div_counts<<<1, 1, 0, s>>>(a);
+  const bool withpre = (c.tstep == GBSPH_STEP_SYMPLECTIC) || (c.tstep == GBSPH_STEP_VERLET);
+  const bool withsps = (c.tvisco == GBSPH_VISCO_LAMINARSPS);
+  const bool withnor = (c.tboundary == GBSPH_BC_MDBC);
+  if (withpre) {
+    if (withsps) {
+      if (withnor) k_reorder<true, true, true><<<grid_p, kDivBlock, 0, s>>>(c, a);
+      else k_reorder<true, true, false><<<grid_p, kDivBlock, 0, s>>>(c, a);
+    } else {
+      if (withnor) k_reorder<true, false, true><<<grid_p, kDivBlock, 0, s>>>(c, a);
+      else k_reorder<true, false, false><<<grid_p, kDivBlock, 0, s>>>(c, a);
+    }
+  } else {
+    if (withsps) {
+      if (withnor) k_reorder<false, true, true><<<grid_p, kDivBlock, 0, s>>>(c, a);
+      else k_reorder<false, true, false><<<grid_p, kDivBlock, 0, s>>>(c, a);
+    } else {
+      if (withnor) k_reorder<false, false, true><<<grid_p, kDivBlock, 0, s>>>(c, a);
+      else k_reorder<false, false, false><<<grid_p, kDivBlock, 0, s>>>(c, a);
+    }
+  }
+  swp(a.px, a.px2); swp(a.py, a.py2); swp(a.pz, a.pz2);
+  swp(a.velrho, a.velrho2);
+  swp(a.idp, a.idp2); swp(a.code, a.code2); swp(a.dcell, a.dcell2);
+  if (withpre) { swp(a.qx, a.qx2); swp(a.qy, a.qy2); swp(a.qz, a.qz2); swp(a.velrhopre, a.velrhopre2); }
+  if (withsps) { swp(a.taua, a.taua2); swp(a.taub, a.taub2); }
+  if (withnor) swp(a.boundnor, a.boundnor2);
+  if (nlaunch) *nlaunch += 7 + 3ull * npasses;
+}
+
+}  // namespace gbk

@@ -1,0 +1,473 @@
+// gbsph_forces.cu -- Interaction_Forces and the mDBC ghost-node correction.
+//
+// Fluid rows restate JSphCpu::InteractionForcesFluid (JSphCpu.cpp:736-1141;
+// GPU twin KerInteractionForcesFluidBox, JSphGpu_ker.cu:542-990): Wendland C2
+// kernel gradient, Tait pressure (precomputed per particle), Monaghan
+// artificial viscosity or Laminar+SPS, Molteni (DDT) or Fourtakas (DDT2)
+// density diffusion with the veto for particles with boundary neighbours.
+// Bound rows restate JSphCpu::InteractionForcesBound (JSphCpu.cpp:633-703).
+// The maxima the dt needs (|ace|^2 over fluid, visc, |v|^2) are reduced in
+// the same kernels (JSphGpuSingle.cpp:719-729, JSphGpu.cpp:846-900).
+//
+// Pair distance: every particle carries its position relative to the origin of
+// its own cell (pscell.xyz, rounded once from double); a neighbour in cell cj
+// is at (lp_i - lp_j) + (ci - cj)*Scell, which needs no FP64 in the pair loop.
+#include <cuda_runtime.h>
+#include <float.h>
+
+#include "gbsph_common.cuh"
+
+namespace {
+
+struct CellGrid {
+  int cx, cy, cz;           // particle cell relative to the trimmed domain
+  int xini, xfin, yini, yfin, zini, zfin;
+};
+
+// nsearch::Init (JCellSearch_inline.h:33-52)
+__device__ __forceinline__ CellGrid gb_grid(int cx, int cy, int cz, int sd, const DivState& d) {
+  CellGrid g;
+  g.cx = cx; g.cy = cy; g.cz = cz;
+  const int ncx = (int)d.ncx, ncy = (int)d.ncy, ncz = (int)d.ncz;
+  g.xini = cx - (cx < sd ? cx : sd);
+  g.xfin = cx + (ncx - cx - 1 < sd ? ncx - cx - 1 : sd) + 1;
+  g.yini = cy - (cy < sd ? cy : sd);
+  g.yfin = cy + (ncy - cy - 1 < sd ? ncy - cy - 1 : sd) + 1;
+  g.zini = cz - (cz < sd ? cz : sd);
+  g.zfin = cz + (ncz - cz - 1 < sd ? ncz - cz - 1 : sd) + 1;
+  return g;
+}
+
+struct FluidAcc {
+  float ax, ay, az, ar, delta, visc;
+  float s0, s1, s2, s3, s4, s5;  // 2*strain (SPS)
+};
+
+// One pass of a fluid row over the fluid (boundp2=false) or boundary
+// (boundp2=true) boxes.
+template <int tvisco, int tdensity, bool boundp2>
+__device__ __forceinline__ void fluid_pass(const gbsph_consts& c, const DevArrays& a, const DivState& d,
+                                           const CellGrid& g, float4 ps1, float4 vr1, float4 ta1, float2 tb1,
+                                           float visco, FluidAcc& r) {
+  const unsigned cellinit = boundp2 ? 0u : d.boxfluid;
+  const float scell = c.scell;
+  const float ks2 = c.kernelsize2, eta2 = c.eta2, h = c.kernelh, bwenh = c.bwenh;
+  const float massp2 = boundp2 ? c.massbound : c.massfluid;
+  const float cbar = (float)c.cs0;
+  float ax = 0, ay = 0, az = 0, arp1 = 0, deltap1 = 0, visc = 0;
+  float s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
+  for (int z = g.zini; z < g.zfin; z++) {
+    for (int y = g.yini; y < g.yfin; y++) {
+      const unsigned rowbase = cellinit + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+      const float offy = (float)(g.cy - y) * scell, offz = (float)(g.cz - z) * scell;
+      for (int x = g.xini; x < g.xfin; x++) {
+        const unsigned box = rowbase + (unsigned)x;
+        const unsigned pini = a.begincell[box], pfin = a.begincell[box + 1];
+        const float bx = ps1.x + (float)(g.cx - x) * scell;
+        const float by = ps1.y + offy;
+        const float bz = ps1.z + offz;
+        for (unsigned p2 = pini; p2 < pfin; p2++) {
+          const float4 ps2 = a.pscell[p2];
+          const float drx = bx - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
+          const float rr2 = drx * drx + dry * dry + drz * drz;
+          if (rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
+            // Wendland C2 gradient factor (FunSphKernel.h:225-231)
+            const float rad = sqrtf(rr2);
+            const float qq = rad / h;
+            const float wqq1 = 1.f - 0.5f * qq;
+            const float fac = bwenh * wqq1 * wqq1 * wqq1;
+            const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
+            const float4 vr2 = a.velrho[p2];
+            // momentum (JSphCpu.cpp:846-852)
+            const float prs = (ps1.w + ps2.w) / (vr1.w * vr2.w);
+            const float p_vpm = -prs * massp2;
+            ax += p_vpm * frx; ay += p_vpm * fry; az += p_vpm * frz;
+            // continuity (JSphCpu.cpp:865-875)
+            const float dvx = vr1.x - vr2.x, dvy = vr1.y - vr2.y, dvz = vr1.z - vr2.z;
+            arp1 += massp2 * (dvx * frx + dvy * fry + dvz * frz) * (vr1.w / vr2.w);
+            // density diffusion (JSphCpu.cpp:915-940)
+            if (tdensity == GBSPH_DDT_DDT && deltap1 != FLT_MAX) {
+              const float visc_densi = c.ddtkh * cbar * (vr1.w / vr2.w - 1.f) / (rr2 + eta2);
+              const float dot3 = drx * frx + dry * fry + drz * frz;
+              const float delta = visc_densi * dot3 * massp2;
+              deltap1 = (boundp2 && c.tboundary == GBSPH_BC_DBC) ? FLT_MAX : deltap1 + delta;
+            }
+            if ((tdensity == GBSPH_DDT_DDT2 || (tdensity == GBSPH_DDT_DDT2FULL && !boundp2)) && deltap1 != FLT_MAX) {
+              if (boundp2) {
+                deltap1 = FLT_MAX;
+              } else {
+                const float rh = 1.f + c.ddtgz * drz;
+                const float drho = c.rhopzero * powf(rh, 1.f / c.gamma) - c.rhopzero;
+                const float visc_densi = c.ddtkh * cbar * ((vr2.w - vr1.w) - drho) / (rr2 + eta2);
+                const float dot3 = drx * frx + dry * fry + drz * frz;
+                const float delta = visc_densi * dot3 * massp2 / vr2.w;
+                deltap1 = deltap1 - delta;
+              }
+            }
+            // viscosity (JSphCpu.cpp:990-1037)
+            const float dot = drx * dvx + dry * dvy + drz * dvz;
+            const float dot_rr2 = dot / (rr2 + eta2);
+            visc = fmaxf(dot_rr2, visc);
+            if (tvisco == GBSPH_VISCO_ARTIFICIAL) {
+              if (dot < 0) {
+                const float amubar = h * dot_rr2;
+                const float robar = (vr1.w + vr2.w) * 0.5f;
+                const float pi_visc = (-visco * cbar * amubar / robar) * massp2;
+                ax -= pi_visc * frx; ay -= pi_visc * fry; az -= pi_visc * frz;
+              }
+            } else {
+              const float robar2 = vr1.w + vr2.w;
+              const float temp = 4.f * visco / ((rr2 + eta2) * robar2);
+              const float vtemp = massp2 * temp * (drx * frx + dry * fry + drz * frz);
+              ax += vtemp * dvx; ay += vtemp * dvy; az += vtemp * dvz;
+              if (tvisco == GBSPH_VISCO_LAMINARSPS) {
+                float t0 = ta1.x, t1 = ta1.y, t2 = ta1.z, t3 = ta1.w, t4 = tb1.x, t5 = tb1.y;
+                if (!boundp2) {
+                  const float4 ta2 = a.taua[p2];
+                  const float2 tb2 = a.taub[p2];
+                  t0 += ta2.x; t1 += ta2.y; t2 += ta2.z; t3 += ta2.w; t4 += tb2.x; t5 += tb2.y;
+                }
+                ax += massp2 * (t0 * frx + t1 * fry + t2 * frz);
+                ay += massp2 * (t1 * frx + t3 * fry + t4 * frz);
+                az += massp2 * (t2 * frx + t4 * fry + t5 * frz);
+                const float volp2 = -massp2 / vr2.w;
+                float dv = dvx * volp2; s0 += dv * frx; s1 += dv * fry; s2 += dv * frz;
+                dv = dvy * volp2; s1 += dv * frx; s3 += dv * fry; s4 += dv * frz;
+                dv = dvz * volp2; s2 += dv * frx; s4 += dv * fry; s5 += dv * frz;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  r.ax = ax; r.ay = ay; r.az = az; r.ar = arp1; r.delta = deltap1; r.visc = visc;
+  r.s0 = s0; r.s1 = s1; r.s2 = s2; r.s3 = s3; r.s4 = s4; r.s5 = s5;
+}
+
+template <int tvisco, int tdensity>
+__global__ void __launch_bounds__(128) k_forces_fluid(gbsph_consts c, DevArrays a) {
+  const DivState& d = *a.div;
+  const unsigned np = d.np, npb = d.npb;
+  const unsigned p1 = npb + blockIdx.x * blockDim.x + threadIdx.x;
+  float acemax2 = 0, visc = 0, vel2 = 0;
+  if (p1 < np) {
+    const float4 ps1 = a.pscell[p1];
+    const float4 vr1 = a.velrho[p1];
+    float4 ta1 = make_float4(0, 0, 0, 0);
+    float2 tb1 = make_float2(0, 0);
+    if (tvisco == GBSPH_VISCO_LAMINARSPS) { ta1 = a.taua[p1]; tb1 = a.taub[p1]; }
+    const unsigned dcc = c.domcellcode, cel = a.dcell[p1];
+    const CellGrid g = gb_grid((int)gb_cx(dcc, cel) - (int)d.cellmin[0], (int)gb_cy(dcc, cel) - (int)d.cellmin[1],
+                               (int)gb_cz(dcc, cel) - (int)d.cellmin[2], c.cellmode_div, d);
+    FluidAcc ff, fb;
+    fluid_pass<tvisco, tdensity, false>(c, a, d, g, ps1, vr1, ta1, tb1, c.visco, ff);
+    fluid_pass<tvisco, tdensity, true>(c, a, d, g, ps1, vr1, ta1, tb1, c.visco * c.viscoboundfactor, fb);
+    // JSphCpu.cpp:1093-1113 and JSphCpuSingle.cpp:727-735
+    float ar = ff.ar + fb.ar;
+    if (tdensity != GBSPH_DDT_NONE) {
+      const float dl = (ff.delta == FLT_MAX || fb.delta == FLT_MAX) ? FLT_MAX : ff.delta + fb.delta;
+      if (dl != FLT_MAX) ar += dl;
+    }
+    const float ax = ff.ax + fb.ax, ay = ff.ay + fb.ay, az = ff.az + fb.az;
+    a.acear[p1] = make_float4(ax, ay, az, ar);
+    if (tvisco == GBSPH_VISCO_LAMINARSPS) {
+      a.straina[p1] = make_float4(ff.s0 + fb.s0, ff.s1 + fb.s1, ff.s2 + fb.s2, ff.s3 + fb.s3);
+      a.strainb[p1] = make_float2(ff.s4 + fb.s4, ff.s5 + fb.s5);
+    }
+    acemax2 = ax * ax + ay * ay + az * az;
+    visc = fmaxf(ff.visc, fb.visc);
+    vel2 = vr1.x * vr1.x + vr1.y * vr1.y + vr1.z * vr1.z;
+  }
+  // block reduction of the maxima, one atomic per block
+  for (int o = 16; o; o >>= 1) {
+    acemax2 = fmaxf(acemax2, __shfl_xor_sync(0xffffffffu, acemax2, o));
+    visc = fmaxf(visc, __shfl_xor_sync(0xffffffffu, visc, o));
+    vel2 = fmaxf(vel2, __shfl_xor_sync(0xffffffffu, vel2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (acemax2 > 0) gb_atomic_max_nonneg(&a.st->acemax2, acemax2);
+    if (visc > 0) gb_atomic_max_nonneg(&a.st->viscdt, visc);
+    if (vel2 > 0) gb_atomic_max_nonneg(&a.st->velmax2, vel2);
+  }
+}
+
+// Bound rows (JSphCpu.cpp:633-703): continuity and visc from fluid neighbours.
+__global__ void __launch_bounds__(128) k_forces_bound(gbsph_consts c, DevArrays a) {
+  const DivState& d = *a.div;
+  const unsigned npb = d.npb, npbok = d.npbok;
+  const unsigned p1 = blockIdx.x * blockDim.x + threadIdx.x;
+  float visc = 0, vel2 = 0;
+  if (p1 < npb) {
+    float arp1 = 0;
+    if (p1 < npbok) {
+      const float4 ps1 = a.pscell[p1];
+      const float4 vr1 = a.velrho[p1];
+      const unsigned dcc = c.domcellcode, cel = a.dcell[p1];
+      const CellGrid g = gb_grid((int)gb_cx(dcc, cel) - (int)d.cellmin[0], (int)gb_cy(dcc, cel) - (int)d.cellmin[1],
+                                 (int)gb_cz(dcc, cel) - (int)d.cellmin[2], c.cellmode_div, d);
+      const float scell = c.scell, ks2 = c.kernelsize2, h = c.kernelh, bwenh = c.bwenh, eta2 = c.eta2;
+      const float massp2 = c.massfluid;
+      for (int z = g.zini; z < g.zfin; z++) {
+        for (int y = g.yini; y < g.yfin; y++) {
+          const unsigned rowbase = d.boxfluid + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+          const float by = ps1.y + (float)(g.cy - y) * scell, bz = ps1.z + (float)(g.cz - z) * scell;
+          for (int x = g.xini; x < g.xfin; x++) {
+            const unsigned box = rowbase + (unsigned)x;
+            const unsigned pini = a.begincell[box], pfin = a.begincell[box + 1];
+            const float bx = ps1.x + (float)(g.cx - x) * scell;
+            for (unsigned p2 = pini; p2 < pfin; p2++) {
+              const float4 ps2 = a.pscell[p2];
+              const float drx = bx - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
+              const float rr2 = drx * drx + dry * dry + drz * drz;
+              if (rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
+                const float rad = sqrtf(rr2);
+                const float qq = rad / h;
+                const float wqq1 = 1.f - 0.5f * qq;
+                const float fac = bwenh * wqq1 * wqq1 * wqq1;
+                const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
+                const float4 vr2 = a.velrho[p2];
+                const float dvx = vr1.x - vr2.x, dvy = vr1.y - vr2.y, dvz = vr1.z - vr2.z;
+                arp1 += massp2 * (dvx * frx + dvy * fry + dvz * frz) * (vr1.w / vr2.w);
+                const float dot = drx * dvx + dry * dvy + drz * dvz;
+                visc = fmaxf(dot / (rr2 + eta2), visc);
+              }
+            }
+          }
+        }
+      }
+      if (c.dtallparticles) vel2 = vr1.x * vr1.x + vr1.y * vr1.y + vr1.z * vr1.z;
+    }
+    a.acear[p1] = make_float4(0.f, 0.f, 0.f, arp1);
+  }
+  for (int o = 16; o; o >>= 1) {
+    visc = fmaxf(visc, __shfl_xor_sync(0xffffffffu, visc, o));
+    vel2 = fmaxf(vel2, __shfl_xor_sync(0xffffffffu, vel2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (visc > 0) gb_atomic_max_nonneg(&a.st->viscdt, visc);
+    if (vel2 > 0) gb_atomic_max_nonneg(&a.st->velmax2, vel2);
+  }
+}
+
+// JSphCpu::ComputeSpsTau (JSphCpu.cpp:1279-1309) for fluid particles.
+__global__ void k_sps_tau(gbsph_consts c, DevArrays a) {
+  const DivState& d = *a.div;
+  const unsigned p = d.npb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.np) return;
+  const float4 sa = a.straina[p];
+  const float2 sb = a.strainb[p];
+  const float xx = sa.x, xy = sa.y, xz = sa.z, yy = sa.w, yz = sb.x, zz = sb.y;
+  const float pow1 = xx * xx + yy * yy + zz * zz;
+  const float prr = xy * xy + xz * xz + yz * yz + pow1 + pow1;
+  const float visc_sps = c.spssmag * sqrtf(prr);
+  const float div_u = xx + yy + zz;
+  const float sps_k = visc_sps * div_u;
+  const float sps_blin = c.spsblin * prr;
+  const float sumsps = -(sps_k + sps_blin);
+  const float twovisc_sps = visc_sps + visc_sps;
+  const float one_rho = 1.0f / a.velrho[p].w;
+  a.taua[p] = make_float4(one_rho * (twovisc_sps * xx + sumsps), one_rho * (visc_sps * xy), one_rho * (visc_sps * xz),
+                          one_rho * (twovisc_sps * yy + sumsps));
+  a.taub[p] = make_float2(one_rho * (visc_sps * yz), one_rho * (twovisc_sps * zz + sumsps));
+}
+
+// ---- mDBC ghost-node correction, SlipMode=vel0, 3-D -------------------------
+// JSphCpu_mdbc.cpp:36-160 (GPU twin KerInteractionMdbcCorrection_Fast,
+// JSphGpu_mdbc_iker.cu:34-151).  The 4x4 moment matrix is accumulated in
+// double as the CPU path does; the first-order system is solved by cofactor
+// expansion in double.
+__device__ __forceinline__ double gb_det3(double a, double b, double cc, double d, double e, double f, double g,
+                                          double h, double i) {
+  return a * (e * i - f * h) - b * (d * i - f * g) + cc * (d * h - e * g);
+}
+
+__global__ void __launch_bounds__(128) k_mdbc(gbsph_consts c, DevArrays a) {
+  const DivState& d = *a.div;
+  const unsigned p1 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p1 >= d.npbok) return;
+  const float4 bn = a.boundnor[p1];
+  if (bn.x == 0.f && bn.y == 0.f && bn.z == 0.f) return;
+  const double gx = a.px[p1] + (double)bn.x, gy = a.py[p1] + (double)bn.y, gz = a.pz[p1] + (double)bn.z;
+  const double sc = (double)c.scell;
+  // cell of the ghost node, truncated toward zero as int() does (JCellSearch_inline.h:59-61)
+  const int gcx = (int)((gx - c.domposmin[0]) / sc), gcy = (int)((gy - c.domposmin[1]) / sc),
+            gcz = (int)((gz - c.domposmin[2]) / sc);
+  const float glx = (float)(gx - c.domposmin[0] - (double)gcx * sc);
+  const float gly = (float)(gy - c.domposmin[1] - (double)gcy * sc);
+  const float glz = (float)(gz - c.domposmin[2] - (double)gcz * sc);
+  const CellGrid g = gb_grid(gcx - (int)d.cellmin[0], gcy - (int)d.cellmin[1], gcz - (int)d.cellmin[2],
+                             c.cellmode_div, d);
+  const float scell = c.scell, ks2 = c.kernelsize2, h = c.kernelh;
+  float rhop1 = 0, grx = 0, gry = 0, grz = 0;
+  double A[4][4];
+  for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) A[i][j] = 0.0;
+  for (int z = g.zini; z < g.zfin; z++) {
+    for (int y = g.yini; y < g.yfin; y++) {
+      const unsigned rowbase = d.boxfluid + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+      const float by = gly + (float)(g.cy - y) * scell, bz = glz + (float)(g.cz - z) * scell;
+      for (int x = g.xini; x < g.xfin; x++) {
+        const unsigned box = rowbase + (unsigned)x;
+        const unsigned pini = a.begincell[box], pfin = a.begincell[box + 1];
+        const float bx = glx + (float)(g.cx - x) * scell;
+        for (unsigned p2 = pini; p2 < pfin; p2++) {
+          const float4 ps2 = a.pscell[p2];
+          const float drx = bx - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
+          const float rr2 = drx * drx + dry * dry + drz * drz;
+          if (rr2 <= ks2 && (a.code[p2] & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID) {
+            // Wendland WabFac (FunSphKernel.h:235-246)
+            const float rad = sqrtf(rr2);
+            const float qq = rad / h;
+            const float wqq1 = 1.f - 0.5f * qq;
+            const float wqq2 = wqq1 * wqq1;
+            const float fac = c.bwenh * wqq2 * wqq1;
+            const float wqq = qq + qq + 1.f;
+            const float wab = c.awen * wqq * wqq2 * wqq2;
+            const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
+            const float rhop2 = a.velrho[p2].w;
+            const float massp2 = c.massfluid;
+            const float volp2 = massp2 / rhop2;
+            rhop1 += massp2 * wab;
+            grx += massp2 * frx; gry += massp2 * fry; grz += massp2 * frz;
+            const float vwab = wab * volp2, vfrx = frx * volp2, vfry = fry * volp2, vfrz = frz * volp2;
+            A[0][0] += vwab; A[0][1] += drx * vwab; A[0][2] += dry * vwab; A[0][3] += drz * vwab;
+            A[1][0] += vfrx; A[1][1] += drx * vfrx; A[1][2] += dry * vfrx; A[1][3] += drz * vfrx;
+            A[2][0] += vfry; A[2][1] += drx * vfry; A[2][2] += dry * vfry; A[2][3] += drz * vfry;
+            A[3][0] += vfrz; A[3][1] += drx * vfrz; A[3][2] += dry * vfrz; A[3][3] += drz * vfrz;
+          }
+        }
+      }
+    }
+  }
+  // cofactors C[i][j]; inverse = C^T/det
+  double C[4][4];
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) {
+      double m[9];
+      int k = 0;
+      for (int r = 0; r < 4; r++) {
+        if (r == i) continue;
+        for (int s = 0; s < 4; s++) {
+          if (s == j) continue;
+          m[k++] = A[r][s];
+        }
+      }
+      const double md = gb_det3(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]);
+      C[i][j] = ((i + j) & 1) ? -md : md;
+    }
+  const double det = A[0][0] * C[0][0] + A[0][1] * C[0][1] + A[0][2] * C[0][2] + A[0][3] * C[0][3];
+  float rhofinal = FLT_MAX;
+  if (fabs(det) >= 1e-3f) {
+    const double b[4] = {rhop1, grx, gry, grz};
+    double xs[4];
+    for (int r = 0; r < 4; r++) xs[r] = (C[0][r] * b[0] + C[1][r] * b[1] + C[2][r] * b[2] + C[3][r] * b[3]) / det;
+    const float rhoghost = (float)xs[0];
+    const float ggx = -(float)xs[1], ggy = -(float)xs[2], ggz = -(float)xs[3];
+    rhofinal = rhoghost + ggx * (-bn.x) + ggy * (-bn.y) + ggz * (-bn.z);
+  } else if (A[0][0] > 0) {
+    rhofinal = (float)(rhop1 / A[0][0]);
+  }
+  rhofinal = (rhofinal != FLT_MAX) ? rhofinal : c.rhopzero;
+  float4 vr = a.velrho[p1];
+  vr.w = rhofinal;
+  a.velrho[p1] = vr;
+  float4 ps = a.pscell[p1];
+  ps.w = gb_press(rhofinal, c.rhopzero, c.cteb, c.gamma);
+  a.pscell[p1] = ps;
+}
+
+// Particle-interaction count (JDsPips::ComputeGpu / KerInteractionNg,
+// JDsPips.cpp:268, JDsPips_ker.cu:66): checked and real (r^2 <= (2h)^2,
+// r^2 >= ALMOSTZERO) pairs of bound rows (fluid neighbours) and of fluid rows
+// (fluid and bound neighbours).  out = {checked bound, real bound, checked fluid,
+// real fluid}.
+__global__ void k_pips(gbsph_consts c, DevArrays a) {
+  const DivState& d = *a.div;
+  const unsigned p1 = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long cnt[4] = {0, 0, 0, 0};
+  const bool bound = p1 < d.npbok;
+  const bool fluid = p1 >= d.npb && p1 < d.np;
+  if (bound || fluid) {
+    const float4 ps1 = a.pscell[p1];
+    const unsigned dcc = c.domcellcode, cel = a.dcell[p1];
+    const CellGrid g = gb_grid((int)gb_cx(dcc, cel) - (int)d.cellmin[0], (int)gb_cy(dcc, cel) - (int)d.cellmin[1],
+                               (int)gb_cz(dcc, cel) - (int)d.cellmin[2], c.cellmode_div, d);
+    for (int pass = 0; pass < (fluid ? 2 : 1); pass++) {
+      const unsigned cellinit = (pass == 0) ? d.boxfluid : 0u;
+      for (int z = g.zini; z < g.zfin; z++)
+        for (int y = g.yini; y < g.yfin; y++)
+          for (int x = g.xini; x < g.xfin; x++) {
+            const unsigned box = cellinit + (unsigned)x + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+            const unsigned pini = a.begincell[box], pfin = a.begincell[box + 1];
+            const float bx = ps1.x + (float)(g.cx - x) * c.scell;
+            const float by = ps1.y + (float)(g.cy - y) * c.scell;
+            const float bz = ps1.z + (float)(g.cz - z) * c.scell;
+            for (unsigned p2 = pini; p2 < pfin; p2++) {
+              const float4 ps2 = a.pscell[p2];
+              const float drx = bx - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
+              const float rr2 = drx * drx + dry * dry + drz * drz;
+              const int k = fluid ? 2 : 0;
+              cnt[k]++;
+              if (rr2 <= c.kernelsize2 && rr2 >= GB_ALMOSTZERO) cnt[k + 1]++;
+            }
+          }
+    }
+  }
+  for (int k = 0; k < 4; k++) {
+    unsigned long long v = cnt[k];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&a.pips[k], v);
+  }
+}
+
+template <int tvisco, int tdensity>
+void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s) {
+  k_forces_fluid<tvisco, tdensity><<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+}
+
+template <int tvisco>
+void launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s) {
+  switch (c.tdensity) {
+    case GBSPH_DDT_NONE: launch_fluid<tvisco, GBSPH_DDT_NONE>(c, a, cap, s); break;
+    case GBSPH_DDT_DDT: launch_fluid<tvisco, GBSPH_DDT_DDT>(c, a, cap, s); break;
+    case GBSPH_DDT_DDT2: launch_fluid<tvisco, GBSPH_DDT_DDT2>(c, a, cap, s); break;
+    default: launch_fluid<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, s); break;
+  }
+}
+
+}  // namespace
+
+namespace gbk {
+
+void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, cudaStream_t s,
+            unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin, cudaEvent_t ev_fluid_end) {
+  (void)bsize;
+  (void)variant;
+  cudaMemsetAsync(&a.st->acemax2, 0, 3 * sizeof(unsigned), s);
+  k_forces_bound<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+  if (ev_fluid_begin) cudaEventRecord(ev_fluid_begin, s);
+  switch (c.tvisco) {
+    case GBSPH_VISCO_ARTIFICIAL: launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, s); break;
+    case GBSPH_VISCO_LAMINAR: launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, s); break;
+    default: launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, s); break;
+  }
+  if (ev_fluid_end) cudaEventRecord(ev_fluid_end, s);
+  if (nlaunch) *nlaunch += 2;
+}
+
+void sps_tau(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch) {
+  k_sps_tau<<<gb_div_up(cap, 256), 256, 0, s>>>(c, a);
+  if (nlaunch) *nlaunch += 1;
+}
+
+void pips(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s) {
+  cudaMemsetAsync(a.pips, 0, 4 * sizeof(unsigned long long), s);
+  k_pips<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+}
+
+void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch) {
+  k_mdbc<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+  if (nlaunch) *nlaunch += 1;
+}
+
+}  // namespace gbk

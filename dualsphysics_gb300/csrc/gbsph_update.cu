@@ -1,0 +1,225 @@
+// gbsph_update.cu -- time integration, position update and adaptive dt.
+//
+// Symplectic predictor/corrector (JSphCpu.cpp:1687-2029; GPU twin
+// KerComputeStepSymplecticPre/Cor, JSphGpuSimple_ker.cu:265-516, plus
+// KerComputeStepPos2, JSphGpu_ker.cu:1523-1580), Verlet (JSphCpu.cpp:1523-1680),
+// UpdatePos with the out-of-domain / MovLimit / rho-out exclusions
+// (JSphCpu.cpp:1464-1516) and DtVariable (JSphCpu.cpp:2035-2078).
+//
+// The integrators evaluate their double-precision expressions with explicit
+// round-to-nearest intrinsics (no FMA contraction), so given the same ace/ar
+// they reproduce the reference CPU results bit for bit.  Each integrator is one
+// fused kernel: density, velocity, displacement, new position and new cell.
+#include <cuda_runtime.h>
+#include <float.h>
+
+#include "gbsph_common.cuh"
+
+namespace {
+
+constexpr int kUpdBlock = 256;
+
+__device__ __forceinline__ double dadd(double x, double y) { return __dadd_rn(x, y); }
+__device__ __forceinline__ double dmul(double x, double y) { return __dmul_rn(x, y); }
+
+// UpdatePos (JSphCpu.cpp:1464-1516) without periodic conditions.
+__device__ __forceinline__ void update_pos(const gbsph_consts& c, const DevArrays& a, unsigned p, double rx, double ry,
+                                           double rz, double movx, double movy, double movz, bool outrho) {
+  const bool outmov = (fabsf((float)movx) > c.movlimit || fabsf((float)movy) > c.movlimit ||
+                       fabsf((float)movz) > c.movlimit);
+  rx = dadd(rx, movx); ry = dadd(ry, movy); rz = dadd(rz, movz);
+  const double dx = __dsub_rn(rx, c.maprealposmin[0]);
+  const double dy = __dsub_rn(ry, c.maprealposmin[1]);
+  const double dz = __dsub_rn(rz, c.maprealposmin[2]);
+  const bool out = (dx != dx || dy != dy || dz != dz || dx < 0 || dy < 0 || dz < 0 || dx >= c.maprealsize[0] ||
+                    dy >= c.maprealsize[1] || dz >= c.maprealsize[2]);
+  a.px[p] = rx; a.py[p] = ry; a.pz[p] = rz;
+  if (outrho || outmov || out) {
+    const unsigned rcode = a.code[p];
+    const unsigned base = rcode & ~GB_CODE_MASKSPECIAL;
+    a.code[p] = (uint16_t)(base | (out ? GB_CODE_OUTPOS : (outrho ? GB_CODE_OUTRHO : GB_CODE_OUTMOV)));
+    a.dcell[p] = 0xffffffffu;
+  } else {
+    const double sc = (double)c.scell;
+    const unsigned cx = (unsigned)__ddiv_rn(dx, sc), cy = (unsigned)__ddiv_rn(dy, sc), cz = (unsigned)__ddiv_rn(dz, sc);
+    a.dcell[p] = gb_cell(c.domcellcode, cx, cy, cz);
+  }
+}
+
+__device__ __forceinline__ double read_dt(const double* dtp, double dth) { return dtp ? *dtp : dth; }
+
+// ComputeSymplecticPre: the current state becomes the PRE state (qx/velrhopre)
+// and the predicted state is written to the current arrays.
+__global__ void k_sym_pre(gbsph_consts c, DevArrays a, const double* dtp, double dth) {
+  const DivState& d = *a.div;
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.np) return;
+  const double dt05 = dmul(read_dt(dtp, dth), 0.5);
+  const double x = a.px[p], y = a.py[p], z = a.pz[p];
+  const float4 vp = a.velrho[p];
+  a.qx[p] = x; a.qy[p] = y; a.qz[p] = z;
+  a.velrhopre[p] = vp;
+  const float ar = a.acear[p].w;
+  if (p < d.npb) {
+    float w = (float)dadd((double)vp.w, dmul(dt05, (double)ar));
+    w = (w < c.rhopzero ? c.rhopzero : w);
+    a.velrho[p] = make_float4(vp.x, vp.y, vp.z, w);
+    return;
+  }
+  const float4 ace = a.acear[p];
+  const unsigned rcode = a.code[p];
+  const float rhonew = (float)dadd((double)vp.w, dmul(dt05, (double)ar));
+  const double dx = dmul((double)vp.x, dt05), dy = dmul((double)vp.y, dt05), dz = dmul((double)vp.z, dt05);
+  const bool outrho = (rhonew < c.rhopoutmin || rhonew > c.rhopoutmax);
+  const float vx = (float)dadd((double)vp.x, dmul(dadd((double)ace.x, (double)c.gravity[0]), dt05));
+  const float vy = (float)dadd((double)vp.y, dmul(dadd((double)ace.y, (double)c.gravity[1]), dt05));
+  const float vz = (float)dadd((double)vp.z, dmul(dadd((double)ace.z, (double)c.gravity[2]), dt05));
+  a.velrho[p] = make_float4(vx, vy, vz, rhonew);
+  unsigned code = rcode;
+  if (outrho && (rcode & GB_CODE_MASKSPECIAL) == GB_CODE_NORMAL) {
+    code = (rcode & ~GB_CODE_MASKSPECIAL) | GB_CODE_OUTRHO;
+    a.code[p] = (uint16_t)code;
+  }
+  if ((code & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID)
+    update_pos(c, a, p, x, y, z, dx, dy, dz, (code & GB_CODE_MASKSPECIAL) == GB_CODE_OUTRHO);
+}
+
+// ComputeSymplecticCorr: PRE state + forces of the predicted state.
+__global__ void k_sym_cor(gbsph_consts c, DevArrays a, const double* dtp, double dth) {
+  const DivState& d = *a.div;
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.np) return;
+  const double dt = read_dt(dtp, dth);
+  const double dt05 = dmul(dt, 0.5);
+  const float4 ace = a.acear[p];
+  const float4 vc = a.velrho[p];   // predicted
+  const float4 vp = a.velrhopre[p];
+  const double eps = dmul(-(double)ace.w / (double)vc.w, dt);
+  const float rhonew = (float)(dmul((double)vp.w, __dsub_rn(2., eps)) / dadd(2., eps));
+  if (p < d.npb) {
+    a.velrho[p] = make_float4(0.f, 0.f, 0.f, (rhonew < c.rhopzero ? c.rhopzero : rhonew));
+    return;
+  }
+  const unsigned rcode = a.code[p];
+  const float vx = (float)dadd((double)vp.x, dmul(dadd((double)ace.x, (double)c.gravity[0]), dt));
+  const float vy = (float)dadd((double)vp.y, dmul(dadd((double)ace.y, (double)c.gravity[1]), dt));
+  const float vz = (float)dadd((double)vp.z, dmul(dadd((double)ace.z, (double)c.gravity[2]), dt));
+  const double dx = dmul(dadd((double)vp.x, (double)vx), dt05);
+  const double dy = dmul(dadd((double)vp.y, (double)vy), dt05);
+  const double dz = dmul(dadd((double)vp.z, (double)vz), dt05);
+  const bool outrho = (rhonew < c.rhopoutmin || rhonew > c.rhopoutmax);
+  unsigned code = rcode;
+  if (outrho && (rcode & GB_CODE_MASKSPECIAL) == GB_CODE_NORMAL) {
+    code = (rcode & ~GB_CODE_MASKSPECIAL) | GB_CODE_OUTRHO;
+    a.code[p] = (uint16_t)code;
+  }
+  a.velrho[p] = make_float4(vx, vy, vz, rhonew);
+  if ((code & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID)
+    update_pos(c, a, p, a.qx[p], a.qy[p], a.qz[p], dx, dy, dz, (code & GB_CODE_MASKSPECIAL) == GB_CODE_OUTRHO);
+  else {
+    a.px[p] = a.qx[p]; a.py[p] = a.qy[p]; a.pz[p] = a.qz[p];
+  }
+}
+
+// ComputeVerlet (JSphCpu.cpp:1523-1680): velrhopre holds VelrhoM1.  The new
+// state is written to velrho and the old velrho moves to velrhopre.
+__global__ void k_verlet(gbsph_consts c, DevArrays a, const double* dtp, double dth, int euler) {
+  const DivState& d = *a.div;
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.np) return;
+  const double dt = read_dt(dtp, dth);
+  const double dt2 = euler ? dt : dadd(dt, dt);
+  const float4 v1 = a.velrho[p];
+  const float4 vm1 = a.velrhopre[p];
+  const float4 v2 = euler ? v1 : vm1;
+  const float ar = a.acear[p].w;
+  const float rhonew = (float)dadd((double)v2.w, dmul(dt2, (double)ar));
+  a.velrhopre[p] = v1;
+  if (p < d.npb) {
+    a.velrho[p] = make_float4(0.f, 0.f, 0.f, (rhonew < c.rhopzero ? c.rhopzero : rhonew));
+    return;
+  }
+  const double dt205 = dmul(dmul(0.5, dt), dt);
+  const float4 ace = a.acear[p];
+  const double ax = dadd((double)ace.x, (double)c.gravity[0]);
+  const double ay = dadd((double)ace.y, (double)c.gravity[1]);
+  const double az = dadd((double)ace.z, (double)c.gravity[2]);
+  const double dx = dadd(dmul((double)v1.x, dt), dmul(ax, dt205));
+  const double dy = dadd(dmul((double)v1.y, dt), dmul(ay, dt205));
+  const double dz = dadd(dmul((double)v1.z, dt), dmul(az, dt205));
+  const bool outrho = (rhonew < c.rhopoutmin || rhonew > c.rhopoutmax);
+  const float nvx = (float)dadd((double)v2.x, dmul(ax, dt2));
+  const float nvy = (float)dadd((double)v2.y, dmul(ay, dt2));
+  const float nvz = (float)dadd((double)v2.z, dmul(az, dt2));
+  a.velrho[p] = make_float4(nvx, nvy, nvz, rhonew);
+  update_pos(c, a, p, a.px[p], a.py[p], a.pz[p], dx, dy, dz, outrho);
+}
+
+// DtVariable (JSphCpu.cpp:2035-2078): which = 0 predictor (dt_p), 1 corrector
+// (dt_c), 2 Verlet (dt_var).
+__global__ void k_dtvar(gbsph_consts c, StepState* st, int which) {
+  const float acemax2 = __uint_as_float(st->acemax2);
+  const double acemax = sqrt((double)acemax2);
+  const float velmax = sqrtf(__uint_as_float(st->velmax2));
+  const float viscdt = __uint_as_float(st->viscdt);
+  const double h = (double)c.kernelh;
+  const double dt1 = (acemax ? sqrt(h / acemax) : DBL_MAX);
+  const double vm = (double)velmax * 10.;
+  const double dt2 = h / ((c.cs0 > vm ? c.cs0 : vm) + h * (double)viscdt);
+  double dt = c.cflnumber * (dt1 < dt2 ? dt1 : dt2);
+  if (isnan(dt) || isinf(dt)) {
+    st->error |= GB_ERR_NANDT;
+    dt = c.dtmin;
+  }
+  if (dt < c.dtmin) dt = c.dtmin;
+  st->dt_var = dt;
+  if (which == 0) st->dt_p = dt;
+  else if (which == 1) st->dt_c = dt;
+}
+
+// End of a step: TimeStep+=dt, SymplecticDtPre=min(dt_p,dt_c) (JSphCpuSingle.cpp:930-935, 1184-1190).
+__global__ void k_step_end(StepState* st, int symplectic) {
+  if (symplectic) {
+    st->dt_last = st->dtpre;
+    st->time += st->dtpre;
+    st->dtpre = (st->dt_p < st->dt_c ? st->dt_p : st->dt_c);
+  } else {
+    st->dt_last = st->dt_var;
+    st->time += st->dt_var;
+  }
+  st->nstep++;
+}
+
+}  // namespace
+
+namespace gbk {
+
+void symplectic_pre(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, cudaStream_t s,
+                    unsigned long long* nlaunch) {
+  k_sym_pre<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, 0.0);
+  if (nlaunch) *nlaunch += 1;
+}
+
+void symplectic_cor(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, cudaStream_t s,
+                    unsigned long long* nlaunch) {
+  k_sym_cor<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, 0.0);
+  if (nlaunch) *nlaunch += 1;
+}
+
+void dtvariable(const gbsph_consts& c, const DevArrays& a, int which, cudaStream_t s, unsigned long long* nlaunch) {
+  k_dtvar<<<1, 1, 0, s>>>(c, a.st, which);
+  if (nlaunch) *nlaunch += 1;
+}
+
+void step_end(const DevArrays& a, int symplectic, cudaStream_t s, unsigned long long* nlaunch) {
+  k_step_end<<<1, 1, 0, s>>>(a.st, symplectic);
+  if (nlaunch) *nlaunch += 1;
+}
+
+void verlet_step(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, int euler, cudaStream_t s,
+                 unsigned long long* nlaunch) {
+  k_verlet<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, 0.0, euler);
+  if (nlaunch) *nlaunch += 1;
+}
+
+}  // namespace gbk

@@ -1,0 +1,197 @@
+/*
+ * gbsph.h -- C ABI of the GB300-native WCSPH step (libgbsph.so).
+ *
+ * Drop-in boundary for DualSPHysics' per-step GPU hot path.  Each entry point
+ * names the reference interface it replaces (paths relative to the DualSPHysics
+ * source tree src/source/).  All functions return a status code (GBSPH_OK=0 or
+ * a negative GBSPH_E* value) and never throw across the ABI; the message of the
+ * last failure of a context is returned by gbsph_last_error().
+ *
+ * Threading: one context per host thread; every context owns one CUDA stream.
+ * Calls enqueue work on that stream and return without synchronising, except
+ * gbsph_download*, gbsph_get_*, gbsph_sync and gbsph_step_dt (they read results
+ * back).  Host pointers passed in are only used for the duration of the call.
+ * All device memory of a context is allocated by gbsph_create/gbsph_upload;
+ * nothing is allocated by the step functions.
+ */
+#ifndef GBSPH_H
+#define GBSPH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (JException/Run_Exceptioon equivalents, JSphGpu.cpp:84-126) */
+#define GBSPH_OK 0
+#define GBSPH_EINVAL -1      /* invalid argument or configuration                         */
+#define GBSPH_ECUDA -2       /* CUDA runtime error                                        */
+#define GBSPH_ENAN_DT -3     /* computed dt is NaN or infinite (JSphGpu.cpp:1122-1131)    */
+#define GBSPH_EBOUND_OUT -4  /* a boundary particle left the domain (JSph.cpp:2837)       */
+#define GBSPH_ECAPACITY -5   /* particles or cells beyond the allocated capacity          */
+#define GBSPH_ENOMEM -6      /* device allocation failed                                  */
+#define GBSPH_ESTATE -7      /* call out of order (e.g. step before upload)               */
+
+/* options (XML <parameters> keys of the reference, JSph.cpp:663-857) */
+#define GBSPH_STEP_VERLET 1
+#define GBSPH_STEP_SYMPLECTIC 2
+#define GBSPH_VISCO_ARTIFICIAL 1
+#define GBSPH_VISCO_LAMINARSPS 2
+#define GBSPH_VISCO_LAMINAR 3
+#define GBSPH_DDT_NONE 0
+#define GBSPH_DDT_DDT 1
+#define GBSPH_DDT_DDT2 2
+#define GBSPH_DDT_DDT2FULL 3
+#define GBSPH_BC_DBC 1
+#define GBSPH_BC_MDBC 2
+
+/* interaction step (TpInterStep, DualSphDef.h) */
+#define GBSPH_INTERSTEP_VERLET 1
+#define GBSPH_INTERSTEP_SYMPREDICTOR 2
+#define GBSPH_INTERSTEP_SYMCORRECTOR 3
+
+/* Raw case parameters as carried by the run XML (case.execution.constants and
+ * .parameters) plus the resolved real map limits.  Replaces the inputs of
+ * JSph::LoadConfigCtes/LoadConfigParameters (JSph.cpp:642-857). */
+typedef struct {
+  int tstep, tvisco, tdensity, tboundary, verletsteps, dtallparticles, simulate2d, cellmode_div;
+  double dp, h, b, rhop0, gamma, massbound, massfluid, cflnumber;
+  double gravity[3];
+  float visco, viscoboundfactor, ddtvalue, coefdtmin, rhopoutmin, rhopoutmax;
+  double dtini, dtmin;
+  double maprealposmin[3], maprealposmax[3];
+} gbsph_params;
+
+/* Derived constants of a case: the members of JSph / StCteSph the hot path
+ * uses (JSph.h:178-365, DualSphDef.h:503-530), same types as the reference. */
+typedef struct {
+  int tstep, tvisco, tdensity, tboundary, verletsteps, dtallparticles, simulate2d, cellmode_div;
+  float kernelh, kernelsize, kernelsize2, cteb, gamma, rhopzero, massfluid, massbound;
+  float eta2, ddtkh, ddtgz, visco, viscoboundfactor, awen, bwenh, spssmag, spsblin;
+  float scell, movlimit, rhopoutmin, rhopoutmax, gravity[3];
+  double dp, cs0, cflnumber, dtmin, dtini;
+  double mapposmin[3], maprealposmin[3], maprealsize[3];
+  double domposmin[3], domrealposmin[3], domrealposmax[3];
+  unsigned mapcells[3], domcells[3], domcellcode;
+} gbsph_consts;
+
+/* Cell-division summary (JCellDivGpuSingle members, JCellDivGpu.h). */
+typedef struct {
+  unsigned np, npb, npbok, nout_total;
+  unsigned cellmin[3], ncells[3], nct, nctt;
+  unsigned dividefull, npfout, npbout;
+} gbsph_divinfo;
+
+/* Maxima of the last interaction pass (AceMax, VelMax, ViscDtMax of JSph). */
+typedef struct {
+  double acemax;
+  float velmax, viscdtmax;
+} gbsph_maxes;
+
+typedef struct gbsph_ctx gbsph_ctx;
+
+/* Derives the constants: JSph::ConfigConstants1/2 (JSph.cpp:1481-1546),
+ * ConfigCellDivision (:1877-1895) and SelecDomain(0,Map_Cells) (:1901-1944). */
+int gbsph_config(const gbsph_params* prm, gbsph_consts* out);
+
+/* Creates a context on CUDA device `device` sized for `capacity` particles.
+ * Replaces JSphGpuSingle::LoadConfig/ConfigDomain memory setup
+ * (JSphGpuSingle.cpp:151-240, JSphGpu.cpp:692-757). */
+int gbsph_create(const gbsph_consts* c, unsigned capacity, int device, gbsph_ctx** out);
+void gbsph_destroy(gbsph_ctx* ctx);
+const char* gbsph_last_error(const gbsph_ctx* ctx);
+
+/* Uploads the initial particle state (ordered as in the case file: boundary
+ * first) and performs the first cell division, as JSphGpuSingle::ConfigDomain
+ * does (ParticlesDataUp + LoadDcellParticles + RunCellDivide,
+ * JSphGpuSingle.cpp:151-240).  pos: 3 doubles per particle; velrho: 4 floats;
+ * boundnor: 3 floats per boundary particle (NULL without mDBC), doubled here as
+ * JSph::ConfigBoundNormals does (JSph.cpp:1411-1418). */
+int gbsph_upload(gbsph_ctx* ctx, unsigned np, unsigned npb, const double* pos, const float* velrho,
+                 const unsigned* idp, const uint16_t* code, const float* boundnor);
+
+/* Neighbour-list build: JSphGpuSingle::RunCellDivide (JSphGpuSingle.cpp:372-480)
+ * = cudiv::PreSort/Sort/CalcBeginEndCell (JCellDivGpu_ker.cu:120-570,
+ * JCellDivGpuSingle_ker.cu:41-165) + SortDataParticles + UpdatePosCell. */
+int gbsph_divide(gbsph_ctx* ctx);
+
+/* mDBC ghost-node correction, SlipMode=vel0:
+ * cusph::Interaction_MdbcCorrection (JSphGpu_mdbc_iker.cu:194). Runs only for
+ * mDBC cases, and only in the predictor (JSphGpuSingle.cpp:686-700). */
+int gbsph_mdbc(gbsph_ctx* ctx, int interstep);
+
+/* PreInteraction_Forces + Interaction_Forces: cusph::Interaction_Forces
+ * (JSphGpu_ker.h:293, JSphGpu_ker.cu:1169) with the fused max reductions of
+ * JSphGpu::PreInteraction_Forces/ComputeAceMax (JSphGpu.cpp:846-900,
+ * JSphGpuSingle.cpp:719-729).  `maxes` may be NULL (no read-back). */
+int gbsph_forces(gbsph_ctx* ctx, int interstep, gbsph_maxes* maxes);
+
+/* JSphGpu::DtVariable (JSphGpu.cpp:1103-1150). Computes dt on the device from
+ * the maxima of the last gbsph_forces call; reads it back into *dt if dt!=NULL. */
+int gbsph_dtvariable(gbsph_ctx* ctx, int final, double* dt);
+
+/* Integrators: JSphGpu::ComputeSymplecticPre/Corr (JSphGpu.cpp:996/1054,
+ * cusphs::ComputeStepSymplecticPre/Cor JSphGpuSimple_ker.cu:358/518,
+ * cusph::ComputeStepPos2 JSphGpu_ker.cu:1553) and JSphGpu::ComputeVerlet. */
+int gbsph_symplectic_pre(gbsph_ctx* ctx, double dt);
+int gbsph_symplectic_cor(gbsph_ctx* ctx, double dt);
+int gbsph_verlet(gbsph_ctx* ctx, double dt);
+
+/* One whole step: JSphGpuSingle::ComputeStep (ComputeStep_Sym/_Ver,
+ * JSphGpuSingle.cpp:785-826) followed by RunCellDivide, as one iteration of
+ * the Run loop (JSphGpuSingle.cpp:998-1005).  dt stays on the device; nothing
+ * is read back. */
+int gbsph_step(gbsph_ctx* ctx);
+/* Runs `nsteps` steps; use_graph=1 captures one step into a CUDA graph once and
+ * replays it nsteps times, use_graph=2 replays a graph holding all nsteps steps
+ * (see gbsph_graph_prepare); no host round trips inside the loop. */
+int gbsph_run(gbsph_ctx* ctx, unsigned nsteps, int use_graph);
+/* Captures `nsteps` Symplectic steps into one CUDA graph (replayed by
+ * gbsph_run(ctx, nsteps, 2)); capture records work without running it. */
+int gbsph_graph_prepare(gbsph_ctx* ctx, unsigned nsteps);
+/* Reads back the dt used by the last step and the next SymplecticDtPre. */
+int gbsph_step_dt(gbsph_ctx* ctx, double* dt_last, double* dt_next, double* time);
+
+/* Read-back (JSphGpu::ParticlesDataDown, JSphGpu.cpp:630).  Any pointer may be
+ * NULL.  Arrays hold the current np particles in the current (cell) order. */
+int gbsph_download(gbsph_ctx* ctx, double* pos, float* velrho, unsigned* idp, uint16_t* code, unsigned* dcell);
+int gbsph_get_forces(gbsph_ctx* ctx, float* ace, float* ar);
+int gbsph_get_divinfo(gbsph_ctx* ctx, gbsph_divinfo* info, unsigned* begincell, unsigned begincell_cap,
+                      unsigned* sortpart, unsigned* cellpart);
+int gbsph_get_maxes(gbsph_ctx* ctx, gbsph_maxes* maxes);
+int gbsph_sync(gbsph_ctx* ctx);
+
+/* Device-pointer variant of gbsph_upload for callers whose particle state is
+ * already in device memory (same layout as gbsph_upload's host arrays). */
+int gbsph_upload_device(gbsph_ctx* ctx, unsigned np, unsigned npb, const double* d_pos, const float* d_velrho,
+                        const unsigned* d_idp, const uint16_t* d_code, const float* d_boundnor);
+
+/* Profiling (JDsTimersGpu counterpart, JDsTimersGpu.h:29-71): with
+ * max_launches>0, the next max_launches fluid Interaction_Forces launches are
+ * bracketed by CUDA events on the context stream; gbsph_profile_read returns
+ * their durations in ms and resets the counter.  0 disables profiling. */
+int gbsph_profile(gbsph_ctx* ctx, unsigned max_launches);
+int gbsph_profile_read(gbsph_ctx* ctx, float* ms, unsigned cap, unsigned* n);
+/* Caller timing on the context stream: records event `slot` (0..15); elapsed
+ * time in ms between two recorded slots (waits for the second). */
+int gbsph_mark(gbsph_ctx* ctx, unsigned slot);
+int gbsph_elapsed(gbsph_ctx* ctx, unsigned a, unsigned b, float* ms);
+
+/* Particle-interaction count of the current state with the reference's PIPS
+ * definition (JDsPips.cpp:187-260): out4 = {checked bound-row pairs, real
+ * bound-row pairs, checked fluid-row pairs, real fluid-row pairs}. */
+int gbsph_pips(gbsph_ctx* ctx, unsigned long long* out4);
+
+/* Kernel-launch counter of the context (launches issued since creation). */
+unsigned long long gbsph_launch_count(const gbsph_ctx* ctx);
+/* CUDA stream of the context (as void*), for callers that order their own work. */
+void* gbsph_stream(gbsph_ctx* ctx);
+/* Sets block sizes / tile options of the hot kernels (autotuner hook):
+ * key 0 = forces block size, 1 = forces variant. */
+int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

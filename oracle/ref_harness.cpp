@@ -1,0 +1,222 @@
+//==============================================================================
+// ref_harness.cpp -- step-level harness around the REFERENCE CPU solver
+// (test infrastructure: it generates the golden fixtures that pin the oracle).
+//
+// Built by oracle/Makefile.ref against the reference's own objects, compiled
+// out of tree from the reference source.  It subclasses JSphCpuSingle (all its
+// arrays and step methods are protected: JSphCpu.h:122-460,
+// JSphCpuSingle.h:37-107), loads a case exactly as JSphCpuSingle::Run does
+// (JSphCpuSingle.cpp:1144-1175), then runs the step piece by piece
+// (ComputeStep_Sym, JSphCpuSingle.cpp:897-936) and dumps the solver arrays as
+// raw little-endian files plus a key=value text file per stage.
+//
+//   ref_harness <casedir> <casename> <outdir> <nsteps_after_first> <threads>
+//==============================================================================
+#include "JSphCpuSingle.h"
+#include "JSphCfgRun.h"
+#include "JAppInfo.h"
+#include "JLog2.h"
+#include "JCellDivCpuSingle.h"
+#include "JException.h"
+#include "Functions.h"
+#include <cstdio>
+#include <fstream>
+#include <string>
+#include <vector>
+
+JAppInfo AppInfo("DualSPHysics5","v5.4.355","08-04-2025");
+
+namespace {
+
+void WriteRaw(const std::string& file,const void* p,size_t bytes){
+  FILE* f=fopen(file.c_str(),"wb");
+  if(!f){ fprintf(stderr,"cannot write %s\n",file.c_str()); exit(2); }
+  if(bytes)fwrite(p,1,bytes,f);
+  fclose(f);
+}
+
+}
+
+class OracleCpu : public JSphCpuSingle{
+ public:
+  std::string Out;
+  std::vector<double> DtList;
+
+  void Prepare(const std::string& appname,const JSphCfgRun* cfg,JLog2* log){
+    // Same sequence as JSphCpuSingle::Run up to the main loop (JSphCpuSingle.cpp:1144-1175).
+    AppName=appname; Log=log; CfgRun=cfg;
+    Arrays_Cpu=new JArraysCpu(Log);
+    Timersc->Config(cfg->SvTimers);
+    LoadConfig(cfg);
+    LoadCaseParticles();
+    VisuConfig();
+    ConfigDomain();
+    ConfigRunMode();
+    InitRunCpu();
+    FreePartsInit();
+    UpdateMaxValues();
+    Part++;
+    InterStep=INTERSTEP_SymPredictor;
+  }
+
+  void Meta(const std::string& tag,const std::string& extra=""){
+    std::ofstream f((Out+"/"+tag+"_meta.txt").c_str());
+    const StDivDataCpu dv=CellDivSingle->GetCellDivData();
+    f.precision(17);
+    f<<"np="<<Np<<"\nnpb="<<Npb<<"\nnpbok="<<NpbOk<<"\n";
+    f<<"ncx="<<dv.nc.x<<"\nncy="<<dv.nc.y<<"\nncz="<<dv.nc.z<<"\nnsheet="<<dv.nc.w<<"\n";
+    f<<"cellmin="<<dv.cellzero.x<<","<<dv.cellzero.y<<","<<dv.cellzero.z<<"\n";
+    f<<"cellfluid="<<dv.cellfluid<<"\n";
+    f<<"domcellcode="<<DomCellCode<<"\n";
+    f<<"scell="<<Scell<<"\nkernelh="<<KernelH<<"\nkernelsize="<<KernelSize<<"\nkernelsize2="<<KernelSize2<<"\n";
+    f<<"cs0="<<Cs0<<"\neta2="<<Eta2<<"\nddtkh="<<DDTkh<<"\nddtgz="<<DDTgz<<"\n";
+    f<<"awen="<<KWend.awen<<"\nbwenh="<<KWend.bwenh<<"\n";
+    f<<"cteb="<<CteB<<"\ngamma="<<Gamma<<"\nrhopzero="<<RhopZero<<"\nmassfluid="<<MassFluid<<"\nmassbound="<<MassBound<<"\n";
+    f<<"dtini="<<DtIni<<"\ndtmin="<<DtMin<<"\ncflnumber="<<CFLnumber<<"\nmovlimit="<<MovLimit<<"\n";
+    f<<"maprealposmin="<<MapRealPosMin.x<<","<<MapRealPosMin.y<<","<<MapRealPosMin.z<<"\n";
+    f<<"maprealposmax="<<MapRealPosMax.x<<","<<MapRealPosMax.y<<","<<MapRealPosMax.z<<"\n";
+    f<<"domposmin="<<DomPosMin.x<<","<<DomPosMin.y<<","<<DomPosMin.z<<"\n";
+    f<<"mapcells="<<Map_Cells.x<<","<<Map_Cells.y<<","<<Map_Cells.z<<"\n";
+    f<<"symplecticdtpre="<<SymplecticDtPre<<"\n";
+    f<<"acemax="<<AceMax<<"\nvelmax="<<VelMax<<"\nviscdtmax="<<ViscDtMax<<"\n";
+    f<<"timestep="<<TimeStep<<"\nnstep="<<Nstep<<"\n";
+    f<<extra;
+  }
+
+  void DumpState(const std::string& tag){
+    const std::string b=Out+"/"+tag+"_";
+    WriteRaw(b+"idp.bin",Idp_c->cptr(),sizeof(unsigned)*Np);
+    WriteRaw(b+"code.bin",Code_c->cptr(),sizeof(typecode)*Np);
+    WriteRaw(b+"dcell.bin",Dcell_c->cptr(),sizeof(unsigned)*Np);
+    WriteRaw(b+"pos.bin",Pos_c->cptr(),sizeof(tdouble3)*Np);
+    WriteRaw(b+"velrho.bin",Velrho_c->cptr(),sizeof(tfloat4)*Np);
+  }
+
+  void DumpDivide(const std::string& tag){
+    const StDivDataCpu dv=CellDivSingle->GetCellDivData();
+    const unsigned nct=unsigned(dv.nc.w)*unsigned(dv.nc.z);
+    const unsigned nctt=nct*2+6;
+    WriteRaw(Out+"/"+tag+"_begincell.bin",dv.begincell,sizeof(unsigned)*nctt);
+  }
+
+  void DumpForces(const std::string& tag){
+    const std::string b=Out+"/"+tag+"_";
+    WriteRaw(b+"ace.bin",Ace_c->cptr(),sizeof(tfloat3)*Np);
+    WriteRaw(b+"ar.bin",Ar_c->cptr(),sizeof(float)*Np);
+    WriteRaw(b+"velrho.bin",Velrho_c->cptr(),sizeof(tfloat4)*Np);
+  }
+
+  // First step piece by piece (ComputeStep_Sym, JSphCpuSingle.cpp:897-936).
+  void FirstStepDetailed(){
+    Meta("s0");
+    DumpState("s0"); DumpDivide("s0");
+    const double dt=SymplecticDtPre;
+    InterStep=INTERSTEP_SymPredictor;
+    DemDtForce=dt*0.5f;
+    MdbcBoundCorrection(InterStep);
+    DumpState("s0mdbc");
+    PreInteraction_Forces(InterStep);
+    Interaction_Forces(InterStep);
+    DumpForces("s0pred");
+    const double dt_p=DtVariable(false);
+    char tx[256]; sprintf(tx,"dt=%.17g\ndt_p=%.17g\n",dt,dt_p);
+    Meta("s0pred",tx);
+    ComputeSymplecticPre(dt);
+    PosInteraction_Forces();
+    DumpState("s0pre");
+    InterStep=INTERSTEP_SymCorrector;
+    DemDtForce=dt;
+    RunCellDivide(true);
+    Meta("s0div");
+    DumpState("s0div"); DumpDivide("s0div");
+    MdbcBoundCorrection(InterStep);
+    PreInteraction_Forces(InterStep);
+    Interaction_Forces(InterStep);
+    DumpForces("s0cor");
+    const double dt_c=DtVariable(true);
+    sprintf(tx,"dt=%.17g\ndt_c=%.17g\n",dt,dt_c);
+    Meta("s0cor",tx);
+    ComputeSymplecticCorr(dt);
+    PosInteraction_Forces();
+    DumpState("s0corr");
+    SymplecticDtPre=std::min(dt_p,dt_c);
+    TimeStep+=dt; Nstep++;
+    RunCellDivide(true);
+    DtList.push_back(dt);
+    Meta("s1");
+    DumpState("s1"); DumpDivide("s1");
+  }
+
+  // First Verlet step piece by piece (ComputeStep_Ver, JSphCpuSingle.cpp:873-892).
+  void FirstStepVerlet(){
+    Meta("s0");
+    DumpState("s0"); DumpDivide("s0");
+    InterStep=INTERSTEP_Verlet;
+    MdbcBoundCorrection(InterStep);
+    DumpState("s0mdbc");
+    PreInteraction_Forces(InterStep);
+    Interaction_Forces(InterStep);
+    DumpForces("s0pred");
+    const double dt=DtVariable(true);
+    char tx[256]; sprintf(tx,"dt=%.17g\ndt_p=%.17g\n",dt,dt);
+    Meta("s0pred",tx);
+    ComputeVerlet(dt);
+    PosInteraction_Forces();
+    DumpState("s0pre");
+    TimeStep+=dt; Nstep++;
+    RunCellDivide(true);
+    DtList.push_back(dt);
+    Meta("s1");
+    DumpState("s1"); DumpDivide("s1");
+  }
+
+  bool IsSymplectic()const{ return(TStep==STEP_Symplectic); }
+
+  void RunSteps(unsigned n){
+    for(unsigned c=0;c<n;c++){
+      const double stepdt=ComputeStep();
+      RunCellDivide(true);
+      TimeStep+=stepdt; Nstep++;
+      DtList.push_back(stepdt);
+    }
+    Meta("end");
+    DumpState("end"); DumpDivide("end");
+    WriteRaw(Out+"/end_dtlist.bin",DtList.data(),sizeof(double)*DtList.size());
+  }
+};
+
+int main(int argc,char** argv){
+  if(argc<6){
+    fprintf(stderr,"usage: %s <casedir> <casename> <outdir> <nsteps> <threads>\n",argv[0]);
+    return 1;
+  }
+  const std::string casedir=argv[1],casename=argv[2],outdir=argv[3];
+  const unsigned nsteps=unsigned(atoi(argv[4]));
+  const std::string thr=std::string("-ompthreads:")+argv[5];
+  AppInfo.ConfigRunPaths(argv[0]);
+  JSphCfgRun cfg;
+  cfg.SetFeatureList(JSph::GetFeatureList());
+  std::string casepath=casedir+"/"+casename;
+  std::vector<std::string> args={"ref_harness","-cpu",thr,"-sv:none","-svres:0",casepath,outdir};
+  std::vector<char*> av;
+  for(auto& s:args)av.push_back(const_cast<char*>(s.c_str()));
+  int rc=1;
+  try{
+    cfg.LoadArgv(int(av.size()),av.data());
+    AppInfo.ConfigOutput(cfg.CreateDirs,cfg.CsvSepComa,cfg.DirOut,cfg.DirDataOut);
+    AppInfo.LogInit(AppInfo.GetDirOut()+"/Run.out");
+    JLog2* log=AppInfo.LogPtr();
+    OracleCpu sph;
+    sph.Out=outdir;
+    sph.Prepare(AppInfo.GetFullName(),&cfg,log);
+    if(sph.IsSymplectic())sph.FirstStepDetailed();
+    else sph.FirstStepVerlet();
+    sph.RunSteps(nsteps);
+    rc=0;
+  }
+  catch(const JException& e){ fprintf(stderr,"JException: %s\n",e.what()); }
+  catch(const std::exception& e){ fprintf(stderr,"exception: %s\n",e.what()); }
+  catch(const std::string& e){ fprintf(stderr,"exception: %s\n",e.c_str()); }
+  catch(const char* e){ fprintf(stderr,"exception: %s\n",e); }
+  return rc;
+}

@@ -1,0 +1,97 @@
+"""Generates the golden fixtures in tests/golden/ from the REFERENCE solver.
+
+Each case is generated with dualsphysics_gb300.casegen (deterministic, seeded),
+run through oracle/_ref/ref_harness -- a step-level harness linked against the
+reference DualSPHysics CPU solver compiled from its own sources (see
+oracle/Makefile.ref) -- and the arrays it dumps are packed into <case>.npz.
+
+Run from the repository root, with the reference source tree available:
+    make -f oracle/Makefile.ref -j8 REFSRC=<reference>/src/source
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from dualsphysics_gb300 import casegen as cg  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+# name -> (spec factory, steps after the detailed first step)
+CASES = {
+    "dbc_d04": (lambda: cg.spec_c1(dp=0.04, name="dbc_d04"), 20),
+    "mdbc_d04": (lambda: cg.spec_c2(dp=0.04, name="mdbc_d04"), 20),
+    "jit_d04": (lambda: cg.spec_c1(dp=0.04, name="jit_d04", jitter=0.01, seed=7), 20),
+    "vel_d04": (lambda: cg.spec_c1(dp=0.04, name="vel_d04", init_vel=0.05, seed=11), 10),
+    "verlet_d04": (lambda: cg.spec_c1(dp=0.04, name="verlet_d04", step_algorithm=1, verlet_steps=5,
+                                      init_vel=0.05, seed=3), 12),
+    "sps_d04": (lambda: cg.spec_c1(dp=0.04, name="sps_d04", visco_treatment=2, visco=1e-6, density_dt=1,
+                                   init_vel=0.05, seed=5), 10),
+}
+
+STATE = (("idp", np.uint32, 1), ("code", np.uint16, 1), ("dcell", np.uint32, 1), ("pos", np.float64, 3),
+         ("velrho", np.float32, 4))
+
+
+def _raw(d, tag, nm, dt, w=1):
+    a = np.fromfile(os.path.join(d, f"{tag}_{nm}.bin"), dtype=dt)
+    return a.reshape(-1, w) if w > 1 else a
+
+
+def _meta(d, tag):
+    out = {}
+    with open(os.path.join(d, f"{tag}_meta.txt")) as f:
+        for line in f:
+            k, v = line.strip().split("=", 1)
+            out[k] = v
+    return out
+
+
+def make(name: str, threads: int = 8) -> str:
+    spec_fn, nsteps = CASES[name]
+    with tempfile.TemporaryDirectory() as tmp:
+        casedir = os.path.join(tmp, "case")
+        outdir = os.path.join(tmp, "out")
+        os.makedirs(outdir)
+        cg.write_case(cg.make_dam_break(spec_fn()), casedir)
+        subprocess.run([HARNESS, casedir, name, outdir, str(nsteps), str(threads)], check=True,
+                       stdout=subprocess.DEVNULL)
+        arr = {}
+        for tag in ("s0", "s0pre", "s1", "end") + (("s0div", "s0corr") if os.path.exists(
+                os.path.join(outdir, "s0div_meta.txt")) else ()):
+            for nm, dt, w in STATE:
+                if tag in ("s0div", "s1") and nm in ("pos", "velrho"):
+                    continue
+                arr[f"{tag}_{nm}"] = _raw(outdir, tag, nm, dt, w)
+        for tag in ("s0", "s0div", "s1", "end"):
+            if os.path.exists(os.path.join(outdir, f"{tag}_begincell.bin")):
+                arr[f"{tag}_begincell"] = _raw(outdir, tag, "begincell", np.uint32)
+        for tag in ("s0pred", "s0cor"):
+            if os.path.exists(os.path.join(outdir, f"{tag}_ace.bin")):
+                arr[f"{tag}_ace"] = _raw(outdir, tag, "ace", np.float32, 3)
+                arr[f"{tag}_ar"] = _raw(outdir, tag, "ar", np.float32)
+        arr["s0mdbc_rho"] = _raw(outdir, "s0mdbc", "velrho", np.float32, 4)[:, 3].copy()
+        arr["dtlist"] = np.fromfile(os.path.join(outdir, "end_dtlist.bin"), dtype=np.float64)
+        meta = {tag: _meta(outdir, tag) for tag in ("s0", "s0pred", "s0cor", "s0div", "s1", "end")
+                if os.path.exists(os.path.join(outdir, f"{tag}_meta.txt"))}
+        arr["meta_json"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        path = os.path.join(OUT, f"{name}.npz")
+        np.savez_compressed(path, **arr)
+        return path
+
+
+if __name__ == "__main__":
+    if not os.path.exists(HARNESS):
+        sys.exit(f"reference harness not built: {HARNESS} (make -f oracle/Makefile.ref)")
+    for nm in (sys.argv[1:] or list(CASES)):
+        p = make(nm)
+        print(nm, os.path.getsize(p), "bytes")

@@ -1,0 +1,63 @@
+"""Helpers shared by the tests: golden fixtures, case regeneration, tolerances."""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+for p in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests", "golden")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+from dualsphysics_gb300 import casegen as cg  # noqa: E402
+from dualsphysics_gb300.case import load_case  # noqa: E402
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+CASE_NAMES = ["dbc_d04", "mdbc_d04", "jit_d04", "vel_d04", "verlet_d04", "sps_d04"]
+
+# Tolerance of FP32 pair sums, stated per particle against the conditioning
+# scale S_i = sum_j |pair term_ij| computed by the FP64 oracle:
+#   |x - x_f64| <= RTOL_SCALED * S_i + ATOL
+# FP32 evaluation (the reference's own CPU path included) lands at ~1e-5..1e-4
+# of S_i for particles whose pressure is near zero (free surface), where the
+# Tait pressure itself loses digits; the bulk is at ~1e-6.
+RTOL_SCALED = 2e-4
+BULK_RTOL_SCALED = 1e-5   # required for 99% of the particles
+
+
+def golden(name: str) -> dict:
+    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    out = {k: z[k] for k in z.files if k != "meta_json"}
+    out["meta"] = json.loads(bytes(z["meta_json"]).decode())
+    return out
+
+
+def case_spec(name: str):
+    import make_golden
+    return make_golden.CASES[name][0]()
+
+
+def case_nsteps(name: str) -> int:
+    import make_golden
+    return make_golden.CASES[name][1]
+
+
+def load_generated(name: str):
+    """Regenerates the case files of golden case `name` and loads them with the product loader."""
+    spec = case_spec(name)
+    tmp = tempfile.mkdtemp(prefix="gbcase_")
+    cg.write_case(cg.make_dam_break(spec), tmp)
+    return load_case(tmp, spec.name)
+
+
+def scaled_err(x, ref, scale):
+    x = np.asarray(x, np.float64)
+    ref = np.asarray(ref, np.float64)
+    e = np.abs(x - ref)
+    if e.ndim == 2:
+        e = e.max(axis=1)
+    return e / np.maximum(scale, 1e-30)
