@@ -470,11 +470,11 @@ int gbsph_graph_prepare(gbsph_ctx* ctx, unsigned nsteps) {
   if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
   if (ctx->c.tstep != GBSPH_STEP_SYMPLECTIC) return set_err(ctx, GBSPH_EINVAL, "multi-step graphs need Symplectic");
   const int parity = (int)(ctx->swaps & 1u);
-  if (ctx->multi_exec && ctx->multi_steps == nsteps && ctx->multi_parity == parity && ctx->prof_n == 0 &&
-      ctx->prof_cap == 0)
-    return GBSPH_OK;
+  if (ctx->multi_exec && ctx->multi_steps == nsteps && ctx->multi_parity == parity) return GBSPH_OK;
   if (ctx->multi_exec) cudaGraphExecDestroy(ctx->multi_exec);
   ctx->multi_exec = nullptr;
+  // profiling events captured into the graph: slots 0..prof_n-1 are recorded on every replay
+  ctx->prof_n = 0;
   const unsigned long long l0 = ctx->launches;
   const unsigned s0 = ctx->swaps;
   const DevArrays a0 = ctx->a;

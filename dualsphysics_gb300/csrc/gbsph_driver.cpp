@@ -1,0 +1,123 @@
+// gbsph_driver.cpp -- gbsph_run: the Run loop of JSphGpuSingle
+// (JSphGpuSingle.cpp:950-1010) over the gbsph C ABI.
+//
+//   gbsph_run <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-sv:none|bi4]
+//             [-nograph] [-device:D]
+//
+// Loads the run XML and Case.bi4 (LoadConfig + LoadCaseParticles), derives the
+// constants, uploads the particles, then steps until TimeMax (or N steps)
+// writing data/Part_%04u.bi4 every TimeOut, and prints the run summary the
+// reference prints at the end of Run.out (JSph::ShowResume, JSph.cpp:3522-3545).
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbsph.h"
+#include "gbsph_io.h"
+
+namespace {
+
+int fail(const char* what, const std::string& msg) {
+  std::fprintf(stderr, "*** Exception: %s: %s\n", what, msg.c_str());
+  return 1;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    std::fprintf(stderr, "usage: %s <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-sv:none|bi4] [-nograph] "
+                         "[-device:D]\n", argv[0]);
+    return 1;
+  }
+  std::string casepath = argv[1], dirout = argv[2];
+  long nsteps = 0;
+  double tmax = -1;
+  bool save = true, graph = true, info = false;
+  int device = 0;
+  for (int i = 3; i < argc; i++) {
+    const std::string a = argv[i];
+    if (a.rfind("-nsteps:", 0) == 0) nsteps = std::atol(a.c_str() + 8);
+    else if (a.rfind("-tmax:", 0) == 0) tmax = std::atof(a.c_str() + 6);
+    else if (a == "-sv:none") save = false;
+    else if (a == "-sv:bi4") save = true;
+    else if (a == "-nograph") graph = false;
+    else if (a.rfind("-device:", 0) == 0) device = std::atoi(a.c_str() + 8);
+    else if (a == "-info") info = true;
+    else if (a == "-gpu" || a == "-symplectic") continue;
+    else return fail("options", "unknown option " + a);
+  }
+  const size_t slash = casepath.find_last_of('/');
+  const std::string casedir = slash == std::string::npos ? "." : casepath.substr(0, slash);
+  const std::string casename = slash == std::string::npos ? casepath : casepath.substr(slash + 1);
+  gbio::Case cs;
+  std::string err;
+  if (!gbio::load_case(casedir, casename, cs, err)) return fail("LoadCase", err);
+  gbsph_consts c;
+  if (gbsph_config(&cs.params, &c) != GBSPH_OK) return fail("ConfigConstants", "invalid case constants");
+  if (info) {
+    // case summary as JSON (host only: no device is touched)
+    std::printf("{\"np\": %u, \"npb\": %u, \"h\": %.17g, \"b\": %.17g, \"dp\": %.17g, \"maprealposmin\": "
+                "[%.17g, %.17g, %.17g], \"maprealposmax\": [%.17g, %.17g, %.17g], \"kernelsize2\": %.9g, "
+                "\"cs0\": %.17g, \"domcellcode\": %u, \"mapcells\": [%u, %u, %u], \"tboundary\": %d, "
+                "\"tstep\": %d, \"tdensity\": %d, \"tvisco\": %d, \"idsum\": %.17g, \"possum\": %.17g, "
+                "\"rhosum\": %.17g, \"norsum\": %.17g, \"codesum\": %.17g}\n",
+                cs.np, cs.npb, cs.params.h, cs.params.b, cs.params.dp, cs.params.maprealposmin[0],
+                cs.params.maprealposmin[1], cs.params.maprealposmin[2], cs.params.maprealposmax[0],
+                cs.params.maprealposmax[1], cs.params.maprealposmax[2], c.kernelsize2, c.cs0, c.domcellcode,
+                c.mapcells[0], c.mapcells[1], c.mapcells[2], c.tboundary, c.tstep, c.tdensity, c.tvisco,
+                [&] { double s = 0; for (unsigned v : cs.idp) s += v; return s; }(),
+                [&] { double s = 0; for (double v : cs.pos) s += v; return s; }(),
+                [&] { double s = 0; for (size_t k = 3; k < cs.velrho.size(); k += 4) s += cs.velrho[k]; return s; }(),
+                [&] { double s = 0; for (float v : cs.boundnor) s += v; return s; }(),
+                [&] { double s = 0; for (uint16_t v : cs.code) s += v; return s; }());
+    return 0;
+  }
+  gbsph_ctx* ctx = nullptr;
+  int rc = gbsph_create(&c, cs.np, device, &ctx);
+  if (rc != GBSPH_OK) return fail("gbsph_create", "code " + std::to_string(rc));
+  rc = gbsph_upload(ctx, cs.np, cs.npb, cs.pos.data(), cs.velrho.data(), cs.idp.data(), cs.code.data(),
+                    cs.boundnor.empty() ? nullptr : cs.boundnor.data());
+  if (rc != GBSPH_OK) return fail("gbsph_upload", gbsph_last_error(ctx));
+  if (tmax < 0) tmax = cs.time_max;
+  const double tout = cs.time_out > 0 ? cs.time_out : tmax;
+  std::printf("Case %s: %u particles (%u boundary, %u fluid), h=%g, dp=%g\n", casename.c_str(), cs.np, cs.npb,
+              cs.np - cs.npb, cs.params.h, cs.params.dp);
+  std::vector<double> pos(3 * (size_t)cs.np);
+  std::vector<float> velrho(4 * (size_t)cs.np);
+  std::vector<unsigned> idp(cs.np);
+  gbsph_divinfo di;
+  auto save_part = [&](unsigned part, double t, unsigned step, double dtn) -> bool {
+    if (!save) return true;
+    if (gbsph_get_divinfo(ctx, &di, nullptr, 0, nullptr, nullptr) != GBSPH_OK) return false;
+    if (gbsph_download(ctx, pos.data(), velrho.data(), idp.data(), nullptr, nullptr) != GBSPH_OK) return false;
+    return gbio::save_part(dirout, cs, part, t, step, dtn, di.np, pos.data(), velrho.data(), idp.data(), err);
+  };
+  if (!save_part(0, 0.0, 0, c.dtini)) return fail("SaveData", err.empty() ? gbsph_last_error(ctx) : err);
+  unsigned part = 1, nstep = 0;
+  double t = 0, tnext = tout, dtl = 0, dtn = c.dtini;
+  const bool sym = c.tstep == GBSPH_STEP_SYMPLECTIC;
+  const auto t0 = std::chrono::steady_clock::now();
+  while (t < tmax && (nsteps == 0 || (long)nstep < nsteps)) {
+    rc = sym ? gbsph_run(ctx, 1, graph ? 1 : 0) : gbsph_step(ctx);
+    if (rc != GBSPH_OK) return fail("ComputeStep", gbsph_last_error(ctx));
+    rc = gbsph_step_dt(ctx, &dtl, &dtn, &t);
+    if (rc != GBSPH_OK) return fail("ComputeStep", gbsph_last_error(ctx));
+    nstep++;
+    if (t >= tnext) {
+      if (!save_part(part, t, nstep, dtn)) return fail("SaveData", err.empty() ? gbsph_last_error(ctx) : err);
+      part++;
+      tnext += tout;
+    }
+  }
+  const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  gbsph_get_divinfo(ctx, &di, nullptr, 0, nullptr, nullptr);
+  std::printf("Simulated time: %.6f s in %u steps (last dt %.6e)\n", t, nstep, dtl);
+  std::printf("Particles: %u (excluded %u)\n", di.np, di.nout_total);
+  std::printf("Runtime: %.3f s\nSteps per second: %.3f\n", wall, nstep / (wall > 0 ? wall : 1));
+  gbsph_destroy(ctx);
+  return 0;
+}

@@ -192,6 +192,220 @@ __global__ void __launch_bounds__(128) k_forces_fluid(gbsph_consts c, DevArrays 
   }
 }
 
+// ---- fluid rows, queued variant -------------------------------------------
+// Lanes are target particles.  The neighbour test (the cheap part, ~1870
+// candidates per particle in 27 cells of size 2h) runs in lock step over the
+// 27 cells; the ~290 candidates per particle that pass it are queued per lane
+// in shared memory (relative position + index) and the pair terms (the
+// expensive part) are evaluated in flushes where every lane works on its own
+// queue, so the warp does not execute the pair body for the union of its
+// lanes' neighbours.  Summation order per particle is the candidate order.
+constexpr int kQCap = 16;
+constexpr int kQBlock = 128;
+
+struct PairAcc {
+  float ax, ay, az, ar, delta, visc;
+  float s0, s1, s2, s3, s4, s5;
+};
+
+// (1+t)^a - 1 for |t| < 0.05 by its binomial series (5 terms: relative
+// truncation error below 1e-8), used for the hydrostatic DDT2 correction
+// rho0*((1+ddtgz*drz)^(1/gamma)-1) without the cancellation of pow()-1.
+struct DdtSeries {
+  float c1, c2, c3, c4, c5;
+};
+
+__device__ __forceinline__ DdtSeries ddt_series(float gamma) {
+  DdtSeries s;
+  const float a = 1.f / gamma;
+  s.c1 = a;
+  s.c2 = s.c1 * (a - 1.f) * 0.5f;
+  s.c3 = s.c2 * (a - 2.f) * (1.f / 3.f);
+  s.c4 = s.c3 * (a - 3.f) * 0.25f;
+  s.c5 = s.c4 * (a - 4.f) * 0.2f;
+  return s;
+}
+
+template <int tvisco, int tdensity, bool boundp2>
+__device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const DevArrays& a, const DdtSeries& ds, float4 e,
+                                           float4 vr1, float p1press, float inv_rho1, float4 ta1, float2 tb1,
+                                           float visco, float massp2, PairAcc& r) {
+  const unsigned p2 = __float_as_uint(e.w);
+  const float drx = e.x, dry = e.y, drz = e.z;
+  const float rr2 = drx * drx + dry * dry + drz * drz;
+  const float rinv = rsqrtf(rr2);
+  const float qq = rr2 * rinv * (1.f / c.kernelh);
+  const float wqq1 = 1.f - 0.5f * qq;
+  const float fac = c.bwenh * wqq1 * wqq1 * wqq1;
+  const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
+  const float4 vr2 = a.velrho[p2];
+  const float p2press = a.pscell[p2].w;
+  const float inv_rho2 = __frcp_rn(vr2.w);
+  // momentum
+  const float p_vpm = -(p1press + p2press) * inv_rho1 * inv_rho2 * massp2;
+  r.ax += p_vpm * frx; r.ay += p_vpm * fry; r.az += p_vpm * frz;
+  // continuity
+  const float dvx = vr1.x - vr2.x, dvy = vr1.y - vr2.y, dvz = vr1.z - vr2.z;
+  r.ar += massp2 * (dvx * frx + dvy * fry + dvz * frz) * (vr1.w * inv_rho2);
+  const float inv_r2eta = __frcp_rn(rr2 + c.eta2);
+  const float cbar = (float)c.cs0;
+  if (tdensity == GBSPH_DDT_DDT && r.delta != FLT_MAX) {
+    const float visc_densi = c.ddtkh * cbar * (vr1.w * inv_rho2 - 1.f) * inv_r2eta;
+    const float dot3 = drx * frx + dry * fry + drz * frz;
+    r.delta = (boundp2 && c.tboundary == GBSPH_BC_DBC) ? FLT_MAX : r.delta + visc_densi * dot3 * massp2;
+  }
+  if ((tdensity == GBSPH_DDT_DDT2 || (tdensity == GBSPH_DDT_DDT2FULL && !boundp2)) && r.delta != FLT_MAX) {
+    if (boundp2) {
+      r.delta = FLT_MAX;
+    } else {
+      const float t = c.ddtgz * drz;
+      float drho;
+      if (fabsf(t) < 0.05f) drho = c.rhopzero * (t * (ds.c1 + t * (ds.c2 + t * (ds.c3 + t * (ds.c4 + t * ds.c5)))));
+      else drho = c.rhopzero * powf(1.f + t, 1.f / c.gamma) - c.rhopzero;
+      const float visc_densi = c.ddtkh * cbar * ((vr2.w - vr1.w) - drho) * inv_r2eta;
+      const float dot3 = drx * frx + dry * fry + drz * frz;
+      r.delta -= visc_densi * dot3 * massp2 * inv_rho2;
+    }
+  }
+  // viscosity
+  const float dot = drx * dvx + dry * dvy + drz * dvz;
+  const float dot_rr2 = dot * inv_r2eta;
+  r.visc = fmaxf(dot_rr2, r.visc);
+  if (tvisco == GBSPH_VISCO_ARTIFICIAL) {
+    if (dot < 0) {
+      const float amubar = c.kernelh * dot_rr2;
+      const float robar = (vr1.w + vr2.w) * 0.5f;
+      const float pi_visc = (-visco * cbar * amubar * __frcp_rn(robar)) * massp2;
+      r.ax -= pi_visc * frx; r.ay -= pi_visc * fry; r.az -= pi_visc * frz;
+    }
+  } else {
+    const float robar2 = vr1.w + vr2.w;
+    const float temp = 4.f * visco * inv_r2eta * __frcp_rn(robar2);
+    const float vtemp = massp2 * temp * (drx * frx + dry * fry + drz * frz);
+    r.ax += vtemp * dvx; r.ay += vtemp * dvy; r.az += vtemp * dvz;
+    if (tvisco == GBSPH_VISCO_LAMINARSPS) {
+      float t0 = ta1.x, t1 = ta1.y, t2 = ta1.z, t3 = ta1.w, t4 = tb1.x, t5 = tb1.y;
+      if (!boundp2) {
+        const float4 ta2 = a.taua[p2];
+        const float2 tb2 = a.taub[p2];
+        t0 += ta2.x; t1 += ta2.y; t2 += ta2.z; t3 += ta2.w; t4 += tb2.x; t5 += tb2.y;
+      }
+      r.ax += massp2 * (t0 * frx + t1 * fry + t2 * frz);
+      r.ay += massp2 * (t1 * frx + t3 * fry + t4 * frz);
+      r.az += massp2 * (t2 * frx + t4 * fry + t5 * frz);
+      const float volp2 = -massp2 * inv_rho2;
+      float dv = dvx * volp2; r.s0 += dv * frx; r.s1 += dv * fry; r.s2 += dv * frz;
+      dv = dvy * volp2; r.s1 += dv * frx; r.s3 += dv * fry; r.s4 += dv * frz;
+      dv = dvz * volp2; r.s2 += dv * frx; r.s4 += dv * fry; r.s5 += dv * frz;
+    }
+  }
+}
+
+template <int tvisco, int tdensity, bool boundp2>
+__device__ __forceinline__ void queued_pass(const gbsph_consts& c, const DevArrays& a, const DivState& d,
+                                            const CellGrid& g, bool active, float4 ps1, float4 vr1, float inv_rho1,
+                                            float4 ta1, float2 tb1, const DdtSeries& ds, float4 (*q)[32],
+                                            PairAcc& r) {
+  const int lane = threadIdx.x & 31;
+  const unsigned cellinit = boundp2 ? 0u : d.boxfluid;
+  const float scell = c.scell, ks2 = c.kernelsize2;
+  const float visco = boundp2 ? c.visco * c.viscoboundfactor : c.visco;
+  const float massp2 = boundp2 ? c.massbound : c.massfluid;
+  const int sd = c.cellmode_div, side = 2 * sd + 1, ncell = side * side * side;
+  int n = 0;
+  for (int k = 0; k < ncell; k++) {
+    const int dz = k / (side * side) - sd, dy = (k / side) % side - sd, dx = k % side - sd;
+    const int x = g.cx + dx, y = g.cy + dy, z = g.cz + dz;
+    const bool valid = active && x >= g.xini && x < g.xfin && y >= g.yini && y < g.yfin && z >= g.zini && z < g.zfin;
+    unsigned pini = 0, len = 0;
+    if (valid) {
+      const unsigned box = cellinit + (unsigned)x + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+      pini = a.begincell[box];
+      len = a.begincell[box + 1] - pini;
+    }
+    const unsigned maxlen = __reduce_max_sync(0xffffffffu, len);
+    const float bx = ps1.x - (float)dx * scell, by = ps1.y - (float)dy * scell, bz = ps1.z - (float)dz * scell;
+    for (unsigned t = 0; t < maxlen; t++) {
+      if (t < len) {
+        const unsigned p2 = pini + t;
+        const float4 ps2 = a.pscell[p2];
+        const float drx = bx - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
+        const float rr2 = drx * drx + dry * dry + drz * drz;
+        if (rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
+          q[n][lane] = make_float4(drx, dry, drz, __uint_as_float(p2));
+          n++;
+        }
+      }
+      if (__any_sync(0xffffffffu, n == kQCap)) {
+        const int maxn = (int)__reduce_max_sync(0xffffffffu, (unsigned)n);
+        for (int e = 0; e < maxn; e++)
+          if (e < n) pair_fluid<tvisco, tdensity, boundp2>(c, a, ds, q[e][lane], vr1, ps1.w, inv_rho1, ta1, tb1, visco, massp2, r);
+        n = 0;
+      }
+    }
+  }
+  const int maxn = (int)__reduce_max_sync(0xffffffffu, (unsigned)n);
+  for (int e = 0; e < maxn; e++)
+    if (e < n) pair_fluid<tvisco, tdensity, boundp2>(c, a, ds, q[e][lane], vr1, ps1.w, inv_rho1, ta1, tb1, visco, massp2, r);
+}
+
+template <int tvisco, int tdensity>
+__global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, DevArrays a) {
+  __shared__ float4 qbuf[kQBlock / 32][kQCap][32];
+  const DivState& d = *a.div;
+  const unsigned np = d.np, npb = d.npb;
+  const unsigned p1 = npb + blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = p1 < np;
+  if (__all_sync(0xffffffffu, !active)) return;
+  float4 ps1 = make_float4(0, 0, 0, 0), vr1 = make_float4(0, 0, 0, 1);
+  float4 ta1 = make_float4(0, 0, 0, 0);
+  float2 tb1 = make_float2(0, 0);
+  CellGrid g;
+  g.cx = g.cy = g.cz = 0; g.xini = g.xfin = g.yini = g.yfin = g.zini = g.zfin = 0;
+  if (active) {
+    ps1 = a.pscell[p1];
+    vr1 = a.velrho[p1];
+    if (tvisco == GBSPH_VISCO_LAMINARSPS) { ta1 = a.taua[p1]; tb1 = a.taub[p1]; }
+    const unsigned dcc = c.domcellcode, cel = a.dcell[p1];
+    g = gb_grid((int)gb_cx(dcc, cel) - (int)d.cellmin[0], (int)gb_cy(dcc, cel) - (int)d.cellmin[1],
+                (int)gb_cz(dcc, cel) - (int)d.cellmin[2], c.cellmode_div, d);
+  }
+  const float inv_rho1 = __frcp_rn(vr1.w);
+  const DdtSeries ds = ddt_series(c.gamma);
+  float4 (*q)[32] = qbuf[threadIdx.x >> 5];
+  PairAcc ff = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  PairAcc fb = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  queued_pass<tvisco, tdensity, false>(c, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, ds, q, ff);
+  queued_pass<tvisco, tdensity, true>(c, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, ds, q, fb);
+  float acemax2 = 0, visc = 0, vel2 = 0;
+  if (active) {
+    float ar = ff.ar + fb.ar;
+    if (tdensity != GBSPH_DDT_NONE) {
+      const float dl = (ff.delta == FLT_MAX || fb.delta == FLT_MAX) ? FLT_MAX : ff.delta + fb.delta;
+      if (dl != FLT_MAX) ar += dl;
+    }
+    const float ax = ff.ax + fb.ax, ay = ff.ay + fb.ay, az = ff.az + fb.az;
+    a.acear[p1] = make_float4(ax, ay, az, ar);
+    if (tvisco == GBSPH_VISCO_LAMINARSPS) {
+      a.straina[p1] = make_float4(ff.s0 + fb.s0, ff.s1 + fb.s1, ff.s2 + fb.s2, ff.s3 + fb.s3);
+      a.strainb[p1] = make_float2(ff.s4 + fb.s4, ff.s5 + fb.s5);
+    }
+    acemax2 = ax * ax + ay * ay + az * az;
+    visc = fmaxf(ff.visc, fb.visc);
+    vel2 = vr1.x * vr1.x + vr1.y * vr1.y + vr1.z * vr1.z;
+  }
+  for (int o = 16; o; o >>= 1) {
+    acemax2 = fmaxf(acemax2, __shfl_xor_sync(0xffffffffu, acemax2, o));
+    visc = fmaxf(visc, __shfl_xor_sync(0xffffffffu, visc, o));
+    vel2 = fmaxf(vel2, __shfl_xor_sync(0xffffffffu, vel2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (acemax2 > 0) gb_atomic_max_nonneg(&a.st->acemax2, acemax2);
+    if (visc > 0) gb_atomic_max_nonneg(&a.st->viscdt, visc);
+    if (vel2 > 0) gb_atomic_max_nonneg(&a.st->velmax2, vel2);
+  }
+}
+
 // Bound rows (JSphCpu.cpp:633-703): continuity and visc from fluid neighbours.
 __global__ void __launch_bounds__(128) k_forces_bound(gbsph_consts c, DevArrays a) {
   const DivState& d = *a.div;
@@ -421,17 +635,18 @@ __global__ void k_pips(gbsph_consts c, DevArrays a) {
 }
 
 template <int tvisco, int tdensity>
-void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s) {
-  k_forces_fluid<tvisco, tdensity><<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s) {
+  if (variant == 1) k_forces_fluid<tvisco, tdensity><<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+  else k_forces_fluid_q<tvisco, tdensity><<<gb_div_up(cap, kQBlock), kQBlock, 0, s>>>(c, a);
 }
 
 template <int tvisco>
-void launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s) {
+void launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s) {
   switch (c.tdensity) {
-    case GBSPH_DDT_NONE: launch_fluid<tvisco, GBSPH_DDT_NONE>(c, a, cap, s); break;
-    case GBSPH_DDT_DDT: launch_fluid<tvisco, GBSPH_DDT_DDT>(c, a, cap, s); break;
-    case GBSPH_DDT_DDT2: launch_fluid<tvisco, GBSPH_DDT_DDT2>(c, a, cap, s); break;
-    default: launch_fluid<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, s); break;
+    case GBSPH_DDT_NONE: launch_fluid<tvisco, GBSPH_DDT_NONE>(c, a, cap, variant, s); break;
+    case GBSPH_DDT_DDT: launch_fluid<tvisco, GBSPH_DDT_DDT>(c, a, cap, variant, s); break;
+    case GBSPH_DDT_DDT2: launch_fluid<tvisco, GBSPH_DDT_DDT2>(c, a, cap, variant, s); break;
+    default: launch_fluid<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, variant, s); break;
   }
 }
 
@@ -442,16 +657,16 @@ namespace gbk {
 void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, cudaStream_t s,
             unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin, cudaEvent_t ev_fluid_end) {
   (void)bsize;
-  (void)variant;
   cudaMemsetAsync(&a.st->acemax2, 0, 3 * sizeof(unsigned), s);
   k_forces_bound<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
-  if (ev_fluid_begin) cudaEventRecord(ev_fluid_begin, s);
+  // external records: inside a captured graph the events are recorded on every replay
+  if (ev_fluid_begin) cudaEventRecordWithFlags(ev_fluid_begin, s, cudaEventRecordExternal);
   switch (c.tvisco) {
-    case GBSPH_VISCO_ARTIFICIAL: launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, s); break;
-    case GBSPH_VISCO_LAMINAR: launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, s); break;
-    default: launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, s); break;
+    case GBSPH_VISCO_ARTIFICIAL: launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, variant, s); break;
+    case GBSPH_VISCO_LAMINAR: launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, variant, s); break;
+    default: launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, variant, s); break;
   }
-  if (ev_fluid_end) cudaEventRecord(ev_fluid_end, s);
+  if (ev_fluid_end) cudaEventRecordWithFlags(ev_fluid_end, s, cudaEventRecordExternal);
   if (nlaunch) *nlaunch += 2;
 }
 

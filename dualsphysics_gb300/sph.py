@@ -181,6 +181,11 @@ class GbSphSingle:
         self._check(lib().gbsph_elapsed(self.ctx, a, b, C.byref(ms)), "elapsed")
         return ms.value
 
+    def set_option(self, key: int, value: int) -> None:
+        """Kernel options: key 0 = forces block size, key 1 = forces variant
+        (0 queued pair evaluation, 1 one-thread-per-particle walk)."""
+        self._check(lib().gbsph_set_option(self.ctx, key, value), "set_option")
+
     def graph_prepare(self, nsteps: int) -> None:
         self._check(lib().gbsph_graph_prepare(self.ctx, nsteps), "graph_prepare")
 

@@ -54,6 +54,20 @@ def load_generated(name: str):
     return load_case(tmp, spec.name)
 
 
+def assert_fp32_parity(x, x_orc32, x_f64, scale, what=""):
+    """FP32 parity of a pair sum: the error of `x` against the FP64 oracle,
+    per particle and relative to the conditioning scale, is at most twice the
+    largest error of the oracle's own FP32 evaluation (the reference's
+    algorithm and evaluation order) plus BULK_RTOL_SCALED, and the median error
+    is at most BULK_RTOL_SCALED."""
+    e = scaled_err(x, x_f64, scale)
+    e_orc = scaled_err(x_orc32, x_f64, scale)
+    bound = 2.0 * e_orc.max() + BULK_RTOL_SCALED
+    assert e.max() <= bound, f"{what}: max scaled error {e.max():.3e} > {bound:.3e}"
+    assert np.percentile(e, 50) <= BULK_RTOL_SCALED, f"{what}: median scaled error {np.percentile(e, 50):.3e}"
+    return e.max(), e_orc.max()
+
+
 def scaled_err(x, ref, scale):
     x = np.asarray(x, np.float64)
     ref = np.asarray(ref, np.float64)
