@@ -154,6 +154,8 @@ def main():
     ap.add_argument("--ref-stride", type=int, default=16)
     ap.add_argument("--cpu-stride", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="fluid-row kernel: 0 queued rounds, 1 one thread per particle")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -180,6 +182,8 @@ def main():
     K, W = args.steps, args.warmup
     s = GbSphSingle(local)
     s.setup(cd)
+    if args.variant is not None:
+        s.set_option(1, args.variant)
     pi = s.pips()
     s.RunSteps(W, use_graph=True)
     s.sync()
@@ -221,6 +225,8 @@ def main():
         t0 = time.perf_counter()
         e = GbSphSingle(local)
         e.setup(cd)
+        if args.variant is not None:
+            e.set_option(1, args.variant)
         for _ in range(K):
             e.ComputeStep()
             e.step_dt()

@@ -125,7 +125,7 @@ size_t layout(gbsph_ctx* ctx, void* base) {
   a.keys = k.take<unsigned>(n); a.keys2 = k.take<unsigned>(n);
   a.vals = k.take<unsigned>(n); a.vals2 = k.take<unsigned>(n);
   const size_t ntiles = (n + 2047) / 2048;
-  a.hist = k.take<unsigned>(ntiles * 256 + 1);
+  a.hist = k.take<unsigned>(ntiles * 256 + 256 + 1);  // tile counts + digit totals
   a.begincell = k.take<unsigned>(ctx->nctt_cap + 1);
   a.div = k.take<DivState>(1);
   a.st = k.take<StepState>(1);
@@ -197,7 +197,9 @@ double* device_scalar(gbsph_ctx* ctx) { return &ctx->a.st->dt_var; }
 extern "C" {
 
 int gbsph_create(const gbsph_consts* c, unsigned capacity, int device, gbsph_ctx** out) {
-  if (!c || !out || capacity == 0) return GBSPH_EINVAL;
+  // particle indices carry a tag in bit 31 inside the fluid-row kernel
+  if (!c || !out || capacity == 0 || capacity > 0x7fffffffu) return GBSPH_EINVAL;
+  if (c->cellmode_div != 1 && c->cellmode_div != 2) return GBSPH_EINVAL;
   *out = nullptr;
   if (c->domcellcode == 0) return GBSPH_EINVAL;
   if (c->tstep != GBSPH_STEP_SYMPLECTIC && c->tstep != GBSPH_STEP_VERLET) return GBSPH_EINVAL;

@@ -209,28 +209,55 @@ __global__ void k_rs_hist(const unsigned* __restrict__ keys, unsigned* __restric
     hist[dgt * ntiles_cap + tile] = (tile < ntiles) ? sh[dgt] : 0;
 }
 
-// Exclusive scan of the histogram in digit-major order (one block).
-__global__ void k_rs_scan(unsigned* __restrict__ hist, unsigned total) {
-  __shared__ unsigned sums[1024];
-  const unsigned t = threadIdx.x, nt = blockDim.x;
-  const unsigned chunk = gb_div_up(total, nt);
-  const unsigned b = t * chunk, e = min(total, b + chunk);
-  unsigned s = 0;
-  for (unsigned i = b; i < e; i++) s += hist[i];
-  sums[t] = s;
-  __syncthreads();
-  for (unsigned o = 1; o < nt; o <<= 1) {
-    const unsigned v = (t >= o) ? sums[t - o] : 0;
-    __syncthreads();
-    sums[t] += v;
-    __syncthreads();
+// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024).
+__device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned* total) {
+  __shared__ unsigned wsum[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  unsigned x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  unsigned run = sums[t] - s;
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    unsigned ws = lane < nw ? wsum[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, ws, o);
+      if (lane >= o) ws += y;
+    }
+    if (lane < nw) wsum[lane] = ws;
+  }
+  __syncthreads();
+  const unsigned excl = x - v + (w ? wsum[w - 1] : 0);
+  if (total) *total = wsum[nw - 1];
+  __syncthreads();
+  return excl;
+}
+
+// Exclusive scan of one digit's column of tile counts (one block per digit);
+// the column total goes to tot[digit].
+__global__ void k_rs_scan_cols(unsigned* __restrict__ hist, unsigned* __restrict__ tot, unsigned ntiles) {
+  unsigned* col = hist + (size_t)blockIdx.x * ntiles;
+  const unsigned chunk = gb_div_up(ntiles, blockDim.x);
+  const unsigned b = threadIdx.x * chunk, e = min(ntiles, b + chunk);
+  unsigned sum = 0;
+  for (unsigned i = b; i < e; i++) sum += col[i];
+  unsigned total;
+  unsigned run = block_exclusive_scan(sum, &total);
   for (unsigned i = b; i < e; i++) {
-    const unsigned v = hist[i];
-    hist[i] = run;
+    const unsigned v = col[i];
+    col[i] = run;
     run += v;
   }
+  if (threadIdx.x == 0) tot[blockIdx.x] = total;
+}
+
+// Exclusive scan of the digit totals (one block of kRadix threads).
+__global__ void k_rs_scan_digits(unsigned* __restrict__ tot) {
+  const unsigned v = tot[threadIdx.x];
+  const unsigned e = block_exclusive_scan(v, nullptr);
+  tot[threadIdx.x] = e;
 }
 
 // Stable scatter: within a tile, items keep their index order per digit.
@@ -250,7 +277,8 @@ __global__ void __launch_bounds__(kSortBlock) k_rs_scatter(const unsigned* __res
   const unsigned ntiles = gb_div_up(n, kSortTile);
   const unsigned tile = blockIdx.x;
   if (tile >= ntiles) return;
-  for (int i = threadIdx.x; i < kRadix; i += blockDim.x) s_off[i] = hist[i * ntiles_cap + tile];
+  const unsigned* tot = hist + (size_t)kRadix * ntiles_cap;
+  for (int i = threadIdx.x; i < kRadix; i += blockDim.x) s_off[i] = hist[i * ntiles_cap + tile] + tot[i];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lanemask_lt = (1u << lane) - 1u;
   const unsigned base = tile * kSortTile;
@@ -408,7 +436,8 @@ void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses,
   for (unsigned pass = 0; pass < npasses; pass++) {
     const int shift = (int)(pass * kRadixBits);
     k_rs_hist<<<ntiles_cap, kSortBlock, 0, s>>>(kin, a.hist, a.div, ntiles_cap, shift);
-    k_rs_scan<<<1, 1024, 0, s>>>(a.hist, ntiles_cap * kRadix);
+    k_rs_scan_cols<<<kRadix, 256, 0, s>>>(a.hist, a.hist + (size_t)kRadix * ntiles_cap, ntiles_cap);
+    k_rs_scan_digits<<<1, kRadix, 0, s>>>(a.hist + (size_t)kRadix * ntiles_cap);
     k_rs_scatter<<<ntiles_cap, kSortBlock, 0, s>>>(kin, vin, kout, vout, a.hist, a.div, ntiles_cap, shift);
     swp(kin, kout);
     swp(vin, vout);
@@ -444,7 +473,7 @@ void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses,
   if (withpre) { swp(a.qx, a.qx2); swp(a.qy, a.qy2); swp(a.qz, a.qz2); swp(a.velrhopre, a.velrhopre2); }
   if (withsps) { swp(a.taua, a.taua2); swp(a.taub, a.taub2); }
   if (withnor) swp(a.boundnor, a.boundnor2);
-  if (nlaunch) *nlaunch += 7 + 3ull * npasses;
+  if (nlaunch) *nlaunch += 7 + 4ull * npasses;
 }
 
 }  // namespace gbk

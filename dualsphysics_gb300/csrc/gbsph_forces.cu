@@ -192,21 +192,52 @@ __global__ void __launch_bounds__(128) k_forces_fluid(gbsph_consts c, DevArrays 
   }
 }
 
-// ---- fluid rows, queued variant -------------------------------------------
+// ---- fluid rows, production kernel ----------------------------------------
 // Lanes are target particles.  The neighbour test (the cheap part, ~1870
 // candidates per particle in 27 cells of size 2h) runs in lock step over the
 // 27 cells; the ~290 candidates per particle that pass it are queued per lane
-// in shared memory (relative position + index) and the pair terms (the
-// expensive part) are evaluated in flushes where every lane works on its own
-// queue, so the warp does not execute the pair body for the union of its
-// lanes' neighbours.  Summation order per particle is the candidate order.
+// in shared memory (relative position + index), a ring of kQCap entries.  The
+// pair terms (the expensive part) run in rounds: one round evaluates the two
+// oldest entries of every lane with a non-empty queue, and rounds are taken when at
+// least kRoundMin lanes have work (or when a queue could not take another
+// unrolled group of checks), so the pair body runs with most lanes active.
+// Summation order per particle is the candidate order.
 constexpr int kQCap = 16;
 constexpr int kQBlock = 128;
+constexpr int kQUnroll = 4;
+constexpr int kRoundMin = 24;
 
 struct PairAcc {
   float ax, ay, az, ar, delta, visc;
   float s0, s1, s2, s3, s4, s5;
 };
+
+// Float constants of the pair terms, derived on the host once per launch with
+// the float operations the pair body would otherwise repeat per pair (the
+// products keep the left-to-right association of the expressions they come
+// from, so the results are bit-identical).  As a kernel argument the struct
+// lives in the constant bank.
+struct PairK {
+  float hinv;            // 1/h
+  float ddt_kc;          // ddtkh * cs0
+  float vfac_f, vfac_b;  // artificial: -visco*cs0; laminar: 4*visco (fluid / boundary neighbours)
+};
+
+PairK make_pairk(const gbsph_consts& c) {
+  PairK k;
+  const float cbar = (float)c.cs0;
+  k.hinv = 1.f / c.kernelh;
+  k.ddt_kc = c.ddtkh * cbar;
+  const float vb = c.visco * c.viscoboundfactor;
+  if (c.tvisco == GBSPH_VISCO_ARTIFICIAL) {
+    k.vfac_f = -c.visco * cbar;
+    k.vfac_b = -vb * cbar;
+  } else {
+    k.vfac_f = 4.f * c.visco;
+    k.vfac_b = 4.f * vb;
+  }
+  return k;
+}
 
 // (1+t)^a - 1 for |t| < 0.05 by its binomial series (5 terms: relative
 // truncation error below 1e-8), used for the hydrostatic DDT2 correction
@@ -214,6 +245,10 @@ struct PairAcc {
 struct DdtSeries {
   float c1, c2, c3, c4, c5;
 };
+
+// Reciprocal with a relative error of at most 2 ulp (__fdividef), used for the
+// 1/rho, 1/(r^2+eta^2) and 1/rhobar factors of the pair terms.
+__device__ __forceinline__ float gb_rcp(float x) { return __fdividef(1.f, x); }
 
 __device__ __forceinline__ DdtSeries ddt_series(float gamma) {
   DdtSeries s;
@@ -226,31 +261,29 @@ __device__ __forceinline__ DdtSeries ddt_series(float gamma) {
   return s;
 }
 
-template <int tvisco, int tdensity, bool boundp2>
-__device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const DevArrays& a, const DdtSeries& ds, float4 e,
-                                           float4 vr1, float p1press, float inv_rho1, float4 ta1, float2 tb1,
-                                           float visco, float massp2, PairAcc& r) {
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen>
+__device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k, const DevArrays& a,
+                                           const DdtSeries& ds, float4 e, float4 vr2, float p2press, float4 vr1,
+                                           float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
+                                           float massp2, PairAcc& r) {
   const unsigned p2 = __float_as_uint(e.w);
   const float drx = e.x, dry = e.y, drz = e.z;
   const float rr2 = drx * drx + dry * dry + drz * drz;
   const float rinv = rsqrtf(rr2);
-  const float qq = rr2 * rinv * (1.f / c.kernelh);
+  const float qq = rr2 * rinv * k.hinv;
   const float wqq1 = 1.f - 0.5f * qq;
   const float fac = c.bwenh * wqq1 * wqq1 * wqq1;
   const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
-  const float4 vr2 = a.velrho[p2];
-  const float p2press = a.pscell[p2].w;
-  const float inv_rho2 = __frcp_rn(vr2.w);
+  const float inv_rho2 = gb_rcp(vr2.w);
   // momentum
   const float p_vpm = -(p1press + p2press) * inv_rho1 * inv_rho2 * massp2;
   r.ax += p_vpm * frx; r.ay += p_vpm * fry; r.az += p_vpm * frz;
   // continuity
   const float dvx = vr1.x - vr2.x, dvy = vr1.y - vr2.y, dvz = vr1.z - vr2.z;
   r.ar += massp2 * (dvx * frx + dvy * fry + dvz * frz) * (vr1.w * inv_rho2);
-  const float inv_r2eta = __frcp_rn(rr2 + c.eta2);
-  const float cbar = (float)c.cs0;
+  const float inv_r2eta = gb_rcp(rr2 + c.eta2);
   if (tdensity == GBSPH_DDT_DDT && r.delta != FLT_MAX) {
-    const float visc_densi = c.ddtkh * cbar * (vr1.w * inv_rho2 - 1.f) * inv_r2eta;
+    const float visc_densi = k.ddt_kc * (vr1.w * inv_rho2 - 1.f) * inv_r2eta;
     const float dot3 = drx * frx + dry * fry + drz * frz;
     r.delta = (boundp2 && c.tboundary == GBSPH_BC_DBC) ? FLT_MAX : r.delta + visc_densi * dot3 * massp2;
   }
@@ -260,9 +293,9 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const DevArray
     } else {
       const float t = c.ddtgz * drz;
       float drho;
-      if (fabsf(t) < 0.05f) drho = c.rhopzero * (t * (ds.c1 + t * (ds.c2 + t * (ds.c3 + t * (ds.c4 + t * ds.c5)))));
-      else drho = c.rhopzero * powf(1.f + t, 1.f / c.gamma) - c.rhopzero;
-      const float visc_densi = c.ddtkh * cbar * ((vr2.w - vr1.w) - drho) * inv_r2eta;
+      if (ddtgen && !(fabsf(t) < 0.05f)) drho = c.rhopzero * powf(1.f + t, 1.f / c.gamma) - c.rhopzero;
+      else drho = c.rhopzero * (t * (ds.c1 + t * (ds.c2 + t * (ds.c3 + t * (ds.c4 + t * ds.c5)))));
+      const float visc_densi = k.ddt_kc * ((vr2.w - vr1.w) - drho) * inv_r2eta;
       const float dot3 = drx * frx + dry * fry + drz * frz;
       r.delta -= visc_densi * dot3 * massp2 * inv_rho2;
     }
@@ -275,12 +308,12 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const DevArray
     if (dot < 0) {
       const float amubar = c.kernelh * dot_rr2;
       const float robar = (vr1.w + vr2.w) * 0.5f;
-      const float pi_visc = (-visco * cbar * amubar * __frcp_rn(robar)) * massp2;
+      const float pi_visc = (vfac * amubar * gb_rcp(robar)) * massp2;
       r.ax -= pi_visc * frx; r.ay -= pi_visc * fry; r.az -= pi_visc * frz;
     }
   } else {
     const float robar2 = vr1.w + vr2.w;
-    const float temp = 4.f * visco * inv_r2eta * __frcp_rn(robar2);
+    const float temp = vfac * inv_r2eta * gb_rcp(robar2);
     const float vtemp = massp2 * temp * (drx * frx + dry * fry + drz * frz);
     r.ax += vtemp * dvx; r.ay += vtemp * dvy; r.az += vtemp * dvz;
     if (tvisco == GBSPH_VISCO_LAMINARSPS) {
@@ -301,20 +334,57 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const DevArray
   }
 }
 
-template <int tvisco, int tdensity, bool boundp2>
-__device__ __forceinline__ void queued_pass(const gbsph_consts& c, const DevArrays& a, const DivState& d,
-                                            const CellGrid& g, bool active, float4 ps1, float4 vr1, float inv_rho1,
-                                            float4 ta1, float2 tb1, const DdtSeries& ds, float4 (*q)[32],
-                                            PairAcc& r) {
+// One round: every lane evaluates up to two of its oldest queued pairs, with
+// the loads of both neighbours issued before either pair's arithmetic.
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen>
+__device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k, const DevArrays& a,
+                                           const DdtSeries& ds, float4 (*q)[32], unsigned& qh, int& n, float4 vr1,
+                                           float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
+                                           float massp2, PairAcc& r) {
+  const int lane = threadIdx.x & 31;
+  const bool va = n > 0, vb = n > 1;
+  float4 ea = make_float4(0, 0, 0, 0), eb = ea, wa = make_float4(0, 0, 0, 1), wb = wa;
+  float pa = 0, pb = 0;
+  if (va) {
+    ea = q[qh][lane];
+    const unsigned p2 = __float_as_uint(ea.w);
+    wa = a.velrho[p2];
+    pa = a.pscell[p2].w;
+  }
+  if (vb) {
+    eb = q[(qh + 1) & (kQCap - 1)][lane];
+    const unsigned p2 = __float_as_uint(eb.w);
+    wb = a.velrho[p2];
+    pb = a.pscell[p2].w;
+  }
+  if (va)
+    pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ds, ea, wa, pa, vr1, p1press, inv_rho1, ta1, tb1, vfac,
+                                                  massp2, r);
+  if (vb)
+    pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ds, eb, wb, pb, vr1, p1press, inv_rho1, ta1, tb1, vfac,
+                                                  massp2, r);
+  const int used = (int)va + (int)vb;
+  qh = (qh + used) & (kQCap - 1);
+  n -= used;
+}
+
+// One pass of the fluid rows over the fluid (boundp2=false) or boundary
+// (boundp2=true) boxes of the 27 neighbour cells.
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen>
+__device__ __forceinline__ void round_pass(const gbsph_consts& c, const PairK& k, const DevArrays& a,
+                                           const DivState& d, const CellGrid& g, bool active, float4 ps1,
+                                           float4 vr1, float inv_rho1, float4 ta1, float2 tb1, const DdtSeries& ds,
+                                           float4 (*q)[32], PairAcc& r) {
   const int lane = threadIdx.x & 31;
   const unsigned cellinit = boundp2 ? 0u : d.boxfluid;
   const float scell = c.scell, ks2 = c.kernelsize2;
-  const float visco = boundp2 ? c.visco * c.viscoboundfactor : c.visco;
+  const float vfac = boundp2 ? k.vfac_b : k.vfac_f;
   const float massp2 = boundp2 ? c.massbound : c.massfluid;
   const int sd = c.cellmode_div, side = 2 * sd + 1, ncell = side * side * side;
   int n = 0;
-  for (int k = 0; k < ncell; k++) {
-    const int dz = k / (side * side) - sd, dy = (k / side) % side - sd, dx = k % side - sd;
+  unsigned qh = 0;
+  for (int ci = 0; ci < ncell; ci++) {
+    const int dz = ci / (side * side) - sd, dy = (ci / side) % side - sd, dx = ci % side - sd;
     const int x = g.cx + dx, y = g.cy + dy, z = g.cz + dz;
     const bool valid = active && x >= g.xini && x < g.xfin && y >= g.yini && y < g.yfin && z >= g.zini && z < g.zfin;
     unsigned pini = 0, len = 0;
@@ -325,32 +395,39 @@ __device__ __forceinline__ void queued_pass(const gbsph_consts& c, const DevArra
     }
     const unsigned maxlen = __reduce_max_sync(0xffffffffu, len);
     const float bx = ps1.x - (float)dx * scell, by = ps1.y - (float)dy * scell, bz = ps1.z - (float)dz * scell;
-    for (unsigned t = 0; t < maxlen; t++) {
-      if (t < len) {
-        const unsigned p2 = pini + t;
-        const float4 ps2 = a.pscell[p2];
-        const float drx = bx - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
-        const float rr2 = drx * drx + dry * dry + drz * drz;
-        if (rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
-          q[n][lane] = make_float4(drx, dry, drz, __uint_as_float(p2));
-          n++;
+    for (unsigned t0 = 0; t0 < maxlen; t0 += kQUnroll) {
+      float4 ps2[kQUnroll];
+#pragma unroll
+      for (int j = 0; j < kQUnroll; j++)
+        if (t0 + j < len) ps2[j] = a.pscell[pini + t0 + j];
+#pragma unroll
+      for (int j = 0; j < kQUnroll; j++) {
+        if (t0 + j < len) {
+          const float drx = bx - ps2[j].x, dry = by - ps2[j].y, drz = bz - ps2[j].z;
+          const float rr2 = drx * drx + dry * dry + drz * drz;
+          if (rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
+            q[(qh + n) & (kQCap - 1)][lane] = make_float4(drx, dry, drz, __uint_as_float(pini + t0 + j));
+            n++;
+          }
         }
       }
-      if (__any_sync(0xffffffffu, n == kQCap)) {
-        const int maxn = (int)__reduce_max_sync(0xffffffffu, (unsigned)n);
-        for (int e = 0; e < maxn; e++)
-          if (e < n) pair_fluid<tvisco, tdensity, boundp2>(c, a, ds, q[e][lane], vr1, ps1.w, inv_rho1, ta1, tb1, visco, massp2, r);
-        n = 0;
+      // rounds while enough lanes have work, or while some queue has no room
+      // for another unrolled group of checks
+      for (;;) {
+        const bool forced = __any_sync(0xffffffffu, n > kQCap - kQUnroll);
+        if (!forced && __popc(__ballot_sync(0xffffffffu, n > 0)) < kRoundMin) break;
+        pair_round<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ds, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
+                                                      massp2, r);
       }
     }
   }
-  const int maxn = (int)__reduce_max_sync(0xffffffffu, (unsigned)n);
-  for (int e = 0; e < maxn; e++)
-    if (e < n) pair_fluid<tvisco, tdensity, boundp2>(c, a, ds, q[e][lane], vr1, ps1.w, inv_rho1, ta1, tb1, visco, massp2, r);
+  while (__any_sync(0xffffffffu, n > 0))
+    pair_round<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ds, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
+                                                  massp2, r);
 }
 
-template <int tvisco, int tdensity>
-__global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, DevArrays a) {
+template <int tvisco, int tdensity, bool ddtgen>
+__global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, PairK k, DevArrays a) {
   __shared__ float4 qbuf[kQBlock / 32][kQCap][32];
   const DivState& d = *a.div;
   const unsigned np = d.np, npb = d.npb;
@@ -370,13 +447,13 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, DevA
     g = gb_grid((int)gb_cx(dcc, cel) - (int)d.cellmin[0], (int)gb_cy(dcc, cel) - (int)d.cellmin[1],
                 (int)gb_cz(dcc, cel) - (int)d.cellmin[2], c.cellmode_div, d);
   }
-  const float inv_rho1 = __frcp_rn(vr1.w);
+  const float inv_rho1 = gb_rcp(vr1.w);
   const DdtSeries ds = ddt_series(c.gamma);
   float4 (*q)[32] = qbuf[threadIdx.x >> 5];
   PairAcc ff = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   PairAcc fb = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  queued_pass<tvisco, tdensity, false>(c, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, ds, q, ff);
-  queued_pass<tvisco, tdensity, true>(c, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, ds, q, fb);
+  round_pass<tvisco, tdensity, false, ddtgen>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, ds, q, ff);
+  round_pass<tvisco, tdensity, true, ddtgen>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, ds, q, fb);
   float acemax2 = 0, visc = 0, vel2 = 0;
   if (active) {
     float ar = ff.ar + fb.ar;
@@ -488,9 +565,19 @@ __global__ void k_sps_tau(gbsph_consts c, DevArrays a) {
 
 // ---- mDBC ghost-node correction, SlipMode=vel0, 3-D -------------------------
 // JSphCpu_mdbc.cpp:36-160 (GPU twin KerInteractionMdbcCorrection_Fast,
-// JSphGpu_mdbc_iker.cu:34-151).  The 4x4 moment matrix is accumulated in
-// double as the CPU path does; the first-order system is solved by cofactor
-// expansion in double.
+// JSphGpu_mdbc_iker.cu:34-151).  The CPU path accumulates the 4x4 moment
+// matrix in double; here each entry is a compensated FP32 sum (TwoSum: the
+// rounding error of every addition is carried in a second float), which keeps
+// about 48 significant bits without FP64 adds.  The first-order system is
+// solved by cofactor expansion in double.
+__device__ __forceinline__ void gb_kadd(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bp = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+  hi = s;
+  lo = __fadd_rn(lo, e);
+}
+
 __device__ __forceinline__ double gb_det3(double a, double b, double cc, double d, double e, double f, double g,
                                           double h, double i) {
   return a * (e * i - f * h) - b * (d * i - f * g) + cc * (d * h - e * g);
@@ -514,8 +601,11 @@ __global__ void __launch_bounds__(128) k_mdbc(gbsph_consts c, DevArrays a) {
                              c.cellmode_div, d);
   const float scell = c.scell, ks2 = c.kernelsize2, h = c.kernelh;
   float rhop1 = 0, grx = 0, gry = 0, grz = 0;
-  double A[4][4];
-  for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) A[i][j] = 0.0;
+  float Ah[4][4], Al[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) Ah[i][j] = Al[i][j] = 0.f;
   for (int z = g.zini; z < g.zfin; z++) {
     for (int y = g.yini; y < g.yfin; y++) {
       const unsigned rowbase = d.boxfluid + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
@@ -544,15 +634,24 @@ __global__ void __launch_bounds__(128) k_mdbc(gbsph_consts c, DevArrays a) {
             rhop1 += massp2 * wab;
             grx += massp2 * frx; gry += massp2 * fry; grz += massp2 * frz;
             const float vwab = wab * volp2, vfrx = frx * volp2, vfry = fry * volp2, vfrz = frz * volp2;
-            A[0][0] += vwab; A[0][1] += drx * vwab; A[0][2] += dry * vwab; A[0][3] += drz * vwab;
-            A[1][0] += vfrx; A[1][1] += drx * vfrx; A[1][2] += dry * vfrx; A[1][3] += drz * vfrx;
-            A[2][0] += vfry; A[2][1] += drx * vfry; A[2][2] += dry * vfry; A[2][3] += drz * vfry;
-            A[3][0] += vfrz; A[3][1] += drx * vfrz; A[3][2] += dry * vfrz; A[3][3] += drz * vfrz;
+            const float rowv[4] = {vwab, vfrx, vfry, vfrz};
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+              gb_kadd(Ah[i][0], Al[i][0], rowv[i]);
+              gb_kadd(Ah[i][1], Al[i][1], __fmul_rn(drx, rowv[i]));
+              gb_kadd(Ah[i][2], Al[i][2], __fmul_rn(dry, rowv[i]));
+              gb_kadd(Ah[i][3], Al[i][3], __fmul_rn(drz, rowv[i]));
+            }
           }
         }
       }
     }
   }
+  double A[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) A[i][j] = (double)Ah[i][j] + (double)Al[i][j];
   // cofactors C[i][j]; inverse = C^T/det
   double C[4][4];
   for (int i = 0; i < 4; i++)
@@ -636,8 +735,21 @@ __global__ void k_pips(gbsph_consts c, DevArrays a) {
 
 template <int tvisco, int tdensity>
 void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s) {
-  if (variant == 1) k_forces_fluid<tvisco, tdensity><<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
-  else k_forces_fluid_q<tvisco, tdensity><<<gb_div_up(cap, kQBlock), kQBlock, 0, s>>>(c, a);
+  if (variant == 1) {
+    k_forces_fluid<tvisco, tdensity><<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+    return;
+  }
+  const PairK k = make_pairk(c);
+  const unsigned grid = gb_div_up(cap, kQBlock);
+  if constexpr (tdensity == GBSPH_DDT_DDT2 || tdensity == GBSPH_DDT_DDT2FULL) {
+    // the series form of the hydrostatic term holds for |ddtgz*drz| < 0.05 and
+    // |drz| <= 2h for every pair; otherwise the general power form is compiled in
+    if (!(fabsf(c.ddtgz) * c.kernelsize < 0.049f)) {
+      k_forces_fluid_q<tvisco, tdensity, true><<<grid, kQBlock, 0, s>>>(c, k, a);
+      return;
+    }
+  }
+  k_forces_fluid_q<tvisco, tdensity, false><<<grid, kQBlock, 0, s>>>(c, k, a);
 }
 
 template <int tvisco>
@@ -659,14 +771,18 @@ void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, 
   (void)bsize;
   cudaMemsetAsync(&a.st->acemax2, 0, 3 * sizeof(unsigned), s);
   k_forces_bound<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
-  // external records: inside a captured graph the events are recorded on every replay
-  if (ev_fluid_begin) cudaEventRecordWithFlags(ev_fluid_begin, s, cudaEventRecordExternal);
+  // inside a stream capture the records must be external nodes so that every
+  // replay of the graph records them; outside a capture they are plain records
+  cudaStreamCaptureStatus cap_st = cudaStreamCaptureStatusNone;
+  if (ev_fluid_begin || ev_fluid_end) cudaStreamIsCapturing(s, &cap_st);
+  const unsigned ev_flags = cap_st == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+  if (ev_fluid_begin) cudaEventRecordWithFlags(ev_fluid_begin, s, ev_flags);
   switch (c.tvisco) {
     case GBSPH_VISCO_ARTIFICIAL: launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, variant, s); break;
     case GBSPH_VISCO_LAMINAR: launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, variant, s); break;
     default: launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, variant, s); break;
   }
-  if (ev_fluid_end) cudaEventRecordWithFlags(ev_fluid_end, s, cudaEventRecordExternal);
+  if (ev_fluid_end) cudaEventRecordWithFlags(ev_fluid_end, s, ev_flags);
   if (nlaunch) *nlaunch += 2;
 }
 

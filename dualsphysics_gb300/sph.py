@@ -182,8 +182,8 @@ class GbSphSingle:
         return ms.value
 
     def set_option(self, key: int, value: int) -> None:
-        """Kernel options: key 0 = forces block size, key 1 = forces variant
-        (0 queued pair evaluation, 1 one-thread-per-particle walk)."""
+        """Kernel options: key 1 = fluid-row kernel (0 queued rounds, 1 one
+        thread per particle)."""
         self._check(lib().gbsph_set_option(self.ctx, key, value), "set_option")
 
     def graph_prepare(self, nsteps: int) -> None:

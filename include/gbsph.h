@@ -170,7 +170,11 @@ int gbsph_upload_device(gbsph_ctx* ctx, unsigned np, unsigned npb, const double*
 /* Profiling (JDsTimersGpu counterpart, JDsTimersGpu.h:29-71): with
  * max_launches>0, the next max_launches fluid Interaction_Forces launches are
  * bracketed by CUDA events on the context stream; gbsph_profile_read returns
- * their durations in ms and resets the counter.  0 disables profiling. */
+ * their durations in ms and resets the counter.  0 disables profiling.  The
+ * events of a launch captured into a graph are recorded on every replay, so
+ * after gbsph_run(ctx, n, 1) (one step captured, replayed n times) the read
+ * returns the launches of the last replay; gbsph_run(ctx, n, 2) holds all n
+ * steps and returns every launch. */
 int gbsph_profile(gbsph_ctx* ctx, unsigned max_launches);
 int gbsph_profile_read(gbsph_ctx* ctx, float* ms, unsigned cap, unsigned* n);
 /* Caller timing on the context stream: records event `slot` (0..15); elapsed
@@ -187,8 +191,9 @@ int gbsph_pips(gbsph_ctx* ctx, unsigned long long* out4);
 unsigned long long gbsph_launch_count(const gbsph_ctx* ctx);
 /* CUDA stream of the context (as void*), for callers that order their own work. */
 void* gbsph_stream(gbsph_ctx* ctx);
-/* Sets block sizes / tile options of the hot kernels (autotuner hook):
- * key 0 = forces block size, 1 = forces variant. */
+/* Kernel options (autotuner hook).  key 1 = fluid-row kernel of
+ * gbsph_forces: 0 (default) per-lane neighbour queues evaluated in rounds,
+ * 1 one thread per particle with no queue.  key 0 is accepted and ignored. */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
 
 #ifdef __cplusplus

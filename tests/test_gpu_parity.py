@@ -80,7 +80,7 @@ def test_forces_within_tolerance(name):
 @pytest.mark.parametrize("name", ["dbc_d04", "vel_d04", "sps_d04", "mdbc_d04"])
 @pytest.mark.parametrize("variant", [0, 1])
 def test_forces_variants_within_tolerance(name, variant):
-    """Both fluid-row kernels (queued pair evaluation / one thread per particle)."""
+    """Both fluid-row kernels: queued rounds (0), one thread per particle (1)."""
     cd = G.load_generated(name)
     s = _gpu(cd)
     s.set_option(1, variant)
@@ -257,3 +257,17 @@ def test_invalid_arguments_are_reported():
     assert b"capacity" in _lib.lib().gbsph_last_error(ctx)
     assert _lib.lib().gbsph_step(ctx) == -7  # GBSPH_ESTATE: nothing uploaded
     _lib.lib().gbsph_destroy(ctx)
+
+
+@pytest.mark.parametrize("use_graph", [0, 1])
+def test_profile_events_eager_and_graph(use_graph):
+    """gbsph_profile brackets the fluid-row launches: every launch when stepping
+    eagerly, the launches of the last replay of a one-step graph."""
+    cd = G.load_generated("dbc_d04")
+    s = _gpu(cd)
+    s.profile(8)
+    s.RunSteps(2, use_graph=use_graph)
+    s.sync()
+    ms = s.profile_read()
+    s.profile(0)
+    assert len(ms) == (4 if use_graph == 0 else 2) and all(t > 0 for t in ms)
