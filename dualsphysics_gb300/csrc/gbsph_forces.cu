@@ -221,6 +221,10 @@ struct PairK {
   float hinv;            // 1/h
   float ddt_kc;          // ddtkh * cs0
   float vfac_f, vfac_b;  // artificial: -visco*cs0; laminar: 4*visco (fluid / boundary neighbours)
+  // (1+t)^a - 1 = t*(c1 + t*(c2 + t*(c3 + t*(c4 + t*c5)))) + O(t^6), a = 1/gamma:
+  // the binomial series of the hydrostatic DDT2 term rho0*((1+ddtgz*drz)^(1/gamma)-1),
+  // which avoids the cancellation of pow()-1 (truncation below 1e-8 relative for |t| < 0.05)
+  float c1, c2, c3, c4, c5;
 };
 
 PairK make_pairk(const gbsph_consts& c) {
@@ -236,34 +240,24 @@ PairK make_pairk(const gbsph_consts& c) {
     k.vfac_f = 4.f * c.visco;
     k.vfac_b = 4.f * vb;
   }
+  const float ga = 1.f / c.gamma;
+  k.c1 = ga;
+  k.c2 = k.c1 * (ga - 1.f) * 0.5f;
+  k.c3 = k.c2 * (ga - 2.f) * (1.f / 3.f);
+  k.c4 = k.c3 * (ga - 3.f) * 0.25f;
+  k.c5 = k.c4 * (ga - 4.f) * 0.2f;
   return k;
 }
 
-// (1+t)^a - 1 for |t| < 0.05 by its binomial series (5 terms: relative
-// truncation error below 1e-8), used for the hydrostatic DDT2 correction
-// rho0*((1+ddtgz*drz)^(1/gamma)-1) without the cancellation of pow()-1.
-struct DdtSeries {
-  float c1, c2, c3, c4, c5;
-};
 
 // Reciprocal with a relative error of at most 2 ulp (__fdividef), used for the
 // 1/rho, 1/(r^2+eta^2) and 1/rhobar factors of the pair terms.
 __device__ __forceinline__ float gb_rcp(float x) { return __fdividef(1.f, x); }
 
-__device__ __forceinline__ DdtSeries ddt_series(float gamma) {
-  DdtSeries s;
-  const float a = 1.f / gamma;
-  s.c1 = a;
-  s.c2 = s.c1 * (a - 1.f) * 0.5f;
-  s.c3 = s.c2 * (a - 2.f) * (1.f / 3.f);
-  s.c4 = s.c3 * (a - 3.f) * 0.25f;
-  s.c5 = s.c4 * (a - 4.f) * 0.2f;
-  return s;
-}
 
 template <int tvisco, int tdensity, bool boundp2, bool ddtgen>
 __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k, const DevArrays& a,
-                                           const DdtSeries& ds, float4 e, float4 vr2, float p2press, float4 vr1,
+                                           float4 e, float4 vr2, float p2press, float4 vr1,
                                            float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
                                            float massp2, PairAcc& r) {
   const unsigned p2 = __float_as_uint(e.w);
@@ -294,7 +288,7 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
       const float t = c.ddtgz * drz;
       float drho;
       if (ddtgen && !(fabsf(t) < 0.05f)) drho = c.rhopzero * powf(1.f + t, 1.f / c.gamma) - c.rhopzero;
-      else drho = c.rhopzero * (t * (ds.c1 + t * (ds.c2 + t * (ds.c3 + t * (ds.c4 + t * ds.c5)))));
+      else drho = c.rhopzero * (t * (k.c1 + t * (k.c2 + t * (k.c3 + t * (k.c4 + t * k.c5)))));
       const float visc_densi = k.ddt_kc * ((vr2.w - vr1.w) - drho) * inv_r2eta;
       const float dot3 = drx * frx + dry * fry + drz * frz;
       r.delta -= visc_densi * dot3 * massp2 * inv_rho2;
@@ -338,7 +332,7 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
 // the loads of both neighbours issued before either pair's arithmetic.
 template <int tvisco, int tdensity, bool boundp2, bool ddtgen>
 __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k, const DevArrays& a,
-                                           const DdtSeries& ds, float4 (*q)[32], unsigned& qh, int& n, float4 vr1,
+                                           float4 (*q)[32], unsigned& qh, int& n, float4 vr1,
                                            float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
                                            float massp2, PairAcc& r) {
   const int lane = threadIdx.x & 31;
@@ -358,10 +352,10 @@ __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k
     pb = a.pscell[p2].w;
   }
   if (va)
-    pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ds, ea, wa, pa, vr1, p1press, inv_rho1, ta1, tb1, vfac,
+    pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ea, wa, pa, vr1, p1press, inv_rho1, ta1, tb1, vfac,
                                                   massp2, r);
   if (vb)
-    pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ds, eb, wb, pb, vr1, p1press, inv_rho1, ta1, tb1, vfac,
+    pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, eb, wb, pb, vr1, p1press, inv_rho1, ta1, tb1, vfac,
                                                   massp2, r);
   const int used = (int)va + (int)vb;
   qh = (qh + used) & (kQCap - 1);
@@ -373,7 +367,7 @@ __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k
 template <int tvisco, int tdensity, bool boundp2, bool ddtgen>
 __device__ __forceinline__ void round_pass(const gbsph_consts& c, const PairK& k, const DevArrays& a,
                                            const DivState& d, const CellGrid& g, bool active, float4 ps1,
-                                           float4 vr1, float inv_rho1, float4 ta1, float2 tb1, const DdtSeries& ds,
+                                           float4 vr1, float inv_rho1, float4 ta1, float2 tb1,
                                            float4 (*q)[32], PairAcc& r) {
   const int lane = threadIdx.x & 31;
   const unsigned cellinit = boundp2 ? 0u : d.boxfluid;
@@ -416,13 +410,13 @@ __device__ __forceinline__ void round_pass(const gbsph_consts& c, const PairK& k
       for (;;) {
         const bool forced = __any_sync(0xffffffffu, n > kQCap - kQUnroll);
         if (!forced && __popc(__ballot_sync(0xffffffffu, n > 0)) < kRoundMin) break;
-        pair_round<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ds, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
+        pair_round<tvisco, tdensity, boundp2, ddtgen>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
                                                       massp2, r);
       }
     }
   }
   while (__any_sync(0xffffffffu, n > 0))
-    pair_round<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ds, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
+    pair_round<tvisco, tdensity, boundp2, ddtgen>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
                                                   massp2, r);
 }
 
@@ -448,27 +442,24 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, Pair
                 (int)gb_cz(dcc, cel) - (int)d.cellmin[2], c.cellmode_div, d);
   }
   const float inv_rho1 = gb_rcp(vr1.w);
-  const DdtSeries ds = ddt_series(c.gamma);
   float4 (*q)[32] = qbuf[threadIdx.x >> 5];
   PairAcc ff = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  PairAcc fb = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  round_pass<tvisco, tdensity, false, ddtgen>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, ds, q, ff);
-  round_pass<tvisco, tdensity, true, ddtgen>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, ds, q, fb);
+  // one accumulator for both passes: the boundary pass adds to the fluid sums
+  // (and sets the DDT veto, FLT_MAX in delta, where it applies)
+  round_pass<tvisco, tdensity, false, ddtgen>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
+  round_pass<tvisco, tdensity, true, ddtgen>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
   float acemax2 = 0, visc = 0, vel2 = 0;
   if (active) {
-    float ar = ff.ar + fb.ar;
-    if (tdensity != GBSPH_DDT_NONE) {
-      const float dl = (ff.delta == FLT_MAX || fb.delta == FLT_MAX) ? FLT_MAX : ff.delta + fb.delta;
-      if (dl != FLT_MAX) ar += dl;
-    }
-    const float ax = ff.ax + fb.ax, ay = ff.ay + fb.ay, az = ff.az + fb.az;
+    float ar = ff.ar;
+    if (tdensity != GBSPH_DDT_NONE && ff.delta != FLT_MAX) ar += ff.delta;
+    const float ax = ff.ax, ay = ff.ay, az = ff.az;
     a.acear[p1] = make_float4(ax, ay, az, ar);
     if (tvisco == GBSPH_VISCO_LAMINARSPS) {
-      a.straina[p1] = make_float4(ff.s0 + fb.s0, ff.s1 + fb.s1, ff.s2 + fb.s2, ff.s3 + fb.s3);
-      a.strainb[p1] = make_float2(ff.s4 + fb.s4, ff.s5 + fb.s5);
+      a.straina[p1] = make_float4(ff.s0, ff.s1, ff.s2, ff.s3);
+      a.strainb[p1] = make_float2(ff.s4, ff.s5);
     }
     acemax2 = ax * ax + ay * ay + az * az;
-    visc = fmaxf(ff.visc, fb.visc);
+    visc = ff.visc;
     vel2 = vr1.x * vr1.x + vr1.y * vr1.y + vr1.z * vr1.z;
   }
   for (int o = 16; o; o >>= 1) {
