@@ -11,11 +11,16 @@ cell divisions, mDBC correction, dt reduction) of the whole particle set.
 * ``e2e``: steps/s through the C ABI as a caller drives it (gbsph_upload from
   host arrays, K x (gbsph_step + dt read-back, as the reference's Run loop
   reads TimeStep every step), gbsph_download of the final state), wall clock.
-* ``roofline``: the fluid Interaction_Forces kernel (the dominant one): each
-  launch is bracketed by CUDA events inside the timed region; algorithmic bytes
-  per launch = 32 B (neighbour position + velocity/density) per checked
-  neighbour of the fluid rows.  ``roofline_fp32`` states the same launches
-  against the FP32 FLOP model (80 FLOP per real fluid-row pair).
+* ``roofline``: the fluid Interaction_Forces kernel (the dominant one), each
+  launch bracketed by CUDA events inside the timed region.  Algorithmic bytes
+  per launch: 52 B per fluid row (pscell, velrho, dcell read; acear written)
+  plus 32 B per boundary particle (read once as a neighbour); ``traffic`` is
+  the DRAM bytes per launch from the ncu capture summarised in
+  profiles/k_forces_fluid_q_c2_dram.md.  The kernel is issue-bound, so its HBM
+  fraction is small by construction; ``roofline_fp32`` states the same
+  launches against the FP32 FLOP model (80 FLOP per real fluid-row pair) and
+  the nominal FFMA rate at the sampled SM clock, and ``gather_gbs`` the
+  neighbour bytes the checks read through L1/L2 (32 B per checked neighbour).
 * ``cpu_baseline``: the oracle (CPU restatement of the reference step, OpenMP
   on all host cores) timed on a bounded sample of the same state.
 * ``--impl reference``: the oracle port on the host cores as the reference arm.
@@ -40,6 +45,34 @@ sys.path.insert(0, ROOT)
 METRIC = "steps/s & particle-interactions/s on 1 GB300"
 FLOP_PER_FLUID_PAIR = 80.0  # Wendland + artificial visc + DDT2 + precomputed EOS
 BYTES_PER_CHECKED = 32.0    # pscell (16 B) + velrho (16 B) per checked neighbour
+BYTES_PER_FLUID_ROW = 52.0  # pscell 16 + velrho 16 + dcell 4 read, acear 16 written
+BYTES_PER_BOUND_NEIGHBOUR = 32.0  # pscell + velrho of a boundary particle, read once
+FP32_LANES_PER_SM = 128     # FFMA lanes per SM (2 FLOP each per clock)
+
+
+def _dram_traffic(dp: float):
+    """DRAM bytes per fluid-row launch from the committed ncu summary, when it
+    was captured on this workload."""
+    try:
+        vals = {}
+        with open(os.path.join(ROOT, "profiles", "k_forces_fluid_q_c2_dram.md")) as f:
+            for line in f:
+                if ":" in line and line.split(":")[0] in ("traffic_bytes_per_launch", "traffic_dp"):
+                    k, v = line.split(":", 1)
+                    vals[k] = float(v)
+        if abs(vals.get("traffic_dp", -1) - dp) < 1e-12:
+            return vals.get("traffic_bytes_per_launch")
+    except OSError:
+        pass
+    return None
+
+
+def _sm_count(dev: int) -> int:
+    try:
+        import torch
+        return int(torch.cuda.get_device_properties(dev).multi_processor_count)
+    except Exception:
+        return 152
 
 
 def _peaks():
@@ -215,8 +248,9 @@ def main():
     # roofline of the fluid Interaction_Forces kernel
     peaks, src = _peaks()
     kavg = float(np.mean(kms)) if len(kms) else float("nan")
-    bytes_launch = BYTES_PER_CHECKED * pi["checked_fluid"]
+    bytes_launch = BYTES_PER_FLUID_ROW * cd.nfluid + BYTES_PER_BOUND_NEIGHBOUR * cd.npb
     ach = bytes_launch / (kavg / 1e3) / 1e9
+    gather_gbs = BYTES_PER_CHECKED * pi["checked_fluid"] / (kavg / 1e3) / 1e9
     flops_launch = FLOP_PER_FLUID_PAIR * pi["real_fluid"]
     # e2e through the C ABI with host buffers
     s.close()
@@ -245,6 +279,11 @@ def main():
         cpu = {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": cores, "kind": "port",
                "sample": f"one oracle step of the same state with 1/{args.cpu_stride} of the interaction rows, "
                          f"full step time extrapolated"}
+    clks = clk.summary()
+    traffic = _dram_traffic(args.dp)
+    fp32_peak = None
+    if clks.get("sm_mhz"):
+        fp32_peak = _sm_count(local) * FP32_LANES_PER_SM * 2 * clks["sm_mhz"] * 1e6 / 1e12
     if rank == 0:
         line = {
             "metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -260,12 +299,16 @@ def main():
             "particle_interactions_per_step": pis_per_step,
             "np_after": info["np"],
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": ach / peaks["hbm_gbs"], "traffic": None,
-                         "kernel": "k_forces_fluid", "model": "gather: 32 B per checked fluid-row neighbour",
-                         "peak_source": src, "launch_ms": kavg, "launches_timed": int(len(kms))},
-            "roofline_fp32": {"achieved_tflops": flops_launch / (kavg / 1e3) / 1e12,
-                              "model": "80 FLOP per real fluid-row pair"},
-            "clocks": clk.summary(),
+                         "frac": ach / peaks["hbm_gbs"], "traffic": traffic,
+                         "kernel": "k_forces_fluid_q",
+                         "model": "52 B per fluid row + 32 B per boundary neighbour per launch",
+                         "peak_source": src, "launch_ms": kavg, "launches_timed": int(len(kms)),
+                         "gather_gbs": gather_gbs},
+            "roofline_fp32": {"achieved_tflops": flops_launch / (kavg / 1e3) / 1e12, "peak_tflops": fp32_peak,
+                              "frac": flops_launch / (kavg / 1e3) / 1e12 / fp32_peak if fp32_peak else None,
+                              "model": "80 FLOP per real fluid-row pair",
+                              "peak_source": "nominal FFMA rate (SMs x 128 lanes x 2 FLOP) at the sampled SM clock"},
+            "clocks": clks,
             "gpu_launches": int(launches),
             "e2e": e2e,
             "cpu_baseline": cpu,
