@@ -1,0 +1,111 @@
+"""The gbsph_run driver: the C++ host side above the C ABI (the Run loop of
+JSphGpuSingle, JSphGpuSingle.cpp:950-1052, and the Part_%04u.bi4 writer of
+JSph::SaveData, JSph.cpp:3062-3110).
+
+* CPU: the driver's case loader (run XML + Case.bi4) reads the same case as the
+  Python loader and derives the same constants (`-info`, no device touched);
+  bad command lines and missing cases fail with the reference's exception line.
+* GPU: the driver and the Python host loop (GbSphSingle.Run) write identical
+  Part files for the same case and end time.
+"""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import goldens as G
+from dualsphysics_gb300 import _lib, bi4
+from dualsphysics_gb300 import casegen as cg
+from dualsphysics_gb300.case import load_case
+from dualsphysics_gb300.sph import GbSphSingle
+
+DRIVER = os.path.join(G.ROOT, "dualsphysics_gb300", "gbsph_run")
+
+
+def _driver():
+    if not os.path.exists(DRIVER):
+        pytest.fail("gbsph_run is not built (run __graft_entry__.build())")
+    return DRIVER
+
+
+def _write_case(tmp_path, name):
+    spec = G.case_spec(name)
+    cg.write_case(cg.make_dam_break(spec), str(tmp_path))
+    return spec.name
+
+
+@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "sps_d04", "verlet_d04"])
+def test_driver_case_summary_matches_python_loader(tmp_path, name):
+    cn = _write_case(tmp_path, name)
+    out = subprocess.run([_driver(), str(tmp_path / cn), str(tmp_path / "out"), "-info"], capture_output=True,
+                         text=True, check=True, timeout=120)
+    info = json.loads(out.stdout)
+    cd = load_case(str(tmp_path), cn)
+    pc = _lib.config(cd.params)
+    assert (info["np"], info["npb"]) == (len(cd.idp), cd.npb)
+    assert (info["h"], info["b"], info["dp"]) == (cd.params.h, cd.params.b, cd.params.dp)
+    assert info["maprealposmin"] == list(cd.params.maprealposmin)
+    assert info["maprealposmax"] == list(cd.params.maprealposmax)
+    assert np.float32(info["kernelsize2"]) == np.float32(pc.kernelsize2)
+    assert info["cs0"] == pc.cs0
+    assert info["domcellcode"] == pc.domcellcode
+    assert info["mapcells"] == list(pc.mapcells)
+    assert (info["tboundary"], info["tstep"], info["tdensity"], info["tvisco"]) == \
+        (pc.tboundary, pc.tstep, pc.tdensity, pc.tvisco)
+    # the particle arrays: exact integer sums, float sums to rounding of the order
+    assert info["idsum"] == float(cd.idp.astype(np.float64).sum())
+    assert info["codesum"] == float(cd.code.astype(np.float64).sum())
+    assert info["possum"] == pytest.approx(float(cd.pos.sum()), rel=1e-12)
+    assert info["rhosum"] == pytest.approx(float(cd.velrho[:, 3].astype(np.float64).sum()), rel=1e-12)
+    nor = 0.0 if cd.boundnor is None else float(cd.boundnor.astype(np.float64).sum())
+    assert info["norsum"] == pytest.approx(nor, rel=1e-9, abs=1e-9)
+
+
+def test_driver_rejects_unknown_option_and_missing_case(tmp_path):
+    cn = _write_case(tmp_path, "dbc_d04")
+    r = subprocess.run([_driver(), str(tmp_path / cn), str(tmp_path / "out"), "-bogus"], capture_output=True,
+                       text=True, timeout=60)
+    assert r.returncode == 1 and "*** Exception" in r.stderr and "-bogus" in r.stderr
+    r = subprocess.run([_driver(), str(tmp_path / "NoSuchCase"), str(tmp_path / "out"), "-info"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "LoadCase" in r.stderr
+    r = subprocess.run([_driver()], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "usage" in r.stderr
+
+
+def _parts(dirout):
+    d = os.path.join(dirout, "data")
+    return sorted(f for f in os.listdir(d) if f.startswith("Part_") and f.endswith(".bi4"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04"])
+def test_driver_parts_equal_python_run(tmp_path, name):
+    """gbsph_run and GbSphSingle.Run step the same case to the same end time
+    and write bit-identical particle data in every Part file."""
+    cn = _write_case(tmp_path, name)
+    tmax = 0.012
+    d_out, p_out = str(tmp_path / "drv"), str(tmp_path / "py")
+    r = subprocess.run([_driver(), str(tmp_path / cn), d_out, f"-tmax:{tmax}", "-sv:bi4"], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert "Steps per second" in r.stdout
+    s = GbSphSingle(0)
+    res = s.Run(str(tmp_path), cn, p_out, time_max=tmax)
+    s.close()
+    dp, pp = _parts(d_out), _parts(p_out)
+    assert dp == pp and len(dp) >= 2, (dp, pp)
+    for f in dp:
+        a = bi4.read(os.path.join(d_out, "data", f), "JPartDataBi4")
+        b = bi4.read(os.path.join(p_out, "data", f), "JPartDataBi4")
+        ka = [it.name for it in a.items if it.name.startswith("PART_")]
+        assert ka == [it.name for it in b.items if it.name.startswith("PART_")] and len(ka) == 1
+        pa, pb = a.item(ka[0]), b.item(ka[0])
+        assert pa.get("Step") == pb.get("Step") and pa.get("TimeStep") == pb.get("TimeStep")
+        for arr in ("Idp", "Vel", "Rhop"):
+            np.testing.assert_array_equal(pa.array(arr), pb.array(arr), err_msg=f"{f}: {arr}")
+        posname = "Posd" if "Posd" in pa.arrays else "Pos"
+        np.testing.assert_array_equal(pa.array(posname), pb.array(posname), err_msg=f"{f}: {posname}")
+    assert res["steps"] > 0
