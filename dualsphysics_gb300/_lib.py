@@ -103,7 +103,10 @@ SIGNATURES = {
     "gbsph_mark": (C.c_int, [P, C.c_uint]),
     "gbsph_elapsed": (C.c_int, [P, C.c_uint, C.c_uint, C.POINTER(C.c_float)]),
     "gbsph_pips": (C.c_int, [P, C.POINTER(C.c_ulonglong * 4)]),
+    "gbsph_sort_keys_noalloc": (C.c_int, [P, P, C.c_uint, C.c_uint, P, P]),
 }
+
+SORT_NOALLOC_MAX_KEYS = 262144  # GBSPH_SORT_NOALLOC_MAX_KEYS
 
 _lib = None
 _lock = threading.Lock()

@@ -12,6 +12,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -523,6 +524,37 @@ int gbsph_profile_read(gbsph_ctx* ctx, float* ms, unsigned cap, unsigned* n) {
   *n = cnt;
   ctx->prof_n = 0;
   return GBSPH_OK;
+}
+
+// Work area of gbsph_sort_keys_noalloc: its device address per device, looked
+// up by the first call made for that device (with that device current).
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_na_mutex;
+void* g_na_work[kMaxDevices] = {};
+}  // namespace
+
+int gbsph_sort_keys_noalloc(gbsph_ctx* ctx, const unsigned* d_keys, unsigned n, unsigned nbits, unsigned* d_perm,
+                            unsigned* d_sorted_keys) {
+  if (!ctx) return GBSPH_EINVAL;
+  if (!d_keys || !d_perm) return set_err(ctx, GBSPH_EINVAL, "gbsph_sort_keys_noalloc: null key or permutation pointer");
+  if (nbits < 1 || nbits > 32) return set_err(ctx, GBSPH_EINVAL, "gbsph_sort_keys_noalloc: nbits=%u is not in 1..32", nbits);
+  const unsigned maxkeys = gbk::sort_noalloc_max_keys();
+  if (n > maxkeys)
+    return set_err(ctx, GBSPH_ECAPACITY, "gbsph_sort_keys_noalloc: n=%u keys exceed the fixed work area of %u keys", n,
+                   maxkeys);
+  if (ctx->device < 0 || ctx->device >= kMaxDevices)
+    return set_err(ctx, GBSPH_EINVAL, "gbsph_sort_keys_noalloc: device %d out of range", ctx->device);
+  CK(cudaSetDevice(ctx->device), "set device");
+  void* work = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_work[ctx->device]) CK(gbk::sort_noalloc_address(&g_na_work[ctx->device]), "work-area address");
+    work = g_na_work[ctx->device];
+  }
+  if (n == 0) return GBSPH_OK;
+  gbk::sort_noalloc((unsigned char*)work, d_keys, n, nbits, d_perm, d_sorted_keys, ctx->stream);
+  return cuda_check(ctx, cudaGetLastError(), "gbsph_sort_keys_noalloc");
 }
 
 int gbsph_pips(gbsph_ctx* ctx, unsigned long long* out4) {

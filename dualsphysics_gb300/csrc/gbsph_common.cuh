@@ -117,6 +117,13 @@ __host__ __device__ __forceinline__ unsigned gb_div_up(unsigned a, unsigned b) {
 namespace gbk {
 void load_dcell(const gbsph_consts& c, const DevArrays& a, unsigned n, cudaStream_t s);  // sets GB_ERR_PARTOUT in DivState::error
 void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses, cudaStream_t s, unsigned long long* nlaunch);
+// Stable sort of n <= sort_noalloc_max_keys() keys of nbits bits on the static
+// work area (work = its device address, from sort_noalloc_address on the
+// current device).
+unsigned sort_noalloc_max_keys();
+cudaError_t sort_noalloc_address(void** p);
+void sort_noalloc(unsigned char* work, const unsigned* keys, unsigned n, unsigned nbits, unsigned* perm,
+                  unsigned* sorted_keys, cudaStream_t s);
 void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, cudaStream_t s, unsigned long long* nlaunch,
             cudaEvent_t ev_fluid_begin = nullptr, cudaEvent_t ev_fluid_end = nullptr);
 void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch);

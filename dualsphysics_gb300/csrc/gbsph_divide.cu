@@ -477,3 +477,82 @@ void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses,
 }
 
 }  // namespace gbk
+
+// ---- no-alloc sort: the radix sort of the cell division on a fixed work area
+// Some callers cannot let a library call cudaMalloc/cudaFree: a host
+// application that sized its own device pool at start-up and treats any other
+// device allocation as an error, or a caller on a latency-bound path where an
+// allocation (and the device synchronisation cudaFree implies) would stall its
+// other streams.  For them the stable key sort of the cell division is also
+// offered on a work area that exists from module load on: a file-scope
+// __device__ array sized for kNoAllocMaxKeys keys.  Its device address is
+// looked up once per device; nothing is allocated afterwards.  There is one
+// work area per process and device, so two calls that overlap in time (two
+// host threads, or two streams) race on it: callers must serialise them.
+namespace {
+
+constexpr unsigned kNoAllocMaxKeys = 1u << 18;  // 262,144 keys (4.3 MB of work area)
+constexpr unsigned kNoAllocTiles = kNoAllocMaxKeys / kSortTile;
+constexpr size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kNaDiv = 0;                                           // DivState: ini / nptot of the sort
+constexpr size_t kNaKeysA = na_align(sizeof(DivState));
+constexpr size_t kNaKeysB = kNaKeysA + na_align(sizeof(unsigned) * kNoAllocMaxKeys);
+constexpr size_t kNaValsA = kNaKeysB + na_align(sizeof(unsigned) * kNoAllocMaxKeys);
+constexpr size_t kNaValsB = kNaValsA + na_align(sizeof(unsigned) * kNoAllocMaxKeys);
+constexpr size_t kNaHist = kNaValsB + na_align(sizeof(unsigned) * kNoAllocMaxKeys);
+constexpr size_t kNaBytes = kNaHist + na_align(sizeof(unsigned) * ((size_t)kNoAllocTiles * kRadix + kRadix + 1));
+
+static __device__ __align__(256) unsigned char g_sort_work[kNaBytes];
+
+// Puts the work area in its starting state: the sort record cleared and set
+// to the range [0, n), and the values set to the identity permutation (the
+// values the first pass reads).  The histogram needs no clearing: every pass
+// writes all of it before reading it.
+__global__ void k_na_init(DivState* d, unsigned* vals, unsigned n) {
+  const unsigned i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i0 == 0) {
+    *d = DivState{};
+    d->ini = 0;
+    d->nptot = n;
+  }
+  for (unsigned i = i0; i < n; i += gridDim.x * blockDim.x) vals[i] = i;
+}
+
+}  // namespace
+
+namespace gbk {
+
+unsigned sort_noalloc_max_keys() { return kNoAllocMaxKeys; }
+
+// Device address of the work area on the current device.
+cudaError_t sort_noalloc_address(void** p) { return cudaGetSymbolAddress(p, g_sort_work); }
+
+void sort_noalloc(unsigned char* work, const unsigned* keys, unsigned n, unsigned nbits, unsigned* perm,
+                  unsigned* sorted_keys, cudaStream_t s) {
+  DivState* d = (DivState*)(work + kNaDiv);
+  unsigned* keys_a = (unsigned*)(work + kNaKeysA);
+  unsigned* keys_b = (unsigned*)(work + kNaKeysB);
+  unsigned* vals_a = (unsigned*)(work + kNaValsA);
+  unsigned* vals_b = (unsigned*)(work + kNaValsB);
+  unsigned* hist = (unsigned*)(work + kNaHist);
+  const unsigned ntiles = gb_div_up(n, kSortTile);
+  k_na_init<<<gb_div_up(n, kDivBlock), kDivBlock, 0, s>>>(d, vals_a, n);
+  const unsigned npasses = gb_div_up(nbits, kRadixBits);
+  const unsigned* kin = keys;
+  const unsigned* vin = vals_a;
+  for (unsigned pass = 0; pass < npasses; pass++) {
+    const int shift = (int)(pass * kRadixBits);
+    unsigned* kout = (pass & 1) ? keys_b : keys_a;
+    unsigned* vout = (pass & 1) ? vals_a : vals_b;
+    k_rs_hist<<<ntiles, kSortBlock, 0, s>>>(kin, hist, d, ntiles, shift);
+    k_rs_scan_cols<<<kRadix, 256, 0, s>>>(hist, hist + (size_t)kRadix * ntiles, ntiles);
+    k_rs_scan_digits<<<1, kRadix, 0, s>>>(hist + (size_t)kRadix * ntiles);
+    k_rs_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, hist, d, ntiles, shift);
+    kin = kout;
+    vin = vout;
+  }
+  cudaMemcpyAsync(perm, vin, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, s);
+  if (sorted_keys) cudaMemcpyAsync(sorted_keys, kin, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, s);
+}
+
+}  // namespace gbk

@@ -182,6 +182,27 @@ int gbsph_profile_read(gbsph_ctx* ctx, float* ms, unsigned cap, unsigned* n);
 int gbsph_mark(gbsph_ctx* ctx, unsigned slot);
 int gbsph_elapsed(gbsph_ctx* ctx, unsigned a, unsigned b, float* ms);
 
+/* No-alloc key sort.  This entry has no counterpart in the reference: it
+ * offers the stable radix sort of the cell division (the sort behind
+ * gbsph_divide) on a fixed work area that the library holds from load time
+ * (a static device array), for callers that must not see a device allocation
+ * or free during the call -- a host application that owns a pre-sized device
+ * pool, or a latency-bound caller that cannot absorb the device
+ * synchronisation of cudaFree.
+ *   d_keys: n keys in device memory, nbits significant bits (1..32);
+ *   d_perm: receives, for each sorted slot, the index of its key (ties keep
+ *           the input order); d_sorted_keys (may be NULL) the sorted keys.
+ * n is limited to GBSPH_SORT_NOALLOC_MAX_KEYS; larger n returns
+ * GBSPH_ECAPACITY with a message in gbsph_last_error.  The work runs on the
+ * context stream; the results are ready when that stream reaches them.  The
+ * first call for a device looks the work area up (cudaGetSymbolAddress with
+ * that device current) and should come before any stream capture.  There is
+ * one work area per process and device: calls that overlap in time (from two
+ * threads or two streams) race on it and must be serialised by the caller. */
+#define GBSPH_SORT_NOALLOC_MAX_KEYS 262144u
+int gbsph_sort_keys_noalloc(gbsph_ctx* ctx, const unsigned* d_keys, unsigned n, unsigned nbits, unsigned* d_perm,
+                            unsigned* d_sorted_keys);
+
 /* Particle-interaction count of the current state with the reference's PIPS
  * definition (JDsPips.cpp:187-260): out4 = {checked bound-row pairs, real
  * bound-row pairs, checked fluid-row pairs, real fluid-row pairs}. */
