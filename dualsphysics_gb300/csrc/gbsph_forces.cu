@@ -197,15 +197,18 @@ __global__ void __launch_bounds__(128) k_forces_fluid(gbsph_consts c, DevArrays 
 // candidates per particle in 27 cells of size 2h) runs in lock step over the
 // 27 cells; the ~290 candidates per particle that pass it are queued per lane
 // in shared memory (relative position + index), a ring of kQCap entries.  The
-// pair terms (the expensive part) run in rounds: one round evaluates the two
-// oldest entries of every lane with a non-empty queue, and rounds are taken when at
-// least kRoundMin lanes have work (or when a queue could not take another
-// unrolled group of checks), so the pair body runs with most lanes active.
+// pair terms (the expensive part) run in rounds: one round evaluates up to
+// kRoundEntries of the oldest entries of every lane, and rounds are taken when
+// kRoundLanes lanes hold that many (or when a queue could not take another
+// unrolled group of checks), so the pair body runs with the lanes active.
+// The checks and the viscosity term are written without branches: a warp
+// nearly always has lanes on both sides of those tests.
 // Summation order per particle is the candidate order.
 constexpr int kQCap = 16;
 constexpr int kQBlock = 128;
 constexpr int kQUnroll = 4;
-constexpr int kRoundMin = 24;
+constexpr int kRoundEntries = 2;  // entries a lane evaluates per round
+constexpr int kRoundLanes = 32;   // lanes that must hold kRoundEntries entries for a round
 
 struct PairAcc {
   float ax, ay, az, ar, delta, visc;
@@ -281,7 +284,9 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
     const float dot3 = drx * frx + dry * fry + drz * frz;
     r.delta = (boundp2 && c.tboundary == GBSPH_BC_DBC) ? FLT_MAX : r.delta + visc_densi * dot3 * massp2;
   }
-  if ((tdensity == GBSPH_DDT_DDT2 || (tdensity == GBSPH_DDT_DDT2FULL && !boundp2)) && r.delta != FLT_MAX) {
+  if (tdensity == GBSPH_DDT_DDT2 || (tdensity == GBSPH_DDT_DDT2FULL && !boundp2)) {
+    // the fluid neighbours are visited first, so only the boundary pass can
+    // meet the veto (and it sets it: DDT2 leaves particles next to the boundary out)
     if (boundp2) {
       r.delta = FLT_MAX;
     } else {
@@ -299,12 +304,12 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
   const float dot_rr2 = dot * inv_r2eta;
   r.visc = fmaxf(dot_rr2, r.visc);
   if (tvisco == GBSPH_VISCO_ARTIFICIAL) {
-    if (dot < 0) {
-      const float amubar = c.kernelh * dot_rr2;
-      const float robar = (vr1.w + vr2.w) * 0.5f;
-      const float pi_visc = (vfac * amubar * gb_rcp(robar)) * massp2;
-      r.ax -= pi_visc * frx; r.ay -= pi_visc * fry; r.az -= pi_visc * frz;
-    }
+    // applied for approaching pairs (dot < 0); evaluated for every pair and
+    // selected, since nearly every warp has lanes on both sides of the test
+    const float amubar = c.kernelh * dot_rr2;
+    const float robar = (vr1.w + vr2.w) * 0.5f;
+    const float pi_visc = dot < 0 ? (vfac * amubar * gb_rcp(robar)) * massp2 : 0.f;
+    r.ax -= pi_visc * frx; r.ay -= pi_visc * fry; r.az -= pi_visc * frz;
   } else {
     const float robar2 = vr1.w + vr2.w;
     const float temp = vfac * inv_r2eta * gb_rcp(robar2);
@@ -330,13 +335,13 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
 
 // One round: every lane evaluates up to two of its oldest queued pairs, with
 // the loads of both neighbours issued before either pair's arithmetic.
-template <int tvisco, int tdensity, bool boundp2, bool ddtgen>
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, int E>
 __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k, const DevArrays& a,
                                            float4 (*q)[32], unsigned& qh, int& n, float4 vr1,
                                            float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
                                            float massp2, PairAcc& r) {
   const int lane = threadIdx.x & 31;
-  const bool va = n > 0, vb = n > 1;
+  const bool va = n > 0, vb = E > 1 && n > 1;
   float4 ea = make_float4(0, 0, 0, 0), eb = ea, wa = make_float4(0, 0, 0, 1), wb = wa;
   float pa = 0, pb = 0;
   if (va) {
@@ -345,7 +350,7 @@ __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k
     wa = a.velrho[p2];
     pa = a.pscell[p2].w;
   }
-  if (vb) {
+  if (E > 1 && vb) {
     eb = q[(qh + 1) & (kQCap - 1)][lane];
     const unsigned p2 = __float_as_uint(eb.w);
     wb = a.velrho[p2];
@@ -354,7 +359,7 @@ __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k
   if (va)
     pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ea, wa, pa, vr1, p1press, inv_rho1, ta1, tb1, vfac,
                                                   massp2, r);
-  if (vb)
+  if (E > 1 && vb)
     pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, eb, wb, pb, vr1, p1press, inv_rho1, ta1, tb1, vfac,
                                                   massp2, r);
   const int used = (int)va + (int)vb;
@@ -364,7 +369,7 @@ __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k
 
 // One pass of the fluid rows over the fluid (boundp2=false) or boundary
 // (boundp2=true) boxes of the 27 neighbour cells.
-template <int tvisco, int tdensity, bool boundp2, bool ddtgen>
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, int E, int F>
 __device__ __forceinline__ void round_pass(const gbsph_consts& c, const PairK& k, const DevArrays& a,
                                            const DivState& d, const CellGrid& g, bool active, float4 ps1,
                                            float4 vr1, float inv_rho1, float4 ta1, float2 tb1,
@@ -390,37 +395,35 @@ __device__ __forceinline__ void round_pass(const gbsph_consts& c, const PairK& k
     const unsigned maxlen = __reduce_max_sync(0xffffffffu, len);
     const float bx = ps1.x - (float)dx * scell, by = ps1.y - (float)dy * scell, bz = ps1.z - (float)dz * scell;
     for (unsigned t0 = 0; t0 < maxlen; t0 += kQUnroll) {
+      // slots past the lane's own cell read particle 0 (always valid) and are masked
       float4 ps2[kQUnroll];
 #pragma unroll
-      for (int j = 0; j < kQUnroll; j++)
-        if (t0 + j < len) ps2[j] = a.pscell[pini + t0 + j];
+      for (int j = 0; j < kQUnroll; j++) ps2[j] = a.pscell[(t0 + j < len) ? pini + t0 + j : 0u];
 #pragma unroll
       for (int j = 0; j < kQUnroll; j++) {
-        if (t0 + j < len) {
-          const float drx = bx - ps2[j].x, dry = by - ps2[j].y, drz = bz - ps2[j].z;
-          const float rr2 = drx * drx + dry * dry + drz * drz;
-          if (rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
-            q[(qh + n) & (kQCap - 1)][lane] = make_float4(drx, dry, drz, __uint_as_float(pini + t0 + j));
-            n++;
-          }
+        const float drx = bx - ps2[j].x, dry = by - ps2[j].y, drz = bz - ps2[j].z;
+        const float rr2 = drx * drx + dry * dry + drz * drz;
+        if (t0 + j < len && rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
+          q[(qh + n) & (kQCap - 1)][lane] = make_float4(drx, dry, drz, __uint_as_float(pini + t0 + j));
+          n++;
         }
       }
       // rounds while enough lanes have work, or while some queue has no room
       // for another unrolled group of checks
       for (;;) {
         const bool forced = __any_sync(0xffffffffu, n > kQCap - kQUnroll);
-        if (!forced && __popc(__ballot_sync(0xffffffffu, n > 0)) < kRoundMin) break;
-        pair_round<tvisco, tdensity, boundp2, ddtgen>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
+        if (!forced && __popc(__ballot_sync(0xffffffffu, n >= E)) < F) break;
+        pair_round<tvisco, tdensity, boundp2, ddtgen, E>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
                                                       massp2, r);
       }
     }
   }
   while (__any_sync(0xffffffffu, n > 0))
-    pair_round<tvisco, tdensity, boundp2, ddtgen>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
+    pair_round<tvisco, tdensity, boundp2, ddtgen, E>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
                                                   massp2, r);
 }
 
-template <int tvisco, int tdensity, bool ddtgen>
+template <int tvisco, int tdensity, bool ddtgen, int E = kRoundEntries, int F = kRoundLanes>
 __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, PairK k, DevArrays a) {
   __shared__ float4 qbuf[kQBlock / 32][kQCap][32];
   const DivState& d = *a.div;
@@ -446,8 +449,8 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, Pair
   PairAcc ff = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   // one accumulator for both passes: the boundary pass adds to the fluid sums
   // (and sets the DDT veto, FLT_MAX in delta, where it applies)
-  round_pass<tvisco, tdensity, false, ddtgen>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
-  round_pass<tvisco, tdensity, true, ddtgen>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
+  round_pass<tvisco, tdensity, false, ddtgen, E, F>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
+  round_pass<tvisco, tdensity, true, ddtgen, E, F>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
   float acemax2 = 0, visc = 0, vel2 = 0;
   if (active) {
     float ar = ff.ar;
