@@ -367,6 +367,22 @@ __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k
   n -= used;
 }
 
+// Candidate range of neighbour cell `ci` for this lane (empty outside the
+// trimmed domain).
+__device__ __forceinline__ void cell_range(const DevArrays& a, const DivState& d, const CellGrid& g, bool active,
+                                           unsigned cellinit, int ci, int sd, int side, unsigned& pini,
+                                           unsigned& len) {
+  const int dz = ci / (side * side) - sd, dy = (ci / side) % side - sd, dx = ci % side - sd;
+  const int x = g.cx + dx, y = g.cy + dy, z = g.cz + dz;
+  pini = 0;
+  len = 0;
+  if (active && x >= g.xini && x < g.xfin && y >= g.yini && y < g.yfin && z >= g.zini && z < g.zfin) {
+    const unsigned box = cellinit + (unsigned)x + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+    pini = a.begincell[box];
+    len = a.begincell[box + 1] - pini;
+  }
+}
+
 // One pass of the fluid rows over the fluid (boundp2=false) or boundary
 // (boundp2=true) boxes of the 27 neighbour cells.
 template <int tvisco, int tdensity, bool boundp2, bool ddtgen, int E, int F>
@@ -379,32 +395,55 @@ __device__ __forceinline__ void round_pass(const gbsph_consts& c, const PairK& k
   const float scell = c.scell, ks2 = c.kernelsize2;
   const float vfac = boundp2 ? k.vfac_b : k.vfac_f;
   const float massp2 = boundp2 ? c.massbound : c.massfluid;
-  const int sd = c.cellmode_div, side = 2 * sd + 1, ncell = side * side * side;
+  const int sd = c.cellmode_div, side = 2 * sd + 1, ncell = side * side * side, centre = ncell / 2;
   int n = 0;
   unsigned qh = 0;
-  for (int ci = 0; ci < ncell; ci++) {
-    const int dz = ci / (side * side) - sd, dy = (ci / side) % side - sd, dx = ci % side - sd;
-    const int x = g.cx + dx, y = g.cy + dy, z = g.cz + dz;
-    const bool valid = active && x >= g.xini && x < g.xfin && y >= g.yini && y < g.yfin && z >= g.zini && z < g.zfin;
-    unsigned pini = 0, len = 0;
-    if (valid) {
-      const unsigned box = cellinit + (unsigned)x + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
-      pini = a.begincell[box];
-      len = a.begincell[box + 1] - pini;
+  // The neighbour cells are taken two ranges at a time -- the centre cell split
+  // in halves, then each cell with its mirror image through the centre -- and
+  // half of every unrolled group of checks is drawn from either range.  A
+  // particle near one face of its cell finds many neighbours in the cells on
+  // that side and few on the opposite one; drawing from both sides at once
+  // keeps the lanes' queues filling at similar rates, so rounds find more
+  // lanes with work.
+  for (int step = 0; step <= centre; step++) {
+    const int cia = step == 0 ? centre : step - 1, cib = ncell - 1 - cia;
+    unsigned pa, la, pb, lb;
+    cell_range(a, d, g, active, cellinit, cia, sd, side, pa, la);
+    if (step == 0) {
+      const unsigned half = (la + 1) / 2;
+      pb = pa + half;
+      lb = la - half;
+      la = half;
+    } else {
+      cell_range(a, d, g, active, cellinit, cib, sd, side, pb, lb);
     }
-    const unsigned maxlen = __reduce_max_sync(0xffffffffu, len);
-    const float bx = ps1.x - (float)dx * scell, by = ps1.y - (float)dy * scell, bz = ps1.z - (float)dz * scell;
-    for (unsigned t0 = 0; t0 < maxlen; t0 += kQUnroll) {
-      // slots past the lane's own cell read particle 0 (always valid) and are masked
+    const unsigned maxlen = __reduce_max_sync(0xffffffffu, la > lb ? la : lb);
+    const int dza = cia / (side * side) - sd, dya = (cia / side) % side - sd, dxa = cia % side - sd;
+    const int dzb = cib / (side * side) - sd, dyb = (cib / side) % side - sd, dxb = cib % side - sd;
+    const float bax = ps1.x - (float)dxa * scell, bay = ps1.y - (float)dya * scell, baz = ps1.z - (float)dza * scell;
+    const float bbx = ps1.x - (float)dxb * scell, bby = ps1.y - (float)dyb * scell, bbz = ps1.z - (float)dzb * scell;
+    for (unsigned t0 = 0; t0 < maxlen; t0 += kQUnroll / 2) {
+      // slots past a range's end read particle 0 (always valid) and are masked
       float4 ps2[kQUnroll];
-#pragma unroll
-      for (int j = 0; j < kQUnroll; j++) ps2[j] = a.pscell[(t0 + j < len) ? pini + t0 + j : 0u];
+      unsigned idx[kQUnroll];
+      bool in[kQUnroll];
 #pragma unroll
       for (int j = 0; j < kQUnroll; j++) {
-        const float drx = bx - ps2[j].x, dry = by - ps2[j].y, drz = bz - ps2[j].z;
+        const bool fromb = j >= kQUnroll / 2;
+        const unsigned t = t0 + (unsigned)(fromb ? j - kQUnroll / 2 : j);
+        in[j] = t < (fromb ? lb : la);
+        idx[j] = in[j] ? (fromb ? pb : pa) + t : 0u;
+        ps2[j] = a.pscell[idx[j]];
+      }
+#pragma unroll
+      for (int j = 0; j < kQUnroll; j++) {
+        const bool fromb = j >= kQUnroll / 2;
+        const float drx = (fromb ? bbx : bax) - ps2[j].x;
+        const float dry = (fromb ? bby : bay) - ps2[j].y;
+        const float drz = (fromb ? bbz : baz) - ps2[j].z;
         const float rr2 = drx * drx + dry * dry + drz * drz;
-        if (t0 + j < len && rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
-          q[(qh + n) & (kQCap - 1)][lane] = make_float4(drx, dry, drz, __uint_as_float(pini + t0 + j));
+        if (in[j] && rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
+          q[(qh + n) & (kQCap - 1)][lane] = make_float4(drx, dry, drz, __uint_as_float(idx[j]));
           n++;
         }
       }
