@@ -263,6 +263,9 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
                                            float4 e, float4 vr2, float p2press, float4 vr1,
                                            float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
                                            float massp2, PairAcc& r) {
+  // fluid neighbours (boundp2=false) are summed without their mass, which the
+  // caller applies once to the pass's sums; the continuity sum leaves out rho1
+  const float m2 = boundp2 ? massp2 : 1.f;
   const unsigned p2 = __float_as_uint(e.w);
   const float drx = e.x, dry = e.y, drz = e.z;
   const float rr2 = drx * drx + dry * dry + drz * drz;
@@ -273,16 +276,16 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
   const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
   const float inv_rho2 = gb_rcp(vr2.w);
   // momentum
-  const float p_vpm = -(p1press + p2press) * inv_rho1 * inv_rho2 * massp2;
+  const float p_vpm = -(p1press + p2press) * inv_rho1 * inv_rho2 * m2;
   r.ax += p_vpm * frx; r.ay += p_vpm * fry; r.az += p_vpm * frz;
   // continuity
   const float dvx = vr1.x - vr2.x, dvy = vr1.y - vr2.y, dvz = vr1.z - vr2.z;
-  r.ar += massp2 * (dvx * frx + dvy * fry + dvz * frz) * (vr1.w * inv_rho2);
+  r.ar += m2 * (dvx * frx + dvy * fry + dvz * frz) * inv_rho2;
   const float inv_r2eta = gb_rcp(rr2 + c.eta2);
   if (tdensity == GBSPH_DDT_DDT && r.delta != FLT_MAX) {
     const float visc_densi = k.ddt_kc * (vr1.w * inv_rho2 - 1.f) * inv_r2eta;
     const float dot3 = drx * frx + dry * fry + drz * frz;
-    r.delta = (boundp2 && c.tboundary == GBSPH_BC_DBC) ? FLT_MAX : r.delta + visc_densi * dot3 * massp2;
+    r.delta = (boundp2 && c.tboundary == GBSPH_BC_DBC) ? FLT_MAX : r.delta + visc_densi * dot3 * m2;
   }
   if (tdensity == GBSPH_DDT_DDT2 || (tdensity == GBSPH_DDT_DDT2FULL && !boundp2)) {
     // the fluid neighbours are visited first, so only the boundary pass can
@@ -296,7 +299,7 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
       else drho = c.rhopzero * (t * (k.c1 + t * (k.c2 + t * (k.c3 + t * (k.c4 + t * k.c5)))));
       const float visc_densi = k.ddt_kc * ((vr2.w - vr1.w) - drho) * inv_r2eta;
       const float dot3 = drx * frx + dry * fry + drz * frz;
-      r.delta -= visc_densi * dot3 * massp2 * inv_rho2;
+      r.delta -= visc_densi * dot3 * m2 * inv_rho2;
     }
   }
   // viscosity
@@ -308,12 +311,12 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
     // selected, since nearly every warp has lanes on both sides of the test
     const float amubar = c.kernelh * dot_rr2;
     const float robar = (vr1.w + vr2.w) * 0.5f;
-    const float pi_visc = dot < 0 ? (vfac * amubar * gb_rcp(robar)) * massp2 : 0.f;
+    const float pi_visc = dot < 0 ? (vfac * amubar * gb_rcp(robar)) * m2 : 0.f;
     r.ax -= pi_visc * frx; r.ay -= pi_visc * fry; r.az -= pi_visc * frz;
   } else {
     const float robar2 = vr1.w + vr2.w;
     const float temp = vfac * inv_r2eta * gb_rcp(robar2);
-    const float vtemp = massp2 * temp * (drx * frx + dry * fry + drz * frz);
+    const float vtemp = m2 * temp * (drx * frx + dry * fry + drz * frz);
     r.ax += vtemp * dvx; r.ay += vtemp * dvy; r.az += vtemp * dvz;
     if (tvisco == GBSPH_VISCO_LAMINARSPS) {
       float t0 = ta1.x, t1 = ta1.y, t2 = ta1.z, t3 = ta1.w, t4 = tb1.x, t5 = tb1.y;
@@ -322,10 +325,10 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
         const float2 tb2 = a.taub[p2];
         t0 += ta2.x; t1 += ta2.y; t2 += ta2.z; t3 += ta2.w; t4 += tb2.x; t5 += tb2.y;
       }
-      r.ax += massp2 * (t0 * frx + t1 * fry + t2 * frz);
-      r.ay += massp2 * (t1 * frx + t3 * fry + t4 * frz);
-      r.az += massp2 * (t2 * frx + t4 * fry + t5 * frz);
-      const float volp2 = -massp2 * inv_rho2;
+      r.ax += m2 * (t0 * frx + t1 * fry + t2 * frz);
+      r.ay += m2 * (t1 * frx + t3 * fry + t4 * frz);
+      r.az += m2 * (t2 * frx + t4 * fry + t5 * frz);
+      const float volp2 = -m2 * inv_rho2;
       float dv = dvx * volp2; r.s0 += dv * frx; r.s1 += dv * fry; r.s2 += dv * frz;
       dv = dvy * volp2; r.s1 += dv * frx; r.s3 += dv * fry; r.s4 += dv * frz;
       dv = dvz * volp2; r.s2 += dv * frx; r.s4 += dv * fry; r.s5 += dv * frz;
@@ -489,7 +492,13 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, Pair
   // one accumulator for both passes: the boundary pass adds to the fluid sums
   // (and sets the DDT veto, FLT_MAX in delta, where it applies)
   round_pass<tvisco, tdensity, false, ddtgen, E, F>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
+  {  // the fluid-neighbour sums carry no mass yet
+    const float mf = c.massfluid;
+    ff.ax *= mf; ff.ay *= mf; ff.az *= mf; ff.ar *= mf; ff.delta *= mf;
+    ff.s0 *= mf; ff.s1 *= mf; ff.s2 *= mf; ff.s3 *= mf; ff.s4 *= mf; ff.s5 *= mf;
+  }
   round_pass<tvisco, tdensity, true, ddtgen, E, F>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
+  ff.ar *= vr1.w;  // the rho1 factor of every continuity term
   float acemax2 = 0, visc = 0, vel2 = 0;
   if (active) {
     float ar = ff.ar;
