@@ -223,10 +223,13 @@ struct PairAcc {
 struct PairK {
   float hinv;            // 1/h
   float ddt_kc;          // ddtkh * cs0
-  float vfac_f, vfac_b;  // artificial: -visco*cs0; laminar: 4*visco (fluid / boundary neighbours)
-  // (1+t)^a - 1 = t*(c1 + t*(c2 + t*(c3 + t*(c4 + t*c5)))) + O(t^6), a = 1/gamma:
-  // the binomial series of the hydrostatic DDT2 term rho0*((1+ddtgz*drz)^(1/gamma)-1),
-  // which avoids the cancellation of pow()-1 (truncation below 1e-8 relative for |t| < 0.05)
+  // artificial: -visco*cs0*2h (the h of mu_ij and the 1/2 of rhobar folded in);
+  // laminar: 4*visco (fluid / boundary neighbours)
+  float vfac_f, vfac_b;
+  // rho0*((1+t)^a - 1) = t*(c1 + t*(c2 + t*(c3 + t*(c4 + t*c5)))) + O(t^6), a = 1/gamma:
+  // the binomial series (times rho0) of the hydrostatic DDT2 term
+  // rho0*((1+ddtgz*drz)^(1/gamma)-1), which avoids the cancellation of
+  // pow()-1 (truncation below 1e-8 relative for |t| < 0.05)
   float c1, c2, c3, c4, c5;
 };
 
@@ -237,18 +240,17 @@ PairK make_pairk(const gbsph_consts& c) {
   k.ddt_kc = c.ddtkh * cbar;
   const float vb = c.visco * c.viscoboundfactor;
   if (c.tvisco == GBSPH_VISCO_ARTIFICIAL) {
-    k.vfac_f = -c.visco * cbar;
-    k.vfac_b = -vb * cbar;
+    k.vfac_f = -c.visco * cbar * c.kernelh * 2.f;
+    k.vfac_b = -vb * cbar * c.kernelh * 2.f;
   } else {
     k.vfac_f = 4.f * c.visco;
     k.vfac_b = 4.f * vb;
   }
   const float ga = 1.f / c.gamma;
-  k.c1 = ga;
-  k.c2 = k.c1 * (ga - 1.f) * 0.5f;
-  k.c3 = k.c2 * (ga - 2.f) * (1.f / 3.f);
-  k.c4 = k.c3 * (ga - 3.f) * 0.25f;
-  k.c5 = k.c4 * (ga - 4.f) * 0.2f;
+  const float b1 = ga, b2 = b1 * (ga - 1.f) * 0.5f, b3 = b2 * (ga - 2.f) * (1.f / 3.f);
+  const float b4 = b3 * (ga - 3.f) * 0.25f, b5 = b4 * (ga - 4.f) * 0.2f;
+  k.c1 = c.rhopzero * b1; k.c2 = c.rhopzero * b2; k.c3 = c.rhopzero * b3;
+  k.c4 = c.rhopzero * b4; k.c5 = c.rhopzero * b5;
   return k;
 }
 
@@ -296,10 +298,11 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
       const float t = c.ddtgz * drz;
       float drho;
       if (ddtgen && !(fabsf(t) < 0.05f)) drho = c.rhopzero * powf(1.f + t, 1.f / c.gamma) - c.rhopzero;
-      else drho = c.rhopzero * (t * (k.c1 + t * (k.c2 + t * (k.c3 + t * (k.c4 + t * k.c5)))));
-      const float visc_densi = k.ddt_kc * ((vr2.w - vr1.w) - drho) * inv_r2eta;
-      const float dot3 = drx * frx + dry * fry + drz * frz;
-      r.delta -= visc_densi * dot3 * m2 * inv_rho2;
+      else drho = t * (k.c1 + t * (k.c2 + t * (k.c3 + t * (k.c4 + t * k.c5))));
+      // the fluid pass sums the term without delta*2h*cs0, applied with the mass
+      const float visc_densi = ((vr2.w - vr1.w) - drho) * inv_r2eta;
+      const float dot3 = fac * rr2;  // r . gradW
+      r.delta -= visc_densi * dot3 * inv_rho2;
     }
   }
   // viscosity
@@ -309,9 +312,8 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
   if (tvisco == GBSPH_VISCO_ARTIFICIAL) {
     // applied for approaching pairs (dot < 0); evaluated for every pair and
     // selected, since nearly every warp has lanes on both sides of the test
-    const float amubar = c.kernelh * dot_rr2;
-    const float robar = (vr1.w + vr2.w) * 0.5f;
-    const float pi_visc = dot < 0 ? (vfac * amubar * gb_rcp(robar)) * m2 : 0.f;
+    // -alpha*cs0*h*dot_rr2 / rhobar with rhobar = (rho1+rho2)/2 (h and 2 in vfac)
+    const float pi_visc = dot < 0 ? (vfac * dot_rr2 * gb_rcp(vr1.w + vr2.w)) * m2 : 0.f;
     r.ax -= pi_visc * frx; r.ay -= pi_visc * fry; r.az -= pi_visc * frz;
   } else {
     const float robar2 = vr1.w + vr2.w;
@@ -495,6 +497,7 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, Pair
   {  // the fluid-neighbour sums carry no mass yet
     const float mf = c.massfluid;
     ff.ax *= mf; ff.ay *= mf; ff.az *= mf; ff.ar *= mf; ff.delta *= mf;
+    if (tdensity == GBSPH_DDT_DDT2 || tdensity == GBSPH_DDT_DDT2FULL) ff.delta *= k.ddt_kc;
     ff.s0 *= mf; ff.s1 *= mf; ff.s2 *= mf; ff.s3 *= mf; ff.s4 *= mf; ff.s5 *= mf;
   }
   round_pass<tvisco, tdensity, true, ddtgen, E, F>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
