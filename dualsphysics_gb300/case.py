@@ -76,7 +76,11 @@ def _pos_value(text: str, isposmin: bool):
     return "fixed", float(v)
 
 
-def load_case(casedir: str, casename: str) -> CaseData:
+def load_case(casedir: str, casename: str, cellmode: str = "full") -> CaseData:
+    """Reads <casename>.xml and <casename>.bi4.  `cellmode` is the reference's
+    -cellmode run option: "full" (cells of 2h) or "half" (cells of h)."""
+    if cellmode not in ("full", "half"):
+        raise CaseError(f"unknown cell mode {cellmode!r} (full or half)")
     xml_path = os.path.join(casedir, casename + ".xml")
     bi4_path = os.path.join(casedir, casename + ".bi4")
     if not os.path.exists(xml_path):
@@ -122,7 +126,7 @@ def load_case(casedir: str, casename: str) -> CaseData:
     prm.dtallparticles = 1 if gi("DtAllParticles", 0) == 1 else 0
     prm.rhopoutmin = gf("RhopOutMin", 700.0)
     prm.rhopoutmax = gf("RhopOutMax", 1300.0)
-    prm.cellmode_div = 1
+    prm.cellmode_div = 2 if cellmode == "half" else 1  # JSph.cpp:1880 (ScellDiv)
     # --- constants (JCaseCtes.cpp:208-222)
     prm.simulate2d = 1 if (cte.find("data2d") is not None and cte.find("data2d").get("value", "false").lower()
                            in ("1", "true")) else 0

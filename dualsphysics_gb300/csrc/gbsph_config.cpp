@@ -73,7 +73,8 @@ extern "C" int gbsph_config(const gbsph_params* p, gbsph_consts* c) {
     c->spssmag = (float)((2. / 3.) * std::pow((0.12 * dp_sps), 2));
     c->spsblin = (float)((2. / 3.) * 0.0066 * dp_sps * dp_sps);
   }
-  c->ddtkh = c->kernelsize * p->ddtvalue;
+  // DDTValue is 0 without density diffusion (JSph.cpp:923); DDTkh = KernelSize*DDTValue (JSph.cpp:1534)
+  c->ddtkh = c->kernelsize * (p->tdensity == GBSPH_DDT_NONE ? 0.f : p->ddtvalue);
   c->ddtgz = (float)((double)c->rhopzero * (double)std::fabs(c->gravity[2]) / (double)c->cteb);
   c->dtini = p->dtini > 0 ? p->dtini : c->kernelh / c->cs0;
   c->dtmin = p->dtmin > 0 ? p->dtmin : (c->kernelh / c->cs0) * p->coefdtmin;

@@ -2,7 +2,7 @@
 // (JSphGpuSingle.cpp:950-1010) over the gbsph C ABI.
 //
 //   gbsph_run <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-sv:none|bi4]
-//             [-nograph] [-device:D]
+//             [-cellmode:full|half] [-nograph] [-device:D] [-info]
 //
 // Loads the run XML and Case.bi4 (LoadConfig + LoadCaseParticles), derives the
 // constants, uploads the particles, then steps until TimeMax (or N steps)
@@ -29,14 +29,15 @@ int fail(const char* what, const std::string& msg) {
 
 int main(int argc, char** argv) {
   if (argc < 3) {
-    std::fprintf(stderr, "usage: %s <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-sv:none|bi4] [-nograph] "
-                         "[-device:D]\n", argv[0]);
+    std::fprintf(stderr, "usage: %s <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-sv:none|bi4] "
+                         "[-cellmode:full|half] [-nograph] [-device:D] [-info]\n", argv[0]);
     return 1;
   }
   std::string casepath = argv[1], dirout = argv[2];
   long nsteps = 0;
   double tmax = -1;
   bool save = true, graph = true, info = false;
+  int cellmode_div = 1;  // -cellmode (JSphCfgRun.cpp:354-355): cells of 2h (full) or h (half)
   int device = 0;
   for (int i = 3; i < argc; i++) {
     const std::string a = argv[i];
@@ -47,6 +48,8 @@ int main(int argc, char** argv) {
     else if (a == "-nograph") graph = false;
     else if (a.rfind("-device:", 0) == 0) device = std::atoi(a.c_str() + 8);
     else if (a == "-info") info = true;
+    else if (a == "-cellmode:half" || a == "-cellmode:h") cellmode_div = 2;
+    else if (a == "-cellmode:full" || a == "-cellmode:2h") cellmode_div = 1;
     else if (a == "-gpu" || a == "-symplectic") continue;
     else return fail("options", "unknown option " + a);
   }
@@ -56,19 +59,20 @@ int main(int argc, char** argv) {
   gbio::Case cs;
   std::string err;
   if (!gbio::load_case(casedir, casename, cs, err)) return fail("LoadCase", err);
+  cs.params.cellmode_div = cellmode_div;
   gbsph_consts c;
   if (gbsph_config(&cs.params, &c) != GBSPH_OK) return fail("ConfigConstants", "invalid case constants");
   if (info) {
     // case summary as JSON (host only: no device is touched)
     std::printf("{\"np\": %u, \"npb\": %u, \"h\": %.17g, \"b\": %.17g, \"dp\": %.17g, \"maprealposmin\": "
                 "[%.17g, %.17g, %.17g], \"maprealposmax\": [%.17g, %.17g, %.17g], \"kernelsize2\": %.9g, "
-                "\"cs0\": %.17g, \"domcellcode\": %u, \"mapcells\": [%u, %u, %u], \"tboundary\": %d, "
+                "\"cs0\": %.17g, \"domcellcode\": %u, \"mapcells\": [%u, %u, %u], \"cellmode_div\": %d, \"tboundary\": %d, "
                 "\"tstep\": %d, \"tdensity\": %d, \"tvisco\": %d, \"idsum\": %.17g, \"possum\": %.17g, "
                 "\"rhosum\": %.17g, \"norsum\": %.17g, \"codesum\": %.17g}\n",
                 cs.np, cs.npb, cs.params.h, cs.params.b, cs.params.dp, cs.params.maprealposmin[0],
                 cs.params.maprealposmin[1], cs.params.maprealposmin[2], cs.params.maprealposmax[0],
                 cs.params.maprealposmax[1], cs.params.maprealposmax[2], c.kernelsize2, c.cs0, c.domcellcode,
-                c.mapcells[0], c.mapcells[1], c.mapcells[2], c.tboundary, c.tstep, c.tdensity, c.tvisco,
+                c.mapcells[0], c.mapcells[1], c.mapcells[2], c.cellmode_div, c.tboundary, c.tstep, c.tdensity, c.tvisco,
                 [&] { double s = 0; for (unsigned v : cs.idp) s += v; return s; }(),
                 [&] { double s = 0; for (double v : cs.pos) s += v; return s; }(),
                 [&] { double s = 0; for (size_t k = 3; k < cs.velrho.size(); k += 4) s += cs.velrho[k]; return s; }(),

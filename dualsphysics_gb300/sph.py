@@ -57,9 +57,9 @@ class GbSphSingle:
         except Exception:
             pass
 
-    def LoadCase(self, casedir: str, casename: str, capacity: int | None = None) -> None:
+    def LoadCase(self, casedir: str, casename: str, capacity: int | None = None, cellmode: str = "full") -> None:
         """LoadConfig + LoadCaseParticles + ConfigDomain (JSphGpuSingle.cpp:151-240)."""
-        self.case = cd = load_case(casedir, casename)
+        self.case = cd = load_case(casedir, casename, cellmode)
         self.setup(cd, capacity)
 
     def setup(self, cd: CaseData, capacity: int | None = None) -> None:
@@ -218,9 +218,9 @@ class GbSphSingle:
         return path
 
     def Run(self, casedir: str, casename: str, dirout: str, time_max: float | None = None,
-            nsteps: int | None = None, use_graph: bool = True, save: bool = True) -> dict:
+            nsteps: int | None = None, use_graph: bool = True, save: bool = True, cellmode: str = "full") -> dict:
         """Main loop (JSphGpuSingle::Run, JSphGpuSingle.cpp:950-1010)."""
-        self.LoadCase(casedir, casename)
+        self.LoadCase(casedir, casename, cellmode=cellmode)
         self.dirout = dirout
         os.makedirs(dirout, exist_ok=True)
         cd = self.case

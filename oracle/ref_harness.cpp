@@ -187,7 +187,7 @@ class OracleCpu : public JSphCpuSingle{
 
 int main(int argc,char** argv){
   if(argc<6){
-    fprintf(stderr,"usage: %s <casedir> <casename> <outdir> <nsteps> <threads>\n",argv[0]);
+    fprintf(stderr,"usage: %s <casedir> <casename> <outdir> <nsteps> <threads> [run options]\n",argv[0]);
     return 1;
   }
   const std::string casedir=argv[1],casename=argv[2],outdir=argv[3];
@@ -197,7 +197,11 @@ int main(int argc,char** argv){
   JSphCfgRun cfg;
   cfg.SetFeatureList(JSph::GetFeatureList());
   std::string casepath=casedir+"/"+casename;
-  std::vector<std::string> args={"ref_harness","-cpu",thr,"-sv:none","-svres:0",casepath,outdir};
+  // run options after <threads> (e.g. -cellmode:half) go to the reference's own parser
+  std::vector<std::string> args={"ref_harness","-cpu",thr,"-sv:none","-svres:0"};
+  for(int i=6;i<argc;i++)args.push_back(argv[i]);
+  args.push_back(casepath);
+  args.push_back(outdir);
   std::vector<char*> av;
   for(auto& s:args)av.push_back(const_cast<char*>(s.c_str()));
   int rc=1;

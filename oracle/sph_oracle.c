@@ -128,7 +128,8 @@ int orc_config(const orc_params* p, orc_ctes* c) {
     c->spssmag = (float)((2. / 3.) * pow((0.12 * dp_sps), 2));
     c->spsblin = (float)((2. / 3.) * 0.0066 * dp_sps * dp_sps);
   }
-  c->ddtkh = c->kernelsize * p->ddtvalue;
+  /* DDTValue is 0 without density diffusion (JSph.cpp:923) */
+  c->ddtkh = c->kernelsize * (p->tdensity == 0 ? 0.f : p->ddtvalue);
   c->ddtgz = (float)((double)c->rhopzero * (double)fabsf(c->gravity[2]) / (double)c->cteb);
   c->dtini = p->dtini;
   c->dtmin = p->dtmin;

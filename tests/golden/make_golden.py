@@ -36,7 +36,18 @@ CASES = {
                                       init_vel=0.05, seed=3), 12),
     "sps_d04": (lambda: cg.spec_c1(dp=0.04, name="sps_d04", visco_treatment=2, visco=1e-6, density_dt=1,
                                    init_vel=0.05, seed=5), 10),
+    "lam_d04": (lambda: cg.spec_c1(dp=0.04, name="lam_d04", visco_treatment=3, visco=1e-6, density_dt=0,
+                                   init_vel=0.05, seed=13), 10),
+    "ddt2f_d04": (lambda: cg.spec_c2(dp=0.04, name="ddt2f_d04", density_dt=3, init_vel=0.02, seed=17), 10),
+    "half_d04": (lambda: cg.spec_c1(dp=0.04, name="half_d04", init_vel=0.02, seed=19), 10, ["-cellmode:half"]),
 }
+
+
+def run_options(name: str) -> list:
+    """Run options of a case beyond the run XML (the reference takes the cell
+    mode from the command line)."""
+    v = CASES[name]
+    return list(v[2]) if len(v) > 2 else []
 
 STATE = (("idp", np.uint32, 1), ("code", np.uint16, 1), ("dcell", np.uint32, 1), ("pos", np.float64, 3),
          ("velrho", np.float32, 4))
@@ -57,13 +68,13 @@ def _meta(d, tag):
 
 
 def make(name: str, threads: int = 8) -> str:
-    spec_fn, nsteps = CASES[name]
+    spec_fn, nsteps = CASES[name][:2]
     with tempfile.TemporaryDirectory() as tmp:
         casedir = os.path.join(tmp, "case")
         outdir = os.path.join(tmp, "out")
         os.makedirs(outdir)
         cg.write_case(cg.make_dam_break(spec_fn()), casedir)
-        subprocess.run([HARNESS, casedir, name, outdir, str(nsteps), str(threads)], check=True,
+        subprocess.run([HARNESS, casedir, name, outdir, str(nsteps), str(threads)] + run_options(name), check=True,
                        stdout=subprocess.DEVNULL)
         arr = {}
         for tag in ("s0", "s0pre", "s1", "end") + (("s0div", "s0corr") if os.path.exists(

@@ -17,7 +17,7 @@ from dualsphysics_gb300 import casegen as cg  # noqa: E402
 from dualsphysics_gb300.case import load_case  # noqa: E402
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-CASE_NAMES = ["dbc_d04", "mdbc_d04", "jit_d04", "vel_d04", "verlet_d04", "sps_d04"]
+CASE_NAMES = ["dbc_d04", "mdbc_d04", "jit_d04", "vel_d04", "verlet_d04", "sps_d04", "lam_d04", "ddt2f_d04", "half_d04"]
 
 # Tolerance of FP32 pair sums, stated per particle against the conditioning
 # scale S_i = sum_j |pair term_ij| computed by the FP64 oracle:
@@ -51,7 +51,9 @@ def load_generated(name: str):
     spec = case_spec(name)
     tmp = tempfile.mkdtemp(prefix="gbcase_")
     cg.write_case(cg.make_dam_break(spec), tmp)
-    return load_case(tmp, spec.name)
+    import make_golden
+    half = "-cellmode:half" in make_golden.run_options(name)
+    return load_case(tmp, spec.name, "half" if half else "full")
 
 
 def assert_fp32_parity(x, x_orc32, x_f64, scale, what=""):

@@ -36,13 +36,15 @@ def _write_case(tmp_path, name):
     return spec.name
 
 
-@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "sps_d04", "verlet_d04"])
+@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "sps_d04", "verlet_d04", "lam_d04", "half_d04"])
 def test_driver_case_summary_matches_python_loader(tmp_path, name):
+    import make_golden
     cn = _write_case(tmp_path, name)
-    out = subprocess.run([_driver(), str(tmp_path / cn), str(tmp_path / "out"), "-info"], capture_output=True,
-                         text=True, check=True, timeout=120)
+    opts = make_golden.run_options(name)  # e.g. -cellmode:half, as the reference takes it
+    out = subprocess.run([_driver(), str(tmp_path / cn), str(tmp_path / "out"), "-info"] + opts,
+                         capture_output=True, text=True, check=True, timeout=120)
     info = json.loads(out.stdout)
-    cd = load_case(str(tmp_path), cn)
+    cd = load_case(str(tmp_path), cn, "half" if "-cellmode:half" in opts else "full")
     pc = _lib.config(cd.params)
     assert (info["np"], info["npb"]) == (len(cd.idp), cd.npb)
     assert (info["h"], info["b"], info["dp"]) == (cd.params.h, cd.params.b, cd.params.dp)
@@ -52,6 +54,7 @@ def test_driver_case_summary_matches_python_loader(tmp_path, name):
     assert info["cs0"] == pc.cs0
     assert info["domcellcode"] == pc.domcellcode
     assert info["mapcells"] == list(pc.mapcells)
+    assert info["cellmode_div"] == cd.params.cellmode_div == pc.cellmode_div
     assert (info["tboundary"], info["tstep"], info["tdensity"], info["tvisco"]) == \
         (pc.tboundary, pc.tstep, pc.tdensity, pc.tvisco)
     # the particle arrays: exact integer sums, float sums to rounding of the order

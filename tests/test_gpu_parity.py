@@ -77,7 +77,7 @@ def test_forces_within_tolerance(name):
     assert mx["viscdtmax"] == pytest.approx(om["viscdtmax"], rel=1e-4, abs=1e-6)
 
 
-@pytest.mark.parametrize("name", ["dbc_d04", "vel_d04", "sps_d04", "mdbc_d04"])
+@pytest.mark.parametrize("name", ["dbc_d04", "vel_d04", "sps_d04", "mdbc_d04", "lam_d04", "ddt2f_d04", "half_d04"])
 @pytest.mark.parametrize("variant", [0, 1])
 def test_forces_variants_within_tolerance(name, variant):
     """Both fluid-row kernels: queued rounds (0), one thread per particle (1)."""
