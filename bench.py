@@ -129,13 +129,13 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def make_case(dp: float):
+def make_case(dp: float, cellmode: str = "full"):
     from dualsphysics_gb300 import casegen as cg
     from dualsphysics_gb300.case import load_case
     tmp = tempfile.mkdtemp(prefix="gbbench_")
     spec = cg.spec_c2(dp=dp, name="DamC2")
     cg.write_case(cg.make_dam_break(spec), tmp)
-    return load_case(tmp, "DamC2")
+    return load_case(tmp, "DamC2", cellmode)
 
 
 def cpu_baseline(cd, stride: int, steps: int = 1):
@@ -187,6 +187,8 @@ def main():
     ap.add_argument("--ref-stride", type=int, default=16)
     ap.add_argument("--cpu-stride", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cellmode", default="full", choices=["full", "half"],
+                    help="the reference's -cellmode run option: cells of 2h (default) or h")
     ap.add_argument("--variant", type=int, default=None,
                     help="fluid-row kernel: 0 queued rounds, 1 one thread per particle")
     args = ap.parse_args()
@@ -203,7 +205,7 @@ def main():
 
     if args.impl == "reference":
         if rank == 0:
-            run_reference(args, make_case(args.dp), rank)
+            run_reference(args, make_case(args.dp, args.cellmode), rank)
         if dist:
             dist.destroy_process_group()
         return
@@ -211,7 +213,7 @@ def main():
     from dualsphysics_gb300 import _lib
     from dualsphysics_gb300.sph import GbSphSingle
 
-    cd = make_case(args.dp)
+    cd = make_case(args.dp, args.cellmode)
     K, W = args.steps, args.warmup
     s = GbSphSingle(local)
     s.setup(cd)
@@ -292,7 +294,7 @@ def main():
             "config": {"workload": f"3-D dam break (tank 1.6x0.67x0.4 m, column 0.4x0.67x0.3 m), mDBC + "
                                    f"0.12x0.12x0.45 m box obstacle, dp={args.dp}, Symplectic, Wendland, "
                                    f"artificial visc 0.01, DDT2 0.1",
-                       "particles": cd.np, "fluid": cd.nfluid, "boundary": cd.npb,
+                       "particles": cd.np, "fluid": cd.nfluid, "boundary": cd.npb, "cellmode": args.cellmode,
                        "parallelism": "replicas only" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (no flush)"},
             "particle_interactions_per_s": steps_per_s * pis_per_step,
