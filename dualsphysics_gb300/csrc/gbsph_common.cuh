@@ -113,6 +113,71 @@ __device__ __forceinline__ float gb_press(float rho, float rhopzero, float cteb,
 
 __host__ __device__ __forceinline__ unsigned gb_div_up(unsigned a, unsigned b) { return (a + b - 1) / b; }
 
+// ---- exact FP64 helpers on the integer pipe ----------------------------------
+// This part executes FP64 instructions (conversions and compares included) at
+// a small fraction of its FP32 / integer rate, so the integrators do the exact
+// operations that need no rounding decisions -- float->double conversion,
+// double->float rounding, sign/order tests -- on the bit patterns, and keep the
+// FP64 pipe for the additions, products and divisions.
+
+// (double)f, exactly: a normal float's exponent is re-biased and its
+// significand widened; zeros, subnormals, infinities and NaNs take the
+// hardware conversion.
+__device__ __forceinline__ double gb_f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned mag = u & 0x7fffffffu;
+  if (mag == 0u) return __longlong_as_double((long long)((unsigned long long)(u >> 31) << 63));
+  if (mag - 0x00800000u >= 0x7f000000u) return (double)f;
+  const unsigned long long b = ((unsigned long long)(u >> 31) << 63) |
+                               ((unsigned long long)((mag >> 23) + 896u) << 52) |
+                               ((unsigned long long)(mag & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)b);
+}
+
+// (float)x with round-to-nearest-even, for results that are normal floats
+// (the 29 dropped significand bits decide the rounding; a carry into the
+// exponent is the correct result, up to infinity); zeros, subnormal results,
+// overflow, infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ float gb_d2f(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (e - 897u > 253u) return (float)x;
+  const unsigned long long m = b & 0xfffffffffffffull;
+  unsigned r = (unsigned)(m >> 29) | ((e - 896u) << 23);
+  const unsigned rem = (unsigned)(m & 0x1fffffffu);
+  if (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) r += 1u;
+  return __uint_as_float(r | ((unsigned)(b >> 63) << 31));
+}
+
+// x < 0 || x >= size || x is NaN, for a finite size > 0 (-0 is not below 0).
+__device__ __forceinline__ bool gb_outside(double x, double size) {
+  const long long b = __double_as_longlong(x);
+  const unsigned long long mag = (unsigned long long)b & 0x7fffffffffffffffull;
+  if (mag > 0x7ff0000000000000ull) return true;
+  if (b < 0) return mag != 0ull;
+  return b >= __double_as_longlong(size);
+}
+
+// Cell index unsigned(d / sc) for 0 <= d, bit for bit as the correctly rounded
+// double division gives it, with the division done only when needed: q =
+// d * rsc (rsc = RN(1/sc)) is within 4 ulp of d / sc, below 1.5e-9 for every
+// quotient under 2^22, so when the fraction of q lies more than 2^-26 from an
+// integer (and q < 2^22), floor(q) is floor(RN(d / sc)); q < 0.5 gives 0.  The
+// integer and fraction parts are read from q's bits.
+__device__ __forceinline__ unsigned gb_cellidx(double d, double sc, double rsc) {
+  const double q = __dmul_rn(d, rsc);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+  const int ef = (int)(b >> 52);  // q >= 0: no sign bit
+  if (ef < 1022) return 0u;
+  if (ef < 1023 + 22) {
+    const int sh = 1075 - ef;  // fraction bits of q, 31..53
+    const unsigned long long m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+    const unsigned long long ip = m >> sh, fr = m & ((1ull << sh) - 1ull), lim = 1ull << (sh - 26);
+    if ((ip == 0ull || fr > lim) && fr < (1ull << sh) - lim) return (unsigned)ip;
+  }
+  return (unsigned)__ddiv_rn(d, sc);
+}
+
 // Launchers implemented in the .cu files (host side).
 namespace gbk {
 void load_dcell(const gbsph_consts& c, const DevArrays& a, unsigned n, cudaStream_t s);  // sets GB_ERR_PARTOUT in DivState::error

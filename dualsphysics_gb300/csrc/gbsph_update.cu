@@ -24,15 +24,16 @@ __device__ __forceinline__ double dmul(double x, double y) { return __dmul_rn(x,
 
 // UpdatePos (JSphCpu.cpp:1464-1516) without periodic conditions.
 __device__ __forceinline__ void update_pos(const gbsph_consts& c, const DevArrays& a, unsigned p, double rx, double ry,
-                                           double rz, double movx, double movy, double movz, bool outrho) {
-  const bool outmov = (fabsf((float)movx) > c.movlimit || fabsf((float)movy) > c.movlimit ||
-                       fabsf((float)movz) > c.movlimit);
+                                           double rz, double movx, double movy, double movz, bool outrho,
+                                           double rsc) {
+  const bool outmov = (fabsf(gb_d2f(movx)) > c.movlimit || fabsf(gb_d2f(movy)) > c.movlimit ||
+                       fabsf(gb_d2f(movz)) > c.movlimit);
   rx = dadd(rx, movx); ry = dadd(ry, movy); rz = dadd(rz, movz);
   const double dx = __dsub_rn(rx, c.maprealposmin[0]);
   const double dy = __dsub_rn(ry, c.maprealposmin[1]);
   const double dz = __dsub_rn(rz, c.maprealposmin[2]);
-  const bool out = (dx != dx || dy != dy || dz != dz || dx < 0 || dy < 0 || dz < 0 || dx >= c.maprealsize[0] ||
-                    dy >= c.maprealsize[1] || dz >= c.maprealsize[2]);
+  const bool out = gb_outside(dx, c.maprealsize[0]) || gb_outside(dy, c.maprealsize[1]) ||
+                   gb_outside(dz, c.maprealsize[2]);
   a.px[p] = rx; a.py[p] = ry; a.pz[p] = rz;
   if (outrho || outmov || out) {
     const unsigned rcode = a.code[p];
@@ -41,7 +42,7 @@ __device__ __forceinline__ void update_pos(const gbsph_consts& c, const DevArray
     a.dcell[p] = 0xffffffffu;
   } else {
     const double sc = (double)c.scell;
-    const unsigned cx = (unsigned)__ddiv_rn(dx, sc), cy = (unsigned)__ddiv_rn(dy, sc), cz = (unsigned)__ddiv_rn(dz, sc);
+    const unsigned cx = gb_cellidx(dx, sc, rsc), cy = gb_cellidx(dy, sc, rsc), cz = gb_cellidx(dz, sc, rsc);
     a.dcell[p] = gb_cell(c.domcellcode, cx, cy, cz);
   }
 }
@@ -50,7 +51,7 @@ __device__ __forceinline__ double read_dt(const double* dtp, double dth) { retur
 
 // ComputeSymplecticPre: the current state becomes the PRE state (qx/velrhopre)
 // and the predicted state is written to the current arrays.
-__global__ void k_sym_pre(gbsph_consts c, DevArrays a, const double* dtp, double dth) {
+__global__ void k_sym_pre(gbsph_consts c, DevArrays a, const double* dtp, double dth, double rsc) {
   const DivState& d = *a.div;
   const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= d.np) return;
@@ -61,19 +62,19 @@ __global__ void k_sym_pre(gbsph_consts c, DevArrays a, const double* dtp, double
   a.velrhopre[p] = vp;
   const float ar = a.acear[p].w;
   if (p < d.npb) {
-    float w = (float)dadd((double)vp.w, dmul(dt05, (double)ar));
+    float w = gb_d2f(dadd(gb_f2d(vp.w), dmul(dt05, gb_f2d(ar))));
     w = (w < c.rhopzero ? c.rhopzero : w);
     a.velrho[p] = make_float4(vp.x, vp.y, vp.z, w);
     return;
   }
   const float4 ace = a.acear[p];
   const unsigned rcode = a.code[p];
-  const float rhonew = (float)dadd((double)vp.w, dmul(dt05, (double)ar));
-  const double dx = dmul((double)vp.x, dt05), dy = dmul((double)vp.y, dt05), dz = dmul((double)vp.z, dt05);
+  const float rhonew = gb_d2f(dadd(gb_f2d(vp.w), dmul(dt05, gb_f2d(ar))));
+  const double dx = dmul(gb_f2d(vp.x), dt05), dy = dmul(gb_f2d(vp.y), dt05), dz = dmul(gb_f2d(vp.z), dt05);
   const bool outrho = (rhonew < c.rhopoutmin || rhonew > c.rhopoutmax);
-  const float vx = (float)dadd((double)vp.x, dmul(dadd((double)ace.x, (double)c.gravity[0]), dt05));
-  const float vy = (float)dadd((double)vp.y, dmul(dadd((double)ace.y, (double)c.gravity[1]), dt05));
-  const float vz = (float)dadd((double)vp.z, dmul(dadd((double)ace.z, (double)c.gravity[2]), dt05));
+  const float vx = gb_d2f(dadd(gb_f2d(vp.x), dmul(dadd(gb_f2d(ace.x), gb_f2d(c.gravity[0])), dt05)));
+  const float vy = gb_d2f(dadd(gb_f2d(vp.y), dmul(dadd(gb_f2d(ace.y), gb_f2d(c.gravity[1])), dt05)));
+  const float vz = gb_d2f(dadd(gb_f2d(vp.z), dmul(dadd(gb_f2d(ace.z), gb_f2d(c.gravity[2])), dt05)));
   a.velrho[p] = make_float4(vx, vy, vz, rhonew);
   unsigned code = rcode;
   if (outrho && (rcode & GB_CODE_MASKSPECIAL) == GB_CODE_NORMAL) {
@@ -81,11 +82,11 @@ __global__ void k_sym_pre(gbsph_consts c, DevArrays a, const double* dtp, double
     a.code[p] = (uint16_t)code;
   }
   if ((code & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID)
-    update_pos(c, a, p, x, y, z, dx, dy, dz, (code & GB_CODE_MASKSPECIAL) == GB_CODE_OUTRHO);
+    update_pos(c, a, p, x, y, z, dx, dy, dz, (code & GB_CODE_MASKSPECIAL) == GB_CODE_OUTRHO, rsc);
 }
 
 // ComputeSymplecticCorr: PRE state + forces of the predicted state.
-__global__ void k_sym_cor(gbsph_consts c, DevArrays a, const double* dtp, double dth) {
+__global__ void k_sym_cor(gbsph_consts c, DevArrays a, const double* dtp, double dth, double rsc) {
   const DivState& d = *a.div;
   const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= d.np) return;
@@ -94,19 +95,19 @@ __global__ void k_sym_cor(gbsph_consts c, DevArrays a, const double* dtp, double
   const float4 ace = a.acear[p];
   const float4 vc = a.velrho[p];   // predicted
   const float4 vp = a.velrhopre[p];
-  const double eps = dmul(-(double)ace.w / (double)vc.w, dt);
-  const float rhonew = (float)(dmul((double)vp.w, __dsub_rn(2., eps)) / dadd(2., eps));
+  const double eps = dmul(-gb_f2d(ace.w) / gb_f2d(vc.w), dt);
+  const float rhonew = gb_d2f((dmul(gb_f2d(vp.w), __dsub_rn(2., eps)) / dadd(2., eps)));
   if (p < d.npb) {
     a.velrho[p] = make_float4(0.f, 0.f, 0.f, (rhonew < c.rhopzero ? c.rhopzero : rhonew));
     return;
   }
   const unsigned rcode = a.code[p];
-  const float vx = (float)dadd((double)vp.x, dmul(dadd((double)ace.x, (double)c.gravity[0]), dt));
-  const float vy = (float)dadd((double)vp.y, dmul(dadd((double)ace.y, (double)c.gravity[1]), dt));
-  const float vz = (float)dadd((double)vp.z, dmul(dadd((double)ace.z, (double)c.gravity[2]), dt));
-  const double dx = dmul(dadd((double)vp.x, (double)vx), dt05);
-  const double dy = dmul(dadd((double)vp.y, (double)vy), dt05);
-  const double dz = dmul(dadd((double)vp.z, (double)vz), dt05);
+  const float vx = gb_d2f(dadd(gb_f2d(vp.x), dmul(dadd(gb_f2d(ace.x), gb_f2d(c.gravity[0])), dt)));
+  const float vy = gb_d2f(dadd(gb_f2d(vp.y), dmul(dadd(gb_f2d(ace.y), gb_f2d(c.gravity[1])), dt)));
+  const float vz = gb_d2f(dadd(gb_f2d(vp.z), dmul(dadd(gb_f2d(ace.z), gb_f2d(c.gravity[2])), dt)));
+  const double dx = dmul(dadd(gb_f2d(vp.x), gb_f2d(vx)), dt05);
+  const double dy = dmul(dadd(gb_f2d(vp.y), gb_f2d(vy)), dt05);
+  const double dz = dmul(dadd(gb_f2d(vp.z), gb_f2d(vz)), dt05);
   const bool outrho = (rhonew < c.rhopoutmin || rhonew > c.rhopoutmax);
   unsigned code = rcode;
   if (outrho && (rcode & GB_CODE_MASKSPECIAL) == GB_CODE_NORMAL) {
@@ -115,7 +116,7 @@ __global__ void k_sym_cor(gbsph_consts c, DevArrays a, const double* dtp, double
   }
   a.velrho[p] = make_float4(vx, vy, vz, rhonew);
   if ((code & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID)
-    update_pos(c, a, p, a.qx[p], a.qy[p], a.qz[p], dx, dy, dz, (code & GB_CODE_MASKSPECIAL) == GB_CODE_OUTRHO);
+    update_pos(c, a, p, a.qx[p], a.qy[p], a.qz[p], dx, dy, dz, (code & GB_CODE_MASKSPECIAL) == GB_CODE_OUTRHO, rsc);
   else {
     a.px[p] = a.qx[p]; a.py[p] = a.qy[p]; a.pz[p] = a.qz[p];
   }
@@ -123,7 +124,7 @@ __global__ void k_sym_cor(gbsph_consts c, DevArrays a, const double* dtp, double
 
 // ComputeVerlet (JSphCpu.cpp:1523-1680): velrhopre holds VelrhoM1.  The new
 // state is written to velrho and the old velrho moves to velrhopre.
-__global__ void k_verlet(gbsph_consts c, DevArrays a, const double* dtp, double dth, int euler) {
+__global__ void k_verlet(gbsph_consts c, DevArrays a, const double* dtp, double dth, int euler, double rsc) {
   const DivState& d = *a.div;
   const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= d.np) return;
@@ -133,7 +134,7 @@ __global__ void k_verlet(gbsph_consts c, DevArrays a, const double* dtp, double 
   const float4 vm1 = a.velrhopre[p];
   const float4 v2 = euler ? v1 : vm1;
   const float ar = a.acear[p].w;
-  const float rhonew = (float)dadd((double)v2.w, dmul(dt2, (double)ar));
+  const float rhonew = gb_d2f(dadd(gb_f2d(v2.w), dmul(dt2, gb_f2d(ar))));
   a.velrhopre[p] = v1;
   if (p < d.npb) {
     a.velrho[p] = make_float4(0.f, 0.f, 0.f, (rhonew < c.rhopzero ? c.rhopzero : rhonew));
@@ -141,18 +142,18 @@ __global__ void k_verlet(gbsph_consts c, DevArrays a, const double* dtp, double 
   }
   const double dt205 = dmul(dmul(0.5, dt), dt);
   const float4 ace = a.acear[p];
-  const double ax = dadd((double)ace.x, (double)c.gravity[0]);
-  const double ay = dadd((double)ace.y, (double)c.gravity[1]);
-  const double az = dadd((double)ace.z, (double)c.gravity[2]);
-  const double dx = dadd(dmul((double)v1.x, dt), dmul(ax, dt205));
-  const double dy = dadd(dmul((double)v1.y, dt), dmul(ay, dt205));
-  const double dz = dadd(dmul((double)v1.z, dt), dmul(az, dt205));
+  const double ax = dadd(gb_f2d(ace.x), gb_f2d(c.gravity[0]));
+  const double ay = dadd(gb_f2d(ace.y), gb_f2d(c.gravity[1]));
+  const double az = dadd(gb_f2d(ace.z), gb_f2d(c.gravity[2]));
+  const double dx = dadd(dmul(gb_f2d(v1.x), dt), dmul(ax, dt205));
+  const double dy = dadd(dmul(gb_f2d(v1.y), dt), dmul(ay, dt205));
+  const double dz = dadd(dmul(gb_f2d(v1.z), dt), dmul(az, dt205));
   const bool outrho = (rhonew < c.rhopoutmin || rhonew > c.rhopoutmax);
-  const float nvx = (float)dadd((double)v2.x, dmul(ax, dt2));
-  const float nvy = (float)dadd((double)v2.y, dmul(ay, dt2));
-  const float nvz = (float)dadd((double)v2.z, dmul(az, dt2));
+  const float nvx = gb_d2f(dadd(gb_f2d(v2.x), dmul(ax, dt2)));
+  const float nvy = gb_d2f(dadd(gb_f2d(v2.y), dmul(ay, dt2)));
+  const float nvz = gb_d2f(dadd(gb_f2d(v2.z), dmul(az, dt2)));
   a.velrho[p] = make_float4(nvx, nvy, nvz, rhonew);
-  update_pos(c, a, p, a.px[p], a.py[p], a.pz[p], dx, dy, dz, outrho);
+  update_pos(c, a, p, a.px[p], a.py[p], a.pz[p], dx, dy, dz, outrho, rsc);
 }
 
 // DtVariable (JSphCpu.cpp:2035-2078): which = 0 predictor (dt_p), 1 corrector
@@ -196,13 +197,13 @@ namespace gbk {
 
 void symplectic_pre(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, cudaStream_t s,
                     unsigned long long* nlaunch) {
-  k_sym_pre<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, 0.0);
+  k_sym_pre<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, 0.0, 1.0 / (double)c.scell);
   if (nlaunch) *nlaunch += 1;
 }
 
 void symplectic_cor(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, cudaStream_t s,
                     unsigned long long* nlaunch) {
-  k_sym_cor<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, 0.0);
+  k_sym_cor<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, 0.0, 1.0 / (double)c.scell);
   if (nlaunch) *nlaunch += 1;
 }
 
@@ -218,7 +219,7 @@ void step_end(const DevArrays& a, int symplectic, cudaStream_t s, unsigned long 
 
 void verlet_step(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, int euler, cudaStream_t s,
                  unsigned long long* nlaunch) {
-  k_verlet<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, 0.0, euler);
+  k_verlet<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, 0.0, euler, 1.0 / (double)c.scell);
   if (nlaunch) *nlaunch += 1;
 }
 
