@@ -20,7 +20,9 @@
 
 struct gbsph_ctx {
   gbsph_consts c;
-  unsigned cap = 0;
+  unsigned cap = 0;    // allocated particles (the capacity rounded up to 256, so that
+                       // consecutive arrays of 4-, 8- and 16-byte elements are contiguous)
+  unsigned limit = 0;  // the capacity the caller asked for
   int device = 0;
   cudaStream_t stream = nullptr;
   void* arena = nullptr;
@@ -206,7 +208,8 @@ int gbsph_create(const gbsph_consts* c, unsigned capacity, int device, gbsph_ctx
   if (c->tstep != GBSPH_STEP_SYMPLECTIC && c->tstep != GBSPH_STEP_VERLET) return GBSPH_EINVAL;
   gbsph_ctx* ctx = new gbsph_ctx();
   ctx->c = *c;
-  ctx->cap = capacity;
+  ctx->limit = capacity;
+  ctx->cap = (capacity + 255u) & ~255u;
   ctx->device = device;
   const unsigned long long maxnct = (unsigned long long)c->domcells[0] * c->domcells[1] * c->domcells[2];
   if (2ull * maxnct + 6 >= 0xffffffffull) {
@@ -290,26 +293,24 @@ static int upload_common(gbsph_ctx* ctx, unsigned np, unsigned npb) {
 int gbsph_upload(gbsph_ctx* ctx, unsigned np, unsigned npb, const double* pos, const float* velrho,
                  const unsigned* idp, const uint16_t* code, const float* boundnor) {
   if (!ctx || !pos || !velrho || !idp || !code) return set_err(ctx, GBSPH_EINVAL, "null argument");
-  if (np > ctx->cap || npb > np) return set_err(ctx, GBSPH_ECAPACITY, "np=%u exceeds capacity %u", np, ctx->cap);
+  if (np > ctx->limit || npb > np) return set_err(ctx, GBSPH_ECAPACITY, "np=%u exceeds capacity %u", np, ctx->limit);
   CK(cudaSetDevice(ctx->device), "set device");
-  std::vector<double> x(np), y(np), z(np);
-  for (unsigned p = 0; p < np; p++) { x[p] = pos[3 * (size_t)p]; y[p] = pos[3 * (size_t)p + 1]; z[p] = pos[3 * (size_t)p + 2]; }
-  CK(cudaMemcpyAsync(ctx->a.px, x.data(), sizeof(double) * np, cudaMemcpyHostToDevice, ctx->stream), "upload pos");
-  CK(cudaMemcpyAsync(ctx->a.py, y.data(), sizeof(double) * np, cudaMemcpyHostToDevice, ctx->stream), "upload pos");
-  CK(cudaMemcpyAsync(ctx->a.pz, z.data(), sizeof(double) * np, cudaMemcpyHostToDevice, ctx->stream), "upload pos");
+  // the caller's arrays are copied as they are; positions are split into x, y,
+  // z and the normals doubled on the device, from the alternate position arrays
+  // and the sort buffers as staging (both unused until the first divide)
+  double* stage = ctx->a.px2;  // px2, py2, pz2: 3*cap contiguous doubles
+  CK(cudaMemcpyAsync(stage, pos, sizeof(double) * 3 * (size_t)np, cudaMemcpyHostToDevice, ctx->stream), "upload pos");
   CK(cudaMemcpyAsync(ctx->a.velrho, velrho, sizeof(float4) * np, cudaMemcpyHostToDevice, ctx->stream), "upload velrho");
   CK(cudaMemcpyAsync(ctx->a.idp, idp, sizeof(unsigned) * np, cudaMemcpyHostToDevice, ctx->stream), "upload idp");
   CK(cudaMemcpyAsync(ctx->a.code, code, sizeof(uint16_t) * np, cudaMemcpyHostToDevice, ctx->stream), "upload code");
-  std::vector<float4> bn;
-  if (ctx->a.boundnor) {
-    // JSph::ConfigBoundNormals: normals of boundary particles are doubled (JSph.cpp:1411-1418)
-    bn.assign(np, make_float4(0.f, 0.f, 0.f, 0.f));
-    if (boundnor)
-      for (unsigned p = 0; p < np; p++)
-        if (idp[p] < npb) bn[p] = make_float4(boundnor[3 * (size_t)p] * 2.f, boundnor[3 * (size_t)p + 1] * 2.f,
-                                              boundnor[3 * (size_t)p + 2] * 2.f, 0.f);
-    CK(cudaMemcpyAsync(ctx->a.boundnor, bn.data(), sizeof(float4) * np, cudaMemcpyHostToDevice, ctx->stream), "upload nor");
+  float* nstage = nullptr;
+  if (ctx->a.boundnor && boundnor) {
+    nstage = (float*)ctx->a.keys;  // keys, keys2, vals, vals2: 16*cap contiguous bytes
+    CK(cudaMemcpyAsync(nstage, boundnor, sizeof(float) * 3 * (size_t)np, cudaMemcpyHostToDevice, ctx->stream),
+       "upload nor");
   }
+  gbk::stage_upload(ctx->a, stage, nstage, np, npb, ctx->stream);
+  CK(cudaGetLastError(), "upload");
   CK(cudaStreamSynchronize(ctx->stream), "upload sync");
   return upload_common(ctx, np, npb);
 }
@@ -317,7 +318,7 @@ int gbsph_upload(gbsph_ctx* ctx, unsigned np, unsigned npb, const double* pos, c
 int gbsph_upload_device(gbsph_ctx* ctx, unsigned np, unsigned npb, const double* d_pos, const float* d_velrho,
                         const unsigned* d_idp, const uint16_t* d_code, const float* d_boundnor) {
   if (!ctx || !d_pos || !d_velrho || !d_idp || !d_code) return set_err(ctx, GBSPH_EINVAL, "null argument");
-  if (np > ctx->cap || npb > np) return set_err(ctx, GBSPH_ECAPACITY, "np=%u exceeds capacity %u", np, ctx->cap);
+  if (np > ctx->limit || npb > np) return set_err(ctx, GBSPH_ECAPACITY, "np=%u exceeds capacity %u", np, ctx->limit);
   CK(cudaSetDevice(ctx->device), "set device");
   // de-interleave xyz with strided 2-D copies
   CK(cudaMemcpy2DAsync(ctx->a.px, sizeof(double), d_pos, 3 * sizeof(double), sizeof(double), np, cudaMemcpyDeviceToDevice, ctx->stream), "pos");
@@ -609,12 +610,11 @@ int gbsph_download(gbsph_ctx* ctx, double* pos, float* velrho, unsigned* idp, ui
   if (int rc = read_div(ctx, &ds)) return rc;
   const unsigned np = ds.np;
   if (pos) {
-    std::vector<double> x(np), y(np), z(np);
-    CK(cudaMemcpyAsync(x.data(), ctx->a.px, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->stream), "pos");
-    CK(cudaMemcpyAsync(y.data(), ctx->a.py, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->stream), "pos");
-    CK(cudaMemcpyAsync(z.data(), ctx->a.pz, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->stream), "pos");
-    CK(cudaStreamSynchronize(ctx->stream), "sync");
-    for (unsigned p = 0; p < np; p++) { pos[3 * (size_t)p] = x[p]; pos[3 * (size_t)p + 1] = y[p]; pos[3 * (size_t)p + 2] = z[p]; }
+    // interleave on the device into the alternate position arrays (free between divides)
+    double* stage = ctx->a.px2;
+    gbk::stage_download(ctx->a, stage, np, ctx->stream);
+    CK(cudaGetLastError(), "download");
+    CK(cudaMemcpyAsync(pos, stage, sizeof(double) * 3 * (size_t)np, cudaMemcpyDeviceToHost, ctx->stream), "pos");
   }
   if (velrho) CK(cudaMemcpyAsync(velrho, ctx->a.velrho, sizeof(float4) * np, cudaMemcpyDeviceToHost, ctx->stream), "velrho");
   if (idp) CK(cudaMemcpyAsync(idp, ctx->a.idp, sizeof(unsigned) * np, cudaMemcpyDeviceToHost, ctx->stream), "idp");

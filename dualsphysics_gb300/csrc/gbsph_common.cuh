@@ -187,6 +187,12 @@ void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses,
 // current device).
 unsigned sort_noalloc_max_keys();
 cudaError_t sort_noalloc_address(void** p);
+// Upload/download reshaping on the device: interleaved (x,y,z) doubles <->
+// the px/py/pz arrays, and the boundary normals (3 floats, doubled as
+// JSph::ConfigBoundNormals does, zero for non-boundary particles; nor3 may be
+// null) into boundnor.  `stage` holds 3*n doubles.
+void stage_upload(const DevArrays& a, const double* stage, const float* nor3, unsigned n, unsigned npb, cudaStream_t s);
+void stage_download(const DevArrays& a, double* stage, unsigned n, cudaStream_t s);
 void sort_noalloc(unsigned char* work, const unsigned* keys, unsigned n, unsigned nbits, unsigned* perm,
                   unsigned* sorted_keys, cudaStream_t s);
 void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, cudaStream_t s, unsigned long long* nlaunch,

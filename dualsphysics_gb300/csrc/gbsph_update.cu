@@ -191,9 +191,43 @@ __global__ void k_step_end(StepState* st, int symplectic) {
   st->nstep++;
 }
 
+// Interleaved positions -> px/py/pz, and the doubled boundary normals
+// (JSph::ConfigBoundNormals, JSph.cpp:1411-1418: boundary particles by id).
+__global__ void k_stage_upload(DevArrays a, const double* __restrict__ stage, const float* __restrict__ nor3,
+                               unsigned n, unsigned npb) {
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  a.px[p] = stage[3 * (size_t)p];
+  a.py[p] = stage[3 * (size_t)p + 1];
+  a.pz[p] = stage[3 * (size_t)p + 2];
+  if (a.boundnor) {
+    float4 bn = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (nor3 && a.idp[p] < npb)
+      bn = make_float4(nor3[3 * (size_t)p] * 2.f, nor3[3 * (size_t)p + 1] * 2.f, nor3[3 * (size_t)p + 2] * 2.f, 0.f);
+    a.boundnor[p] = bn;
+  }
+}
+
+__global__ void k_stage_download(DevArrays a, double* __restrict__ stage, unsigned n) {
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  stage[3 * (size_t)p] = a.px[p];
+  stage[3 * (size_t)p + 1] = a.py[p];
+  stage[3 * (size_t)p + 2] = a.pz[p];
+}
+
 }  // namespace
 
 namespace gbk {
+
+void stage_upload(const DevArrays& a, const double* stage, const float* nor3, unsigned n, unsigned npb, cudaStream_t s) {
+  if (n) k_stage_upload<<<gb_div_up(n, kUpdBlock), kUpdBlock, 0, s>>>(a, stage, nor3, n, npb);
+}
+
+void stage_download(const DevArrays& a, double* stage, unsigned n, cudaStream_t s) {
+  if (n) k_stage_download<<<gb_div_up(n, kUpdBlock), kUpdBlock, 0, s>>>(a, stage, n);
+}
+
 
 void symplectic_pre(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, cudaStream_t s,
                     unsigned long long* nlaunch) {

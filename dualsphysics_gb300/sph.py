@@ -151,6 +151,17 @@ class GbSphSingle:
         self._check(lib().gbsph_download(self.ctx, ptr(pos), ptr(vr), ptr(idp), ptr(code), ptr(dcell)), "download")
         return {"pos": pos, "velrho": vr, "idp": idp, "code": code, "dcell": dcell}
 
+    def download_into(self, out: dict) -> dict:
+        """download() into caller-provided arrays (e.g. page-locked ones) of at
+        least np rows; returns the views holding the np current particles."""
+        n = self.divinfo()["np"]
+        for k, w in (("pos", 3), ("velrho", 4), ("idp", 1), ("code", 1), ("dcell", 1)):
+            a = out[k]
+            assert a.shape[0] >= n and a.flags["C_CONTIGUOUS"] and (a.ndim == 1 or a.shape[1] == w), k
+        self._check(lib().gbsph_download(self.ctx, ptr(out["pos"]), ptr(out["velrho"]), ptr(out["idp"]),
+                                         ptr(out["code"]), ptr(out["dcell"])), "download")
+        return {k: v[:n] for k, v in out.items()}
+
     def forces(self) -> tuple[np.ndarray, np.ndarray]:
         n = self.divinfo()["np"]
         ace = np.empty((n, 3), np.float32)
