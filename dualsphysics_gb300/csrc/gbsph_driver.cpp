@@ -1,7 +1,7 @@
 // gbsph_driver.cpp -- gbsph_run: the Run loop of JSphGpuSingle
 // (JSphGpuSingle.cpp:950-1010) over the gbsph C ABI.
 //
-//   gbsph_run <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-sv:none|bi4]
+//   gbsph_run <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-tout:T] [-sv:none|bi4]
 //             [-cellmode:full|half] [-nograph] [-device:D] [-info]
 //
 // Loads the run XML and Case.bi4 (LoadConfig + LoadCaseParticles), derives the
@@ -9,10 +9,13 @@
 // writing data/Part_%04u.bi4 every TimeOut, and prints the run summary the
 // reference prints at the end of Run.out (JSph::ShowResume, JSph.cpp:3522-3545).
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gbsph.h"
@@ -25,17 +28,116 @@ int fail(const char* what, const std::string& msg) {
   return 1;
 }
 
+// Part files are written off the stepping thread: the particle data is read
+// back into one of two host buffer sets, and a writer thread sorts it by id,
+// encodes it and writes the file while the GPU goes on stepping (the reference
+// writes its Parts inline in the Run loop).  With both buffer sets in use the
+// next save waits for the writer, so at most two Parts are held in memory.
+class PartWriter {
+ public:
+  struct Job {
+    std::vector<double> pos;
+    std::vector<float> velrho;
+    std::vector<unsigned> idp;
+    unsigned part = 0, step = 0, np = 0;
+    double t = 0, dtn = 0;
+  };
+
+  PartWriter(const std::string& dirout, const gbio::Case& cs) : dirout_(dirout), cs_(cs), th_([this] { loop(); }) {
+    std::lock_guard<std::mutex> lk(mu_);
+    for (auto& b : bufs_) {
+      b.pos.resize(3 * (size_t)cs.np);
+      b.velrho.resize(4 * (size_t)cs.np);
+      b.idp.resize(cs.np);
+      free_.push_back(&b);
+    }
+  }
+  ~PartWriter() { finish(); }
+
+  // A free buffer set (waits while both are being written).
+  Job* acquire() {
+    std::unique_lock<std::mutex> lk(mu_);
+    cv_.wait(lk, [this] { return !free_.empty(); });
+    Job* j = free_.back();
+    free_.pop_back();
+    return j;
+  }
+  // Returns a buffer set unwritten.
+  void release(Job* j) {
+    { std::lock_guard<std::mutex> lk(mu_); free_.push_back(j); }
+    cv_.notify_all();
+  }
+  void submit(Job* j) {
+    { std::lock_guard<std::mutex> lk(mu_); todo_.push_back(j); }
+    cv_.notify_all();
+  }
+  // Waits for every submitted Part; returns false (with the message) if a write failed.
+  bool finish() {
+    std::unique_lock<std::mutex> lk(mu_);
+    if (!stop_) {
+      cv_.wait(lk, [this] { return todo_.empty() && free_.size() == 2; });
+      stop_ = true;
+      lk.unlock();
+      cv_.notify_all();
+      th_.join();
+      lk.lock();
+    }
+    return err_.empty();
+  }
+  std::string error() {
+    std::lock_guard<std::mutex> lk(mu_);
+    return err_;
+  }
+  double write_seconds() const { return write_s_; }
+
+ private:
+  void loop() {
+    for (;;) {
+      Job* j = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [this] { return stop_ || !todo_.empty(); });
+        if (todo_.empty()) return;
+        j = todo_.front();
+        todo_.erase(todo_.begin());
+      }
+      const auto t0 = std::chrono::steady_clock::now();
+      std::string e;
+      const bool ok = gbio::save_part(dirout_, cs_, j->part, j->t, j->step, j->dtn, j->np, j->pos.data(),
+                                      j->velrho.data(), j->idp.data(), e);
+      write_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!ok && err_.empty()) err_ = e;
+        free_.push_back(j);
+      }
+      cv_.notify_all();
+    }
+  }
+
+  std::string dirout_;
+  const gbio::Case& cs_;
+  Job bufs_[2];
+  std::vector<Job*> free_, todo_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  bool stop_ = false;
+  std::string err_;
+  double write_s_ = 0;
+  std::thread th_;
+};
+
 }  // namespace
 
 int main(int argc, char** argv) {
   if (argc < 3) {
-    std::fprintf(stderr, "usage: %s <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-sv:none|bi4] "
+    std::fprintf(stderr, "usage: %s <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-tout:T] [-sv:none|bi4] "
                          "[-cellmode:full|half] [-nograph] [-device:D] [-info]\n", argv[0]);
     return 1;
   }
   std::string casepath = argv[1], dirout = argv[2];
   long nsteps = 0;
-  double tmax = -1;
+  double tmax = -1, toutarg = -1;
   bool save = true, graph = true, info = false;
   int cellmode_div = 1;  // -cellmode (JSphCfgRun.cpp:354-355): cells of 2h (full) or h (half)
   int device = 0;
@@ -43,6 +145,7 @@ int main(int argc, char** argv) {
     const std::string a = argv[i];
     if (a.rfind("-nsteps:", 0) == 0) nsteps = std::atol(a.c_str() + 8);
     else if (a.rfind("-tmax:", 0) == 0) tmax = std::atof(a.c_str() + 6);
+    else if (a.rfind("-tout:", 0) == 0) toutarg = std::atof(a.c_str() + 6);
     else if (a == "-sv:none") save = false;
     else if (a == "-sv:bi4") save = true;
     else if (a == "-nograph") graph = false;
@@ -87,18 +190,24 @@ int main(int argc, char** argv) {
                     cs.boundnor.empty() ? nullptr : cs.boundnor.data());
   if (rc != GBSPH_OK) return fail("gbsph_upload", gbsph_last_error(ctx));
   if (tmax < 0) tmax = cs.time_max;
-  const double tout = cs.time_out > 0 ? cs.time_out : tmax;
+  const double tout = toutarg > 0 ? toutarg : (cs.time_out > 0 ? cs.time_out : tmax);
   std::printf("Case %s: %u particles (%u boundary, %u fluid), h=%g, dp=%g\n", casename.c_str(), cs.np, cs.npb,
               cs.np - cs.npb, cs.params.h, cs.params.dp);
-  std::vector<double> pos(3 * (size_t)cs.np);
-  std::vector<float> velrho(4 * (size_t)cs.np);
-  std::vector<unsigned> idp(cs.np);
   gbsph_divinfo di;
+  PartWriter writer(dirout, cs);
   auto save_part = [&](unsigned part, double t, unsigned step, double dtn) -> bool {
     if (!save) return true;
+    const std::string werr = writer.error();
+    if (!werr.empty()) { err = werr; return false; }
     if (gbsph_get_divinfo(ctx, &di, nullptr, 0, nullptr, nullptr) != GBSPH_OK) return false;
-    if (gbsph_download(ctx, pos.data(), velrho.data(), idp.data(), nullptr, nullptr) != GBSPH_OK) return false;
-    return gbio::save_part(dirout, cs, part, t, step, dtn, di.np, pos.data(), velrho.data(), idp.data(), err);
+    PartWriter::Job* j = writer.acquire();
+    if (gbsph_download(ctx, j->pos.data(), j->velrho.data(), j->idp.data(), nullptr, nullptr) != GBSPH_OK) {
+      writer.release(j);
+      return false;
+    }
+    j->part = part; j->t = t; j->step = step; j->dtn = dtn; j->np = di.np;
+    writer.submit(j);
+    return true;
   };
   if (!save_part(0, 0.0, 0, c.dtini)) return fail("SaveData", err.empty() ? gbsph_last_error(ctx) : err);
   unsigned part = 1, nstep = 0;
@@ -118,10 +227,12 @@ int main(int argc, char** argv) {
     }
   }
   const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (!writer.finish()) return fail("SaveData", writer.error());
   gbsph_get_divinfo(ctx, &di, nullptr, 0, nullptr, nullptr);
   std::printf("Simulated time: %.6f s in %u steps (last dt %.6e)\n", t, nstep, dtl);
   std::printf("Particles: %u (excluded %u)\n", di.np, di.nout_total);
   std::printf("Runtime: %.3f s\nSteps per second: %.3f\n", wall, nstep / (wall > 0 ? wall : 1));
+  if (save) std::printf("Part writing (overlapped with the steps): %.3f s\n", writer.write_seconds());
   gbsph_destroy(ctx);
   return 0;
 }

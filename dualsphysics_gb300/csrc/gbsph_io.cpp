@@ -526,9 +526,27 @@ bool save_part(const std::string& dirout, const Case& c, unsigned part, double t
   const std::string dd = dirout + "/data";
   mkdir(dirout.c_str(), 0755);
   mkdir(dd.c_str(), 0755);
-  std::vector<unsigned> order(np);
-  for (unsigned k = 0; k < np; k++) order[k] = k;
-  std::stable_sort(order.begin(), order.end(), [&](unsigned x, unsigned y) { return idp[x] < idp[y]; });
+  // particles in id order: ids are unique and below the case count, so each
+  // particle is placed at its id and the occupied slots are read in order (O(n))
+  std::vector<unsigned> order;
+  order.reserve(np);
+  {
+    const unsigned ncase = c.np;
+    std::vector<unsigned> slot(ncase, 0xffffffffu);
+    bool placed = true;
+    for (unsigned k = 0; k < np; k++) {
+      if (idp[k] >= ncase || slot[idp[k]] != 0xffffffffu) { placed = false; break; }
+      slot[idp[k]] = k;
+    }
+    if (placed) {
+      for (unsigned i = 0; i < ncase; i++)
+        if (slot[i] != 0xffffffffu) order.push_back(slot[i]);
+    } else {  // ids outside the case range or repeated: sort instead
+      order.resize(np);
+      for (unsigned k = 0; k < np; k++) order[k] = k;
+      std::stable_sort(order.begin(), order.end(), [&](unsigned x, unsigned y) { return idp[x] < idp[y]; });
+    }
+  }
   std::vector<unsigned> oidp(np);
   std::vector<double> opos(3 * (size_t)np);
   std::vector<float> ofpos(3 * (size_t)np), ovel(3 * (size_t)np), orho(np);
