@@ -53,6 +53,7 @@ class Consts(C.Structure):
         ("dp", C.c_double), ("cs0", C.c_double), ("cflnumber", C.c_double), ("dtmin", C.c_double),
         ("dtini", C.c_double),
         ("mapposmin", C.c_double * 3), ("maprealposmin", C.c_double * 3), ("maprealsize", C.c_double * 3),
+        ("maprealposmax", C.c_double * 3),
         ("domposmin", C.c_double * 3), ("domrealposmin", C.c_double * 3), ("domrealposmax", C.c_double * 3),
         ("mapcells", C.c_uint * 3), ("domcells", C.c_uint * 3), ("domcellcode", C.c_uint),
     ]
@@ -104,6 +105,9 @@ SIGNATURES = {
     "gbsph_elapsed": (C.c_int, [P, C.c_uint, C.c_uint, C.POINTER(C.c_float)]),
     "gbsph_pips": (C.c_int, [P, C.POINTER(C.c_ulonglong * 4)]),
     "gbsph_sort_keys_noalloc": (C.c_int, [P, P, C.c_uint, C.c_uint, P, P]),
+    "gbsph_gauge_velocity": (C.c_int, [P, C.c_uint, P, P]),
+    "gbsph_gauge_swl": (C.c_int, [P, C.c_uint, P, P, P, P]),
+    "gbsph_gauge_maxz": (C.c_int, [P, C.c_uint, P, P, P]),
 }
 
 SORT_NOALLOC_MAX_KEYS = 262144  # GBSPH_SORT_NOALLOC_MAX_KEYS

@@ -9,6 +9,7 @@
 // into a CUDA graph and replayed.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -48,6 +49,8 @@ struct gbsph_ctx {
   std::vector<cudaEvent_t> prof_ev;
   unsigned prof_cap = 0, prof_n = 0;
   cudaEvent_t marks[16] = {};
+  void* gauge_buf = nullptr;  // gauge inputs and results (grown on demand)
+  size_t gauge_bytes = 0;
   std::string err;
 };
 
@@ -248,6 +251,7 @@ void gbsph_destroy(gbsph_ctx* ctx) {
   for (auto ev : ctx->marks) if (ev) cudaEventDestroy(ev);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->arena) cudaFree(ctx->arena);
+  if (ctx->gauge_buf) cudaFree(ctx->gauge_buf);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -657,6 +661,119 @@ int gbsph_get_divinfo(gbsph_ctx* ctx, gbsph_divinfo* info, unsigned* begincell, 
   if (sortpart) CK(cudaMemcpyAsync(sortpart, ctx->a.vals, sizeof(unsigned) * ds.nptot, cudaMemcpyDeviceToHost, ctx->stream), "sp");
   if (cellpart) CK(cudaMemcpyAsync(cellpart, ctx->a.keys, sizeof(unsigned) * ds.nptot, cudaMemcpyDeviceToHost, ctx->stream), "cp");
   CK(cudaStreamSynchronize(ctx->stream), "sync");
+  return GBSPH_OK;
+}
+
+// ---- gauges -------------------------------------------------------------------
+// The inputs are packed on the host into one staging block, copied in one
+// transfer, measured by one launch and the results copied back.
+static int gauge_begin(gbsph_ctx* ctx, unsigned n, size_t bytes, bool args_ok) {
+  if (!ctx) return GBSPH_EINVAL;
+  if (!args_ok) return set_err(ctx, GBSPH_EINVAL, "null gauge argument");
+  if (!ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (n > (1u << 26)) return set_err(ctx, GBSPH_EINVAL, "too many gauges (%u)", n);
+  CK(cudaSetDevice(ctx->device), "set device");
+  if (bytes > ctx->gauge_bytes) {
+    CK(cudaStreamSynchronize(ctx->stream), "gauge sync");
+    if (ctx->gauge_buf) cudaFree(ctx->gauge_buf);
+    ctx->gauge_buf = nullptr;
+    ctx->gauge_bytes = 0;
+    const size_t want = bytes < 4096 ? 4096 : bytes;
+    if (cudaMalloc(&ctx->gauge_buf, want) != cudaSuccess) {
+      cudaGetLastError();
+      return set_err(ctx, GBSPH_ENOMEM, "gauge scratch of %zu bytes", want);
+    }
+    ctx->gauge_bytes = want;
+  }
+  return GBSPH_OK;
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int gbsph_gauge_velocity(gbsph_ctx* ctx, unsigned n, const double* points, float* vel) {
+  const size_t ob = align256(sizeof(double) * 3 * (size_t)n);
+  if (int rc = gauge_begin(ctx, n, ob + sizeof(float) * 3 * (size_t)n, n == 0 || (points && vel))) return rc;
+  if (!n) return GBSPH_OK;
+  char* buf = (char*)ctx->gauge_buf;
+  CK(cudaMemcpyAsync(buf, points, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream), "gauge in");
+  gbk::gauge_velocity(ctx->c, ctx->a, n, (const double*)buf, (float*)(buf + ob), ctx->stream);
+  ctx->launches++;
+  CK(cudaGetLastError(), "gauge velocity");
+  CK(cudaMemcpyAsync(vel, buf + ob, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream), "gauge out");
+  CK(cudaStreamSynchronize(ctx->stream), "gauge sync");
+  return GBSPH_OK;
+}
+
+int gbsph_gauge_swl(gbsph_ctx* ctx, unsigned n, const double* p0p2, const double* pointdp, const float* masslimit,
+                    float* surf) {
+  const size_t o1 = align256(sizeof(double) * 6 * (size_t)n);
+  const size_t o2 = o1 + align256(sizeof(unsigned) * (size_t)n);
+  const size_t o3 = o2 + align256(sizeof(float) * (size_t)n);
+  if (int rc = gauge_begin(ctx, n, o3 + sizeof(float) * 3 * (size_t)n,
+                           n == 0 || (p0p2 && pointdp && masslimit && surf)))
+    return rc;
+  if (!n) return GBSPH_OK;
+  std::vector<char> host(o3);
+  double* par = (double*)host.data();
+  unsigned* npts = (unsigned*)(host.data() + o1);
+  float* mlim = (float*)(host.data() + o2);
+  for (unsigned i = 0; i < n; i++) {
+    // JGaugeSwl::SetPoints (JDsGaugeItem.cpp:614-641): PointNp steps of PointDir
+    const double* q = p0p2 + 6 * (size_t)i;
+    const double vx = q[0] - q[3], vy = q[1] - q[4], vz = q[2] - q[5];
+    const double dis = std::sqrt(vx * vx + vy * vy + vz * vz);
+    const double pdp = pointdp[i];
+    unsigned np = 0;
+    double dx = 0, dy = 0, dz = 0;
+    if (dis > 0 && pdp > 0) {
+      if (!(dis / pdp < 1048576.0)) return set_err(ctx, GBSPH_EINVAL, "SWL gauge %u: too many points", i);
+      np = (unsigned)(dis / pdp);
+      if (dis - (pdp * np) >= pdp * 0.1) np++;
+      if (np < 1) np++;
+      const double dp = dis / np;
+      double ux = q[3] - q[0], uy = q[4] - q[1], uz = q[5] - q[2];
+      const double m = std::sqrt(ux * ux + uy * uy + uz * uz);
+      if (m) {
+        ux = ux / m;
+        uy = uy / m;
+        uz = uz / m;
+      }
+      dx = ux * dp;
+      dy = uy * dp;
+      dz = uz * dp;
+    }
+    double* pr = par + 6 * (size_t)i;
+    pr[0] = q[0]; pr[1] = q[1]; pr[2] = q[2];
+    pr[3] = dx; pr[4] = dy; pr[5] = dz;
+    npts[i] = np;
+    // JGaugeSystem::AddGaugeSwl (JDsGaugeSystem.cpp:408): the default limit
+    mlim[i] = masslimit[i] > 0 ? masslimit[i] : ctx->c.massfluid * (ctx->c.simulate2d ? 0.4f : 0.5f);
+  }
+  char* buf = (char*)ctx->gauge_buf;
+  CK(cudaMemcpyAsync(buf, host.data(), o3, cudaMemcpyHostToDevice, ctx->stream), "gauge in");
+  gbk::gauge_swl(ctx->c, ctx->a, n, (const double*)buf, (const unsigned*)(buf + o1), (const float*)(buf + o2),
+                 (float*)(buf + o3), ctx->stream);
+  ctx->launches++;
+  CK(cudaGetLastError(), "gauge swl");
+  CK(cudaMemcpyAsync(surf, buf + o3, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream), "gauge out");
+  // the staging vector is read by the copy above before it goes out of scope
+  CK(cudaStreamSynchronize(ctx->stream), "gauge sync");
+  return GBSPH_OK;
+}
+
+int gbsph_gauge_maxz(gbsph_ctx* ctx, unsigned n, const double* p0h, const float* distlimit, float* zmax) {
+  const size_t o1 = align256(sizeof(double) * 4 * (size_t)n);
+  const size_t o2 = o1 + align256(sizeof(float) * (size_t)n);
+  if (int rc = gauge_begin(ctx, n, o2 + sizeof(float) * (size_t)n, n == 0 || (p0h && distlimit && zmax))) return rc;
+  if (!n) return GBSPH_OK;
+  char* buf = (char*)ctx->gauge_buf;
+  CK(cudaMemcpyAsync(buf, p0h, sizeof(double) * 4 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream), "gauge in");
+  CK(cudaMemcpyAsync(buf + o1, distlimit, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream), "gauge in");
+  gbk::gauge_maxz(ctx->c, ctx->a, n, (const double*)buf, (const float*)(buf + o1), (float*)(buf + o2), ctx->stream);
+  ctx->launches++;
+  CK(cudaGetLastError(), "gauge maxz");
+  CK(cudaMemcpyAsync(zmax, buf + o2, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream), "gauge out");
+  CK(cudaStreamSynchronize(ctx->stream), "gauge sync");
   return GBSPH_OK;
 }
 

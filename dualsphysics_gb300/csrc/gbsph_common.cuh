@@ -205,4 +205,12 @@ void verlet_step(const gbsph_consts& c, DevArrays& a, unsigned cap, const double
 void sps_tau(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch);
 void pips(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s);
 void step_end(const DevArrays& a, int symplectic, cudaStream_t s, unsigned long long* nlaunch);
+// Gauges (gbsph_gauges.cu): device arrays in and out, n gauges per launch.
+// swl par: p0 (3) and step vector (3) per gauge; npts: PointNp; mlim: mass limit.
+// maxz par: p0 (3) and height per gauge.
+void gauge_velocity(const gbsph_consts& c, const DevArrays& a, unsigned n, const double* pts, float* vel, cudaStream_t s);
+void gauge_swl(const gbsph_consts& c, const DevArrays& a, unsigned n, const double* par, const unsigned* npts,
+               const float* mlim, float* surf, cudaStream_t s);
+void gauge_maxz(const gbsph_consts& c, const DevArrays& a, unsigned n, const double* par, const float* dist,
+                float* zmax, cudaStream_t s);
 }  // namespace gbk

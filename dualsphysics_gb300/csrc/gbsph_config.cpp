@@ -85,6 +85,7 @@ extern "C" int gbsph_config(const gbsph_params* p, gbsph_consts* c) {
     if (!(mapsize > 0)) return GBSPH_EINVAL;
     c->maprealposmin[k] = p->maprealposmin[k];
     c->maprealsize[k] = mapsize;
+    c->maprealposmax[k] = p->maprealposmax[k];
     c->mapposmin[k] = p->maprealposmin[k];
     c->mapcells[k] = (unsigned)std::ceil(mapsize / c->scell);
     c->domcells[k] = c->mapcells[k];

@@ -9,10 +9,11 @@
  *
  * Threading: one context per host thread; every context owns one CUDA stream.
  * Calls enqueue work on that stream and return without synchronising, except
- * gbsph_download*, gbsph_get_*, gbsph_sync and gbsph_step_dt (they read results
- * back).  Host pointers passed in are only used for the duration of the call.
- * All device memory of a context is allocated by gbsph_create/gbsph_upload;
- * nothing is allocated by the step functions.
+ * gbsph_download*, gbsph_get_*, gbsph_gauge_*, gbsph_sync and gbsph_step_dt
+ * (they read results back).  Host pointers passed in are only used for the duration of the call.
+ * All device memory of a context is allocated by gbsph_create/gbsph_upload
+ * (and the gauges' scratch by the first gauge call); nothing is allocated by
+ * the step functions.
  */
 #ifndef GBSPH_H
 #define GBSPH_H
@@ -71,7 +72,7 @@ typedef struct {
   float eta2, ddtkh, ddtgz, visco, viscoboundfactor, awen, bwenh, spssmag, spsblin;
   float scell, movlimit, rhopoutmin, rhopoutmax, gravity[3];
   double dp, cs0, cflnumber, dtmin, dtini;
-  double mapposmin[3], maprealposmin[3], maprealsize[3];
+  double mapposmin[3], maprealposmin[3], maprealsize[3], maprealposmax[3];
   double domposmin[3], domrealposmin[3], domrealposmax[3];
   unsigned mapcells[3], domcells[3], domcellcode;
 } gbsph_consts;
@@ -207,6 +208,31 @@ int gbsph_sort_keys_noalloc(gbsph_ctx* ctx, const unsigned* d_keys, unsigned n, 
  * definition (JDsPips.cpp:187-260): out4 = {checked bound-row pairs, real
  * bound-row pairs, checked fluid-row pairs, real fluid-row pairs}. */
 int gbsph_pips(gbsph_ctx* ctx, unsigned long long* out4);
+
+/* Measurement gauges on the current divided state (after gbsph_upload,
+ * gbsph_divide, gbsph_step or gbsph_run): the velocity, surface-water-level and
+ * maximum-height gauges of the reference's gauge system (JGaugeSystem::
+ * AddGaugeVel/AddGaugeSwl/AddGaugeMaxZ + CalculeGpu + GetResult,
+ * JDsGaugeSystem.cpp:383-441, JDsGaugeItem.cpp:427-478, 614-641, 728-790,
+ * 1023-1087), n gauges per call.  Host arrays in and out; the call waits for
+ * the result.  The results follow the reference's CPU gauges: unnormalised
+ * kernel sums W*m/rho accumulated in double, the domain of the gauges being the
+ * map (maprealposmin..maprealposmax).  A small device scratch is allocated on
+ * the first gauge call of a context (and grown for larger n).
+ *   velocity: points 3n doubles (x,y,z) -> vel 3n floats, zero for a point
+ *             outside the map;
+ *   swl:      p0p2 6n doubles (point0 x,y,z, point2 x,y,z), pointdp n doubles,
+ *             masslimit n floats (<= 0 takes massfluid*0.5, 0.4 in 2-D)
+ *             -> surf 3n floats, the first point going from point0 to point2
+ *             where the kernel mass drops below the limit (at most 2^20
+ *             points per line, GBSPH_EINVAL beyond);
+ *   maxz:     p0h 4n doubles (point0 x,y,z, height), distlimit n floats
+ *             -> zmax n floats, the highest fluid particle within distlimit of
+ *             the vertical segment, at least the map's lower z. */
+int gbsph_gauge_velocity(gbsph_ctx* ctx, unsigned n, const double* points, float* vel);
+int gbsph_gauge_swl(gbsph_ctx* ctx, unsigned n, const double* p0p2, const double* pointdp, const float* masslimit,
+                    float* surf);
+int gbsph_gauge_maxz(gbsph_ctx* ctx, unsigned n, const double* p0h, const float* distlimit, float* zmax);
 
 /* Kernel-launch counter of the context (launches issued since creation). */
 unsigned long long gbsph_launch_count(const gbsph_ctx* ctx);

@@ -43,6 +43,7 @@ class OrcCtes(C.Structure):
         ("dp", C.c_double), ("cs0", C.c_double), ("cflnumber", C.c_double), ("dtmin", C.c_double),
         ("dtini", C.c_double),
         ("mapposmin", C.c_double * 3), ("maprealposmin", C.c_double * 3), ("maprealsize", C.c_double * 3),
+        ("maprealposmax", C.c_double * 3),
         ("domposmin", C.c_double * 3), ("domrealposmin", C.c_double * 3), ("domrealposmax", C.c_double * 3),
         ("mapcells", C.c_uint * 3), ("domcells", C.c_uint * 3), ("domcellcode", C.c_uint),
     ]

@@ -14,6 +14,8 @@
 //==============================================================================
 #include "JSphCpuSingle.h"
 #include "JSphCfgRun.h"
+#include "JDsGaugeSystem.h"
+#include "JDsGaugeItem.h"
 #include "JAppInfo.h"
 #include "JLog2.h"
 #include "JCellDivCpuSingle.h"
@@ -183,6 +185,58 @@ class OracleCpu : public JSphCpuSingle{
     DumpState("end"); DumpDivide("end");
     WriteRaw(Out+"/end_dtlist.bin",DtList.data(),sizeof(double)*DtList.size());
   }
+
+  // Gauges of the final state with the reference's own gauge classes
+  // (JGaugeSystem::AddGauge*, JGaugeItem::CalculeCpu).  Input lines:
+  //   vel  x y z
+  //   swl  x0 y0 z0 x2 y2 z2 pointdp masslimit
+  //   maxz x y z height distlimit
+  // Output: one line per gauge with the result (velocity / surface point / zmax).
+  void RunGauges(const std::string& infile){
+    FILE* f=fopen(infile.c_str(),"r");
+    if(!f)return;
+    std::vector<std::string> kinds;
+    char kind[16];
+    unsigned ng=0;
+    while(fscanf(f,"%15s",kind)==1){
+      const std::string k=kind,name=std::string("g")+std::to_string(ng++);
+      if(k=="vel"){
+        double x,y,z; if(fscanf(f,"%lf %lf %lf",&x,&y,&z)!=3)break;
+        GaugeSystem->AddGaugeVel(name,0,1e30,0,true,TDouble3(x,y,z));
+      }
+      else if(k=="swl"){
+        double x0,y0,z0,x2,y2,z2,pdp; float ml;
+        if(fscanf(f,"%lf %lf %lf %lf %lf %lf %lf %f",&x0,&y0,&z0,&x2,&y2,&z2,&pdp,&ml)!=8)break;
+        GaugeSystem->AddGaugeSwl(name,0,1e30,0,true,TDouble3(x0,y0,z0),TDouble3(x2,y2,z2),pdp,ml);
+      }
+      else if(k=="maxz"){
+        double x,y,z,hgt; float dl;
+        if(fscanf(f,"%lf %lf %lf %lf %f",&x,&y,&z,&hgt,&dl)!=5)break;
+        GaugeSystem->AddGaugeMaxZ(name,0,1e30,0,true,TDouble3(x,y,z),hgt,dl);
+      }
+      else break;
+      kinds.push_back(k);
+    }
+    fclose(f);
+    GaugeSystem->ConfigArraysCpu(Pos_c,Code_c,Idp_c,Velrho_c);
+    GaugeSystem->CalculeCpu(TimeStep,DivData,NpbOk,Npb,Np,false);
+    FILE* o=fopen((Out+"/gauges_out.txt").c_str(),"w");
+    for(unsigned c=0;c<unsigned(kinds.size());c++){
+      JGaugeItem* g=GaugeSystem->GetGauge(c);
+      if(kinds[c]=="vel"){
+        const tfloat3 v=((JGaugeVelocity*)g)->GetResult().vel;
+        fprintf(o,"vel %.9g %.9g %.9g\n",v.x,v.y,v.z);
+      }
+      else if(kinds[c]=="swl"){
+        const tfloat3 v=((JGaugeSwl*)g)->GetResult().posswl;
+        fprintf(o,"swl %.9g %.9g %.9g\n",v.x,v.y,v.z);
+      }
+      else{
+        fprintf(o,"maxz %.9g\n",((JGaugeMaxZ*)g)->GetResult().zmax);
+      }
+    }
+    fclose(o);
+  }
 };
 
 int main(int argc,char** argv){
@@ -216,6 +270,7 @@ int main(int argc,char** argv){
     if(sph.IsSymplectic())sph.FirstStepDetailed();
     else sph.FirstStepVerlet();
     sph.RunSteps(nsteps);
+    sph.RunGauges(casedir+"/gauges.txt");
     rc=0;
   }
   catch(const JException& e){ fprintf(stderr,"JException: %s\n",e.what()); }

@@ -141,6 +141,7 @@ int orc_config(const orc_params* p, orc_ctes* c) {
   for (int k = 0; k < 3; k++) {
     c->maprealposmin[k] = p->maprealposmin[k];
     c->maprealsize[k] = p->maprealposmax[k] - p->maprealposmin[k];
+    c->maprealposmax[k] = p->maprealposmax[k];
     c->mapposmin[k] = p->maprealposmin[k];
     const double mapsize = p->maprealposmax[k] - p->maprealposmin[k];
     c->mapcells[k] = (unsigned)ceil(mapsize / c->scell);

@@ -67,7 +67,7 @@ typedef struct {
   float scell, movlimit, rhopoutmin, rhopoutmax, gravity[3];
   double dp, cs0, cflnumber, dtmin, dtini;
   /* domain */
-  double mapposmin[3], maprealposmin[3], maprealsize[3];
+  double mapposmin[3], maprealposmin[3], maprealsize[3], maprealposmax[3];
   double domposmin[3], domrealposmin[3], domrealposmax[3];
   unsigned mapcells[3], domcells[3], domcellcode;
 } orc_ctes;

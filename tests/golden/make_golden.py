@@ -43,6 +43,37 @@ CASES = {
 }
 
 
+GAUGE_CASES = ("dbc_d04", "mdbc_d04")
+GAUGE_KINDS = {"vel": 0, "swl": 1, "maxz": 2}
+
+
+def gauges_for(spec) -> list:
+    """Gauges of a dam-break case, as (kind, 8 parameters): vel (x,y,z), swl
+    (x0,y0,z0,x2,y2,z2,pointdp,masslimit), maxz (x,y,z,height,distlimit) --
+    inside the column, near its front and surface, where there is no fluid and
+    outside the map."""
+    tx, ty, tz = spec.tank
+    cx, cy, cz = spec.column
+    dp = spec.dp
+    h2 = 2.0 * spec.coefh * (3.0 ** 0.5) * dp
+    ym = cy / 2
+    g = [("vel", (cx * 0.5, ym, cz * 0.5)), ("vel", (cx * 0.95, ym * 0.9, cz * 0.2)),
+         ("vel", (cx * 0.5, ym, cz * 0.98)), ("vel", (tx * 0.8, ym, tz * 0.5)), ("vel", (-1.0, ym, 0.1)),
+         ("swl", (cx * 0.5, ym, dp, cx * 0.5, ym, tz - dp, dp / 2, 0.0)),
+         ("swl", (cx * 0.9, ym * 0.7, dp, cx * 0.9, ym * 0.7, tz - dp, dp / 2, 0.0)),
+         ("swl", (tx * 0.8, ym, dp, tx * 0.8, ym, tz - dp, dp / 2, 0.0)),
+         ("maxz", (cx * 0.5, ym, 0.0, tz, h2)), ("maxz", (cx * 0.9, ym, 0.0, tz, h2)),
+         ("maxz", (tx * 0.8, ym, 0.0, tz, h2))]
+    return [(k, tuple(float(v) for v in p) + (0.0,) * (8 - len(p))) for k, p in g]
+
+
+def _write_gauges(casedir: str, gauges: list) -> None:
+    nargs = {"vel": 3, "swl": 8, "maxz": 5}
+    with open(os.path.join(casedir, "gauges.txt"), "w") as f:
+        for k, p in gauges:
+            f.write(k + " " + " ".join(repr(v) for v in p[:nargs[k]]) + "\n")
+
+
 def run_options(name: str) -> list:
     """Run options of a case beyond the run XML (the reference takes the cell
     mode from the command line)."""
@@ -73,7 +104,11 @@ def make(name: str, threads: int = 8) -> str:
         casedir = os.path.join(tmp, "case")
         outdir = os.path.join(tmp, "out")
         os.makedirs(outdir)
-        cg.write_case(cg.make_dam_break(spec_fn()), casedir)
+        spec = spec_fn()
+        cg.write_case(cg.make_dam_break(spec), casedir)
+        gauges = gauges_for(spec) if name in GAUGE_CASES else []
+        if gauges:
+            _write_gauges(casedir, gauges)
         subprocess.run([HARNESS, casedir, name, outdir, str(nsteps), str(threads)] + run_options(name), check=True,
                        stdout=subprocess.DEVNULL)
         arr = {}
@@ -94,6 +129,15 @@ def make(name: str, threads: int = 8) -> str:
         arr["dtlist"] = np.fromfile(os.path.join(outdir, "end_dtlist.bin"), dtype=np.float64)
         meta = {tag: _meta(outdir, tag) for tag in ("s0", "s0pred", "s0cor", "s0div", "s1", "end")
                 if os.path.exists(os.path.join(outdir, f"{tag}_meta.txt"))}
+        if gauges:  # gauges of the final state, computed by the reference's gauge classes
+            out = []
+            with open(os.path.join(outdir, "gauges_out.txt")) as f:
+                for line in f:
+                    v = [float(x) for x in line.split()[1:]]
+                    out.append(v + [0.0] * (3 - len(v)))
+            arr["gauge_kind"] = np.array([GAUGE_KINDS[k] for k, _ in gauges], np.uint8)
+            arr["gauge_par"] = np.array([p for _, p in gauges], np.float64)
+            arr["gauge_out"] = np.array(out, np.float64)
         arr["meta_json"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
         path = os.path.join(OUT, f"{name}.npz")
         np.savez_compressed(path, **arr)
