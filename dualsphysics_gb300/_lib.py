@@ -67,6 +67,14 @@ class DivInfo(C.Structure):
     ]
 
 
+class Mesh(C.Structure):
+    """gbsph_mesh: a mesh gauge's grid (jmsh::StMeshBasic)."""
+    _fields_ = [
+        ("ptref", C.c_double * 3), ("vec1", C.c_double * 3), ("vec2", C.c_double * 3), ("vec3", C.c_double * 3),
+        ("dis", C.c_double * 3), ("dispt", C.c_double * 3), ("dirdat", C.c_float * 3),
+    ]
+
+
 class Maxes(C.Structure):
     _fields_ = [("acemax", C.c_double), ("velmax", C.c_float), ("viscdtmax", C.c_float)]
 
@@ -108,6 +116,9 @@ SIGNATURES = {
     "gbsph_gauge_velocity": (C.c_int, [P, C.c_uint, P, P]),
     "gbsph_gauge_swl": (C.c_int, [P, C.c_uint, P, P, P, P]),
     "gbsph_gauge_maxz": (C.c_int, [P, C.c_uint, P, P, P]),
+    "gbsph_mesh_points": (C.c_int, [C.POINTER(Mesh), C.POINTER(C.c_uint * 3)]),
+    "gbsph_gauge_mesh": (C.c_int, [P, C.POINTER(Mesh), C.c_float, C.c_float, C.c_float, P, P, P, P, P]),
+    "gbsph_fluid_front": (C.c_int, [P, P, P, P, C.POINTER(C.c_double), C.POINTER(C.c_uint)]),
 }
 
 SORT_NOALLOC_MAX_KEYS = 262144  # GBSPH_SORT_NOALLOC_MAX_KEYS

@@ -777,6 +777,95 @@ int gbsph_gauge_maxz(gbsph_ctx* ctx, unsigned n, const double* p0h, const float*
   return GBSPH_OK;
 }
 
+// JMeshData::MakeMeshPt (JMeshData.cpp:474-503) with fgeo::VecUnitary.
+static bool make_mesh_pts(const gbsph_mesh* mb, GaugeMeshPts* m) {
+  memset(m, 0, sizeof(*m));
+  unsigned npt[3] = {1, 1, 1};
+  const double* vecs[3] = {mb->vec1, mb->vec2, mb->vec3};
+  double* vdps[3] = {m->vdp1, m->vdp2, m->vdp3};
+  for (int a = 0; a < 3; a++) {
+    const double* v = vecs[a];
+    const double dis = mb->dis[a], dispt = mb->dispt[a];
+    if ((v[0] != 0 || v[1] != 0 || v[2] != 0) && dispt > 0 && dis >= dispt) {
+      const double q = (dis + dispt * 0.01) / dispt;
+      if (!(q < 67108864.0)) return false;
+      const double mod = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      for (int k = 0; k < 3; k++) vdps[a][k] = (v[k] / mod) * dispt;
+      npt[a] = (unsigned)q + 1;
+    }
+  }
+  const unsigned long long n = (unsigned long long)npt[0] * npt[1] * npt[2];
+  if (n > (1ull << 26)) return false;
+  for (int k = 0; k < 3; k++) m->ptref[k] = mb->ptref[k];
+  m->npt1 = npt[0];
+  m->npt2 = npt[1];
+  m->npt3 = npt[2];
+  m->npt = (unsigned)n;
+  const float* d = mb->dirdat;
+  const float mod = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  for (int k = 0; k < 3; k++) m->dirdat[k] = mod ? d[k] / mod : d[k];
+  return true;
+}
+
+int gbsph_mesh_points(const gbsph_mesh* mesh, unsigned* npt3) {
+  GaugeMeshPts m;
+  if (!mesh || !npt3 || !make_mesh_pts(mesh, &m)) return GBSPH_EINVAL;
+  npt3[0] = m.npt1;
+  npt3[1] = m.npt2;
+  npt3[2] = m.npt3;
+  return GBSPH_OK;
+}
+
+int gbsph_gauge_mesh(gbsph_ctx* ctx, const gbsph_mesh* mesh, float kclimit, float kcdummy, float masslimit,
+                     float* vel, float* veldir, float* rhop, float* mass, float* zsurf) {
+  GaugeMeshPts m;
+  if (!ctx) return GBSPH_EINVAL;
+  if (!mesh || !make_mesh_pts(mesh, &m)) return set_err(ctx, GBSPH_EINVAL, "invalid mesh (more than 2^26 points?)");
+  const size_t n = m.npt, n12 = (size_t)m.npt1 * m.npt2;
+  const size_t ov = 0, od = align256(12 * n), orh = od + align256(4 * n), om = orh + align256(4 * n),
+               oz = om + align256(4 * n), total = oz + 4 * n12;
+  if (int rc = gauge_begin(ctx, 0, total, true)) return rc;
+  char* buf = (char*)ctx->gauge_buf;
+  const float ml = masslimit > 0 ? masslimit : ctx->c.massfluid * (ctx->c.simulate2d ? 0.4f : 0.5f);
+  gbk::gauge_mesh(ctx->c, ctx->a, m, kclimit, kcdummy, ml, vel ? (float*)(buf + ov) : nullptr,
+                  veldir ? (float*)(buf + od) : nullptr, rhop ? (float*)(buf + orh) : nullptr, (float*)(buf + om),
+                  zsurf ? (float*)(buf + oz) : nullptr, ctx->stream);
+  ctx->launches += zsurf ? 2 : 1;
+  CK(cudaGetLastError(), "gauge mesh");
+  if (vel) CK(cudaMemcpyAsync(vel, buf + ov, 12 * n, cudaMemcpyDeviceToHost, ctx->stream), "gauge out");
+  if (veldir) CK(cudaMemcpyAsync(veldir, buf + od, 4 * n, cudaMemcpyDeviceToHost, ctx->stream), "gauge out");
+  if (rhop) CK(cudaMemcpyAsync(rhop, buf + orh, 4 * n, cudaMemcpyDeviceToHost, ctx->stream), "gauge out");
+  if (mass) CK(cudaMemcpyAsync(mass, buf + om, 4 * n, cudaMemcpyDeviceToHost, ctx->stream), "gauge out");
+  if (zsurf) CK(cudaMemcpyAsync(zsurf, buf + oz, 4 * n12, cudaMemcpyDeviceToHost, ctx->stream), "gauge out");
+  CK(cudaStreamSynchronize(ctx->stream), "gauge sync");
+  return GBSPH_OK;
+}
+
+int gbsph_fluid_front(gbsph_ctx* ctx, const double* dir, const double* bmin, const double* bmax, double* front,
+                      unsigned* count) {
+  if (int rc = gauge_begin(ctx, 0, 16, dir && bmin && bmax && front)) return rc;
+  unsigned long long* key = (unsigned long long*)ctx->gauge_buf;
+  unsigned* cnt = (unsigned*)(key + 1);
+  CK(cudaMemsetAsync(ctx->gauge_buf, 0, 16, ctx->stream), "front init");
+  int nsm = 0;
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device), "attribute");
+  gbk::fluid_front(ctx->a, dir, bmin, bmax, key, cnt, nsm, ctx->stream);
+  ctx->launches++;
+  CK(cudaGetLastError(), "fluid front");
+  unsigned long long hk[2];
+  CK(cudaMemcpyAsync(hk, ctx->gauge_buf, 16, cudaMemcpyDeviceToHost, ctx->stream), "front out");
+  CK(cudaStreamSynchronize(ctx->stream), "front sync");
+  const unsigned n = (unsigned)(hk[1] & 0xffffffffu);
+  if (count) *count = n;
+  if (!n) {
+    *front = -HUGE_VAL;
+  } else {
+    const unsigned long long b = (hk[0] >> 63) ? (hk[0] & 0x7fffffffffffffffull) : ~hk[0];
+    memcpy(front, &b, sizeof(double));
+  }
+  return GBSPH_OK;
+}
+
 unsigned long long gbsph_launch_count(const gbsph_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 void* gbsph_stream(gbsph_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }

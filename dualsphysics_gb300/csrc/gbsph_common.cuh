@@ -178,6 +178,15 @@ __device__ __forceinline__ unsigned gb_cellidx(double d, double sc, double rsc) 
   return (unsigned)__ddiv_rn(d, sc);
 }
 
+// A mesh gauge's grid (jmsh::StMeshPts, JMeshDataDef.h:87-96): npt1 x npt2 x
+// npt3 points ptref + vdp1*i + vdp2*j + vdp3*k, and the direction of the
+// projected velocity.
+struct GaugeMeshPts {
+  double ptref[3], vdp1[3], vdp2[3], vdp3[3];
+  unsigned npt1, npt2, npt3, npt;
+  float dirdat[3];
+};
+
 // Launchers implemented in the .cu files (host side).
 namespace gbk {
 void load_dcell(const gbsph_consts& c, const DevArrays& a, unsigned n, cudaStream_t s);  // sets GB_ERR_PARTOUT in DivState::error
@@ -213,4 +222,11 @@ void gauge_swl(const gbsph_consts& c, const DevArrays& a, unsigned n, const doub
                const float* mlim, float* surf, cudaStream_t s);
 void gauge_maxz(const gbsph_consts& c, const DevArrays& a, unsigned n, const double* par, const float* dist,
                 float* zmax, cudaStream_t s);
+// Largest pos.dir over the fluid particles in [bmin, bmax] as an ordered key
+// (zero-initialised by the caller) and their count; nsm = the device's SMs.
+void fluid_front(const DevArrays& a, const double* dir, const double* bmin, const double* bmax,
+                 unsigned long long* key, unsigned* count, int nsm, cudaStream_t s);
+// mass (npt floats) is required; vel, vdir, rhop and zsurf may be null.
+void gauge_mesh(const gbsph_consts& c, const DevArrays& a, const GaugeMeshPts& m, float kclimit, float kcdummy,
+                float masslimit, float* vel, float* vdir, float* rhop, float* mass, float* zsurf, cudaStream_t s);
 }  // namespace gbk

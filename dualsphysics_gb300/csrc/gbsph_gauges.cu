@@ -286,9 +286,167 @@ __global__ void k_gauge_maxz(gbsph_consts c, DevArrays a, unsigned n, const doub
   if (lane == 0) zmax_out[w] = fmaxf(zmax, (float)c.maprealposmin[2]);
 }
 
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Mesh gauge: one warp per grid point.  Kernel sums W*m/rho of (1, m, rho,
+// vx, vy, vz) over the fluid particles within the kernel (no minimum
+// distance), in float as the reference, then the kernel correction: divided
+// by sum W*m/rho when that reaches kclimit, else kcdummy (FLT_MAX disables
+// either) (JGaugeMesh::CalculeCpuT, JDsGaugeItem.cpp:1513-1571).  The point is
+// ptref + vdp1*cp1 + vdp2*cp2 + vdp3*cp3, summed in that order.
+__global__ void k_gauge_mesh(gbsph_consts c, DevArrays a, GaugeMeshPts m, float kclimit, float kcdummy,
+                             float* __restrict__ vel, float* __restrict__ vdir, float* __restrict__ rhop,
+                             float* __restrict__ mass) {
+  const unsigned cp = blockIdx.x * kGaugeWarps + (threadIdx.x >> 5);
+  if (cp >= m.npt) return;
+  const int lane = threadIdx.x & 31;
+  const DivState& d = *a.div;
+  const unsigned npt12 = m.npt1 * m.npt2;
+  const unsigned cp3 = cp / npt12, cp3r = cp - cp3 * npt12;
+  const unsigned cp2 = cp3r / m.npt1, cp1 = cp3r - cp2 * m.npt1;
+  double pt[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    pt[k] = __dadd_rn(__dadd_rn(__dadd_rn(m.ptref[k], __dmul_rn(m.vdp1[k], (double)cp1)),
+                                __dmul_rn(m.vdp2[k], (double)cp2)),
+                      __dmul_rn(m.vdp3[k], (double)cp3));
+  float sw = 0.f, sm = 0.f, sr = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+  const GaugeCells g = gauge_cells(c, d, pt[0], pt[1], pt[2]);
+  if (g.ok) {
+    const float ks2 = c.kernelsize2, h = c.kernelh, awen = c.awen, massf = c.massfluid;
+    for (int z = g.zini; z < g.zfin; z++) {
+      for (int y = g.yini; y < g.yfin; y++) {
+        const unsigned row = d.boxfluid + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+        const unsigned pini = a.begincell[row + (unsigned)g.xini], pfin = a.begincell[row + (unsigned)g.xfin];
+        for (unsigned p = pini + lane; p < pfin; p += 32) {
+          const float rr2 = gauge_rr2(pt[0], pt[1], pt[2], a, p);
+          if (rr2 <= ks2 && gauge_fluid(a.code[p])) {
+            const float4 vr = a.velrho[p];
+            const float wab = __fmul_rn(gauge_wab(rr2, h, awen), __fdiv_rn(massf, vr.w));
+            sw = __fadd_rn(sw, wab);
+            sm = __fadd_rn(sm, __fmul_rn(wab, massf));
+            sr = __fadd_rn(sr, __fmul_rn(wab, vr.w));
+            sx = __fadd_rn(sx, __fmul_rn(wab, vr.x));
+            sy = __fadd_rn(sy, __fmul_rn(wab, vr.y));
+            sz = __fadd_rn(sz, __fmul_rn(wab, vr.z));
+          }
+        }
+      }
+    }
+  }
+  sw = warp_sumf(sw);
+  sm = warp_sumf(sm);
+  sr = warp_sumf(sr);
+  sx = warp_sumf(sx);
+  sy = warp_sumf(sy);
+  sz = warp_sumf(sz);
+  if (lane) return;
+  if (kclimit != FLT_MAX) {
+    if (sw >= kclimit) {
+      sx = __fdiv_rn(sx, sw);
+      sy = __fdiv_rn(sy, sw);
+      sz = __fdiv_rn(sz, sw);
+      sr = __fdiv_rn(sr, sw);
+    } else if (kcdummy != FLT_MAX) {
+      sx = sy = sz = sr = kcdummy;
+    }
+  }
+  if (vel) {
+    vel[3 * cp] = sx;
+    vel[3 * cp + 1] = sy;
+    vel[3 * cp + 2] = sz;
+  }
+  if (vdir)
+    vdir[cp] = __fadd_rn(__fadd_rn(__fmul_rn(sx, m.dirdat[0]), __fmul_rn(sy, m.dirdat[1])), __fmul_rn(sz, m.dirdat[2]));
+  if (rhop) rhop[cp] = sr;
+  mass[cp] = sm;
+}
+
+// Surface z of each column of the mesh along its third axis: the first
+// point where the mass drops below the limit, interpolated from the last
+// point above it (JDsGaugeItem.cpp:1573-1596).  One thread per column.
+__global__ void k_gauge_mesh_zsurf(GaugeMeshPts m, float masslimit, const float* __restrict__ mass,
+                                   float* __restrict__ zsurf) {
+  const unsigned col = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned npt12 = m.npt1 * m.npt2;
+  if (col >= npt12) return;
+  const unsigned cp2 = col / m.npt1, cp1 = col - cp2 * m.npt1;
+  float masspre = 0.f, fsurf = 0.f;
+  unsigned cpsurf = 0, cp = col;
+  for (unsigned cp3 = 0; cp3 < m.npt3 && !cpsurf; cp3++) {
+    const float ms = mass[cp];
+    if (ms > masslimit) masspre = ms;
+    if (ms < masslimit && masspre != 0.f) {
+      fsurf = __fdiv_rn(__fsub_rn(masslimit, masspre), __fsub_rn(ms, masspre));
+      cpsurf = cp3;
+    }
+    cp += npt12;
+  }
+  float z = (float)__dadd_rn(__dadd_rn(m.ptref[2], __dmul_rn(m.vdp1[2], (double)cp1)), __dmul_rn(m.vdp2[2], (double)cp2));
+  if (cpsurf == 0 && masspre != 0.f) z = __fadd_rn(z, (float)__dmul_rn(m.vdp3[2], (double)(m.npt3 - 1)));
+  if (cpsurf)
+    z = __fadd_rn(z, (float)__dadd_rn(__dmul_rn(m.vdp3[2], (double)(cpsurf - 1)), __dmul_rn(m.vdp3[2], (double)fsurf)));
+  zsurf[col] = z;
+}
+
+// Order-preserving map of a double onto unsigned 64-bit keys (for atomicMax).
+__device__ __forceinline__ unsigned long long gauge_dkey(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// Surge front: the largest pos.dir over the fluid particles inside the box
+// [bmin, bmax] (a flow front's position along dir, e.g. the dam-break tip for
+// dir = +x), and how many fluid particles the box holds.  Grid-stride over the
+// np particles of the divided state; warp max, then one atomic per warp.
+__global__ void k_fluid_front(DevArrays a, double3 dir, double3 bmin, double3 bmax,
+                              unsigned long long* __restrict__ key, unsigned* __restrict__ count) {
+  const unsigned np = a.div->np;
+  unsigned long long best = 0ull;
+  unsigned cnt = 0;
+  for (unsigned p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    const double x = a.px[p], y = a.py[p], z = a.pz[p];
+    if (gauge_fluid(a.code[p]) && x >= bmin.x && y >= bmin.y && z >= bmin.z && x <= bmax.x && y <= bmax.y &&
+        z <= bmax.z) {
+      const double v = __dadd_rn(__dadd_rn(__dmul_rn(x, dir.x), __dmul_rn(y, dir.y)), __dmul_rn(z, dir.z));
+      const unsigned long long k = gauge_dkey(v);
+      best = k > best ? k : best;
+      cnt++;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+    best = ob > best ? ob : best;
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0 && cnt) {
+    atomicMax(key, best);
+    atomicAdd(count, cnt);
+  }
+}
+
 }  // namespace
 
 namespace gbk {
+
+void fluid_front(const DevArrays& a, const double* dir, const double* bmin, const double* bmax,
+                 unsigned long long* key, unsigned* count, int nsm, cudaStream_t s) {
+  k_fluid_front<<<nsm * 4, 256, 0, s>>>(a, make_double3(dir[0], dir[1], dir[2]), make_double3(bmin[0], bmin[1], bmin[2]),
+                                        make_double3(bmax[0], bmax[1], bmax[2]), key, count);
+}
+
+void gauge_mesh(const gbsph_consts& c, const DevArrays& a, const GaugeMeshPts& m, float kclimit, float kcdummy,
+                float masslimit, float* vel, float* vdir, float* rhop, float* mass, float* zsurf, cudaStream_t s) {
+  if (!m.npt) return;
+  k_gauge_mesh<<<gb_div_up(m.npt, kGaugeWarps), kGaugeWarps * 32, 0, s>>>(c, a, m, kclimit, kcdummy, vel, vdir,
+                                                                         rhop, mass);
+  if (zsurf) k_gauge_mesh_zsurf<<<gb_div_up(m.npt1 * m.npt2, 128), 128, 0, s>>>(m, masslimit, mass, zsurf);
+}
 
 void gauge_velocity(const gbsph_consts& c, const DevArrays& a, unsigned n, const double* pts, float* vel,
                     cudaStream_t s) {

@@ -1,11 +1,15 @@
 """Gauge system on the GPU state: the host side of the reference's JGaugeSystem
-(JDsGaugeSystem.cpp:383-441) for the velocity, SWL and max-z gauges.
+(JDsGaugeSystem.cpp:383-468) for the velocity, SWL, max-z and mesh gauges.
 
-Gauges are added by name (AddGaugeVel / AddGaugeSwl / AddGaugeMaxZ), computed
-together on the current divided state by CalculeGpu (one gbsph_gauge_* call per
-gauge type, each one kernel launch) and read with GetResult; SaveResults writes
-the per-gauge CSV files the reference writes (Gauges<Type>_<name>.csv with the
-same columns, JDsGaugeItem.cpp:385-398, 679-693, 966-979).
+Gauges are added by name (AddGaugeVel / AddGaugeSwl / AddGaugeMaxZ /
+AddGaugeMesh), computed together on the current divided state by CalculeGpu
+(one gbsph_gauge_* call per gauge type, one per mesh gauge) and read with
+GetResult: a velocity or surface point (3 floats), a zmax, or for a mesh gauge
+a dict of vel, veldir, rhop, mass (per point) and zsurf (per column).
+Pressure() turns a mesh gauge's density into pressure probes.  SaveResults
+writes the per-gauge CSV files the reference writes for the point gauges
+(Gauges<Type>_<name>.csv with the same columns, JDsGaugeItem.cpp:385-398,
+679-693, 966-979).
 """
 from __future__ import annotations
 
@@ -17,7 +21,8 @@ import numpy as np
 
 from ._lib import lib
 
-VEL, SWL, MAXZ = "Vel", "SWL", "MaxZ"
+VEL, SWL, MAXZ, MESH = "Vel", "SWL", "MaxZ", "Mesh"
+FLT_MAX = float(np.finfo(np.float32).max)
 
 
 def _ptr(a: np.ndarray):
@@ -34,6 +39,9 @@ class Gauge:
     masslimit: float = 0.0
     height: float = 0.0
     distlimit: float = 0.0
+    mesh: object = None            # _lib.Mesh of a mesh gauge
+    kclimit: float = 0.5
+    kcdummy: float = 0.0
     results: list = field(default_factory=list)   # (timestep, value) per CalculeGpu
 
 
@@ -61,6 +69,31 @@ class GaugeSystem:
     def AddGaugeMaxZ(self, name: str, point0, height: float, distlimit: float) -> Gauge:
         return self._add(Gauge(name, MAXZ, tuple(float(v) for v in point0), height=float(height),
                                distlimit=float(distlimit)))
+
+    def AddGaugeMesh(self, name: str, ptref, vec1, vec2, vec3, dis, dispt, dirdat=(0.0, 0.0, 0.0),
+                     kclimit: float = 0.5, kcdummy: float = 0.0, masslimit: float = 0.0) -> Gauge:
+        """Mesh gauge (JGaugeSystem::AddGaugeMesh): a grid of npt1 x npt2 x npt3
+        points; kclimit / kcdummy None disable the kernel correction / the dummy
+        value (the reference's "none"); dirdat is made unitary as the
+        reference's XML loader does."""
+        from ._lib import Mesh
+        m = Mesh()
+        for f, v in (("ptref", ptref), ("vec1", vec1), ("vec2", vec2), ("vec3", vec3), ("dis", dis),
+                     ("dispt", dispt)):
+            getattr(m, f)[:] = [float(x) for x in v]
+        d = np.asarray(dirdat, np.float32)
+        n = np.float32(np.sqrt(np.float32(np.float32(d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])))
+        m.dirdat[:] = [float(x) for x in ((d / n).astype(np.float32) if n else d)]
+        return self._add(Gauge(name, MESH, tuple(float(v) for v in ptref), mesh=m, masslimit=float(masslimit),
+                               kclimit=FLT_MAX if kclimit is None else float(kclimit),
+                               kcdummy=FLT_MAX if kcdummy is None else float(kcdummy)))
+
+    @staticmethod
+    def MeshPoints(g: Gauge) -> tuple[int, int, int]:
+        out = (C.c_uint * 3)()
+        if lib().gbsph_mesh_points(C.byref(g.mesh), C.byref(out)) != 0:
+            raise ValueError(f"invalid mesh of gauge '{g.name}'")
+        return tuple(int(x) for x in out)
 
     def GetGauge(self, key) -> Gauge:
         if isinstance(key, int):
@@ -99,6 +132,24 @@ class GaugeSystem:
             self.sph._check(L.gbsph_gauge_maxz(ctx, len(mz), _ptr(p), _ptr(dl), _ptr(out)), "gauge maxz")
             for g, v in zip(mz, out):
                 g.results.append((timestep, np.float32(v)))
+        for g in (x for x in self.gauges if x.kind == MESH):
+            n1, n2, n3 = self.MeshPoints(g)
+            n = n1 * n2 * n3
+            r = {"npt": (n1, n2, n3), "vel": np.empty((n, 3), np.float32), "veldir": np.empty(n, np.float32),
+                 "rhop": np.empty(n, np.float32), "mass": np.empty(n, np.float32),
+                 "zsurf": np.empty(n1 * n2, np.float32)}
+            self.sph._check(L.gbsph_gauge_mesh(ctx, C.byref(g.mesh), g.kclimit, g.kcdummy, g.masslimit,
+                                               _ptr(r["vel"]), _ptr(r["veldir"]), _ptr(r["rhop"]), _ptr(r["mass"]),
+                                               _ptr(r["zsurf"])), "gauge mesh")
+            g.results.append((timestep, r))
+
+    def Pressure(self, rhop) -> np.ndarray:
+        """Pressure probes from a mesh gauge's kernel-corrected density, with the
+        case's Tait equation of state p = B((rho/rho0)^gamma - 1)
+        (FunSphEos.h:38-40)."""
+        c = self.sph.consts
+        r = np.asarray(rhop, np.float64)
+        return c.cteb * ((r / c.rhopzero) ** c.gamma - 1.0)
 
     def GetResult(self, key):
         """Last result of a gauge: velocity (3 floats), surface point (3 floats) or zmax."""
@@ -112,6 +163,8 @@ class GaugeSystem:
         """Writes dirout/Gauges<Type>_<name>.csv for every gauge (all results so far)."""
         files = []
         for g in self.gauges:
+            if g.kind == MESH:  # the reference writes mesh data through its own mesh-data files
+                continue
             path = os.path.join(dirout, f"Gauges{g.kind}_{g.name}.csv")
             p0 = ";".join("%g" % np.float32(v) for v in g.point0)
             with open(path, "w") as f:

@@ -175,6 +175,19 @@ class GbSphSingle:
         self._check(lib().gbsph_pips(self.ctx, C.byref(out)), "pips")
         return {"checked_bound": out[0], "real_bound": out[1], "checked_fluid": out[2], "real_fluid": out[3]}
 
+    def fluid_front(self, direction=(1.0, 0.0, 0.0), bmin=None, bmax=None) -> tuple[float, int]:
+        """Surge front: the largest pos.direction over the fluid particles in
+        the box [bmin, bmax] (default: everywhere) and how many fluid particles
+        the box holds; -inf when it holds none."""
+        big = 1e300
+        d = np.ascontiguousarray(direction, np.float64)
+        lo = np.ascontiguousarray(bmin if bmin is not None else (-big,) * 3, np.float64)
+        hi = np.ascontiguousarray(bmax if bmax is not None else (big,) * 3, np.float64)
+        front, n = C.c_double(), C.c_uint()
+        self._check(lib().gbsph_fluid_front(self.ctx, ptr(d), ptr(lo), ptr(hi), C.byref(front), C.byref(n)),
+                    "fluid_front")
+        return front.value, n.value
+
     def profile(self, max_launches: int) -> None:
         self._check(lib().gbsph_profile(self.ctx, max_launches), "profile")
 

@@ -234,6 +234,37 @@ int gbsph_gauge_swl(gbsph_ctx* ctx, unsigned n, const double* p0p2, const double
                     float* surf);
 int gbsph_gauge_maxz(gbsph_ctx* ctx, unsigned n, const double* p0h, const float* distlimit, float* zmax);
 
+/* Mesh gauge (JGaugeMesh, JDsGaugeItem.cpp:1484-1596; the grid of
+ * JMeshData::MakeMeshPt, JMeshData.cpp:474-503): kernel-corrected velocity,
+ * velocity along dirdat, density and kernel mass at the npt1 x npt2 x npt3
+ * points ptref + i*dispt1*vec1/|vec1| + j*... + k*..., and the surface z of each
+ * (i,j) column along the third axis.  An axis with a zero vector, dispt <= 0
+ * or dis < dispt has one point; otherwise unsigned((dis+dispt/100)/dispt)+1.
+ * Sums are float, as the reference's.  The kernel correction divides by sum
+ * W*m/rho when that is >= kclimit, else sets kcdummy (FLT_MAX disables
+ * either; the reference's defaults are 0.5 and 0); masslimit <= 0 takes
+ * massfluid*0.5 (0.4 in 2-D).  Outputs (host arrays) may be NULL: vel 3*npt,
+ * veldir/rhop/mass npt, zsurf npt1*npt2 floats, point index i + j*npt1 +
+ * k*npt1*npt2.  At most 2^26 points. */
+typedef struct {
+  double ptref[3], vec1[3], vec2[3], vec3[3];
+  double dis[3], dispt[3];
+  float dirdat[3];
+} gbsph_mesh;
+int gbsph_mesh_points(const gbsph_mesh* mesh, unsigned* npt3);
+int gbsph_gauge_mesh(gbsph_ctx* ctx, const gbsph_mesh* mesh, float kclimit, float kcdummy, float masslimit,
+                     float* vel, float* veldir, float* rhop, float* mass, float* zsurf);
+
+/* Surge front: the largest pos.dir over the fluid particles inside the box
+ * [bmin, bmax] (bounds included), e.g. the dam-break tip position for
+ * dir = (1,0,0), and the number of fluid particles in the box (*count may be
+ * NULL).  With no fluid particle in the box, *front is -infinity.  This is the
+ * surge-front extraction that the reference does in post-processing from Part
+ * files (its experimental comparison X-DamTipPosition), done on the device
+ * state. */
+int gbsph_fluid_front(gbsph_ctx* ctx, const double* dir, const double* bmin, const double* bmax, double* front,
+                      unsigned* count);
+
 /* Kernel-launch counter of the context (launches issued since creation). */
 unsigned long long gbsph_launch_count(const gbsph_ctx* ctx);
 /* CUDA stream of the context (as void*), for callers that order their own work. */

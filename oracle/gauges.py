@@ -114,3 +114,148 @@ def gauge_maxz(p0, height, distlimit, pos, code, mapmin_z) -> np.float32:
     sel = (rr2 <= F(F(distlimit) * F(distlimit))) & _fluid(code)
     zmax = F(pos[sel, 2].max()) if sel.any() else F(-np.finfo(np.float32).max)
     return max(zmax, F(mapmin_z))
+
+
+# ---- mesh gauge ---------------------------------------------------------------
+def _vec_unitary(v):
+    """fgeo::VecUnitary for tdouble3 (FunGeo3d.h:293-296)."""
+    v = np.asarray(v, np.float64)
+    m = float(np.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]))
+    return np.array([v[0] / m, v[1] / m, v[2] / m]) if m else v
+
+
+def _vec_unitary_f(v):
+    """fgeo::VecUnitary for tfloat3 (FunGeo3d.h:302-305), in float."""
+    v = np.asarray(v, np.float32)
+    m = F(np.sqrt(F(F(v[0] * v[0] + v[1] * v[1]) + v[2] * v[2])))
+    return np.array([v[0] / m, v[1] / m, v[2] / m], np.float32) if m else v
+
+
+def mesh_points(mb):
+    """JMeshData::MakeMeshPt (JMeshData.cpp:474-503).  mb: 24 parameters
+    (ptref, vec1, vec2, vec3, dis1..3, dispt1..3, dirdat, ...).  Returns
+    (ptref, [vdp1, vdp2, vdp3], [npt1, npt2, npt3], dirdat)."""
+    mb = [float(x) for x in mb]
+    vdp, npt = [], []
+    for a in range(3):
+        vec = np.array(mb[3 + 3 * a:6 + 3 * a])
+        dis, dispt = mb[12 + a], mb[15 + a]
+        if vec.any() and dispt > 0 and dis >= dispt:
+            vdp.append(_vec_unitary(vec) * dispt)
+            npt.append(int((dis + dispt * 0.01) / dispt) + 1)
+        else:
+            vdp.append(np.zeros(3))
+            npt.append(1)
+    return np.array(mb[0:3]), vdp, npt, _vec_unitary_f(_vec_unitary_f(mb[18:21]))
+
+
+def _ordered_candidates(pt, div, c) -> np.ndarray:
+    """Particle indices nsearch::Init(pos)/ParticleRange visit for a point, in
+    their order: z, then y, then the x run of cells (JCellSearch_inline.h:43-68)."""
+    sd = int(div["scelldiv"])
+    nc = (int(div["ncx"]), int(div["ncy"]), int(div["ncz"]))
+    cel = []
+    for k in range(3):
+        q = (float(pt[k]) - float(c.domposmin[k])) / float(np.float32(c.scell))
+        cel.append(int(q) - int(div["cellmin"][k]))
+    lo, hi = [], []
+    for k in range(3):
+        ck = cel[k]
+        lo.append(ck - (ck if ck < sd else sd))
+        hi.append(ck + ((nc[k] - ck - 1) if nc[k] - ck - 1 < sd else sd) + 1)
+    if not (lo[0] < hi[0]):
+        return np.zeros(0, np.int64)
+    bc = div["begincell"]
+    idx = []
+    for z in range(lo[2], hi[2]):
+        for y in range(lo[1], hi[1]):
+            v = int(div["nsheet"]) * z + nc[0] * y + int(div["cellfluid"])
+            a, b = int(bc[v + lo[0]]), int(bc[v + hi[0]])
+            if b > a:
+                idx.append(np.arange(a, b))
+    return np.concatenate(idx) if idx else np.zeros(0, np.int64)
+
+
+def _serial_sum(x: np.ndarray) -> np.float32:
+    """Sum in float32 one term after another from 0 (the reference's loop)."""
+    return np.add.accumulate(x.astype(F), dtype=F)[-1] if len(x) else F(0)
+
+
+def gauge_mesh(mb, kclimit, kcdummy, masslimit, pos, velrho, code, div, c):
+    """JGaugeMesh::CalculeCpuT (JDsGaugeItem.cpp:1484-1596) on a divided state
+    (pos/velrho/code in cell order, div: ncx, ncy, ncz, nsheet, cellmin,
+    cellfluid, scelldiv, begincell).  Float sums one term after another in the
+    reference's cell order; the reference itself is compiled with -ffast-math,
+    which lets the compiler reassociate them, so the two agree to a few float
+    ulps of the sums' scale (also returned: S_vel = sum |w*v| per component,
+    S_rho = sum w*rho, each divided by sum w where the kernel correction
+    applies).  Returns vel (npt,3), veldir, rhop, mass (npt), zsurf
+    (npt1*npt2), S_vel (npt,3), S_rho (npt)."""
+    ptref, vdp, npt, vdir = mesh_points(mb)
+    n1, n2, n3 = npt
+    n12, n = n1 * n2, n1 * n2 * n3
+    ml = F(masslimit) if masslimit > 0 else F(F(c.massfluid) * F(0.4 if c.simulate2d else 0.5))
+    fmax = F(np.finfo(np.float32).max)
+    kcl, kcd = F(kclimit), F(kcdummy)
+    massf = F(c.massfluid)
+    vel = np.zeros((n, 3), F)
+    vdd = np.zeros(n, F)
+    rho = np.zeros(n, F)
+    mass = np.zeros(n, F)
+    s_vel = np.zeros((n, 3))
+    s_rho = np.zeros(n)
+    fl = _fluid(code)
+    for cp in range(n):
+        cp3, r = divmod(cp, n12)
+        cp2, cp1 = divmod(r, n1)
+        pt = ((ptref + vdp[0] * float(cp1)) + vdp[1] * float(cp2)) + vdp[2] * float(cp3)
+        cand = _ordered_candidates(pt, div, c)
+        rr2 = _rr2(pt, pos[cand]) if len(cand) else np.zeros(0, F)
+        sel = cand[(rr2 <= F(c.kernelsize2)) & fl[cand]]
+        rr2 = rr2[(rr2 <= F(c.kernelsize2)) & fl[cand]]
+        w = _wendland_wab(rr2, c.awen, c.kernelh)
+        vr = velrho[sel].astype(F)
+        w = (w * (massf / vr[:, 3]).astype(F)).astype(F)
+        swab = _serial_sum(w)
+        smass = _serial_sum((w * massf).astype(F))
+        srho = _serial_sum((w * vr[:, 3]).astype(F))
+        sv = np.array([_serial_sum((w * vr[:, k]).astype(F)) for k in range(3)], F)
+        s_vel[cp] = [float(np.abs(w.astype(np.float64) * vr[:, k]).sum()) for k in range(3)]
+        s_rho[cp] = float((w.astype(np.float64) * vr[:, 3]).sum())
+        if kcl != fmax:
+            if swab >= kcl:
+                sv = (sv / swab).astype(F)
+                srho = F(srho / swab)
+                s_vel[cp] /= float(swab)
+                s_rho[cp] /= float(swab)
+            elif kcd != fmax:
+                sv = np.array([kcd, kcd, kcd], F)
+                srho = kcd
+                s_vel[cp] = 0.0
+                s_rho[cp] = 0.0
+        vel[cp] = sv
+        vdd[cp] = F(F(F(sv[0] * vdir[0]) + F(sv[1] * vdir[1])) + F(sv[2] * vdir[2]))
+        rho[cp] = srho
+        mass[cp] = smass
+    zs = np.zeros(n12, F)
+    for cp2 in range(n2):
+        for cp1 in range(n1):
+            masspre, cpsurf, fsurf = F(0), 0, F(0)
+            cp = cp1 + cp2 * n1
+            for cp3 in range(n3):
+                if cpsurf:
+                    break
+                m = mass[cp]
+                if m > ml:
+                    masspre = m
+                if m < ml and masspre:
+                    fsurf = F(F(ml - masspre) / F(m - masspre))
+                    cpsurf = cp3
+                cp += n12
+            z = F(ptref[2] + vdp[0][2] * cp1 + vdp[1][2] * cp2)
+            if cpsurf == 0 and masspre:
+                z = F(z + F(vdp[2][2] * (n3 - 1)))
+            if cpsurf:
+                z = F(z + F(vdp[2][2] * (cpsurf - 1) + vdp[2][2] * float(fsurf)))
+            zs[cp1 + cp2 * n1] = z
+    return vel, vdd, rho, mass, zs, s_vel, s_rho

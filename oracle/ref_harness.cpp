@@ -21,6 +21,8 @@
 #include "JCellDivCpuSingle.h"
 #include "JException.h"
 #include "Functions.h"
+#include "FunGeo3d.h"
+#include "JMeshData.h"
 #include <cstdio>
 #include <fstream>
 #include <string>
@@ -191,7 +193,11 @@ class OracleCpu : public JSphCpuSingle{
   //   vel  x y z
   //   swl  x0 y0 z0 x2 y2 z2 pointdp masslimit
   //   maxz x y z height distlimit
-  // Output: one line per gauge with the result (velocity / surface point / zmax).
+  //   mesh ptref(3) vec1(3) vec2(3) vec3(3) dis1 dis2 dis3 dispt1 dispt2 dispt3
+  //        dirdat(3) kclimit kcdummy masslimit
+  // Output: one line per gauge with the result (velocity / surface point /
+  // zmax); a mesh gauge writes "mesh npt1 npt2 npt3", then one "pt vx vy vz
+  // vdir rhop" line per point and one "zs zsurf" line per column.
   void RunGauges(const std::string& infile){
     FILE* f=fopen(infile.c_str(),"r");
     if(!f)return;
@@ -214,6 +220,18 @@ class OracleCpu : public JSphCpuSingle{
         if(fscanf(f,"%lf %lf %lf %lf %f",&x,&y,&z,&hgt,&dl)!=5)break;
         GaugeSystem->AddGaugeMaxZ(name,0,1e30,0,true,TDouble3(x,y,z),hgt,dl);
       }
+      else if(k=="mesh"){
+        double v[18]; float d[3],kcl,kcd,ml; bool ok=true;
+        for(unsigned c=0;c<18 && ok;c++)ok=(fscanf(f,"%lf",v+c)==1);
+        if(!ok || fscanf(f,"%f %f %f %f %f %f",d,d+1,d+2,&kcl,&kcd,&ml)!=6)break;
+        jmsh::StMeshBasic mb;
+        mb.ptref=TDouble3(v[0],v[1],v[2]); mb.vec1=TDouble3(v[3],v[4],v[5]);
+        mb.vec2=TDouble3(v[6],v[7],v[8]); mb.vec3=TDouble3(v[9],v[10],v[11]);
+        mb.dis1=v[12]; mb.dis2=v[13]; mb.dis3=v[14];
+        mb.dispt1=v[15]; mb.dispt2=v[16]; mb.dispt3=v[17];
+        mb.dirdat=fgeo::VecUnitary(TFloat3(d[0],d[1],d[2]));
+        GaugeSystem->AddGaugeMesh(name,0,1e30,0,true,mb,"vel,veldir,rhop,zsurf",0,0,kcl,kcd,ml);
+      }
       else break;
       kinds.push_back(k);
     }
@@ -231,8 +249,20 @@ class OracleCpu : public JSphCpuSingle{
         const tfloat3 v=((JGaugeSwl*)g)->GetResult().posswl;
         fprintf(o,"swl %.9g %.9g %.9g\n",v.x,v.y,v.z);
       }
-      else{
+      else if(kinds[c]=="maxz"){
         fprintf(o,"maxz %.9g\n",((JGaugeMaxZ*)g)->GetResult().zmax);
+      }
+      else{
+        JGaugeMesh* gm=(JGaugeMesh*)g;
+        const jmsh::StMeshPts m=gm->GetMesh();
+        jmsh::JMeshData* md=gm->GetResult().meshdat;
+        const tfloat3* vel=md->GetVarFloat3("Vel");
+        const float* vdir=md->GetVarFloat("VelDir");
+        const float* rhop=md->GetVarFloat("Rhop");
+        const float* zsurf=md->GetVarFloat("Zsurf");
+        fprintf(o,"mesh %u %u %u\n",m.npt1,m.npt2,m.npt3);
+        for(unsigned p=0;p<m.npt;p++)fprintf(o,"pt %.9g %.9g %.9g %.9g %.9g\n",vel[p].x,vel[p].y,vel[p].z,vdir[p],rhop[p]);
+        for(unsigned p=0;p<m.npt1*m.npt2;p++)fprintf(o,"zs %.9g\n",zsurf[p]);
       }
     }
     fclose(o);

@@ -67,11 +67,33 @@ def gauges_for(spec) -> list:
     return [(k, tuple(float(v) for v in p) + (0.0,) * (8 - len(p))) for k, p in g]
 
 
-def _write_gauges(casedir: str, gauges: list) -> None:
+FLT_MAX = float(np.finfo(np.float32).max)
+
+
+def mesh_gauges_for(spec) -> list:
+    """Mesh gauges of a dam-break case, 24 parameters each: ptref (3), vec1..3
+    (9), dis1..3, dispt1..3, dirdat (3), kclimit, kcdummy, masslimit -- a
+    vertical x-z grid through the column and the flow (density for pressure
+    probes, surface z), and a y-z plane across the column without kernel
+    correction."""
+    tx, ty, tz = spec.tank
+    cx, cy, cz = spec.column
+    dp = spec.dp
+    ym = cy / 2
+    a = (0.05, ym, 0.02, 1, 0, 0, 0, 1, 0, 0, 0, 1, cx * 1.5, 0.0, tz - 0.04, dp, dp, dp / 2, 1, 0, 0,
+         0.5, 0.0, 0.0)
+    b = (cx * 0.5, 0.02, 0.02, 0, 1, 0, 0, 0, 1, 0, 0, 0, cy * 0.8, cz, 0.0, 2 * dp, dp, 0.0, 0, 0, 1,
+         FLT_MAX, FLT_MAX, 0.0)
+    return [tuple(float(v) for v in g) for g in (a, b)]
+
+
+def _write_gauges(casedir: str, gauges: list, meshes: list = ()) -> None:
     nargs = {"vel": 3, "swl": 8, "maxz": 5}
     with open(os.path.join(casedir, "gauges.txt"), "w") as f:
         for k, p in gauges:
             f.write(k + " " + " ".join(repr(v) for v in p[:nargs[k]]) + "\n")
+        for p in meshes:
+            f.write("mesh " + " ".join(repr(v) for v in p) + "\n")
 
 
 def run_options(name: str) -> list:
@@ -107,8 +129,9 @@ def make(name: str, threads: int = 8) -> str:
         spec = spec_fn()
         cg.write_case(cg.make_dam_break(spec), casedir)
         gauges = gauges_for(spec) if name in GAUGE_CASES else []
+        meshes = mesh_gauges_for(spec) if name in GAUGE_CASES else []
         if gauges:
-            _write_gauges(casedir, gauges)
+            _write_gauges(casedir, gauges, meshes)
         subprocess.run([HARNESS, casedir, name, outdir, str(nsteps), str(threads)] + run_options(name), check=True,
                        stdout=subprocess.DEVNULL)
         arr = {}
@@ -130,14 +153,26 @@ def make(name: str, threads: int = 8) -> str:
         meta = {tag: _meta(outdir, tag) for tag in ("s0", "s0pred", "s0cor", "s0div", "s1", "end")
                 if os.path.exists(os.path.join(outdir, f"{tag}_meta.txt"))}
         if gauges:  # gauges of the final state, computed by the reference's gauge classes
-            out = []
+            out, mnpt, mpt, mzs = [], [], [], []
             with open(os.path.join(outdir, "gauges_out.txt")) as f:
                 for line in f:
-                    v = [float(x) for x in line.split()[1:]]
-                    out.append(v + [0.0] * (3 - len(v)))
+                    t = line.split()
+                    v = [float(x) for x in t[1:]]
+                    if t[0] == "mesh":
+                        mnpt.append([int(x) for x in t[1:]])
+                    elif t[0] == "pt":
+                        mpt.append(v)
+                    elif t[0] == "zs":
+                        mzs.append(v[0])
+                    else:
+                        out.append(v + [0.0] * (3 - len(v)))
             arr["gauge_kind"] = np.array([GAUGE_KINDS[k] for k, _ in gauges], np.uint8)
             arr["gauge_par"] = np.array([p for _, p in gauges], np.float64)
             arr["gauge_out"] = np.array(out, np.float64)
+            arr["mesh_par"] = np.array(meshes, np.float64)
+            arr["mesh_npt"] = np.array(mnpt, np.uint32)
+            arr["mesh_pt"] = np.array(mpt, np.float64)
+            arr["mesh_zs"] = np.array(mzs, np.float64)
         arr["meta_json"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
         path = os.path.join(OUT, f"{name}.npz")
         np.savez_compressed(path, **arr)

@@ -79,6 +79,72 @@ def test_oracle_swl_points_follow_setpoints():
     assert n == 0 and not d.any()
 
 
+MESH_RTOL = 2e-6    # of the conditioning scale (float sums; about 16 ulp)
+ZSURF_ATOL = 1e-6
+
+
+def _div(g, pc):
+    m = g["meta"]["end"]
+    return dict(ncx=m["ncx"], ncy=m["ncy"], ncz=m["ncz"], nsheet=m["nsheet"],
+                cellmin=[int(x) for x in m["cellmin"].split(",")], cellfluid=m["cellfluid"],
+                scelldiv=pc.cellmode_div, begincell=g["end_begincell"])
+
+
+def _mesh_oracle(g, pc, k):
+    mb = g["mesh_par"][k]
+    return OG.gauge_mesh(mb[:21], mb[21], mb[22], mb[23], g["end_pos"], g["end_velrho"], g["end_code"],
+                         _div(g, pc), pc)
+
+
+def _mesh_ref(g, k):
+    """The reference's mesh gauge k: (vel, veldir, rhop) per point, zsurf per column."""
+    npt = g["mesh_npt"]
+    o1 = int(sum(int(np.prod(n)) for n in npt[:k]))
+    o2 = int(sum(int(n[0] * n[1]) for n in npt[:k]))
+    n, n12 = int(np.prod(npt[k])), int(npt[k][0] * npt[k][1])
+    pt = g["mesh_pt"][o1:o1 + n]
+    return pt[:, :3], pt[:, 3], pt[:, 4], g["mesh_zs"][o2:o2 + n12]
+
+
+def _check_mesh(got, ref, s_vel, s_rho, what):
+    vel, vdir, rho, zs = got
+    rvel, rvdir, rrho, rzs = ref
+    assert (np.abs(np.asarray(vel, np.float64) - rvel) <= MESH_RTOL * s_vel + 1e-12).all(), what + " vel"
+    assert (np.abs(np.asarray(vdir, np.float64) - rvdir) <= MESH_RTOL * s_vel.sum(axis=1) + 1e-12).all(), what + " vdir"
+    assert (np.abs(np.asarray(rho, np.float64) - rrho) <= MESH_RTOL * s_rho + 1e-12).all(), what + " rhop"
+    np.testing.assert_allclose(zs, rzs, rtol=0, atol=ZSURF_ATOL, err_msg=what + " zsurf")
+
+
+@pytest.mark.parametrize("name", GAUGE_CASES)
+def test_oracle_mesh_gauges_match_reference(name):
+    g, cd, pc = _state(name)
+    assert len(g["mesh_par"]) == 2
+    for k in range(2):
+        vel, vdir, rho, mass, zs, s_vel, s_rho = _mesh_oracle(g, pc, k)
+        _check_mesh((vel, vdir, rho, zs), _mesh_ref(g, k), s_vel, s_rho, f"{name} mesh {k}")
+    # the vertical grid crosses the free surface: columns inside the column of
+    # water find it near its height, columns past the front stay at ptref.z
+    zs = _mesh_ref(g, 0)[3]
+    spec = G.case_spec(name)
+    assert abs(zs[0] - spec.column[2]) < spec.dp and np.float32(zs[-1]) == np.float32(g["mesh_par"][0][2])
+
+
+def test_mesh_points_host_entry_matches_reference_grid():
+    from dualsphysics_gb300.gauges import GaugeSystem as GS
+    g = G.golden("dbc_d04")
+    gs = GS(_FakeSph())
+    for k, mb in enumerate(g["mesh_par"]):
+        gg = gs.AddGaugeMesh(f"m{k}", mb[0:3], mb[3:6], mb[6:9], mb[9:12], mb[12:15], mb[15:18], mb[18:21])
+        assert GS.MeshPoints(gg) == tuple(int(x) for x in g["mesh_npt"][k])
+        assert list(OG.mesh_points(mb)[2]) == list(g["mesh_npt"][k])
+    # an axis with dis < dispt has one point; 2^26 points are the limit
+    gg = gs.AddGaugeMesh("one", (0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (0.005, 0.0, 1.0), (0.01, 0.01, 0.5))
+    assert GS.MeshPoints(gg) == (1, 1, 3)
+    gg = gs.AddGaugeMesh("big", (0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (1.0, 1.0, 1.0), (1e-3, 1e-3, 1e-2))
+    with pytest.raises(ValueError):
+        GS.MeshPoints(gg)
+
+
 class _FakeSph:
     ctx = None
 
@@ -183,6 +249,49 @@ def test_gpu_gauges_random_points_match_restatement():
     for i in range(m):
         par = np.concatenate([p0h[i], [dl[i], 0, 0, 0]])
         _check(2, np.array([zmax[i], 0, 0], np.float64), _oracle_gauge(2, par, g, cd, pc), f"maxz line {i}")
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", GAUGE_CASES)
+def test_gpu_mesh_gauges_match_reference_and_restatement(name):
+    g, cd, pc = _state(name)
+    s = _gpu_on_end_state(g, cd)
+    gs = GaugeSystem(s)
+    for k, mb in enumerate(g["mesh_par"]):
+        kcl = None if mb[21] == np.float32(np.finfo(np.float32).max) else mb[21]
+        kcd = None if mb[22] == np.float32(np.finfo(np.float32).max) else mb[22]
+        gs.AddGaugeMesh(f"m{k}", mb[0:3], mb[3:6], mb[6:9], mb[9:12], mb[12:15], mb[15:18], mb[18:21],
+                        kclimit=kcl, kcdummy=kcd, masslimit=mb[23])
+    gs.CalculeGpu(0.0)
+    for k in range(2):
+        r = gs.GetResult(k)
+        vel, vdir, rho, mass, zs, s_vel, s_rho = _mesh_oracle(g, pc, k)
+        got = (r["vel"], r["veldir"], r["rhop"], r["zsurf"])
+        _check_mesh(got, _mesh_ref(g, k), s_vel, s_rho, f"{name} mesh {k} vs reference")
+        _check_mesh(got, (vel, vdir, rho, zs), s_vel, s_rho, f"{name} mesh {k} vs restatement")
+        np.testing.assert_allclose(r["mass"], mass, rtol=MESH_RTOL, atol=1e-12)
+    p = gs.Pressure(gs.GetResult(0)["rhop"])
+    assert np.isfinite(p).all() and p.max() > 0
+    s.close()
+
+
+@pytest.mark.gpu
+def test_gpu_fluid_front_equals_numpy():
+    g, cd, pc = _state("dbc_d04")
+    s = _gpu_on_end_state(g, cd)
+    pos, fl = g["end_pos"], (g["end_code"] & 0x1800) == 0x1800
+    front, n = s.fluid_front()
+    assert front == pos[fl, 0].max() and n == int(fl.sum())
+    lo, hi = (0.0, 0.0, 0.0), (10.0, 10.0, 2 * cd.params.dp)
+    inb = fl & (pos >= lo).all(axis=1) & (pos <= hi).all(axis=1)
+    front, n = s.fluid_front((1.0, 0.0, 0.0), lo, hi)
+    assert front == pos[inb, 0].max() and n == int(inb.sum())
+    d = np.array([0.6, 0.0, -0.8])
+    front, n = s.fluid_front(d)
+    assert front == ((pos[fl, 0] * d[0] + pos[fl, 1] * d[1]) + pos[fl, 2] * d[2]).max()
+    front, n = s.fluid_front((1.0, 0.0, 0.0), (5.0, 5.0, 5.0), (6.0, 6.0, 6.0))
+    assert front == -np.inf and n == 0
     s.close()
 
 
