@@ -23,6 +23,7 @@
 #include "Functions.h"
 #include "FunGeo3d.h"
 #include "JMeshData.h"
+#include <cfloat>
 #include <cstdio>
 #include <fstream>
 #include <string>
@@ -198,9 +199,8 @@ class OracleCpu : public JSphCpuSingle{
   // Output: one line per gauge with the result (velocity / surface point /
   // zmax); a mesh gauge writes "mesh npt1 npt2 npt3", then one "pt vx vy vz
   // vdir rhop" line per point and one "zs zsurf" line per column.
-  void RunGauges(const std::string& infile){
-    FILE* f=fopen(infile.c_str(),"r");
-    if(!f)return;
+  // Adds the gauges listed in f to the gauge system; returns their kinds.
+  std::vector<std::string> ParseGauges(FILE* f){
     std::vector<std::string> kinds;
     char kind[16];
     unsigned ng=0;
@@ -235,10 +235,14 @@ class OracleCpu : public JSphCpuSingle{
       else break;
       kinds.push_back(k);
     }
-    fclose(f);
+    return(kinds);
+  }
+
+  // Computes every gauge on the current divided state with the reference's
+  // JGaugeSystem::CalculeCpu and writes their results to o.
+  void CalculeAndWriteGauges(FILE* o,const std::vector<std::string>& kinds){
     GaugeSystem->ConfigArraysCpu(Pos_c,Code_c,Idp_c,Velrho_c);
     GaugeSystem->CalculeCpu(TimeStep,DivData,NpbOk,Npb,Np,false);
-    FILE* o=fopen((Out+"/gauges_out.txt").c_str(),"w");
     for(unsigned c=0;c<unsigned(kinds.size());c++){
       JGaugeItem* g=GaugeSystem->GetGauge(c);
       if(kinds[c]=="vel"){
@@ -263,6 +267,46 @@ class OracleCpu : public JSphCpuSingle{
         fprintf(o,"mesh %u %u %u\n",m.npt1,m.npt2,m.npt3);
         for(unsigned p=0;p<m.npt;p++)fprintf(o,"pt %.9g %.9g %.9g %.9g %.9g\n",vel[p].x,vel[p].y,vel[p].z,vdir[p],rhop[p]);
         for(unsigned p=0;p<m.npt1*m.npt2;p++)fprintf(o,"zs %.9g\n",zsurf[p]);
+      }
+    }
+  }
+
+  void RunGauges(const std::string& infile){
+    FILE* f=fopen(infile.c_str(),"r");
+    if(!f)return;
+    const std::vector<std::string> kinds=ParseGauges(f);
+    fclose(f);
+    FILE* o=fopen((Out+"/gauges_out.txt").c_str(),"w");
+    CalculeAndWriteGauges(o,kinds);
+    fclose(o);
+  }
+
+  // Long run with samples (series.txt: "<nsteps> <every>", then gauge lines):
+  // steps as the Run loop does (ComputeStep, then RunCellDivide,
+  // JSphCpuSingle.cpp:1183-1196) and, at step 0 and every <every> steps,
+  // writes "sample <nstep> <time> <np> <nfluid> <xfront>" (xfront: the largest
+  // x of a fluid particle) followed by the gauges' results.
+  void RunSeries(const std::string& infile){
+    FILE* f=fopen(infile.c_str(),"r");
+    if(!f)return;
+    unsigned nsteps=0,every=1;
+    if(fscanf(f,"%u %u",&nsteps,&every)!=2 || !every){ fclose(f); return; }
+    const std::vector<std::string> kinds=ParseGauges(f);
+    fclose(f);
+    FILE* o=fopen((Out+"/series_out.txt").c_str(),"w");
+    for(unsigned c=0;c<=nsteps;c++){
+      if(c){
+        const double stepdt=ComputeStep();
+        RunCellDivide(true);
+        TimeStep+=stepdt; Nstep++;
+      }
+      if(c%every==0){
+        const tdouble3* pos=Pos_c->cptr();
+        const typecode* code=Code_c->cptr();
+        double xf=-DBL_MAX; unsigned nf=0;
+        for(unsigned p=0;p<Np;p++)if(CODE_IsFluid(code[p])){ nf++; if(pos[p].x>xf)xf=pos[p].x; }
+        fprintf(o,"sample %u %.17g %u %u %.17g\n",Nstep,TimeStep,Np,nf,xf);
+        CalculeAndWriteGauges(o,kinds);
       }
     }
     fclose(o);
@@ -297,10 +341,13 @@ int main(int argc,char** argv){
     OracleCpu sph;
     sph.Out=outdir;
     sph.Prepare(AppInfo.GetFullName(),&cfg,log);
-    if(sph.IsSymplectic())sph.FirstStepDetailed();
-    else sph.FirstStepVerlet();
-    sph.RunSteps(nsteps);
-    sph.RunGauges(casedir+"/gauges.txt");
+    if(fun::FileExists(casedir+"/series.txt"))sph.RunSeries(casedir+"/series.txt");
+    else{
+      if(sph.IsSymplectic())sph.FirstStepDetailed();
+      else sph.FirstStepVerlet();
+      sph.RunSteps(nsteps);
+      sph.RunGauges(casedir+"/gauges.txt");
+    }
     rc=0;
   }
   catch(const JException& e){ fprintf(stderr,"JException: %s\n",e.what()); }

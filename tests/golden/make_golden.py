@@ -179,9 +179,64 @@ def make(name: str, threads: int = 8) -> str:
         return path
 
 
+SERIES = {"dbc_d04": (1800, 30)}   # case -> (steps, sample interval)
+
+
+def series_probes(spec) -> tuple:
+    """Pressure probes of a series: a mesh gauge of 7 heights x 2 columns at
+    mid-width, 1.5h off the wall behind the water column (x = 0) and at
+    x = 2 column lengths, where the surge passes."""
+    h = spec.coefh * (3.0 ** 0.5) * spec.dp
+    dz = 0.04
+    dx = 2 * spec.column[0] - 1.5 * h
+    return (1.5 * h, spec.column[1] / 2, spec.dp / 2, 0, 0, 1, 1, 0, 0, 0, 0, 0,
+            6 * dz, dx, 0.0, dz, dx, 0.0, 0, 0, 0, 0.5, 0.0, 0.0)
+
+
+def make_series(name: str, threads: int = 8) -> str:
+    """Runs the reference for SERIES[name] steps from the case's initial state
+    and records, every interval: step, time, particle and fluid counts, the
+    surge front (largest fluid x) and the probes' kernel-corrected density."""
+    nsteps, every = SERIES[name]
+    spec_fn = CASES[name][0]
+    with tempfile.TemporaryDirectory() as tmp:
+        casedir = os.path.join(tmp, "case")
+        outdir = os.path.join(tmp, "out")
+        os.makedirs(outdir)
+        spec = spec_fn()
+        cg.write_case(cg.make_dam_break(spec), casedir)
+        probes = series_probes(spec)
+        with open(os.path.join(casedir, "series.txt"), "w") as f:
+            f.write(f"{nsteps} {every}\n")
+            f.write("mesh " + " ".join(repr(float(v)) for v in probes) + "\n")
+        subprocess.run([HARNESS, casedir, name, outdir, "0", str(threads)] + run_options(name), check=True,
+                       stdout=subprocess.DEVNULL)
+        smp, rho = [], []
+        with open(os.path.join(outdir, "series_out.txt")) as f:
+            for line in f:
+                t = line.split()
+                if t[0] == "sample":
+                    smp.append([float(x) for x in t[1:]])
+                    rho.append([])
+                elif t[0] == "pt":
+                    rho[-1].append(float(t[5]))
+        smp = np.array(smp)
+        arr = {"step": smp[:, 0].astype(np.uint32), "time": smp[:, 1], "np": smp[:, 2].astype(np.uint32),
+               "nfluid": smp[:, 3].astype(np.uint32), "xfront": smp[:, 4], "probe_rhop": np.array(rho, np.float64),
+               "probe_par": np.array(probes, np.float64)}
+        path = os.path.join(OUT, f"series_{name}.npz")
+        np.savez_compressed(path, **arr)
+        return path
+
+
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit(f"reference harness not built: {HARNESS} (make -f oracle/Makefile.ref)")
-    for nm in (sys.argv[1:] or list(CASES)):
+    for nm in (sys.argv[1:] or list(CASES) + ["series"]):
+        if nm == "series":
+            for sn in SERIES:
+                p = make_series(sn)
+                print("series", sn, os.path.getsize(p), "bytes")
+            continue
         p = make(nm)
         print(nm, os.path.getsize(p), "bytes")
