@@ -75,6 +75,32 @@ class Mesh(C.Structure):
     ]
 
 
+class Movement(C.Structure):
+    """gbsph_movement: one predefined movement of a moving object."""
+    _fields_ = [
+        ("type", C.c_int), ("obj", C.c_uint), ("id", C.c_uint), ("nextid", C.c_uint), ("duration", C.c_double),
+        ("angdegrees", C.c_int), ("prev", C.c_int), ("v", C.c_double * 3), ("a", C.c_double * 3),
+        ("p", C.c_double * 3), ("axisp1", C.c_double * 3), ("axisp2", C.c_double * 3), ("s", C.c_double * 3),
+    ]
+
+
+class MotionEvent(C.Structure):
+    _fields_ = [("obj", C.c_uint), ("mov", C.c_uint), ("start", C.c_double), ("finish", C.c_double)]
+
+
+class MotionObject(C.Structure):
+    _fields_ = [("idbegin", C.c_uint), ("count", C.c_uint)]
+
+
+class MotionData(C.Structure):
+    _fields_ = [("type", C.c_int), ("linmov", C.c_double * 3), ("linvel", C.c_double * 3),
+                ("mat", C.c_double * 16)]
+
+
+MOV_TYPES = {"wait": 1, "mvrect": 2, "mvrectace": 3, "mvrot": 4, "mvrotace": 5, "mvrectsinu": 6, "mvrotsinu": 7,
+             "mvnull": 8}
+
+
 class Maxes(C.Structure):
     _fields_ = [("acemax", C.c_double), ("velmax", C.c_float), ("viscdtmax", C.c_float)]
 
@@ -119,6 +145,10 @@ SIGNATURES = {
     "gbsph_mesh_points": (C.c_int, [C.POINTER(Mesh), C.POINTER(C.c_uint * 3)]),
     "gbsph_gauge_mesh": (C.c_int, [P, C.POINTER(Mesh), C.c_float, C.c_float, C.c_float, P, P, P, P, P]),
     "gbsph_fluid_front": (C.c_int, [P, P, P, P, C.POINTER(C.c_double), C.POINTER(C.c_uint)]),
+    "gbsph_motion_create": (C.c_int, [C.c_uint, P, C.c_uint, P, C.c_uint, P, C.c_int, C.POINTER(P)]),
+    "gbsph_motion_destroy": (None, [P]),
+    "gbsph_motion_process": (C.c_int, [P, C.c_double, C.c_double, P]),
+    "gbsph_set_motion": (C.c_int, [P, P]),
 }
 
 SORT_NOALLOC_MAX_KEYS = 262144  # GBSPH_SORT_NOALLOC_MAX_KEYS

@@ -41,6 +41,9 @@ class CaseData:
     time_out: float
     savepos_double: bool
     raw: dict = field(default_factory=dict)
+    # moving boundaries: {"objects": [(idbegin, count)], "movements": [dict],
+    # "events": [(obj, mov, start, finish)]} or None (read_motion)
+    motion: dict | None = None
 
     @property
     def np(self) -> int:
@@ -150,18 +153,24 @@ def load_case(casedir: str, casename: str, cellmode: str = "full") -> CaseData:
             continue
         if el.tag not in counters:
             raise CaseError(f"unknown particle block <{el.tag}>")
-        if el.tag in ("moving", "floating"):
+        if el.tag == "floating":
             raise CaseError(f"<{el.tag}> particle blocks are outside the implemented hot path")
         blocks.append((el.tag, int(el.get("begin")), int(el.get("count"))))
+    order_kinds = [{"fixed": 0, "moving": 1, "fluid": 3}[b[0]] for b in blocks]
+    if order_kinds != sorted(order_kinds):
+        raise CaseError("particle blocks must come as fixed, moving, fluid")
     code_of = []
-    nfixed = sum(1 for b in blocks if b[0] == "fixed")
-    ifix = ifl = 0
+    ifix = imov = ifl = 0
     for kind, begin, count in blocks:
         if kind == "fixed":
             code_of.append((begin, count, CODE_TYPE_FIXED | ifix)); ifix += 1
+        elif kind == "moving":
+            code_of.append((begin, count, CODE_TYPE_MOVING | imov)); imov += 1
         else:
             code_of.append((begin, count, CODE_TYPE_FLUID | ifl)); ifl += 1
-    _ = nfixed
+    motion = None
+    if imov:
+        motion = read_motion(ex.find("motion"), [(b, c) for k, b, c in blocks if k == "moving"])
     # --- particles (JPartsLoad4.cpp:164-290)
     root_b = bi4.read(bi4_path, "JPartDataBi4")
     part = root_b.item("PART_0000")
@@ -238,7 +247,104 @@ def load_case(casedir: str, casename: str, cellmode: str = "full") -> CaseData:
                     code=np.ascontiguousarray(code[order]),
                     boundnor=None if boundnor is None else np.ascontiguousarray(boundnor[order]),
                     npb=nb, nfluid=npok - nb, time_max=gf("TimeMax", 0.0), time_out=gf("TimeOut", 0.0),
-                    savepos_double=bool(gi("SavePosDouble", 0)), raw={"params": kv})
+                    savepos_double=bool(gi("SavePosDouble", 0)), raw={"params": kv}, motion=motion)
+
+
+_VEC3 = ("vel", "ace", "velini", "freq", "ampl", "phase", "axisp1", "axisp2")
+
+
+def _f32(v) -> float:
+    """A value the reference reads with GetAttributeFloat (float, then double)."""
+    return float(np.float32(float(v)))
+
+
+def read_motion(node, objects: list) -> dict:
+    """``case.execution.motion`` as JMotion::ReadXml reads it (JMotion.cpp:692-905):
+    one ``<objreal ref>`` per moving block (ref k = the k-th moving block,
+    JDsMotion::ConfigObjects), its movements and its ``<begin>`` events.
+    Durations and event times are floats in the reference's reader."""
+    if node is None:
+        raise CaseError("moving particles without <motion> in the case XML")
+    movs, evts = [], []
+    seen = set()
+    for obj in node:
+        if obj.tag.startswith("_"):
+            continue
+        if obj.tag != "objreal":
+            raise CaseError(f"<{obj.tag}> in <motion> is not supported (only <objreal> without children)")
+        ref = int(obj.get("ref"))
+        if ref < 0 or ref >= len(objects) or ref in seen:
+            raise CaseError(f"motion reference {ref} does not match the moving blocks")
+        seen.add(ref)
+        for el in obj:
+            if el.tag.startswith("_"):
+                continue
+            if el.tag == "begin":
+                evts.append((ref, int(el.get("mov")), _f32(el.get("start")),
+                             _f32(el.get("finish")) if el.get("finish") is not None else -1.0))
+                continue
+            if el.tag in ("obj", "objreal"):
+                raise CaseError("nested motion objects are not supported")
+            if el.tag not in ("wait", "mvrect", "mvrectace", "mvrot", "mvrotace", "mvrectsinu", "mvrotsinu",
+                              "mvnull"):
+                raise CaseError(f"movement <{el.tag}> is not supported")
+            m = {"type": el.tag, "obj": ref, "id": int(el.get("id")), "next": int(el.get("next", 0)),
+                 "duration": _f32(el.get("duration")) if el.tag != "mvnull" else 0.0,
+                 "angdegrees": el.get("anglesunits", "degrees") == "degrees"}
+            if el.get("anglesunits", "degrees") not in ("degrees", "radians"):
+                raise CaseError("anglesunits must be degrees or radians")
+            for ch in el:
+                if ch.tag in ("axisp1", "axisp2") or (ch.tag in _VEC3 and el.tag in ("mvrect", "mvrectace",
+                                                                                      "mvrectsinu")):
+                    m[ch.tag] = (float(ch.get("x")), float(ch.get("y")), float(ch.get("z")))
+                elif ch.tag in ("vel", "ace", "velini"):
+                    m[ch.tag] = float(ch.get("ang"))
+                elif ch.tag in ("freq", "ampl", "phase"):
+                    m[ch.tag] = float(ch.get("v"))
+            movs.append(m)
+    if len(seen) != len(objects):
+        raise CaseError("the number of moving objects does not match the predefined motions")
+    return {"objects": list(objects), "movements": movs, "events": evts}
+
+
+def motion_structs(motion: dict):
+    """The gbsph_motion_create arguments of a read_motion() result."""
+    from . import _lib
+    objs = (_lib.MotionObject * len(motion["objects"]))(*[_lib.MotionObject(b, c) for b, c in motion["objects"]])
+    movs = (_lib.Movement * max(1, len(motion["movements"])))()
+    for i, m in enumerate(motion["movements"]):
+        d = movs[i]
+        d.type = _lib.MOV_TYPES[m["type"]]
+        d.obj, d.id, d.nextid, d.duration = m["obj"], m["id"], m["next"], m["duration"]
+        d.angdegrees = int(m["angdegrees"])
+        t = m["type"]
+        if t == "mvrect":
+            d.v[:] = m["vel"]
+        elif t == "mvrectace":
+            d.a[:] = m["ace"]
+            d.prev = int("velini" not in m)
+            if "velini" in m:
+                d.v[:] = m["velini"]
+        elif t == "mvrectsinu":
+            d.v[:], d.a[:] = m["freq"], m["ampl"]
+            d.prev = int("phase" not in m)
+            if "phase" in m:
+                d.p[:] = m["phase"]
+        elif t in ("mvrot", "mvrotace", "mvrotsinu"):
+            d.axisp1[:], d.axisp2[:] = m["axisp1"], m["axisp2"]
+            if t == "mvrot":
+                d.s[0] = m["vel"]
+            elif t == "mvrotace":
+                d.s[1] = m["ace"]
+                d.prev = int("velini" not in m)
+                d.s[0] = m.get("velini", 0.0)
+            else:
+                d.s[0], d.s[1] = m["freq"], m["ampl"]
+                d.prev = int("phase" not in m)
+                d.s[2] = m.get("phase", 0.0)
+    evts = (_lib.MotionEvent * max(1, len(motion["events"])))(
+        *[_lib.MotionEvent(o, mv, st, fi) for o, mv, st, fi in motion["events"]])
+    return objs, movs, len(motion["movements"]), evts, len(motion["events"])
 
 
 def params_to_dict(p: Params) -> dict:

@@ -19,7 +19,10 @@ Geometry (all sizes in metres):
 * mDBC normals (``BoundNor``): vector from each boundary particle to the
   nearest point of the boundary surface, which lies dp/2 outside the outer
   particle layer of each solid; the solver doubles it to reach the ghost node
-  (JSph.cpp:1411-1418).
+  (JSph.cpp:1411-1418);
+* optional tank motion (sloshing): the walls become one moving block with a
+  chain of predefined movements in the run XML's ``case.execution.motion``
+  (the schema JMotion::ReadXml reads, JMotion.cpp:692-905), starting at t=0.
 """
 from __future__ import annotations
 
@@ -32,6 +35,7 @@ import numpy as np
 from . import bi4
 
 CODE_TYPE_FLUID = 0x1800
+CODE_TYPE_MOVING = 0x0800
 
 
 @dataclass
@@ -62,7 +66,15 @@ class CaseSpec:
     time_max: float = 0.5
     time_out: float = 0.01
     posmax_z: str = "default + 50%"
+    posmin_x: str = "default"               # a moving tank needs room beyond its walls
+    posmax_x: str = "default"
     extra_params: dict = field(default_factory=dict)
+    # movements of the tank walls (JMotion XML), each a dict with type
+    # (mvrect, mvrectace, mvrot, mvrotace, mvrectsinu, mvrotsinu, wait), id,
+    # duration, optional next and anglesunits, and its elements (vector
+    # values as (x, y, z), rotation scalars as numbers); the first one starts
+    # at t=0.  None: fixed walls.
+    motion: list | None = None
 
 
 @dataclass
@@ -138,11 +150,18 @@ def make_dam_break(spec: CaseSpec) -> Case:
         htop = fl[:, 2].max()
         depth = np.maximum(htop - fl[:, 2], 0.0)
         rhop[npb:] = spec.rhop0 * (1.0 + spec.rhop0 * g * depth / b) ** (1.0 / spec.gamma)
-    # --- codes: fixed blocks 0 (tank), 1 (obstacle); fluid block 0
+    # --- codes: fixed blocks 0 (tank), 1 (obstacle); fluid block 0 -- or,
+    # with a tank motion, the walls as moving block 0 (JSphMk.cpp:86-123)
     code = np.zeros(n, dtype=np.uint16)
     code[nbw:npb] = 1
     code[npb:] = CODE_TYPE_FLUID
-    blocks = [("fixed", 0, 0, nbw)]
+    if spec.motion:
+        if nbo:
+            raise ValueError("a moving tank with an obstacle is not generated (fixed blocks must come first)")
+        code[:nbw] = CODE_TYPE_MOVING
+        blocks = [("moving", 0, 0, nbw)]
+    else:
+        blocks = [("fixed", 0, 0, nbw)]
     if nbo:
         blocks.append(("fixed", 1, nbw, nbo))
     blocks.append(("fluid", 0, npb, nf))
@@ -179,11 +198,40 @@ def _fmt(v: float) -> str:
     return repr(float(v))
 
 
+_ROT_SCALAR = {"vel": "ang", "ace": "ang", "velini": "ang", "freq": "v", "ampl": "v", "phase": "v"}
+
+
+def _motion_xml(movements: list) -> list:
+    """``case.execution.motion`` for moving object 0 (the tank walls)."""
+    lines = ['    <motion>', '      <objreal ref="0">',
+             f'        <begin mov="{int(movements[0]["id"])}" start="0" />']
+    for m in movements:
+        attrs = f'id="{int(m["id"])}"'
+        if m["type"] != "mvnull":
+            attrs += f' duration="{_fmt(m["duration"])}"'
+            if m.get("next"):
+                attrs += f' next="{int(m["next"])}"'
+            if m.get("anglesunits"):
+                attrs += f' anglesunits="{m["anglesunits"]}"'
+        lines.append(f'        <{m["type"]} {attrs}>')
+        for k, v in m.items():
+            if k in ("type", "id", "duration", "next", "anglesunits"):
+                continue
+            if isinstance(v, (tuple, list)):
+                lines.append(f'          <{k} x="{_fmt(v[0])}" y="{_fmt(v[1])}" z="{_fmt(v[2])}" />')
+            else:
+                lines.append(f'          <{k} {_ROT_SCALAR[k]}="{_fmt(v)}" />')
+        lines.append(f'        </{m["type"]}>')
+    lines += ['      </objreal>', '    </motion>']
+    return lines
+
+
 def write_case(case: Case, dirpath: str) -> tuple[str, str]:
     """Writes ``<name>.xml`` and ``<name>.bi4`` into ``dirpath``; returns their paths."""
     s = case.spec
     os.makedirs(dirpath, exist_ok=True)
     nf = case.np - case.npb
+    nmoving = sum(c for k, _, _, c in case.blocks if k == "moving")
     params = {
         "SavePosDouble": 1, "StepAlgorithm": s.step_algorithm, "VerletSteps": s.verlet_steps,
         "Kernel": 2, "ViscoTreatment": s.visco_treatment, "Visco": s.visco,
@@ -202,8 +250,8 @@ def write_case(case: Case, dirpath: str) -> tuple[str, str]:
     for k, v in params.items():
         lines.append(f'      <parameter key="{k}" value="{v}" />')
     lines += ['      <simulationdomain>',
-              '        <posmin x="default" y="default" z="default" />',
-              f'        <posmax x="default" y="default" z="{s.posmax_z}" />',
+              f'        <posmin x="{s.posmin_x}" y="default" z="default" />',
+              f'        <posmax x="{s.posmax_x}" y="default" z="{s.posmax_z}" />',
               '      </simulationdomain>',
               '    </parameters>',
               '    <constants>',
@@ -218,19 +266,26 @@ def write_case(case: Case, dirpath: str) -> tuple[str, str]:
               f'      <massbound value="{_fmt(case.mass)}" />',
               f'      <massfluid value="{_fmt(case.mass)}" />',
               '    </constants>',
-              f'    <particles np="{case.np}" nb="{case.npb}" nbf="{case.npb}" mkboundfirst="11" mkfluidfirst="1">']
+              f'    <particles np="{case.np}" nb="{case.npb}" nbf="{case.npb - nmoving}" mkboundfirst="11" '
+              'mkfluidfirst="1">']
     for kind, mk, begin, count in case.blocks:
         if kind == "fixed":
             lines.append(f'      <fixed mkbound="{mk}" mk="{11 + mk}" begin="{begin}" count="{count}" />')
+        elif kind == "moving":
+            lines.append(f'      <moving mkbound="{mk}" mk="{11 + mk}" begin="{begin}" count="{count}" '
+                         'refmotion="0" />')
         else:
             lines.append(f'      <fluid mkfluid="{mk}" mk="{1 + mk}" begin="{begin}" count="{count}" />')
-    lines += ['    </particles>', '  </execution>', '</case>', '']
+    lines += ['    </particles>']
+    if s.motion:
+        lines += _motion_xml(s.motion)
+    lines += ['  </execution>', '</case>', '']
     xml_path = os.path.join(dirpath, s.name + ".xml")
     with open(xml_path, "w") as f:
         f.write("\n".join(lines))
     root = bi4.make_partdata_root(
         casename=s.name, appname="dualsphysics_gb300.casegen", data2d=False, casenp=case.np,
-        casenfixed=case.npb, casenmoving=0, casenfloat=0, casenfluid=nf,
+        casenfixed=case.npb - nmoving, casenmoving=nmoving, casenfloat=0, casenfluid=nf,
         caseposmin=case.pos.min(axis=0), caseposmax=case.pos.max(axis=0), dp=s.dp, h=case.h, b=case.b,
         rhop0=s.rhop0, gamma=s.gamma, massbound=case.mass, massfluid=case.mass)
     part = bi4.make_part(0, 0.0, case.np, 0, 0, case.pos.min(axis=0), case.pos.max(axis=0), case.idp, case.pos,

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "gbsph_common.cuh"
+#include "gbsph_motion_internal.h"
 
 struct gbsph_ctx {
   gbsph_consts c;
@@ -49,6 +50,12 @@ struct gbsph_ctx {
   std::vector<cudaEvent_t> prof_ev;
   unsigned prof_cap = 0, prof_n = 0;
   cudaEvent_t marks[16] = {};
+  // moving boundaries: the attached motion, its per-step table on the device
+  // (MotionStep, nobj MotionObjDev, the ridp of nmoving ids) and a host copy
+  gbsph_motion* motion = nullptr;
+  unsigned mot_nobj = 0, mot_idmin = 0, mot_nmoving = 0;
+  void* mot_buf = nullptr;
+  std::vector<char> mot_host;
   void* gauge_buf = nullptr;  // gauge inputs and results (grown on demand)
   size_t gauge_bytes = 0;
   std::string err;
@@ -169,6 +176,9 @@ int do_forces(gbsph_ctx* ctx) {
   return cuda_check(ctx, cudaGetLastError(), "forces");
 }
 
+// Bytes of the device motion table before the ridp array.
+size_t motion_table_bytes(unsigned nobj) { return 256 + 256 * ((sizeof(MotionObjDev) * nobj + 255) / 256); }
+
 // One step, enqueued: ComputeStep_Sym/_Ver + RunCellDivide.
 int enqueue_step(gbsph_ctx* ctx) {
   const gbsph_consts& c = ctx->c;
@@ -183,6 +193,12 @@ int enqueue_step(gbsph_ctx* ctx) {
     gbk::dtvariable(c, ctx->a, 1, ctx->stream, &ctx->launches);
     gbk::symplectic_cor(c, ctx->a, ctx->cap, dtpre, ctx->stream, &ctx->launches);
     gbk::step_end(ctx->a, 1, ctx->stream, &ctx->launches);
+    if (ctx->motion) {  // RunMotion, before the divide that ends the step
+      char* mb = (char*)ctx->mot_buf;
+      gbk::motion_move(c, ctx->a, (const MotionStep*)mb, (const MotionObjDev*)(mb + 256), ctx->mot_nobj,
+                       (unsigned*)(mb + motion_table_bytes(ctx->mot_nobj)), ctx->mot_idmin, ctx->mot_nmoving,
+                       ctx->cap, ctx->stream, &ctx->launches);
+    }
   } else {
     if (c.tboundary == GBSPH_BC_MDBC) gbk::mdbc(c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
     if (int rc = do_forces(ctx)) return rc;
@@ -252,6 +268,7 @@ void gbsph_destroy(gbsph_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->gauge_buf) cudaFree(ctx->gauge_buf);
+  if (ctx->mot_buf) cudaFree(ctx->mot_buf);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -422,8 +439,78 @@ int gbsph_verlet(gbsph_ctx* ctx, double dt) {
   return cuda_check(ctx, cudaGetLastError(), "verlet");
 }
 
+// JSph::CalcMotion at the start of a Symplectic step (JSphGpuSingle.cpp:787):
+// the host advances the motion over [time, time+SymplecticDtPre] and copies
+// the step's motion table to the device.
+static int motion_prepare(gbsph_ctx* ctx) {
+  StepState st;
+  CK(cudaMemcpyAsync(&st, ctx->a.st, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream), "motion dt");
+  CK(cudaStreamSynchronize(ctx->stream), "motion sync");
+  const unsigned n = ctx->mot_nobj;
+  std::vector<gbsph_motion_data> md(n);
+  const int rc = gbsph_motion_process(ctx->motion, st.time, st.dtpre, md.data());
+  if (rc < 0) return set_err(ctx, GBSPH_EINVAL, "motion: time %.17g is before the motion's last interval", st.time);
+  std::vector<char>& h = ctx->mot_host;
+  h.assign(motion_table_bytes(n), 0);
+  MotionStep* hdr = (MotionStep*)h.data();
+  hdr->active = rc;
+  hdr->nobj = n;
+  hdr->dt = st.dtpre;
+  MotionObjDev* o = (MotionObjDev*)(h.data() + 256);
+  const gbsph_motion_object* info = gbmotion::objects(ctx->motion);
+  for (unsigned k = 0; k < n; k++) {
+    o[k].type = md[k].type;
+    o[k].idbegin = info[k].idbegin;
+    o[k].count = info[k].count;
+    for (int c = 0; c < 3; c++) {
+      o[k].linmov[c] = md[k].linmov[c];
+      o[k].linvel[c] = (float)md[k].linvel[c];  // ToTFloat3(m.linvel)
+    }
+    for (int c = 0; c < 12; c++) o[k].mat[c] = md[k].mat[c];
+  }
+  // pageable source: the copy has read it when the call returns
+  CK(cudaMemcpyAsync(ctx->mot_buf, h.data(), h.size(), cudaMemcpyHostToDevice, ctx->stream), "motion table");
+  return GBSPH_OK;
+}
+
+int gbsph_set_motion(gbsph_ctx* ctx, gbsph_motion* m) {
+  if (!ctx) return GBSPH_EINVAL;
+  CK(cudaSetDevice(ctx->device), "set device");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  reset_graph(ctx);
+  if (ctx->mot_buf) cudaFree(ctx->mot_buf);
+  ctx->mot_buf = nullptr;
+  ctx->motion = nullptr;
+  ctx->mot_nobj = ctx->mot_idmin = ctx->mot_nmoving = 0;
+  if (!m) return GBSPH_OK;
+  if (ctx->c.tstep != GBSPH_STEP_SYMPLECTIC) return set_err(ctx, GBSPH_EINVAL, "moving boundaries need Symplectic");
+  const unsigned n = gbmotion::object_count(m);
+  const gbsph_motion_object* info = gbmotion::objects(m);
+  unsigned long long lo = ~0ull, hi = 0;
+  for (unsigned k = 0; k < n; k++) {
+    lo = info[k].idbegin < lo ? info[k].idbegin : lo;
+    const unsigned long long e = (unsigned long long)info[k].idbegin + info[k].count;
+    hi = e > hi ? e : hi;
+  }
+  if (!n || hi <= lo || hi - lo > ctx->limit) return set_err(ctx, GBSPH_EINVAL, "motion objects do not fit the particles");
+  const size_t bytes = motion_table_bytes(n) + sizeof(unsigned) * (size_t)(hi - lo);
+  if (cudaMalloc(&ctx->mot_buf, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->mot_buf = nullptr;
+    return set_err(ctx, GBSPH_ENOMEM, "motion table");
+  }
+  CK(cudaMemset(ctx->mot_buf, 0, bytes), "motion table");
+  ctx->motion = m;
+  ctx->mot_nobj = n;
+  ctx->mot_idmin = (unsigned)lo;
+  ctx->mot_nmoving = (unsigned)(hi - lo);
+  return GBSPH_OK;
+}
+
 int gbsph_step(gbsph_ctx* ctx) {
   if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (ctx->motion)
+    if (int rc = motion_prepare(ctx)) return rc;
   return enqueue_step(ctx);
 }
 
@@ -433,12 +520,15 @@ int gbsph_run(gbsph_ctx* ctx, unsigned nsteps, int use_graph) {
   // only with the pointer parity they were captured with.  Verlet steps (one
   // divide and a host-side Euler counter) run eagerly.
   if (!use_graph || ctx->c.tstep != GBSPH_STEP_SYMPLECTIC) {
-    for (unsigned i = 0; i < nsteps; i++)
+    for (unsigned i = 0; i < nsteps; i++) {
+      if (ctx->motion)
+        if (int rc = motion_prepare(ctx)) return rc;
       if (int rc = enqueue_step(ctx)) return rc;
+    }
     return cuda_check(ctx, cudaGetLastError(), "run");
   }
   const int parity = (int)(ctx->swaps & 1u);
-  if (use_graph == 2) {
+  if (use_graph == 2 && !ctx->motion) {
     if (int rc = gbsph_graph_prepare(ctx, nsteps)) return rc;
     CK(cudaGraphLaunch(ctx->multi_exec, ctx->stream), "graph launch");
     ctx->swaps += 2 * nsteps;
@@ -466,6 +556,10 @@ int gbsph_run(gbsph_ctx* ctx, unsigned nsteps, int use_graph) {
     ctx->graph_parity = parity;
   }
   for (unsigned i = 0; i < nsteps; i++) {
+    // a motion is advanced on the host before each replay; its table lives in
+    // device memory, which the captured step reads
+    if (ctx->motion)
+      if (int rc = motion_prepare(ctx)) return rc;
     CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream), "graph launch");
     // the captured step swapped every cur/alt pair twice: parity unchanged
     ctx->swaps += 2;
@@ -477,6 +571,7 @@ int gbsph_run(gbsph_ctx* ctx, unsigned nsteps, int use_graph) {
 int gbsph_graph_prepare(gbsph_ctx* ctx, unsigned nsteps) {
   if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
   if (ctx->c.tstep != GBSPH_STEP_SYMPLECTIC) return set_err(ctx, GBSPH_EINVAL, "multi-step graphs need Symplectic");
+  if (ctx->motion) return set_err(ctx, GBSPH_EINVAL, "multi-step graphs cannot hold a motion advanced on the host");
   const int parity = (int)(ctx->swaps & 1u);
   if (ctx->multi_exec && ctx->multi_steps == nsteps && ctx->multi_parity == parity) return GBSPH_OK;
   if (ctx->multi_exec) cudaGraphExecDestroy(ctx->multi_exec);

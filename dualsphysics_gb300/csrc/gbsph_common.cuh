@@ -187,6 +187,22 @@ struct GaugeMeshPts {
   float dirdat[3];
 };
 
+// Motion of the moving objects over one step, written by the host before the
+// step and read by the move kernels (JDsMotion's StMotionData,
+// JDsMotionDef.h:33-44).
+struct MotionObjDev {
+  int type;               // 0 none, 1 linear, 2 matrix
+  unsigned idbegin, count;
+  double linmov[3];
+  float linvel[3];
+  double mat[12];         // rows 1..3 of the 4x4 matrix, row-major
+};
+struct MotionStep {
+  int active;             // some object is active: the boundary changes
+  unsigned nobj;
+  double dt;
+};
+
 // Launchers implemented in the .cu files (host side).
 namespace gbk {
 void load_dcell(const gbsph_consts& c, const DevArrays& a, unsigned n, cudaStream_t s);  // sets GB_ERR_PARTOUT in DivState::error
@@ -214,6 +230,12 @@ void verlet_step(const gbsph_consts& c, DevArrays& a, unsigned cap, const double
 void sps_tau(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch);
 void pips(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s);
 void step_end(const DevArrays& a, int symplectic, cudaStream_t s, unsigned long long* nlaunch);
+// RunMotion (JSphCpu.cpp:2189-2245): index of each moving particle by id, then
+// the linear or matrix movement of its object; marks the boundary changed.
+// ridp holds nmoving entries for the ids idmin..idmin+nmoving-1.
+void motion_move(const gbsph_consts& c, const DevArrays& a, const MotionStep* hdr, const MotionObjDev* objs,
+                 unsigned nobj, unsigned* ridp, unsigned idmin, unsigned nmoving, unsigned cap, cudaStream_t s,
+                 unsigned long long* nlaunch);
 // Gauges (gbsph_gauges.cu): device arrays in and out, n gauges per launch.
 // swl par: p0 (3) and step vector (3) per gauge; npts: PointNp; mlim: mass limit.
 // maxz par: p0 (3) and height per gauge.

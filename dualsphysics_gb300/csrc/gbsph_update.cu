@@ -216,9 +216,76 @@ __global__ void k_stage_download(DevArrays a, double* __restrict__ stage, unsign
   stage[3 * (size_t)p + 2] = a.pz[p];
 }
 
+// CalcRidp (JSphCpu.cpp:2099-2127) over the npb boundary particles: the
+// current index of each moving particle by id (ridp preset to UINT_MAX).
+// Thread 0 also marks the boundary changed when some object is active
+// (JSphCpu::RunMotion sets BoundChanged, JSphCpu.cpp:2196).
+__global__ void k_motion_ridp(DevArrays a, const MotionStep* __restrict__ hdr, unsigned idmin, unsigned nmoving,
+                              unsigned* __restrict__ ridp) {
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p == 0 && hdr->active) a.div->boundchanged = 1;
+  if (p >= a.div->npb) return;
+  const unsigned rel = a.idp[p] - idmin;
+  if (rel < nmoving) ridp[rel] = p;
+}
+
+// MatrixMulPoint: rows 1..3 of a 4x4 matrix times (x, y, z, 1).
+__device__ __forceinline__ double mat_row(const double* m, double x, double y, double z) {
+  return dadd(dadd(dadd(dmul(x, m[0]), dmul(y, m[1])), dmul(z, m[2])), m[3]);
+}
+
+// MoveLinBound / MoveMatBound (JSphCpu.cpp:2133-2173): one thread per moving
+// particle; the position goes through UpdatePos (cell, out flags), the
+// velocity becomes the object's (linear) or displacement/dt (matrix), and a
+// matrix movement also turns the mDBC normal.
+__global__ void k_motion_move(gbsph_consts c, DevArrays a, const MotionStep* __restrict__ hdr,
+                              const MotionObjDev* __restrict__ objs, unsigned nobj, const unsigned* __restrict__ ridp,
+                              unsigned idmin, unsigned nmoving, double rsc) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nmoving) return;
+  const unsigned id = idmin + i;
+  unsigned k = 0;
+  while (k < nobj && !(id >= objs[k].idbegin && id - objs[k].idbegin < objs[k].count)) k++;
+  if (k == nobj || objs[k].type == 0) return;
+  const unsigned p = ridp[i];
+  if (p == 0xffffffffu) return;
+  const MotionObjDev& o = objs[k];
+  const double x = a.px[p], y = a.py[p], z = a.pz[p];
+  const float4 v = a.velrho[p];
+  if (o.type == 1) {
+    update_pos(c, a, p, x, y, z, o.linmov[0], o.linmov[1], o.linmov[2], false, rsc);
+    a.velrho[p] = make_float4(o.linvel[0], o.linvel[1], o.linvel[2], v.w);
+    return;
+  }
+  const double* m = o.mat;
+  const double x2 = mat_row(m, x, y, z), z2 = mat_row(m + 8, x, y, z);
+  const double y2 = c.simulate2d ? y : mat_row(m + 4, x, y, z);
+  const double dx = __dsub_rn(x2, x), dy = __dsub_rn(y2, y), dz = __dsub_rn(z2, z);
+  update_pos(c, a, p, x, y, z, dx, dy, dz, false, rsc);
+  const double dt = hdr->dt;
+  a.velrho[p] = make_float4(gb_d2f(__ddiv_rn(dx, dt)), gb_d2f(__ddiv_rn(dy, dt)), gb_d2f(__ddiv_rn(dz, dt)), v.w);
+  if (a.boundnor) {
+    const float4 bn = a.boundnor[p];
+    const double gx = dadd(x, gb_f2d(bn.x)), gy = dadd(y, gb_f2d(bn.y)), gz = dadd(z, gb_f2d(bn.z));
+    a.boundnor[p] = make_float4(gb_d2f(__dsub_rn(mat_row(m, gx, gy, gz), x2)),
+                                gb_d2f(__dsub_rn(mat_row(m + 4, gx, gy, gz), y2)),
+                                gb_d2f(__dsub_rn(mat_row(m + 8, gx, gy, gz), z2)), bn.w);
+  }
+}
+
 }  // namespace
 
 namespace gbk {
+
+void motion_move(const gbsph_consts& c, const DevArrays& a, const MotionStep* hdr, const MotionObjDev* objs,
+                 unsigned nobj, unsigned* ridp, unsigned idmin, unsigned nmoving, unsigned cap, cudaStream_t s,
+                 unsigned long long* nlaunch) {
+  cudaMemsetAsync(ridp, 0xff, sizeof(unsigned) * nmoving, s);
+  k_motion_ridp<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(a, hdr, idmin, nmoving, ridp);
+  k_motion_move<<<gb_div_up(nmoving, kUpdBlock), kUpdBlock, 0, s>>>(c, a, hdr, objs, nobj, ridp, idmin, nmoving,
+                                                                    1.0 / (double)c.scell);
+  if (nlaunch) *nlaunch += 2;
+}
 
 void stage_upload(const DevArrays& a, const double* stage, const float* nor3, unsigned n, unsigned npb, cudaStream_t s) {
   if (n) k_stage_upload<<<gb_div_up(n, kUpdBlock), kUpdBlock, 0, s>>>(a, stage, nor3, n, npb);

@@ -39,6 +39,7 @@ class GbSphSingle:
         self.nstep = 0
         self.part = 0
         self.dirout = None
+        self.motion = C.c_void_p()   # gbsph_motion of a case with moving boundaries
 
     # ---- lifetime -------------------------------------------------------
     def _check(self, rc: int, what: str):
@@ -50,6 +51,9 @@ class GbSphSingle:
         if self.ctx:
             lib().gbsph_destroy(self.ctx)
             self.ctx = C.c_void_p()
+        if self.motion:
+            lib().gbsph_motion_destroy(self.motion)
+            self.motion = C.c_void_p()
 
     def __del__(self):
         try:
@@ -70,6 +74,13 @@ class GbSphSingle:
         self._check(lib().gbsph_create(C.byref(self.consts), cap, self.device, C.byref(self.ctx)), "gbsph_create")
         self._check(lib().gbsph_upload(self.ctx, cd.np, cd.npb, ptr(cd.pos), ptr(cd.velrho), ptr(cd.idp),
                                        ptr(cd.code), ptr(cd.boundnor)), "gbsph_upload")
+        if cd.motion:  # JSph::LoadCaseConfig -> JDsMotion::Init (JSph.cpp:1064-1067)
+            from .case import motion_structs
+            objs, movs, nmov, evts, nevt = motion_structs(cd.motion)
+            self._check(lib().gbsph_motion_create(len(cd.motion["objects"]), objs, nmov, movs, nevt, evts,
+                                                  int(cd.params.simulate2d), C.byref(self.motion)),
+                        "gbsph_motion_create")
+            self._check(lib().gbsph_set_motion(self.ctx, self.motion), "gbsph_set_motion")
         self.timestep = 0.0
         self.nstep = 0
 

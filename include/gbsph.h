@@ -265,6 +265,63 @@ int gbsph_gauge_mesh(gbsph_ctx* ctx, const gbsph_mesh* mesh, float kclimit, floa
 int gbsph_fluid_front(gbsph_ctx* ctx, const double* dir, const double* bmin, const double* bmax, double* front,
                       unsigned* count);
 
+/* ---- Moving boundaries (JDsMotion / JMotion: JDsMotion.cpp:66-136,
+ * JMotion.cpp:427-590, JMotionObj.cpp:416-690; applied as JSphGpu::RunMotion,
+ * JSphGpu.cpp:1173-1228).
+ * A motion holds the moving objects (the moving particle blocks, in block
+ * order: object k is motion reference k), their movements and the events that
+ * start them.  gbsph_motion_process advances it by one interval, as the
+ * reference does once per step with that step's dt, and returns each object's
+ * displacement: linear (linmov, with velocity linvel = linmov/dt) or a 4x4
+ * matrix (rotations); an object with no active movement returns type 0.  The
+ * motion is stateful (phases, velocities, chained movements), so it must be
+ * advanced once per step in order.  Host-only: no device is touched. */
+#define GBSPH_MOV_WAIT 1
+#define GBSPH_MOV_RECT 2        /* vel (v) */
+#define GBSPH_MOV_RECTACE 3     /* ace (a), velini (v) unless prev */
+#define GBSPH_MOV_ROT 4         /* axisp1, axisp2, angular vel (s[0]) */
+#define GBSPH_MOV_ROTACE 5      /* axisp1, axisp2, angular ace (s[1]), velini (s[0]) unless prev */
+#define GBSPH_MOV_RECTSINU 6    /* freq (v), ampl (a), phase (p) unless prev */
+#define GBSPH_MOV_ROTSINU 7     /* axisp1, axisp2, freq (s[0]), ampl (s[1]), phase (s[2]) unless prev */
+#define GBSPH_MOV_NULL 8
+typedef struct {
+  int type;            /* GBSPH_MOV_* */
+  unsigned obj;        /* moving object (reference) the movement belongs to */
+  unsigned id, nextid; /* movement id within its object; the next movement's id (0: none) */
+  double duration;     /* seconds; < 0 is an instantaneous movement */
+  int angdegrees;      /* anglesunits: 1 degrees, 0 radians */
+  int prev;            /* velini/phase taken from the previous movement */
+  double v[3], a[3], p[3], axisp1[3], axisp2[3], s[3];  /* parameters, as the XML gives them */
+} gbsph_movement;
+typedef struct {
+  unsigned obj, mov;   /* object and movement id */
+  double start, finish;  /* finish < 0: none */
+} gbsph_motion_event;
+typedef struct {
+  unsigned idbegin, count;  /* ids of the object's particles */
+} gbsph_motion_object;
+typedef struct {
+  int type;              /* 0 none, 1 linear, 2 matrix */
+  double linmov[3], linvel[3];
+  double mat[16];        /* row-major a11..a44 */
+} gbsph_motion_data;
+typedef struct gbsph_motion gbsph_motion;
+int gbsph_motion_create(unsigned nobj, const gbsph_motion_object* objs, unsigned nmov, const gbsph_movement* movs,
+                        unsigned nevt, const gbsph_motion_event* evts, int simulate2d, gbsph_motion** out);
+void gbsph_motion_destroy(gbsph_motion* m);
+/* Advances the motion over [timestep, timestep+dt]; out: one entry per object.
+ * Returns 1 when some object moves in the interval, 0 when none, < 0 on error. */
+int gbsph_motion_process(gbsph_motion* m, double timestep, double dt, gbsph_motion_data* out);
+/* Attaches a motion to a context (NULL detaches).  Each following step (and
+ * every step of gbsph_run) reads back its dt and time, advances the motion on
+ * the host, and after the step's update moves the objects' particles
+ * (position by UpdatePos, velocity set to the motion's, normals rotated by a
+ * matrix motion) and marks the boundary changed, so the next divide is full.
+ * gbsph_run's multi-step graph (mode 2) is not used with a motion.  Verlet
+ * steps with a motion are not supported (GBSPH_EINVAL).  The motion stays
+ * owned by the caller and must outlive the attachment. */
+int gbsph_set_motion(gbsph_ctx* ctx, gbsph_motion* m);
+
 /* Kernel-launch counter of the context (launches issued since creation). */
 unsigned long long gbsph_launch_count(const gbsph_ctx* ctx);
 /* CUDA stream of the context (as void*), for callers that order their own work. */

@@ -16,6 +16,7 @@
 #include "JSphCfgRun.h"
 #include "JDsGaugeSystem.h"
 #include "JDsGaugeItem.h"
+#include "JDsMotion.h"
 #include "JAppInfo.h"
 #include "JLog2.h"
 #include "JCellDivCpuSingle.h"
@@ -111,11 +112,35 @@ class OracleCpu : public JSphCpuSingle{
     WriteRaw(b+"velrho.bin",Velrho_c->cptr(),sizeof(tfloat4)*Np);
   }
 
-  // First step piece by piece (ComputeStep_Sym, JSphCpuSingle.cpp:897-936).
+  // Motion data of every moving object for the interval just computed by
+  // CalcMotion (JDsMotion::GetMotionData): "<time> <dt> <ref> <type>
+  // <linmov 3> <linvel 3> <matmov 16>" lines in motion.txt.
+  FILE* MotionOut=NULL;
+  void DumpMotion(double dt){
+    if(!CaseNmoving)return;
+    if(!MotionOut)MotionOut=fopen((Out+"/motion.txt").c_str(),"w");
+    for(unsigned ref=0;ref<DsMotion->GetNumObjects();ref++){
+      const StMotionData& m=DsMotion->GetMotionData(ref);
+      fprintf(MotionOut,"%.17g %.17g %u %d",TimeStep,dt,ref,int(m.type));
+      const double* lm=&m.linmov.x; const double* lv=&m.linvel.x;
+      for(int c=0;c<3;c++)fprintf(MotionOut," %.17g",lm[c]);
+      for(int c=0;c<3;c++)fprintf(MotionOut," %.17g",lv[c]);
+      const tmatrix4d& a=m.matmov;
+      const double mm[16]={a.a11,a.a12,a.a13,a.a14,a.a21,a.a22,a.a23,a.a24,a.a31,a.a32,a.a33,a.a34,a.a41,a.a42,a.a43,a.a44};
+      for(int c=0;c<16;c++)fprintf(MotionOut," %.17g",mm[c]);
+      fprintf(MotionOut,"\n");
+    }
+    fflush(MotionOut);
+  }
+
+  // First step piece by piece (ComputeStep_Sym, JSphCpuSingle.cpp:897-936;
+  // with moving boundaries, CalcMotion at its start and RunMotion before the
+  // divide that ends it, as the Run loop does, JSphCpuSingle.cpp:1183-1196).
   void FirstStepDetailed(){
     Meta("s0");
     DumpState("s0"); DumpDivide("s0");
     const double dt=SymplecticDtPre;
+    if(CaseNmoving){ CalcMotion(dt); DumpMotion(dt); }
     InterStep=INTERSTEP_SymPredictor;
     DemDtForce=dt*0.5f;
     MdbcBoundCorrection(InterStep);
@@ -145,6 +170,7 @@ class OracleCpu : public JSphCpuSingle{
     PosInteraction_Forces();
     DumpState("s0corr");
     SymplecticDtPre=std::min(dt_p,dt_c);
+    if(CaseNmoving)RunMotion(dt);
     TimeStep+=dt; Nstep++;
     RunCellDivide(true);
     DtList.push_back(dt);
@@ -180,6 +206,7 @@ class OracleCpu : public JSphCpuSingle{
   void RunSteps(unsigned n){
     for(unsigned c=0;c<n;c++){
       const double stepdt=ComputeStep();
+      if(CaseNmoving){ DumpMotion(stepdt); RunMotion(stepdt); }
       RunCellDivide(true);
       TimeStep+=stepdt; Nstep++;
       DtList.push_back(stepdt);

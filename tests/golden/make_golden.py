@@ -40,7 +40,26 @@ CASES = {
                                    init_vel=0.05, seed=13), 10),
     "ddt2f_d04": (lambda: cg.spec_c2(dp=0.04, name="ddt2f_d04", density_dt=3, init_vel=0.02, seed=17), 10),
     "half_d04": (lambda: cg.spec_c1(dp=0.04, name="half_d04", init_vel=0.02, seed=19), 10, ["-cellmode:half"]),
+    "mov_d04": (lambda: spec_moving(), 20),
 }
+
+# A sloshing tank: the walls move through a chain of movements -- sinusoidal
+# translation, sinusoidal pitch about a y axis (phase carried over), uniform
+# translation, uniform acceleration (velocity carried over) -- with durations
+# that end inside steps, so the handover of the rest of a step is exercised.
+MOVING_TANK = [
+    dict(type="mvrectsinu", id=1, duration=0.004, next=2, anglesunits="radians", freq=(1.5, 0.0, 0.0),
+         ampl=(0.03, 0.0, 0.0), phase=(0.3, 0.0, 0.0)),
+    dict(type="mvrotsinu", id=2, duration=0.003, next=3, anglesunits="degrees", axisp1=(0.8, -1.0, 0.2),
+         axisp2=(0.8, 1.0, 0.2), freq=2.0, ampl=3.0),
+    dict(type="mvrect", id=3, duration=0.002, next=4, vel=(0.05, 0.0, 0.01)),
+    dict(type="mvrectace", id=4, duration=1.0, ace=(0.5, 0.0, 0.0)),
+]
+
+
+def spec_moving():
+    return cg.spec_c1(dp=0.04, name="mov_d04", motion=MOVING_TANK, posmin_x="default - 0.1",
+                      posmax_x="default + 0.1", init_vel=0.02, seed=23)
 
 
 GAUGE_CASES = ("dbc_d04", "mdbc_d04")
@@ -150,6 +169,8 @@ def make(name: str, threads: int = 8) -> str:
                 arr[f"{tag}_ar"] = _raw(outdir, tag, "ar", np.float32)
         arr["s0mdbc_rho"] = _raw(outdir, "s0mdbc", "velrho", np.float32, 4)[:, 3].copy()
         arr["dtlist"] = np.fromfile(os.path.join(outdir, "end_dtlist.bin"), dtype=np.float64)
+        if os.path.exists(os.path.join(outdir, "motion.txt")):  # per-step motion data of the moving objects
+            arr["motion"] = np.loadtxt(os.path.join(outdir, "motion.txt"), dtype=np.float64, ndmin=2)
         meta = {tag: _meta(outdir, tag) for tag in ("s0", "s0pred", "s0cor", "s0div", "s1", "end")
                 if os.path.exists(os.path.join(outdir, f"{tag}_meta.txt"))}
         if gauges:  # gauges of the final state, computed by the reference's gauge classes
