@@ -171,7 +171,8 @@ int main(int argc, char** argv) {
                 "[%.17g, %.17g, %.17g], \"maprealposmax\": [%.17g, %.17g, %.17g], \"kernelsize2\": %.9g, "
                 "\"cs0\": %.17g, \"domcellcode\": %u, \"mapcells\": [%u, %u, %u], \"cellmode_div\": %d, \"tboundary\": %d, "
                 "\"tstep\": %d, \"tdensity\": %d, \"tvisco\": %d, \"idsum\": %.17g, \"possum\": %.17g, "
-                "\"rhosum\": %.17g, \"norsum\": %.17g, \"codesum\": %.17g}\n",
+                "\"rhosum\": %.17g, \"norsum\": %.17g, \"codesum\": %.17g, \"nmoving\": %u, \"nmovements\": %u, "
+                "\"nevents\": %u}\n",
                 cs.np, cs.npb, cs.params.h, cs.params.b, cs.params.dp, cs.params.maprealposmin[0],
                 cs.params.maprealposmin[1], cs.params.maprealposmin[2], cs.params.maprealposmax[0],
                 cs.params.maprealposmax[1], cs.params.maprealposmax[2], c.kernelsize2, c.cs0, c.domcellcode,
@@ -180,7 +181,8 @@ int main(int argc, char** argv) {
                 [&] { double s = 0; for (double v : cs.pos) s += v; return s; }(),
                 [&] { double s = 0; for (size_t k = 3; k < cs.velrho.size(); k += 4) s += cs.velrho[k]; return s; }(),
                 [&] { double s = 0; for (float v : cs.boundnor) s += v; return s; }(),
-                [&] { double s = 0; for (uint16_t v : cs.code) s += v; return s; }());
+                [&] { double s = 0; for (uint16_t v : cs.code) s += v; return s; }(), cs.nmoving,
+                (unsigned)cs.movs.size(), (unsigned)cs.evts.size());
     return 0;
   }
   gbsph_ctx* ctx = nullptr;
@@ -189,6 +191,15 @@ int main(int argc, char** argv) {
   rc = gbsph_upload(ctx, cs.np, cs.npb, cs.pos.data(), cs.velrho.data(), cs.idp.data(), cs.code.data(),
                     cs.boundnor.empty() ? nullptr : cs.boundnor.data());
   if (rc != GBSPH_OK) return fail("gbsph_upload", gbsph_last_error(ctx));
+  // moving boundaries: JDsMotion::Init from the case's motion (JSph.cpp:1064-1067)
+  gbsph_motion* motion = nullptr;
+  if (!cs.mot_objs.empty()) {
+    rc = gbsph_motion_create((unsigned)cs.mot_objs.size(), cs.mot_objs.data(), (unsigned)cs.movs.size(),
+                             cs.movs.data(), (unsigned)cs.evts.size(), cs.evts.data(), cs.params.simulate2d, &motion);
+    if (rc != GBSPH_OK) return fail("motion", "invalid motion in the case XML");
+    rc = gbsph_set_motion(ctx, motion);
+    if (rc != GBSPH_OK) return fail("motion", gbsph_last_error(ctx));
+  }
   if (tmax < 0) tmax = cs.time_max;
   const double tout = toutarg > 0 ? toutarg : (cs.time_out > 0 ? cs.time_out : tmax);
   std::printf("Case %s: %u particles (%u boundary, %u fluid), h=%g, dp=%g\n", casename.c_str(), cs.np, cs.npb,
@@ -234,5 +245,6 @@ int main(int argc, char** argv) {
   std::printf("Runtime: %.3f s\nSteps per second: %.3f\n", wall, nstep / (wall > 0 ? wall : 1));
   if (save) std::printf("Part writing (overlapped with the steps): %.3f s\n", writer.write_seconds());
   gbsph_destroy(ctx);
+  gbsph_motion_destroy(motion);
   return 0;
 }

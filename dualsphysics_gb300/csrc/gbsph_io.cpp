@@ -385,6 +385,81 @@ bool pos_value(const std::string& in, bool isposmin, int& mode, double& value) {
 
 }  // namespace
 
+// case.execution.motion as JMotion::ReadXml reads it (JMotion.cpp:692-905):
+// one <objreal ref> per moving block (ref k = the k-th moving block), its
+// movements and <begin> events; durations and event times are floats there.
+static bool read_motion(const XmlNode* node, Case& c, std::string& err) {
+  if (!node) { err = "moving particles without <motion> in the case XML"; return false; }
+  auto f32 = [](double v) { return (double)(float)v; };
+  auto vec3 = [](const XmlNode* e, double* v) {
+    if (e) { v[0] = e->getd("x"); v[1] = e->getd("y"); v[2] = e->getd("z"); }
+  };
+  std::vector<char> seen(c.mot_objs.size(), 0);
+  for (auto* obj : node->children("")) {
+    if (obj->name.empty() || obj->name[0] == '_') continue;
+    if (obj->name != "objreal") { err = "<" + obj->name + "> in <motion> is not supported"; return false; }
+    const long ref = std::lround(obj->getd("ref"));
+    if (ref < 0 || ref >= (long)c.mot_objs.size() || seen[ref]) { err = "motion reference does not match the moving blocks"; return false; }
+    seen[ref] = 1;
+    for (auto* e : obj->children("")) {
+      if (e->name.empty() || e->name[0] == '_') continue;
+      if (e->name == "begin") {
+        c.evts.push_back(gbsph_motion_event{(unsigned)ref, (unsigned)e->getd("mov"), f32(e->getd("start")),
+                                           e->has("finish") ? f32(e->getd("finish")) : -1.0});
+        continue;
+      }
+      static const char* names[] = {"wait", "mvrect", "mvrectace", "mvrot", "mvrotace", "mvrectsinu", "mvrotsinu", "mvnull"};
+      int type = 0;
+      for (int k = 0; k < 8; k++) if (e->name == names[k]) type = k + 1;
+      if (!type) { err = "movement <" + e->name + "> is not supported"; return false; }
+      gbsph_movement m;
+      memset(&m, 0, sizeof(m));
+      m.type = type;
+      m.obj = (unsigned)ref;
+      m.id = (unsigned)e->getd("id");
+      m.nextid = e->has("next") ? (unsigned)e->getd("next") : 0u;
+      m.duration = type == GBSPH_MOV_NULL ? 0.0 : f32(e->getd("duration"));
+      const std::string units = e->get("anglesunits", "degrees");
+      if (units != "degrees" && units != "radians") { err = "anglesunits must be degrees or radians"; return false; }
+      m.angdegrees = units == "degrees";
+      auto ang = [&](const char* n, const char* a) { const XmlNode* x = e->child(n); return x ? x->getd(a) : 0.0; };
+      switch (type) {
+        case GBSPH_MOV_RECT: vec3(e->child("vel"), m.v); break;
+        case GBSPH_MOV_RECTACE:
+          vec3(e->child("ace"), m.a);
+          m.prev = e->child("velini") == nullptr;
+          vec3(e->child("velini"), m.v);
+          break;
+        case GBSPH_MOV_RECTSINU:
+          vec3(e->child("freq"), m.v);
+          vec3(e->child("ampl"), m.a);
+          m.prev = e->child("phase") == nullptr;
+          vec3(e->child("phase"), m.p);
+          break;
+        case GBSPH_MOV_ROT: case GBSPH_MOV_ROTACE: case GBSPH_MOV_ROTSINU:
+          vec3(e->child("axisp1"), m.axisp1);
+          vec3(e->child("axisp2"), m.axisp2);
+          if (type == GBSPH_MOV_ROT) m.s[0] = ang("vel", "ang");
+          else if (type == GBSPH_MOV_ROTACE) {
+            m.s[1] = ang("ace", "ang");
+            m.prev = e->child("velini") == nullptr;
+            m.s[0] = ang("velini", "ang");
+          } else {
+            m.s[0] = ang("freq", "v");
+            m.s[1] = ang("ampl", "v");
+            m.prev = e->child("phase") == nullptr;
+            m.s[2] = ang("phase", "v");
+          }
+          break;
+        default: break;
+      }
+      c.movs.push_back(m);
+    }
+  }
+  for (char v : seen) if (!v) { err = "the number of moving objects does not match the predefined motions"; return false; }
+  return true;
+}
+
 bool load_case(const std::string& casedir, const std::string& casename, Case& c, std::string& err) {
   c = Case();
   c.name = casename;
@@ -435,13 +510,23 @@ bool load_case(const std::string& casedir, const std::string& casename, Case& c,
   // blocks and codes (JCaseParts.cpp:540-577, JSphMk.cpp:86-123)
   struct Blk { bool fluid; unsigned begin, count, code; };
   std::vector<Blk> blocks;
-  unsigned ifix = 0, ifl = 0;
+  unsigned ifix = 0, imov = 0, ifl = 0;
+  int lastkind = 0;  // fixed 0, moving 1, fluid 2: the reference's block order
   for (auto* b : parts->children("")) {
     if (b->name.empty() || b->name[0] == '_' || b->name == "properties") continue;
-    if (b->name == "fixed") blocks.push_back({false, (unsigned)b->getd("begin"), (unsigned)b->getd("count"), 0x0000u | ifix++});
-    else if (b->name == "fluid") blocks.push_back({true, (unsigned)b->getd("begin"), (unsigned)b->getd("count"), 0x1800u | ifl++});
-    else { err = "particle block <" + b->name + "> is outside the implemented hot path"; return false; }
+    const int kind = b->name == "fixed" ? 0 : b->name == "moving" ? 1 : b->name == "fluid" ? 2 : -1;
+    if (kind < 0) { err = "particle block <" + b->name + "> is outside the implemented hot path"; return false; }
+    if (kind < lastkind) { err = "particle blocks must come as fixed, moving, fluid"; return false; }
+    lastkind = kind;
+    const unsigned begin = (unsigned)b->getd("begin"), count = (unsigned)b->getd("count");
+    if (kind == 0) blocks.push_back({false, begin, count, 0x0000u | ifix++});
+    else if (kind == 1) {
+      blocks.push_back({false, begin, count, 0x0800u | imov++});
+      c.mot_objs.push_back(gbsph_motion_object{begin, count});
+      c.nmoving += count;
+    } else blocks.push_back({true, begin, count, 0x1800u | ifl++});
   }
+  if (imov && !read_motion(ex->child("motion"), c, err)) return false;
   c.npb = (unsigned)parts->getd("nb");
   // particles (JPartsLoad4.cpp:164-290)
   Bi4Item bd;
@@ -584,8 +669,8 @@ bool save_part(const std::string& dirout, const Case& c, unsigned part, double t
   root.set_triple("PeriZinc", DatDouble3, z3);
   root.set_num("AxisDiv", DatInt, 0);
   root.set_u64("CaseNp", DatUllong, c.np);
-  root.set_u64("CaseNfixed", DatUllong, c.npb);
-  root.set_u64("CaseNmoving", DatUllong, 0);
+  root.set_u64("CaseNfixed", DatUllong, c.npb - c.nmoving);
+  root.set_u64("CaseNmoving", DatUllong, c.nmoving);
   root.set_u64("CaseNfloat", DatUllong, 0);
   root.set_u64("CaseNfluid", DatUllong, c.np - c.npb);
   root.set_triple("CasePosMin", DatDouble3, c.caseposmin);

@@ -79,6 +79,11 @@ struct Case {
   double time_max = 0, time_out = 0;
   bool savepos_double = false;
   double caseposmin[3] = {0, 0, 0}, caseposmax[3] = {0, 0, 0};
+  // moving boundaries (case.execution.motion; empty without moving blocks)
+  unsigned nmoving = 0;
+  std::vector<gbsph_motion_object> mot_objs;
+  std::vector<gbsph_movement> movs;
+  std::vector<gbsph_motion_event> evts;
 };
 
 bool load_case(const std::string& casedir, const std::string& casename, Case& c, std::string& err);

@@ -234,9 +234,10 @@ class GbSphSingle:
         st = self.download()
         order = np.argsort(st["idp"], kind="stable")
         dtl, dtn, t = self.step_dt()
+        nmov = sum(c for _, c in cd.motion["objects"]) if cd.motion else 0
         root = bi4.make_partdata_root(
-            casename=cd.name, appname="dualsphysics_gb300", data2d=False, casenp=cd.np, casenfixed=cd.npb,
-            casenmoving=0, casenfloat=0, casenfluid=cd.nfluid, caseposmin=cd.pos.min(axis=0),
+            casename=cd.name, appname="dualsphysics_gb300", data2d=False, casenp=cd.np, casenfixed=cd.npb - nmov,
+            casenmoving=nmov, casenfloat=0, casenfluid=cd.nfluid, caseposmin=cd.pos.min(axis=0),
             caseposmax=cd.pos.max(axis=0), dp=cd.params.dp, h=cd.params.h, b=cd.params.b, rhop0=cd.params.rhop0,
             gamma=cd.params.gamma, massbound=cd.params.massbound, massfluid=cd.params.massfluid,
             mapposmin=tuple(cd.params.maprealposmin), mapposmax=tuple(cd.params.maprealposmax))

@@ -36,7 +36,7 @@ def _write_case(tmp_path, name):
     return spec.name
 
 
-@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "sps_d04", "verlet_d04", "lam_d04", "half_d04"])
+@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "sps_d04", "verlet_d04", "lam_d04", "half_d04", "mov_d04"])
 def test_driver_case_summary_matches_python_loader(tmp_path, name):
     import make_golden
     cn = _write_case(tmp_path, name)
@@ -64,6 +64,9 @@ def test_driver_case_summary_matches_python_loader(tmp_path, name):
     assert info["rhosum"] == pytest.approx(float(cd.velrho[:, 3].astype(np.float64).sum()), rel=1e-12)
     nor = 0.0 if cd.boundnor is None else float(cd.boundnor.astype(np.float64).sum())
     assert info["norsum"] == pytest.approx(nor, rel=1e-9, abs=1e-9)
+    mot = cd.motion or {"objects": [], "movements": [], "events": []}
+    assert info["nmoving"] == sum(c for _, c in mot["objects"])
+    assert (info["nmovements"], info["nevents"]) == (len(mot["movements"]), len(mot["events"]))
 
 
 def test_driver_rejects_unknown_option_and_missing_case(tmp_path):
@@ -84,7 +87,7 @@ def _parts(dirout):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04"])
+@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "mov_d04"])
 def test_driver_parts_equal_python_run(tmp_path, name):
     """gbsph_run and GbSphSingle.Run step the same case to the same end time
     and write bit-identical particle data in every Part file."""
