@@ -37,6 +37,7 @@ class Params(C.Structure):
         ("rhopoutmin", C.c_float), ("rhopoutmax", C.c_float),
         ("dtini", C.c_double), ("dtmin", C.c_double),
         ("maprealposmin", C.c_double * 3), ("maprealposmax", C.c_double * 3),
+        ("tshift", C.c_int), ("shiftcoef", C.c_float), ("shifttfs", C.c_float),
     ]
 
 
@@ -56,6 +57,7 @@ class Consts(C.Structure):
         ("maprealposmax", C.c_double * 3),
         ("domposmin", C.c_double * 3), ("domrealposmin", C.c_double * 3), ("domrealposmax", C.c_double * 3),
         ("mapcells", C.c_uint * 3), ("domcells", C.c_uint * 3), ("domcellcode", C.c_uint),
+        ("tshift", C.c_int), ("shiftcoef", C.c_float), ("shifttfs", C.c_float),
     ]
 
 
@@ -149,6 +151,8 @@ SIGNATURES = {
     "gbsph_motion_destroy": (None, [P]),
     "gbsph_motion_process": (C.c_int, [P, C.c_double, C.c_double, P]),
     "gbsph_set_motion": (C.c_int, [P, P]),
+    "gbsph_run_shifting": (C.c_int, [P, C.c_double]),
+    "gbsph_get_shiftpos": (C.c_int, [P, P]),
 }
 
 SORT_NOALLOC_MAX_KEYS = 262144  # GBSPH_SORT_NOALLOC_MAX_KEYS

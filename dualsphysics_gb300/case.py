@@ -110,9 +110,15 @@ def load_case(casedir: str, casename: str, cellmode: str = "full") -> CaseData:
 
     if gi("Kernel", 2) != 2:
         raise CaseError("only the Wendland kernel (Kernel=2) is implemented")
-    if gi("Shifting", 0) != 0:
-        raise CaseError("shifting is outside the implemented hot path")
+    # standard shifting (JSph.cpp:744-759); advanced shifting (4) is not built
+    tshift = gi("Shifting", 0)
+    if tshift not in (0, 1, 2, 3):
+        raise CaseError(f"Shifting mode {tshift} is not supported (0-3)")
     prm = Params()
+    prm.tshift = tshift
+    if tshift:
+        prm.shiftcoef = gf("ShiftCoef", -2.0)
+        prm.shifttfs = gf("ShiftTFS", 0.0)
     prm.tstep = gi("StepAlgorithm", 1)
     prm.verletsteps = gi("VerletSteps", 40)
     prm.tvisco = gi("ViscoTreatment", 1)

@@ -135,6 +135,7 @@ size_t layout(gbsph_ctx* ctx, void* base) {
   a.strainb = sps ? k.take<float2>(n) : nullptr;
   a.pscell = k.take<float4>(n);
   a.acear = k.take<float4>(n);
+  a.shiftpos = ctx->c.tshift ? k.take<float4>(n) : nullptr;
   a.keys = k.take<unsigned>(n); a.keys2 = k.take<unsigned>(n);
   a.vals = k.take<unsigned>(n); a.vals2 = k.take<unsigned>(n);
   const size_t ntiles = (n + 2047) / 2048;
@@ -191,6 +192,10 @@ int enqueue_step(gbsph_ctx* ctx) {
     if (int rc = do_divide(ctx)) return rc;
     if (int rc = do_forces(ctx)) return rc;
     gbk::dtvariable(c, ctx->a, 1, ctx->stream, &ctx->launches);
+    // RunShifting(dt) before the corrector; the predictor's RunShifting(dt/2)
+    // is not enqueued: the reference's predictor does not apply it and the
+    // corrector's interaction recomputes the sums
+    if (c.tshift) gbk::run_shifting(c, ctx->a, ctx->cap, dtpre, 1.0, ctx->stream, &ctx->launches);
     gbk::symplectic_cor(c, ctx->a, ctx->cap, dtpre, ctx->stream, &ctx->launches);
     gbk::step_end(ctx->a, 1, ctx->stream, &ctx->launches);
     if (ctx->motion) {  // RunMotion, before the divide that ends the step
@@ -203,6 +208,7 @@ int enqueue_step(gbsph_ctx* ctx) {
     if (c.tboundary == GBSPH_BC_MDBC) gbk::mdbc(c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
     if (int rc = do_forces(ctx)) return rc;
     gbk::dtvariable(c, ctx->a, 2, ctx->stream, &ctx->launches);
+    if (c.tshift) gbk::run_shifting(c, ctx->a, ctx->cap, &ctx->a.st->dt_var, 1.0, ctx->stream, &ctx->launches);
     ctx->verletstep++;
     const int euler = !(ctx->verletstep < c.verletsteps);
     if (euler) ctx->verletstep = 0;
@@ -427,6 +433,26 @@ int gbsph_symplectic_cor(gbsph_ctx* ctx, double dt) {
   if (int rc = set_device_dt(ctx, dt)) return rc;
   gbk::symplectic_cor(ctx->c, ctx->a, ctx->cap, device_scalar(ctx), ctx->stream, &ctx->launches);
   return cuda_check(ctx, cudaGetLastError(), "symplectic_cor");
+}
+
+int gbsph_run_shifting(gbsph_ctx* ctx, double dt) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (!ctx->c.tshift) return GBSPH_OK;
+  if (int rc = set_device_dt(ctx, dt)) return rc;
+  gbk::run_shifting(ctx->c, ctx->a, ctx->cap, device_scalar(ctx), 1.0, ctx->stream, &ctx->launches);
+  return cuda_check(ctx, cudaGetLastError(), "run_shifting");
+}
+
+static int read_div(gbsph_ctx* ctx, DivState* ds);
+
+int gbsph_get_shiftpos(gbsph_ctx* ctx, float* shiftpos) {
+  if (!ctx || !ctx->uploaded || !shiftpos) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (!ctx->a.shiftpos) return set_err(ctx, GBSPH_EINVAL, "the case has no shifting");
+  DivState ds;
+  if (int rc = read_div(ctx, &ds)) return rc;
+  CK(cudaMemcpyAsync(shiftpos, ctx->a.shiftpos, sizeof(float4) * ds.np, cudaMemcpyDeviceToHost, ctx->stream), "shiftpos");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  return GBSPH_OK;
 }
 
 int gbsph_verlet(gbsph_ctx* ctx, double dt) {

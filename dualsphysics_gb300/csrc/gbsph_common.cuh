@@ -72,6 +72,7 @@ struct DevArrays {
   float2 *strainb;                               // SPS 2*strain yz,zz
   float4 *pscell;                                // (x,y,z) relative to the particle's cell origin, w=pressure
   float4 *acear;                                 // (ace.x,ace.y,ace.z,ar)
+  float4 *shiftpos;                              // shifting sums, then displacements (fluid rows; tshift)
   unsigned *keys, *keys2, *vals, *vals2;         // radix sort buffers
   unsigned *hist;                                // radix sort tile histograms
   unsigned *begincell;                           // BeginCell (nctt entries, JCellDivCpu.h:150)
@@ -230,6 +231,9 @@ void verlet_step(const gbsph_consts& c, DevArrays& a, unsigned cap, const double
 void sps_tau(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch);
 void pips(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s);
 void step_end(const DevArrays& a, int symplectic, cudaStream_t s, unsigned long long* nlaunch);
+// RunShifting (JSphCpu.cpp:2084-2088) over the fluid rows, dt = dtfactor * *dtp.
+void run_shifting(const gbsph_consts& c, const DevArrays& a, unsigned cap, const double* dtp, double dtfactor,
+                  cudaStream_t s, unsigned long long* nlaunch);
 // RunMotion (JSphCpu.cpp:2189-2245): index of each moving particle by id, then
 // the linear or matrix movement of its object; marks the boundary changed.
 // ridp holds nmoving entries for the ids idmin..idmin+nmoving-1.

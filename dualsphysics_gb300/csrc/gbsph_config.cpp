@@ -43,6 +43,11 @@ extern "C" int gbsph_config(const gbsph_params* p, gbsph_consts* c) {
   c->tvisco = p->tvisco;
   c->tdensity = p->tdensity;
   c->tboundary = p->tboundary;
+  // standard shifting (JSph.cpp:744-759); advanced shifting (4) is not built
+  if (p->tshift < 0 || p->tshift > 3) return GBSPH_EINVAL;
+  c->tshift = p->tshift;
+  c->shiftcoef = p->tshift ? p->shiftcoef : 0.f;
+  c->shifttfs = p->tshift ? p->shifttfs : 0.f;
   c->verletsteps = p->verletsteps > 0 ? p->verletsteps : 40;
   c->dtallparticles = p->dtallparticles;
   c->simulate2d = 0;

@@ -45,10 +45,10 @@ struct FluidAcc {
 
 // One pass of a fluid row over the fluid (boundp2=false) or boundary
 // (boundp2=true) boxes.
-template <int tvisco, int tdensity, bool boundp2>
+template <int tvisco, int tdensity, bool boundp2, bool tshift>
 __device__ __forceinline__ void fluid_pass(const gbsph_consts& c, const DevArrays& a, const DivState& d,
                                            const CellGrid& g, float4 ps1, float4 vr1, float4 ta1, float2 tb1,
-                                           float visco, FluidAcc& r) {
+                                           float visco, FluidAcc& r, float4& sh) {
   const unsigned cellinit = boundp2 ? 0u : d.boxfluid;
   const float scell = c.scell;
   const float ks2 = c.kernelsize2, eta2 = c.eta2, h = c.kernelh, bwenh = c.bwenh;
@@ -104,6 +104,16 @@ __device__ __forceinline__ void fluid_pass(const gbsph_consts& c, const DevArray
                 deltap1 = deltap1 - delta;
               }
             }
+            // shifting sums (JSphCpu.cpp:942-950); a boundary neighbour cancels
+            // them in NoBound mode, a fixed one in NoFixed mode
+            if (tshift && sh.x != FLT_MAX) {
+              const float massrho = massp2 / vr2.w;
+              const bool noshift = boundp2 && (c.tshift == 1 || (c.tshift == 2 && (a.code[p2] & GB_CODE_MASKTYPE) == 0u));
+              sh.x = noshift ? FLT_MAX : sh.x + massrho * frx;
+              sh.y += massrho * fry;
+              sh.z += massrho * frz;
+              sh.w -= massrho * (drx * frx + dry * fry + drz * frz);
+            }
             // viscosity (JSphCpu.cpp:990-1037)
             const float dot = drx * dvx + dry * dvy + drz * dvz;
             const float dot_rr2 = dot / (rr2 + eta2);
@@ -145,7 +155,7 @@ __device__ __forceinline__ void fluid_pass(const gbsph_consts& c, const DevArray
   r.s0 = s0; r.s1 = s1; r.s2 = s2; r.s3 = s3; r.s4 = s4; r.s5 = s5;
 }
 
-template <int tvisco, int tdensity>
+template <int tvisco, int tdensity, bool tshift>
 __global__ void __launch_bounds__(128) k_forces_fluid(gbsph_consts c, DevArrays a) {
   const DivState& d = *a.div;
   const unsigned np = d.np, npb = d.npb;
@@ -161,8 +171,10 @@ __global__ void __launch_bounds__(128) k_forces_fluid(gbsph_consts c, DevArrays 
     const CellGrid g = gb_grid((int)gb_cx(dcc, cel) - (int)d.cellmin[0], (int)gb_cy(dcc, cel) - (int)d.cellmin[1],
                                (int)gb_cz(dcc, cel) - (int)d.cellmin[2], c.cellmode_div, d);
     FluidAcc ff, fb;
-    fluid_pass<tvisco, tdensity, false>(c, a, d, g, ps1, vr1, ta1, tb1, c.visco, ff);
-    fluid_pass<tvisco, tdensity, true>(c, a, d, g, ps1, vr1, ta1, tb1, c.visco * c.viscoboundfactor, fb);
+    float4 sh = make_float4(0.f, 0.f, 0.f, 0.f);  // InitCpu without zones: zero
+    fluid_pass<tvisco, tdensity, false, tshift>(c, a, d, g, ps1, vr1, ta1, tb1, c.visco, ff, sh);
+    fluid_pass<tvisco, tdensity, true, tshift>(c, a, d, g, ps1, vr1, ta1, tb1, c.visco * c.viscoboundfactor, fb, sh);
+    if (tshift) a.shiftpos[p1] = sh;
     // JSphCpu.cpp:1093-1113 and JSphCpuSingle.cpp:727-735
     float ar = ff.ar + fb.ar;
     if (tdensity != GBSPH_DDT_NONE) {
@@ -213,6 +225,7 @@ constexpr int kRoundLanes = 32;   // lanes that must hold kRoundEntries entries 
 struct PairAcc {
   float ax, ay, az, ar, delta, visc;
   float s0, s1, s2, s3, s4, s5;
+  float sh0, sh1, sh2, sh3;  // shifting sums (sh0 = FLT_MAX: cancelled)
 };
 
 // Float constants of the pair terms, derived on the host once per launch with
@@ -260,7 +273,7 @@ PairK make_pairk(const gbsph_consts& c) {
 __device__ __forceinline__ float gb_rcp(float x) { return __fdividef(1.f, x); }
 
 
-template <int tvisco, int tdensity, bool boundp2, bool ddtgen>
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift>
 __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k, const DevArrays& a,
                                            float4 e, float4 vr2, float p2press, float4 vr1,
                                            float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
@@ -305,6 +318,15 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
       r.delta -= visc_densi * dot3 * inv_rho2;
     }
   }
+  // shifting sums (JSphCpu.cpp:942-950), fluid ones without the mass
+  if (tshift && r.sh0 != FLT_MAX) {
+    const float massrho = m2 * inv_rho2;
+    const bool noshift = boundp2 && (c.tshift == 1 || (c.tshift == 2 && (a.code[p2] & GB_CODE_MASKTYPE) == 0u));
+    r.sh0 = noshift ? FLT_MAX : r.sh0 + massrho * frx;
+    r.sh1 += massrho * fry;
+    r.sh2 += massrho * frz;
+    r.sh3 -= massrho * (fac * rr2);  // r . gradW
+  }
   // viscosity
   const float dot = drx * dvx + dry * dvy + drz * dvz;
   const float dot_rr2 = dot * inv_r2eta;
@@ -340,7 +362,7 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
 
 // One round: every lane evaluates up to two of its oldest queued pairs, with
 // the loads of both neighbours issued before either pair's arithmetic.
-template <int tvisco, int tdensity, bool boundp2, bool ddtgen, int E>
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, int E>
 __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k, const DevArrays& a,
                                            float4 (*q)[32], unsigned& qh, int& n, float4 vr1,
                                            float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
@@ -362,10 +384,10 @@ __device__ __forceinline__ void pair_round(const gbsph_consts& c, const PairK& k
     pb = a.pscell[p2].w;
   }
   if (va)
-    pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, ea, wa, pa, vr1, p1press, inv_rho1, ta1, tb1, vfac,
+    pair_fluid<tvisco, tdensity, boundp2, ddtgen, tshift>(c, k, a, ea, wa, pa, vr1, p1press, inv_rho1, ta1, tb1, vfac,
                                                   massp2, r);
   if (E > 1 && vb)
-    pair_fluid<tvisco, tdensity, boundp2, ddtgen>(c, k, a, eb, wb, pb, vr1, p1press, inv_rho1, ta1, tb1, vfac,
+    pair_fluid<tvisco, tdensity, boundp2, ddtgen, tshift>(c, k, a, eb, wb, pb, vr1, p1press, inv_rho1, ta1, tb1, vfac,
                                                   massp2, r);
   const int used = (int)va + (int)vb;
   qh = (qh + used) & (kQCap - 1);
@@ -390,7 +412,7 @@ __device__ __forceinline__ void cell_range(const DevArrays& a, const DivState& d
 
 // One pass of the fluid rows over the fluid (boundp2=false) or boundary
 // (boundp2=true) boxes of the 27 neighbour cells.
-template <int tvisco, int tdensity, bool boundp2, bool ddtgen, int E, int F>
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, int E, int F>
 __device__ __forceinline__ void round_pass(const gbsph_consts& c, const PairK& k, const DevArrays& a,
                                            const DivState& d, const CellGrid& g, bool active, float4 ps1,
                                            float4 vr1, float inv_rho1, float4 ta1, float2 tb1,
@@ -457,17 +479,17 @@ __device__ __forceinline__ void round_pass(const gbsph_consts& c, const PairK& k
       for (;;) {
         const bool forced = __any_sync(0xffffffffu, n > kQCap - kQUnroll);
         if (!forced && __popc(__ballot_sync(0xffffffffu, n >= E)) < F) break;
-        pair_round<tvisco, tdensity, boundp2, ddtgen, E>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
+        pair_round<tvisco, tdensity, boundp2, ddtgen, tshift, E>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
                                                       massp2, r);
       }
     }
   }
   while (__any_sync(0xffffffffu, n > 0))
-    pair_round<tvisco, tdensity, boundp2, ddtgen, E>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
+    pair_round<tvisco, tdensity, boundp2, ddtgen, tshift, E>(c, k, a, q, qh, n, vr1, ps1.w, inv_rho1, ta1, tb1, vfac,
                                                   massp2, r);
 }
 
-template <int tvisco, int tdensity, bool ddtgen, int E = kRoundEntries, int F = kRoundLanes>
+template <int tvisco, int tdensity, bool ddtgen, bool tshift, int E = kRoundEntries, int F = kRoundLanes>
 __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, PairK k, DevArrays a) {
   __shared__ float4 qbuf[kQBlock / 32][kQCap][32];
   const DivState& d = *a.div;
@@ -490,17 +512,18 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, Pair
   }
   const float inv_rho1 = gb_rcp(vr1.w);
   float4 (*q)[32] = qbuf[threadIdx.x >> 5];
-  PairAcc ff = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  PairAcc ff = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   // one accumulator for both passes: the boundary pass adds to the fluid sums
   // (and sets the DDT veto, FLT_MAX in delta, where it applies)
-  round_pass<tvisco, tdensity, false, ddtgen, E, F>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
+  round_pass<tvisco, tdensity, false, ddtgen, tshift, E, F>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
   {  // the fluid-neighbour sums carry no mass yet
     const float mf = c.massfluid;
     ff.ax *= mf; ff.ay *= mf; ff.az *= mf; ff.ar *= mf; ff.delta *= mf;
     if (tdensity == GBSPH_DDT_DDT2 || tdensity == GBSPH_DDT_DDT2FULL) ff.delta *= k.ddt_kc;
     ff.s0 *= mf; ff.s1 *= mf; ff.s2 *= mf; ff.s3 *= mf; ff.s4 *= mf; ff.s5 *= mf;
+    if (tshift) { ff.sh0 *= mf; ff.sh1 *= mf; ff.sh2 *= mf; ff.sh3 *= mf; }
   }
-  round_pass<tvisco, tdensity, true, ddtgen, E, F>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
+  round_pass<tvisco, tdensity, true, ddtgen, tshift, E, F>(c, k, a, d, g, active, ps1, vr1, inv_rho1, ta1, tb1, q, ff);
   ff.ar *= vr1.w;  // the rho1 factor of every continuity term
   float acemax2 = 0, visc = 0, vel2 = 0;
   if (active) {
@@ -512,6 +535,7 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, Pair
       a.straina[p1] = make_float4(ff.s0, ff.s1, ff.s2, ff.s3);
       a.strainb[p1] = make_float2(ff.s4, ff.s5);
     }
+    if (tshift) a.shiftpos[p1] = make_float4(ff.sh0, ff.sh1, ff.sh2, ff.sh3);
     acemax2 = ax * ax + ay * ay + az * az;
     visc = ff.visc;
     vel2 = vr1.x * vr1.x + vr1.y * vr1.y + vr1.z * vr1.z;
@@ -799,10 +823,10 @@ __global__ void k_pips(gbsph_consts c, DevArrays a) {
   }
 }
 
-template <int tvisco, int tdensity>
+template <int tvisco, int tdensity, bool tshift>
 void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s) {
   if (variant == 1) {
-    k_forces_fluid<tvisco, tdensity><<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+    k_forces_fluid<tvisco, tdensity, tshift><<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
     return;
   }
   const PairK k = make_pairk(c);
@@ -811,20 +835,26 @@ void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int v
     // the series form of the hydrostatic term holds for |ddtgz*drz| < 0.05 and
     // |drz| <= 2h for every pair; otherwise the general power form is compiled in
     if (!(fabsf(c.ddtgz) * c.kernelsize < 0.049f)) {
-      k_forces_fluid_q<tvisco, tdensity, true><<<grid, kQBlock, 0, s>>>(c, k, a);
+      k_forces_fluid_q<tvisco, tdensity, true, tshift><<<grid, kQBlock, 0, s>>>(c, k, a);
       return;
     }
   }
-  k_forces_fluid_q<tvisco, tdensity, false><<<grid, kQBlock, 0, s>>>(c, k, a);
+  k_forces_fluid_q<tvisco, tdensity, false, tshift><<<grid, kQBlock, 0, s>>>(c, k, a);
+}
+
+template <int tvisco, int tdensity>
+void launch_fluid_s(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s) {
+  if (c.tshift) launch_fluid<tvisco, tdensity, true>(c, a, cap, variant, s);
+  else launch_fluid<tvisco, tdensity, false>(c, a, cap, variant, s);
 }
 
 template <int tvisco>
 void launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s) {
   switch (c.tdensity) {
-    case GBSPH_DDT_NONE: launch_fluid<tvisco, GBSPH_DDT_NONE>(c, a, cap, variant, s); break;
-    case GBSPH_DDT_DDT: launch_fluid<tvisco, GBSPH_DDT_DDT>(c, a, cap, variant, s); break;
-    case GBSPH_DDT_DDT2: launch_fluid<tvisco, GBSPH_DDT_DDT2>(c, a, cap, variant, s); break;
-    default: launch_fluid<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, variant, s); break;
+    case GBSPH_DDT_NONE: launch_fluid_s<tvisco, GBSPH_DDT_NONE>(c, a, cap, variant, s); break;
+    case GBSPH_DDT_DDT: launch_fluid_s<tvisco, GBSPH_DDT_DDT>(c, a, cap, variant, s); break;
+    case GBSPH_DDT_DDT2: launch_fluid_s<tvisco, GBSPH_DDT_DDT2>(c, a, cap, variant, s); break;
+    default: launch_fluid_s<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, variant, s); break;
   }
 }
 

@@ -475,9 +475,16 @@ bool load_case(const std::string& casedir, const std::string& casename, Case& c,
   auto gi = [&](const char* k, int d) { return kv.count(k) ? (int)std::strtod(kv[k].c_str(), nullptr) : d; };
   auto gf = [&](const char* k, double d) { return kv.count(k) ? std::strtod(kv[k].c_str(), nullptr) : d; };
   if (gi("Kernel", 2) != 2) { err = "only the Wendland kernel (Kernel=2) is implemented"; return false; }
-  if (gi("Shifting", 0) != 0) { err = "shifting is outside the implemented hot path"; return false; }
+  // standard shifting (JSph.cpp:744-759); advanced shifting (4) is not built
+  const int tshift = gi("Shifting", 0);
+  if (tshift < 0 || tshift > 3) { err = "Shifting mode " + std::to_string(tshift) + " is not supported (0-3)"; return false; }
   gbsph_params& p = c.params;
   std::memset(&p, 0, sizeof(p));
+  p.tshift = tshift;
+  if (tshift) {
+    p.shiftcoef = (float)gf("ShiftCoef", -2);
+    p.shifttfs = (float)gf("ShiftTFS", 0);
+  }
   p.tstep = gi("StepAlgorithm", 1);
   p.verletsteps = gi("VerletSteps", 40);
   p.tvisco = gi("ViscoTreatment", 1);

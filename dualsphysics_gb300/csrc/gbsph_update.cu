@@ -105,9 +105,13 @@ __global__ void k_sym_cor(gbsph_consts c, DevArrays a, const double* dtp, double
   const float vx = gb_d2f(dadd(gb_f2d(vp.x), dmul(dadd(gb_f2d(ace.x), gb_f2d(c.gravity[0])), dt)));
   const float vy = gb_d2f(dadd(gb_f2d(vp.y), dmul(dadd(gb_f2d(ace.y), gb_f2d(c.gravity[1])), dt)));
   const float vz = gb_d2f(dadd(gb_f2d(vp.z), dmul(dadd(gb_f2d(ace.z), gb_f2d(c.gravity[2])), dt)));
-  const double dx = dmul(dadd(gb_f2d(vp.x), gb_f2d(vx)), dt05);
-  const double dy = dmul(dadd(gb_f2d(vp.y), gb_f2d(vy)), dt05);
-  const double dz = dmul(dadd(gb_f2d(vp.z), gb_f2d(vz)), dt05);
+  double dx = dmul(dadd(gb_f2d(vp.x), gb_f2d(vx)), dt05);
+  double dy = dmul(dadd(gb_f2d(vp.y), gb_f2d(vy)), dt05);
+  double dz = dmul(dadd(gb_f2d(vp.z), gb_f2d(vz)), dt05);
+  if (c.tshift) {  // the shifting displacement (JSphCpu.cpp:1940-1944)
+    const float4 sh = a.shiftpos[p];
+    dx = dadd(dx, gb_f2d(sh.x)); dy = dadd(dy, gb_f2d(sh.y)); dz = dadd(dz, gb_f2d(sh.z));
+  }
   const bool outrho = (rhonew < c.rhopoutmin || rhonew > c.rhopoutmax);
   unsigned code = rcode;
   if (outrho && (rcode & GB_CODE_MASKSPECIAL) == GB_CODE_NORMAL) {
@@ -145,9 +149,13 @@ __global__ void k_verlet(gbsph_consts c, DevArrays a, const double* dtp, double 
   const double ax = dadd(gb_f2d(ace.x), gb_f2d(c.gravity[0]));
   const double ay = dadd(gb_f2d(ace.y), gb_f2d(c.gravity[1]));
   const double az = dadd(gb_f2d(ace.z), gb_f2d(c.gravity[2]));
-  const double dx = dadd(dmul(gb_f2d(v1.x), dt), dmul(ax, dt205));
-  const double dy = dadd(dmul(gb_f2d(v1.y), dt), dmul(ay, dt205));
-  const double dz = dadd(dmul(gb_f2d(v1.z), dt), dmul(az, dt205));
+  double dx = dadd(dmul(gb_f2d(v1.x), dt), dmul(ax, dt205));
+  double dy = dadd(dmul(gb_f2d(v1.y), dt), dmul(ay, dt205));
+  double dz = dadd(dmul(gb_f2d(v1.z), dt), dmul(az, dt205));
+  if (c.tshift) {  // the shifting displacement (JSphCpu.cpp:1543-1547)
+    const float4 sh = a.shiftpos[p];
+    dx = dadd(dx, gb_f2d(sh.x)); dy = dadd(dy, gb_f2d(sh.y)); dz = dadd(dz, gb_f2d(sh.z));
+  }
   const bool outrho = (rhonew < c.rhopoutmin || rhonew > c.rhopoutmax);
   const float nvx = gb_d2f(dadd(gb_f2d(v2.x), dmul(ax, dt2)));
   const float nvy = gb_d2f(dadd(gb_f2d(v2.y), dmul(ay, dt2)));
@@ -216,6 +224,38 @@ __global__ void k_stage_download(DevArrays a, double* __restrict__ stage, unsign
   stage[3 * (size_t)p + 2] = a.pz[p];
 }
 
+// JSphShifting::RunCpu (JSphShifting.cpp:390-418): the shifting sums of each
+// fluid row become its displacement, dt*coef*h*|v| along the sums, cut below
+// the free-surface threshold and limited to dp/10; rows cancelled next to the
+// boundary get none.  dt = dtfactor * *dtp (the step's dt, or half of it).
+__global__ void k_run_shifting(gbsph_consts c, DevArrays a, const double* __restrict__ dtp, double dtfactor) {
+  const DivState& d = *a.div;
+  const unsigned p = d.npb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.np) return;
+  const float4 rs = a.shiftpos[p];
+  if (rs.x == FLT_MAX) {
+    a.shiftpos[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const double dt = dmul(*dtp, dtfactor);
+  const double coefumagn = dmul(dmul(dt, gb_f2d(c.shiftcoef)), gb_f2d(c.kernelh));
+  const double coeftfs = __dsub_rn(c.simulate2d ? 2.0 : 3.0, gb_f2d(c.shifttfs));
+  const float maxdist = gb_d2f(dmul(c.dp, 0.1));
+  const float4 v = a.velrho[p];
+  const double vx = gb_f2d(v.x), vy = gb_f2d(v.y), vz = gb_f2d(v.z);
+  double umagn = dmul(coefumagn, __dsqrt_rn(dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz))));
+  if (c.shifttfs != 0.f) {
+    if (rs.w < c.shifttfs) umagn = 0;
+    else umagn = dmul(umagn, __ddiv_rn(__dsub_rn(gb_f2d(rs.w), gb_f2d(c.shifttfs)), coeftfs));
+  }
+  const float sx = gb_d2f(dmul(gb_f2d(rs.x), umagn));
+  const float sy = gb_d2f(dmul(gb_f2d(rs.y), umagn));
+  const float sz = gb_d2f(dmul(gb_f2d(rs.z), umagn));
+  a.shiftpos[p] = make_float4(fabsf(sx) < maxdist ? sx : (sx >= 0 ? maxdist : -maxdist),
+                              fabsf(sy) < maxdist ? sy : (sy >= 0 ? maxdist : -maxdist),
+                              fabsf(sz) < maxdist ? sz : (sz >= 0 ? maxdist : -maxdist), rs.w);
+}
+
 // CalcRidp (JSphCpu.cpp:2099-2127) over the npb boundary particles: the
 // current index of each moving particle by id (ridp preset to UINT_MAX).
 // Thread 0 also marks the boundary changed when some object is active
@@ -276,6 +316,12 @@ __global__ void k_motion_move(gbsph_consts c, DevArrays a, const MotionStep* __r
 }  // namespace
 
 namespace gbk {
+
+void run_shifting(const gbsph_consts& c, const DevArrays& a, unsigned cap, const double* dtp, double dtfactor,
+                  cudaStream_t s, unsigned long long* nlaunch) {
+  k_run_shifting<<<gb_div_up(cap, kUpdBlock), kUpdBlock, 0, s>>>(c, a, dtp, dtfactor);
+  if (nlaunch) *nlaunch += 1;
+}
 
 void motion_move(const gbsph_consts& c, const DevArrays& a, const MotionStep* hdr, const MotionObjDev* objs,
                  unsigned nobj, unsigned* ridp, unsigned idmin, unsigned nmoving, unsigned cap, cudaStream_t s,

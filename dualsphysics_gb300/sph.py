@@ -110,6 +110,17 @@ class GbSphSingle:
     def ComputeVerlet(self, dt: float) -> None:
         self._check(lib().gbsph_verlet(self.ctx, dt), "ComputeVerlet")
 
+    def RunShifting(self, dt: float) -> None:
+        """JSphCpu::RunShifting: shifting sums -> displacements (no-op without shifting)."""
+        self._check(lib().gbsph_run_shifting(self.ctx, dt), "RunShifting")
+
+    def shiftpos(self) -> np.ndarray:
+        """The shifting sums after an interaction, or the displacements after RunShifting."""
+        n = self.divinfo()["np"]
+        out = np.empty((n, 4), np.float32)
+        self._check(lib().gbsph_get_shiftpos(self.ctx, ptr(out)), "shiftpos")
+        return out
+
     def ComputeStep_Sym(self, dtpre: float) -> tuple[float, float]:
         """Host-sequenced Symplectic step (JSphGpuSingle.cpp:785-826); returns (dt, next dt)."""
         dt = dtpre
@@ -121,6 +132,7 @@ class GbSphSingle:
         self.MdbcBoundCorrection(INTERSTEP_SYMCORRECTOR)
         self.Interaction_Forces(INTERSTEP_SYMCORRECTOR)
         dt_c = self.DtVariable(True)
+        self.RunShifting(dt)  # the predictor's RunShifting(dt/2) is not applied by the reference
         self.ComputeSymplecticCorr(dt)
         return dt, min(dt_p, dt_c)
 

@@ -62,6 +62,8 @@ typedef struct {
   float visco, viscoboundfactor, ddtvalue, coefdtmin, rhopoutmin, rhopoutmax;
   double dtini, dtmin;
   double maprealposmin[3], maprealposmax[3];
+  int tshift;                 /* Shifting: 0 none, 1 NoBound, 2 NoFixed, 3 Full */
+  float shiftcoef, shifttfs;  /* ShiftCoef (default -2), ShiftTFS (0: no free-surface threshold) */
 } gbsph_params;
 
 /* Derived constants of a case: the members of JSph / StCteSph the hot path
@@ -75,6 +77,8 @@ typedef struct {
   double mapposmin[3], maprealposmin[3], maprealsize[3], maprealposmax[3];
   double domposmin[3], domrealposmin[3], domrealposmax[3];
   unsigned mapcells[3], domcells[3], domcellcode;
+  int tshift;
+  float shiftcoef, shifttfs;
 } gbsph_consts;
 
 /* Cell-division summary (JCellDivGpuSingle members, JCellDivGpu.h). */
@@ -153,6 +157,18 @@ int gbsph_run(gbsph_ctx* ctx, unsigned nsteps, int use_graph);
 int gbsph_graph_prepare(gbsph_ctx* ctx, unsigned nsteps);
 /* Reads back the dt used by the last step and the next SymplecticDtPre. */
 int gbsph_step_dt(gbsph_ctx* ctx, double* dt_last, double* dt_next, double* time);
+
+/* Standard shifting (JSphShifting, JSphShifting.cpp:390-418; modes 1-3 in
+ * gbsph_consts.tshift): each fluid-row interaction writes the shifting sums
+ * (m/rho grad W, and -m/rho r.grad W in w; x = FLT_MAX where a boundary
+ * neighbour cancels them); gbsph_run_shifting(dt) turns them into the
+ * displacements the next corrector (Symplectic) or Verlet update adds, as
+ * RunShifting does.  gbsph_step / gbsph_run do this by themselves.  The
+ * reference's predictor computes RunShifting(dt/2) but never applies it
+ * (JSphCpu.cpp:1689), so the device step leaves it out.
+ * gbsph_get_shiftpos reads the np float4 values (GBSPH_EINVAL without shifting). */
+int gbsph_run_shifting(gbsph_ctx* ctx, double dt);
+int gbsph_get_shiftpos(gbsph_ctx* ctx, float* shiftpos);
 
 /* Read-back (JSphGpu::ParticlesDataDown, JSphGpu.cpp:630).  Any pointer may be
  * NULL.  Arrays hold the current np particles in the current (cell) order. */

@@ -27,6 +27,7 @@ class OrcParams(C.Structure):
         ("rhopoutmin", C.c_float), ("rhopoutmax", C.c_float),
         ("dtini", C.c_double), ("dtmin", C.c_double),
         ("maprealposmin", C.c_double * 3), ("maprealposmax", C.c_double * 3),
+        ("tshift", C.c_int), ("shiftcoef", C.c_float), ("shifttfs", C.c_float),
     ]
 
 
@@ -46,6 +47,7 @@ class OrcCtes(C.Structure):
         ("maprealposmax", C.c_double * 3),
         ("domposmin", C.c_double * 3), ("domrealposmin", C.c_double * 3), ("domrealposmax", C.c_double * 3),
         ("mapcells", C.c_uint * 3), ("domcells", C.c_uint * 3), ("domcellcode", C.c_uint),
+        ("tshift", C.c_int), ("shiftcoef", C.c_float), ("shifttfs", C.c_float),
     ]
 
 
@@ -74,9 +76,9 @@ _SIG = {
     "orc_divide": (C.c_int, [C.POINTER(OrcCtes), C.POINTER(OrcDiv), C.c_uint, C.c_uint, C.c_int, P, P, P, P, P,
                              C.c_uint]),
     "orc_interaction_forces": (None, [C.POINTER(OrcCtes), C.POINTER(OrcDiv), P, C.c_uint, C.c_uint, C.c_uint, P, P,
-                                      P, P, P, P, P, P, C.POINTER(C.c_float), C.c_int]),
+                                      P, P, P, P, P, P, C.POINTER(C.c_float), C.c_int, P]),
     "orc_interaction_forces_f64": (None, [C.POINTER(OrcCtes), C.POINTER(OrcDiv), P, C.c_uint, C.c_uint, C.c_uint,
-                                          P, P, P, P, P, P, P, P, C.POINTER(C.c_double), C.c_int, P, P]),
+                                          P, P, P, P, P, P, P, P, C.POINTER(C.c_double), C.c_int, P, P, P, P]),
     "orc_mdbc_correction": (None, [C.POINTER(OrcCtes), C.POINTER(OrcDiv), P, C.c_uint, P, P, P, P, C.c_int]),
     "orc_pips": (None, [C.POINTER(OrcCtes), C.POINTER(OrcDiv), P, C.c_uint, C.c_uint, C.c_uint, P, P,
                         C.POINTER(C.c_ulonglong * 4), C.c_int]),
@@ -90,6 +92,9 @@ _SIG = {
     "orc_sim_symplectic_pre": (C.c_int, [P, C.c_double]),
     "orc_sim_symplectic_cor": (C.c_int, [P, C.c_double]),
     "orc_sim_verlet": (C.c_int, [P, C.c_double]),
+    "orc_sim_run_shifting": (C.c_int, [P, C.c_double]),
+    "orc_sim_get_shiftpos": (None, [P, P]),
+    "orc_sim_set_shiftpos": (None, [P, P]),
     "orc_sim_step": (C.c_int, [P, C.POINTER(C.c_double)]),
     "orc_sim_np": (C.c_uint, [P]),
     "orc_sim_npb": (C.c_uint, [P]),
@@ -248,6 +253,17 @@ class Sim:
     def verlet(self, dt):
         lib().orc_sim_verlet(self.h, dt)
 
+    def run_shifting(self, dt):
+        lib().orc_sim_run_shifting(self.h, dt)
+
+    def shiftpos(self):
+        out = np.empty((self.np, 4), np.float32)
+        lib().orc_sim_get_shiftpos(self.h, _p(out))
+        return out
+
+    def set_shiftpos(self, sh):
+        lib().orc_sim_set_shiftpos(self.h, _p(np.ascontiguousarray(sh, np.float32)))
+
     def step(self):
         dt = C.c_double()
         rc = lib().orc_sim_step(self.h, C.byref(dt))
@@ -292,10 +308,14 @@ def forces_f64(sim: Sim):
     visc = C.c_double()
     absace = np.zeros(n, np.float64)
     absar = np.zeros(n, np.float64)
+    shift = np.zeros((n, 4), np.float64)
+    absshift = np.zeros(n, np.float64)
     lib().orc_interaction_forces_f64(C.byref(sim.ctes), C.byref(d), _p(bc), n, sim.npb, sim.npbok,
                                      _p(st["dcell"]), _p(st["pos"]), _p(st["velrho"]), _p(st["code"]), _p(tau),
-                                     _p(ace), _p(ar), _p(strain), C.byref(visc), 0, _p(absace), _p(absar))
-    return {"ace": ace, "ar": ar, "viscdt": visc.value, "absace": absace, "absar": absar}
+                                     _p(ace), _p(ar), _p(strain), C.byref(visc), 0, _p(absace), _p(absar),
+                                     _p(shift), _p(absshift))
+    return {"ace": ace, "ar": ar, "viscdt": visc.value, "absace": absace, "absar": absar, "shiftpos": shift,
+            "absshift": absshift}
 
 
 def pips(sim: Sim):

@@ -110,6 +110,14 @@ class OracleCpu : public JSphCpuSingle{
     WriteRaw(b+"ace.bin",Ace_c->cptr(),sizeof(tfloat3)*Np);
     WriteRaw(b+"ar.bin",Ar_c->cptr(),sizeof(float)*Np);
     WriteRaw(b+"velrho.bin",Velrho_c->cptr(),sizeof(tfloat4)*Np);
+    if(Shifting)WriteRaw(b+"shiftpos.bin",ShiftPosfs_c->cptr(),sizeof(tfloat4)*Np);
+  }
+
+  // Shifting displacements after RunShifting (JSphCpu.cpp:2084-2088).
+  void ShiftAndDump(double dt,const std::string& tag){
+    if(!Shifting)return;
+    RunShifting(dt);
+    WriteRaw(Out+"/"+tag+"_shiftpos.bin",ShiftPosfs_c->cptr(),sizeof(tfloat4)*Np);
   }
 
   // Motion data of every moving object for the interval just computed by
@@ -151,6 +159,7 @@ class OracleCpu : public JSphCpuSingle{
     const double dt_p=DtVariable(false);
     char tx[256]; sprintf(tx,"dt=%.17g\ndt_p=%.17g\n",dt,dt_p);
     Meta("s0pred",tx);
+    ShiftAndDump(dt*.5,"s0predsh");
     ComputeSymplecticPre(dt);
     PosInteraction_Forces();
     DumpState("s0pre");
@@ -166,6 +175,7 @@ class OracleCpu : public JSphCpuSingle{
     const double dt_c=DtVariable(true);
     sprintf(tx,"dt=%.17g\ndt_c=%.17g\n",dt,dt_c);
     Meta("s0cor",tx);
+    ShiftAndDump(dt,"s0corsh");
     ComputeSymplecticCorr(dt);
     PosInteraction_Forces();
     DumpState("s0corr");
@@ -191,6 +201,7 @@ class OracleCpu : public JSphCpuSingle{
     const double dt=DtVariable(true);
     char tx[256]; sprintf(tx,"dt=%.17g\ndt_p=%.17g\n",dt,dt);
     Meta("s0pred",tx);
+    ShiftAndDump(dt,"s0predsh");
     ComputeVerlet(dt);
     PosInteraction_Forces();
     DumpState("s0pre");

@@ -89,6 +89,7 @@ void orc_cell_decode(unsigned dcc, unsigned cel, unsigned* cx, unsigned* cy, uns
 int orc_config(const orc_params* p, orc_ctes* c) {
   memset(c, 0, sizeof(*c));
   c->tstep = p->tstep; c->tvisco = p->tvisco; c->tdensity = p->tdensity; c->tboundary = p->tboundary;
+  c->tshift = p->tshift; c->shiftcoef = p->tshift ? p->shiftcoef : 0.f; c->shifttfs = p->tshift ? p->shifttfs : 0.f;
   c->verletsteps = p->verletsteps; c->dtallparticles = p->dtallparticles; c->simulate2d = p->simulate2d;
   c->cellmode_div = p->cellmode_div ? p->cellmode_div : 1;
   /* JSph::LoadConfigCtes (JSph.cpp:642-658): float members */
@@ -415,9 +416,10 @@ void orc_interaction_forces(const orc_ctes* c, const orc_div* d, const unsigned*
                             unsigned np, unsigned npb, unsigned npbok,
                             const unsigned* dcell, const double* pos, const float* velrho,
                             const uint16_t* code, const float* tau,
-                            float* ace, float* ar, float* two_strain, float* viscdt_out, int nthreads) {
+                            float* ace, float* ar, float* two_strain, float* viscdt_out, int nthreads,
+                            float* shiftpos) {
   interaction_forces_f32(c, d, begincell, np, npb, npbok, dcell, pos, velrho, code, tau, ace, ar, two_strain,
-                         viscdt_out, nthreads, NULL, NULL);
+                         viscdt_out, nthreads, NULL, NULL, shiftpos, NULL);
 }
 
 void orc_interaction_forces_f64(const orc_ctes* c, const orc_div* d, const unsigned* begincell,
@@ -425,9 +427,9 @@ void orc_interaction_forces_f64(const orc_ctes* c, const orc_div* d, const unsig
                                 const unsigned* dcell, const double* pos, const float* velrho,
                                 const uint16_t* code, const double* tau,
                                 double* ace, double* ar, double* two_strain, double* viscdt_out, int nthreads,
-                                double* absace, double* absar) {
+                                double* absace, double* absar, double* shiftpos, double* absshift) {
   interaction_forces_f64(c, d, begincell, np, npb, npbok, dcell, pos, velrho, code, tau, ace, ar, two_strain,
-                         viscdt_out, nthreads, absace, absar);
+                         viscdt_out, nthreads, absace, absar, shiftpos, absshift);
 }
 
 /* JSphCpu::ComputeSpsTau (JSphCpu.cpp:1279-1309) */
@@ -665,6 +667,7 @@ struct orc_sim {
   unsigned *idp, *dcell;
   uint16_t* code;
   float *boundnor, *tau, *strain, *ace, *ar;
+  float* shiftpos; /* 4 per particle: shifting sums, then displacements (ShiftPosfs_c) */
   unsigned *cellpart, *sortpart, *begincell;
   unsigned begincell_cap;
   void* scratch;
@@ -703,6 +706,7 @@ orc_sim* orc_sim_create(const orc_ctes* c, unsigned np, unsigned npb, const doub
   s->strain = (float*)calloc((size_t)6 * np + 1, sizeof(float));
   s->ace = (float*)calloc((size_t)3 * np + 1, sizeof(float));
   s->ar = (float*)calloc((size_t)np + 1, sizeof(float));
+  s->shiftpos = (float*)calloc((size_t)4 * np + 1, sizeof(float));
   s->cellpart = (unsigned*)xmalloc(sizeof(unsigned) * np);
   s->sortpart = (unsigned*)xmalloc(sizeof(unsigned) * np);
   const unsigned long long maxnct =
@@ -735,7 +739,7 @@ void orc_sim_destroy(orc_sim* s) {
   if (!s) return;
   free(s->pos); free(s->pospre); free(s->velrho); free(s->velrhopre); free(s->velrhom1);
   free(s->idp); free(s->dcell); free(s->code); free(s->boundnor); free(s->tau); free(s->strain);
-  free(s->ace); free(s->ar); free(s->cellpart); free(s->sortpart); free(s->begincell); free(s->scratch);
+  free(s->ace); free(s->ar); free(s->shiftpos); free(s->cellpart); free(s->sortpart); free(s->begincell); free(s->scratch);
   free(s);
 }
 
@@ -792,7 +796,7 @@ int orc_sim_interaction(orc_sim* s) {
   s->velmax = orc_velmax(s->np - pini, s->velrho + 4 * (size_t)pini);
   float viscdt = 0;
   orc_interaction_forces(&s->c, &s->d, s->begincell, s->np, s->npb, s->npbok, s->dcell, s->pos, s->velrho, s->code,
-                         s->tau, s->ace, s->ar, s->strain, &viscdt, s->nthreads);
+                         s->tau, s->ace, s->ar, s->strain, &viscdt, s->nthreads, s->c.tshift ? s->shiftpos : NULL);
   s->viscdtmax = viscdt;
   /* ComputeSpsTau runs inside the interaction (JSphCpu.cpp:1366-1367) */
   if (s->c.tvisco == ORC_VISCO_LAMINARSPS) orc_sps_tau(&s->c, s->np - s->npb, s->npb, s->velrho, s->strain, s->tau);
@@ -855,6 +859,8 @@ int orc_sim_symplectic_pre(orc_sim* s, double dt) {
     const float* vp = s->velrhopre + 4 * (size_t)p;
     const float* a = s->ace + 3 * (size_t)p;
     const float rhonew = (float)((double)vp[3] + dt05 * s->ar[p]);
+    /* no shifting in the predictor: the reference applies it in the corrector
+       only (shift=false in ComputeSymplecticPre, JSphCpu.cpp:1689) */
     const double dx = (double)vp[0] * dt05;
     const double dy = (double)vp[1] * dt05;
     const double dz = (double)vp[2] * dt05;
@@ -880,6 +886,45 @@ int orc_sim_symplectic_pre(orc_sim* s, double dt) {
   }
   memcpy(s->pos, s->pospre, sizeof(double) * 3 * (size_t)npb);
   return 0;
+}
+
+/* JSphShifting::RunCpu (JSphShifting.cpp:390-418): the shifting sums of each
+ * fluid particle become its displacement, proportional to dt*coef*h*|v|, cut
+ * below the free-surface threshold and limited to dp/10; a particle whose
+ * sums were cancelled near the boundary gets none. */
+int orc_sim_run_shifting(orc_sim* s, double dt) {
+  const orc_ctes* c = &s->c;
+  if (!c->tshift) return 0;
+  const double coefumagn = dt * c->shiftcoef * c->kernelh;
+  const double coeftfs = (c->simulate2d ? 2.0 : 3.0) - c->shifttfs;
+  const float maxdist = (float)(c->dp * 0.1);
+  for (unsigned p = s->npb; p < s->np; p++) {
+    float* rs = s->shiftpos + 4 * (size_t)p;
+    if (rs[0] != FLT_MAX) {
+      const float* v = s->velrho + 4 * (size_t)p;
+      const double vx = (double)v[0], vy = (double)v[1], vz = (double)v[2];
+      double umagn = coefumagn * sqrt(vx * vx + vy * vy + vz * vz);
+      if (c->shifttfs) {
+        if (rs[3] < c->shifttfs) umagn = 0;
+        else umagn *= ((double)rs[3] - c->shifttfs) / coeftfs;
+      }
+      for (int k = 0; k < 3; k++) {
+        const float d = (float)((double)rs[k] * umagn);
+        rs[k] = (fabsf(d) < maxdist ? d : (d >= 0 ? maxdist : -maxdist));
+      }
+    } else {
+      rs[0] = rs[1] = rs[2] = rs[3] = 0;
+    }
+  }
+  return 0;
+}
+
+void orc_sim_get_shiftpos(const orc_sim* s, float* out) {
+  memcpy(out, s->shiftpos, sizeof(float) * 4 * (size_t)s->np);
+}
+
+void orc_sim_set_shiftpos(orc_sim* s, const float* in) {
+  memcpy(s->shiftpos, in, sizeof(float) * 4 * (size_t)s->np);
 }
 
 /* JSphCpu::ComputeSymplecticCorr (JSphCpu.cpp:1850-2029). */
@@ -909,9 +954,13 @@ int orc_sim_symplectic_cor(orc_sim* s, double dt) {
     const float nx = (float)((double)vp[0] + ((double)a[0] + c->gravity[0]) * dt);
     const float ny = (float)((double)vp[1] + ((double)a[1] + c->gravity[1]) * dt);
     const float nz = (float)((double)vp[2] + ((double)a[2] + c->gravity[2]) * dt);
-    const double dx = ((double)vp[0] + (double)nx) * dt05;
-    const double dy = ((double)vp[1] + (double)ny) * dt05;
-    const double dz = ((double)vp[2] + (double)nz) * dt05;
+    double dx = ((double)vp[0] + (double)nx) * dt05;
+    double dy = ((double)vp[1] + (double)ny) * dt05;
+    double dz = ((double)vp[2] + (double)nz) * dt05;
+    if (c->tshift) {
+      const float* sh = s->shiftpos + 4 * (size_t)p;
+      dx += (double)sh[0]; dy += (double)sh[1]; dz += (double)sh[2];
+    }
     const int outrho = (rhonew < c->rhopoutmin || rhonew > c->rhopoutmax);
     mov[3 * (size_t)p] = dx; mov[3 * (size_t)p + 1] = dy; mov[3 * (size_t)p + 2] = dz;
     if (outrho && codespecial(rcode) == ORC_CODE_NORMAL) s->code[p] = (uint16_t)((rcode & ~ORC_CODE_MASKSPECIAL) | ORC_CODE_OUTRHO);
@@ -950,9 +999,13 @@ int orc_sim_verlet(orc_sim* s, double dt) {
     const float* a = s->ace + 3 * (size_t)p;
     const float rhonew = (float)((double)v2[3] + dt2 * s->ar[p]);
     const double ax = (double)a[0] + g[0], ay = (double)a[1] + g[1], az = (double)a[2] + g[2];
-    const double dx = (double)v1[0] * dt + ax * dt205;
-    const double dy = (double)v1[1] * dt + ay * dt205;
-    const double dz = (double)v1[2] * dt + az * dt205;
+    double dx = (double)v1[0] * dt + ax * dt205;
+    double dy = (double)v1[1] * dt + ay * dt205;
+    double dz = (double)v1[2] * dt + az * dt205;
+    if (c->tshift) {
+      const float* sh = s->shiftpos + 4 * (size_t)p;
+      dx += (double)sh[0]; dy += (double)sh[1]; dz += (double)sh[2];
+    }
     const int outrho = (rhonew < c->rhopoutmin || rhonew > c->rhopoutmax);
     float* nv = newv + 4 * (size_t)p;
     nv[0] = (float)((double)v2[0] + ax * dt2);
@@ -988,12 +1041,14 @@ int orc_sim_step(orc_sim* s, double* dtused) {
     orc_sim_interaction(s);
     const double dt_p = orc_sim_dtvariable(s, &err);
     if (err) return -4;
+    orc_sim_run_shifting(s, dt * .5);
     orc_sim_symplectic_pre(s, dt);
     if ((r = orc_sim_run_cell_divide(s))) return r;
     orc_sim_mdbc(s, 1);
     orc_sim_interaction(s);
     const double dt_c = orc_sim_dtvariable(s, &err);
     if (err) return -4;
+    orc_sim_run_shifting(s, dt);
     orc_sim_symplectic_cor(s, dt);
     s->symplecticdtpre = (dt_p < dt_c ? dt_p : dt_c);
     if (dtused) *dtused = dt;
@@ -1003,6 +1058,7 @@ int orc_sim_step(orc_sim* s, double* dtused) {
     orc_sim_interaction(s);
     const double dt = orc_sim_dtvariable(s, &err);
     if (err) return -4;
+    orc_sim_run_shifting(s, dt);
     orc_sim_verlet(s, dt);
     if (dtused) *dtused = dt;
     s->timestep += dt;

@@ -70,6 +70,8 @@ typedef struct {
   double mapposmin[3], maprealposmin[3], maprealsize[3], maprealposmax[3];
   double domposmin[3], domrealposmin[3], domrealposmax[3];
   unsigned mapcells[3], domcells[3], domcellcode;
+  int tshift;
+  float shiftcoef, shifttfs;
 } orc_ctes;
 
 /* Raw case parameters (what the run XML carries) from which orc_config derives
@@ -82,6 +84,8 @@ typedef struct {
   float visco, viscoboundfactor, ddtvalue, coefdtmin, rhopoutmin, rhopoutmax;
   double dtini, dtmin;               /* 0 = automatic */
   double maprealposmin[3], maprealposmax[3];
+  int tshift;
+  float shiftcoef, shifttfs;
 } orc_params;
 
 /* Cell-division state: JCellDivCpu/JCellDivCpuSingle members. */
@@ -117,13 +121,14 @@ void orc_interaction_forces(const orc_ctes* c, const orc_div* d, const unsigned*
                             unsigned np, unsigned npb, unsigned npbok,
                             const unsigned* dcell, const double* pos, const float* velrho,
                             const uint16_t* code, const float* tau,
-                            float* ace, float* ar, float* two_strain, float* viscdt_out, int nthreads);
+                            float* ace, float* ar, float* two_strain, float* viscdt_out, int nthreads,
+                            float* shiftpos);  /* 4 per particle or NULL: shifting sums (tshift) */
 void orc_interaction_forces_f64(const orc_ctes* c, const orc_div* d, const unsigned* begincell,
                                 unsigned np, unsigned npb, unsigned npbok,
                                 const unsigned* dcell, const double* pos, const float* velrho,
                                 const uint16_t* code, const double* tau,
                                 double* ace, double* ar, double* two_strain, double* viscdt_out, int nthreads,
-                                double* absace, double* absar);
+                                double* absace, double* absar, double* shiftpos, double* absshift);
 void orc_sps_tau(const orc_ctes* c, unsigned n, unsigned pini, const float* velrho,
                  const float* two_strain, float* tau);
 void orc_mdbc_correction(const orc_ctes* c, const orc_div* d, const unsigned* begincell,
@@ -150,6 +155,9 @@ double orc_sim_dtvariable(orc_sim* s, int* err);
 int orc_sim_symplectic_pre(orc_sim* s, double dt);
 int orc_sim_symplectic_cor(orc_sim* s, double dt);
 int orc_sim_verlet(orc_sim* s, double dt);
+int orc_sim_run_shifting(orc_sim* s, double dt);   /* JSphShifting::RunCpu */
+void orc_sim_get_shiftpos(const orc_sim* s, float* out);
+void orc_sim_set_shiftpos(orc_sim* s, const float* in);
 int orc_sim_step(orc_sim* s, double* dtused);
 unsigned orc_sim_np(const orc_sim* s);
 unsigned orc_sim_npb(const orc_sim* s);

@@ -41,6 +41,12 @@ CASES = {
     "ddt2f_d04": (lambda: cg.spec_c2(dp=0.04, name="ddt2f_d04", density_dt=3, init_vel=0.02, seed=17), 10),
     "half_d04": (lambda: cg.spec_c1(dp=0.04, name="half_d04", init_vel=0.02, seed=19), 10, ["-cellmode:half"]),
     "mov_d04": (lambda: spec_moving(), 20),
+    # standard shifting: Full with the free-surface threshold (Symplectic), and
+    # NoBound without it (Verlet)
+    "shift_d04": (lambda: cg.spec_c1(dp=0.04, name="shift_d04", init_vel=0.05, seed=29,
+                                     extra_params={"Shifting": 3, "ShiftCoef": -2, "ShiftTFS": 2.75}), 12),
+    "shiftnb_d04": (lambda: cg.spec_c1(dp=0.04, name="shiftnb_d04", step_algorithm=1, verlet_steps=5,
+                                       init_vel=0.05, seed=31, extra_params={"Shifting": 1}), 12),
 }
 
 # A sloshing tank: the walls move through a chain of movements -- sinusoidal
@@ -167,6 +173,9 @@ def make(name: str, threads: int = 8) -> str:
             if os.path.exists(os.path.join(outdir, f"{tag}_ace.bin")):
                 arr[f"{tag}_ace"] = _raw(outdir, tag, "ace", np.float32, 3)
                 arr[f"{tag}_ar"] = _raw(outdir, tag, "ar", np.float32)
+        for tag in ("s0pred", "s0cor", "s0predsh", "s0corsh"):  # shifting sums, then displacements
+            if os.path.exists(os.path.join(outdir, f"{tag}_shiftpos.bin")):
+                arr[f"{tag}_shiftpos"] = _raw(outdir, tag, "shiftpos", np.float32, 4)
         arr["s0mdbc_rho"] = _raw(outdir, "s0mdbc", "velrho", np.float32, 4)[:, 3].copy()
         arr["dtlist"] = np.fromfile(os.path.join(outdir, "end_dtlist.bin"), dtype=np.float64)
         if os.path.exists(os.path.join(outdir, "motion.txt")):  # per-step motion data of the moving objects

@@ -71,13 +71,17 @@ def test_forces_within_tolerance(name):
     if cd.params.tboundary != _lib.BC_MDBC:
         G.assert_fp32_parity(ace[npb:], g["s0pred_ace"][npb:], f64["ace"][npb:], f64["absace"][npb:], "ace vs ref")
     assert np.all(ace[:npb] == 0)
+    if name in G.SHIFT_CASES:  # the shifting sums of the same interaction
+        G.assert_shift_sums(s.shiftpos()[npb:], o.shiftpos()[npb:], f64["shiftpos"][npb:], f64["absshift"][npb:],
+                            "shifting sums")
     om = o.maxes()
     assert mx["acemax"] == pytest.approx(om["acemax"], rel=1e-5)
     assert mx["velmax"] == pytest.approx(om["velmax"], rel=1e-6)
     assert mx["viscdtmax"] == pytest.approx(om["viscdtmax"], rel=1e-4, abs=1e-6)
 
 
-@pytest.mark.parametrize("name", ["dbc_d04", "vel_d04", "sps_d04", "mdbc_d04", "lam_d04", "ddt2f_d04", "half_d04"])
+@pytest.mark.parametrize("name", ["dbc_d04", "vel_d04", "sps_d04", "mdbc_d04", "lam_d04", "ddt2f_d04", "half_d04",
+                                  "shift_d04", "shiftnb_d04"])
 @pytest.mark.parametrize("variant", [0, 1])
 def test_forces_variants_within_tolerance(name, variant):
     """Both fluid-row kernels: queued rounds (0), one thread per particle (1)."""
@@ -99,9 +103,31 @@ def test_forces_variants_within_tolerance(name, variant):
     npb = o2.npb
     G.assert_fp32_parity(ace[npb:], a32[npb:], f64["ace"][npb:], f64["absace"][npb:], "ace")
     G.assert_fp32_parity(ar, r32, f64["ar"], f64["absar"], "ar")
+    if name in G.SHIFT_CASES:
+        G.assert_shift_sums(s.shiftpos()[npb:], o2.shiftpos()[npb:], f64["shiftpos"][npb:], f64["absshift"][npb:],
+                            "shifting sums")
 
 
-@pytest.mark.parametrize("name", [n for n in G.CASE_NAMES if n != "verlet_d04"])
+@pytest.mark.parametrize("name", G.SHIFT_CASES)
+def test_run_shifting_bit_exact_given_same_sums(name):
+    """RunShifting on the device equals the oracle's fed the same sums and
+    velocities (double arithmetic, bit for bit)."""
+    cd = G.load_generated(name)
+    s = _gpu(cd)
+    o = _oracle(cd)
+    s.Interaction_Forces(_lib.INTERSTEP_SYMPREDICTOR)
+    o.interaction()
+    o.set_shiftpos(s.shiftpos())
+    dt = 3.0e-4
+    s.RunShifting(dt)
+    o.run_shifting(dt)
+    gsh, osh = s.shiftpos(), o.shiftpos()
+    npb = o.npb
+    np.testing.assert_array_equal(gsh[npb:], osh[npb:])
+    assert np.abs(gsh[npb:, :3]).max() > 0
+
+
+@pytest.mark.parametrize("name", [n for n in G.CASE_NAMES if not G.is_verlet(n)])
 def test_symplectic_step_bit_exact_given_same_forces(name):
     """GPU integrator + divide vs the oracle fed the GPU's own forces."""
     cd = G.load_generated(name)
@@ -129,6 +155,9 @@ def test_symplectic_step_bit_exact_given_same_forces(name):
     ace, ar = s.forces()
     o.interaction()
     o.set_forces(ace, ar)
+    if name in G.SHIFT_CASES:  # the device's displacements, for the integrator alone
+        s.RunShifting(dt)
+        o.set_shiftpos(s.shiftpos())
     s.ComputeSymplecticCorr(dt)
     o.symplectic_cor(dt)
     gs, os_ = s.download(), o.state()
@@ -136,8 +165,9 @@ def test_symplectic_step_bit_exact_given_same_forces(name):
         np.testing.assert_array_equal(gs[k], os_[k], err_msg=k)
 
 
-def test_verlet_step_bit_exact_given_same_forces():
-    cd = G.load_generated("verlet_d04")
+@pytest.mark.parametrize("name", [n for n in G.CASE_NAMES if G.is_verlet(n)])
+def test_verlet_step_bit_exact_given_same_forces(name):
+    cd = G.load_generated(name)
     s = _gpu(cd)
     o = _oracle(cd)
     for it in range(6):  # crosses the Euler step (VerletSteps=5)
@@ -146,6 +176,9 @@ def test_verlet_step_bit_exact_given_same_forces():
         o.interaction()
         o.set_forces(ace, ar)
         dt = 2.0e-4
+        if name in G.SHIFT_CASES:
+            s.RunShifting(dt)
+            o.set_shiftpos(s.shiftpos())
         s.ComputeVerlet(dt)
         o.verlet(dt)
         s.RunCellDivide()
@@ -155,7 +188,7 @@ def test_verlet_step_bit_exact_given_same_forces():
             np.testing.assert_array_equal(gs[k], os_[k], err_msg=f"{k} at step {it}")
 
 
-@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "sps_d04"])
+@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "sps_d04", "shift_d04"])
 def test_device_step_matches_host_sequenced_step(name):
     """gbsph_step (dt kept on the device) equals the host-sequenced
     ComputeStep_Sym + RunCellDivide on the same device."""

@@ -65,9 +65,12 @@ def test_forces_within_fp32_tolerance(name):
                              (r32, g["s0pred_ar"], f64["ar"], f64["absar"])):
         # the oracle's FP32 evaluation and the reference's land at the same level
         G.assert_fp32_parity(x32, ref, x64, s, "oracle vs reference error level")
+    if name in G.SHIFT_CASES:
+        G.assert_shift_sums(sim.shiftpos()[npb:], g["s0pred_shiftpos"][npb:], f64["shiftpos"][npb:],
+                            f64["absshift"][npb:], "oracle vs reference shifting")
 
 
-@pytest.mark.parametrize("name", [n for n in G.CASE_NAMES if n != "verlet_d04"])
+@pytest.mark.parametrize("name", [n for n in G.CASE_NAMES if not G.is_verlet(n)])
 def test_symplectic_step_bit_exact_given_reference_forces(name):
     """Integrator + divide: fed the reference's own ace/ar, the oracle reproduces
     the reference state bit for bit."""
@@ -80,6 +83,8 @@ def test_symplectic_step_bit_exact_given_reference_forces(name):
     sim.set_state(None, vr)
     sim.interaction()
     sim.set_forces(g["s0pred_ace"], g["s0pred_ar"])
+    if "s0predsh_shiftpos" in g:  # the reference's shifting displacements
+        sim.set_shiftpos(g["s0predsh_shiftpos"])
     dt = float(g["meta"]["s0pred"]["dt"])
     sim.symplectic_pre(dt)
     st = sim.state()
@@ -92,17 +97,22 @@ def test_symplectic_step_bit_exact_given_reference_forces(name):
     np.testing.assert_array_equal(sim.begincell(), g["s0div_begincell"])
     sim.interaction()
     sim.set_forces(g["s0cor_ace"], g["s0cor_ar"])
+    if "s0corsh_shiftpos" in g:
+        sim.set_shiftpos(g["s0corsh_shiftpos"])
     sim.symplectic_cor(dt)
     st = sim.state()
     for k in ("idp", "code", "dcell", "pos", "velrho"):
         np.testing.assert_array_equal(st[k], g[f"s0corr_{k}"], err_msg=k)
 
 
-def test_verlet_step_bit_exact_given_reference_forces():
-    g = G.golden("verlet_d04")
-    _, _, sim = _sim("verlet_d04")
+@pytest.mark.parametrize("name", [n for n in G.CASE_NAMES if G.is_verlet(n)])
+def test_verlet_step_bit_exact_given_reference_forces(name):
+    g = G.golden(name)
+    _, _, sim = _sim(name)
     sim.interaction()
     sim.set_forces(g["s0pred_ace"], g["s0pred_ar"])
+    if "s0predsh_shiftpos" in g:
+        sim.set_shiftpos(g["s0predsh_shiftpos"])
     sim.verlet(float(g["meta"]["s0pred"]["dt"]))
     st = sim.state()
     for k in ("idp", "code", "dcell", "pos", "velrho"):
@@ -110,6 +120,21 @@ def test_verlet_step_bit_exact_given_reference_forces():
     sim.divide()
     np.testing.assert_array_equal(sim.state()["idp"], g["s1_idp"])
     np.testing.assert_array_equal(sim.begincell(), g["s1_begincell"])
+
+
+@pytest.mark.parametrize("name", G.SHIFT_CASES)
+def test_run_shifting_bit_exact_given_reference_sums(name):
+    """JSphShifting::RunCpu: fed the reference's shifting sums, the oracle's
+    displacements equal the reference's bit for bit (double arithmetic)."""
+    g = G.golden(name)
+    _, _, sim = _sim(name)
+    sim.interaction()
+    dt = float(g["meta"]["s0pred"]["dt"])
+    sim.set_shiftpos(g["s0pred_shiftpos"])
+    sim.run_shifting(dt if G.is_verlet(name) else dt * 0.5)
+    npb = sim.npb
+    np.testing.assert_array_equal(sim.shiftpos()[npb:], g["s0predsh_shiftpos"][npb:])
+    assert np.abs(g["s0predsh_shiftpos"][npb:, :3]).max() > 0   # some particles shift
 
 
 @pytest.mark.parametrize("name", G.CASE_NAMES)
