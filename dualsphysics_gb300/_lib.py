@@ -38,6 +38,7 @@ class Params(C.Structure):
         ("dtini", C.c_double), ("dtmin", C.c_double),
         ("maprealposmin", C.c_double * 3), ("maprealposmax", C.c_double * 3),
         ("tshift", C.c_int), ("shiftcoef", C.c_float), ("shifttfs", C.c_float),
+        ("peri", C.c_int * 3), ("periinc", C.c_double * 9),
     ]
 
 
@@ -58,6 +59,7 @@ class Consts(C.Structure):
         ("domposmin", C.c_double * 3), ("domrealposmin", C.c_double * 3), ("domrealposmax", C.c_double * 3),
         ("mapcells", C.c_uint * 3), ("domcells", C.c_uint * 3), ("domcellcode", C.c_uint),
         ("tshift", C.c_int), ("shiftcoef", C.c_float), ("shifttfs", C.c_float),
+        ("peri", C.c_int * 3), ("periinc", C.c_double * 9), ("mapposmax", C.c_double * 3),
     ]
 
 

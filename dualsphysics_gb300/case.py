@@ -115,6 +115,18 @@ def load_case(casedir: str, casename: str, cellmode: str = "full") -> CaseData:
     if tshift not in (0, 1, 2, 3):
         raise CaseError(f"Shifting mode {tshift} is not supported (0-3)")
     prm = Params()
+    # periodic conditions (JSph.cpp:815-826): Xperiodic with increments in y/z, ...
+    for key, ax, comp in (("XPeriodicIncY", 0, 1), ("XPeriodicIncZ", 0, 2), ("YPeriodicIncX", 1, 0),
+                          ("YPeriodicIncZ", 1, 2), ("ZPeriodicIncX", 2, 0), ("ZPeriodicIncY", 2, 1)):
+        if key in kv:
+            prm.peri[ax] = 1
+            prm.periinc[3 * ax + comp] = float(kv[key])
+    for key, axes in (("XYPeriodic", (0, 1)), ("XZPeriodic", (0, 2)), ("YZPeriodic", (1, 2))):
+        if key in kv:
+            for k in range(3):
+                prm.peri[k] = int(k in axes)
+            for k in range(9):
+                prm.periinc[k] = 0.0
     prm.tshift = tshift
     if tshift:
         prm.shiftcoef = gf("ShiftCoef", -2.0)
@@ -215,7 +227,9 @@ def load_case(casedir: str, casename: str, cellmode: str = "full") -> CaseData:
         cmax = np.array(root_b.get("CasePosMax"), dtype=np.float64)
         if np.all(cmin == cmax):
             cmin, cmax = pos.min(axis=0), pos.max(axis=0)
-        border = float(np.float32(prm.h)) * BORDER_MAP
+        # JPartsLoad4::CalculeLimitsPos: dp/2 on periodic axes (JPartsLoad4.cpp:389-399)
+        border = np.array([prm.dp / 2.0 if prm.peri[k] else float(np.float32(prm.h)) * BORDER_MAP
+                           for k in range(3)])
         mapmin, mapmax = cmin - border, cmax + border
         # simulationdomain
         sd = par.find("simulationdomain")
@@ -242,7 +256,10 @@ def load_case(casedir: str, casename: str, cellmode: str = "full") -> CaseData:
                         dmax[k] = v
             if np.any(dmin > mapmin) or np.any(dmax < mapmax):
                 raise CaseError("domain limits are not valid")
-        mapmin, mapmax = dmin, dmax
+        # ResizeMapLimits applies the domain to non-periodic axes only (JSph.cpp:1473-1475)
+        for k in range(3):
+            if not prm.peri[k]:
+                mapmin[k], mapmax[k] = dmin[k], dmax[k]
     for k in range(3):
         prm.maprealposmin[k] = float(mapmin[k])
         prm.maprealposmax[k] = float(mapmax[k])

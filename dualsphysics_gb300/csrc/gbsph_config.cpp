@@ -86,19 +86,30 @@ extern "C" int gbsph_config(const gbsph_params* p, gbsph_consts* c) {
   c->scell = c->kernelsize / (float)c->cellmode_div;
   c->movlimit = c->scell * 0.9f;
   for (int k = 0; k < 3; k++) {
-    const double mapsize = p->maprealposmax[k] - p->maprealposmin[k];
-    if (!(mapsize > 0)) return GBSPH_EINVAL;
+    if (!(p->maprealposmax[k] - p->maprealposmin[k] > 0)) return GBSPH_EINVAL;
     c->maprealposmin[k] = p->maprealposmin[k];
-    c->maprealsize[k] = mapsize;
     c->maprealposmax[k] = p->maprealposmax[k];
-    c->mapposmin[k] = p->maprealposmin[k];
+    c->maprealsize[k] = p->maprealposmax[k] - p->maprealposmin[k];
+    c->peri[k] = p->peri[k] != 0;
+  }
+  // periodic increments: the own component is -MapRealSize (JSph.cpp:2186-2188)
+  for (int k = 0; k < 3; k++)
+    for (int j = 0; j < 3; j++)
+      c->periinc[3 * k + j] = c->peri[k] ? (j == k ? -c->maprealsize[k] : p->periinc[3 * k + j]) : 0.0;
+  // Map_PosMin/Max with a KernelSize halo on periodic axes (JSph.cpp:2190-2194),
+  // the map cells (JSph.cpp:1883-1885) and SelecDomain(0,Map_Cells) (JSph.cpp:1901-1931)
+  for (int k = 0; k < 3; k++) {
+    const double ks = (double)c->kernelsize;
+    c->mapposmin[k] = c->peri[k] ? c->maprealposmin[k] - ks : c->maprealposmin[k];
+    c->mapposmax[k] = c->peri[k] ? c->maprealposmax[k] + ks : c->maprealposmax[k];
+    const double mapsize = c->mapposmax[k] - c->mapposmin[k];
     c->mapcells[k] = (unsigned)std::ceil(mapsize / c->scell);
     c->domcells[k] = c->mapcells[k];
     c->domposmin[k] = c->mapposmin[k];
     double dmax = c->mapposmin[k] + (c->mapcells[k] * c->scell);
-    if (dmax > p->maprealposmax[k]) dmax = p->maprealposmax[k];
-    c->domrealposmin[k] = c->domposmin[k];
-    c->domrealposmax[k] = dmax;
+    if (dmax > c->mapposmax[k]) dmax = c->mapposmax[k];
+    c->domrealposmin[k] = c->domposmin[k] < c->maprealposmin[k] ? c->maprealposmin[k] : c->domposmin[k];
+    c->domrealposmax[k] = dmax > c->maprealposmax[k] ? c->maprealposmax[k] : dmax;
   }
   c->domcellcode = cell_code(c->domcells[0] + 1, c->domcells[1] + 1, c->domcells[2] + 1);
   return c->domcellcode ? GBSPH_OK : GBSPH_ECAPACITY;

@@ -480,6 +480,20 @@ bool load_case(const std::string& casedir, const std::string& casename, Case& c,
   if (tshift < 0 || tshift > 3) { err = "Shifting mode " + std::to_string(tshift) + " is not supported (0-3)"; return false; }
   gbsph_params& p = c.params;
   std::memset(&p, 0, sizeof(p));
+  // periodic conditions (JSph.cpp:815-826)
+  {
+    static const char* keys[6] = {"XPeriodicIncY", "XPeriodicIncZ", "YPeriodicIncX", "YPeriodicIncZ", "ZPeriodicIncX", "ZPeriodicIncY"};
+    static const int axis[6] = {0, 0, 1, 1, 2, 2}, comp[6] = {1, 2, 0, 2, 0, 1};
+    for (int k = 0; k < 6; k++)
+      if (kv.count(keys[k])) { p.peri[axis[k]] = 1; p.periinc[3 * axis[k] + comp[k]] = gf(keys[k], 0); }
+    static const char* pkeys[3] = {"XYPeriodic", "XZPeriodic", "YZPeriodic"};
+    static const int pax[3][3] = {{1, 1, 0}, {1, 0, 1}, {0, 1, 1}};
+    for (int k = 0; k < 3; k++)
+      if (kv.count(pkeys[k])) {
+        for (int j = 0; j < 3; j++) p.peri[j] = pax[k][j];
+        for (int j = 0; j < 9; j++) p.periinc[j] = 0;
+      }
+  }
   p.tshift = tshift;
   if (tshift) {
     p.shiftcoef = (float)gf("ShiftCoef", -2);
@@ -586,9 +600,13 @@ bool load_case(const std::string& casedir, const std::string& casename, Case& c,
       for (int j = 0; j < 3; j++) { cmin[j] = std::min(cmin[j], c.pos[3 * (size_t)k + j]); cmax[j] = std::max(cmax[j], c.pos[3 * (size_t)k + j]); }
   }
   for (int j = 0; j < 3; j++) { c.caseposmin[j] = cmin[j]; c.caseposmax[j] = cmax[j]; }
-  const double border = (double)(float)p.h * 0.05;
+  // JPartsLoad4::CalculeLimitsPos: dp/2 on periodic axes (JPartsLoad4.cpp:389-399)
   double mmin[3], mmax[3];
-  for (int j = 0; j < 3; j++) { mmin[j] = cmin[j] - border; mmax[j] = cmax[j] + border; }
+  for (int j = 0; j < 3; j++) {
+    const double border = p.peri[j] ? p.dp / 2. : (double)(float)p.h * 0.05;
+    mmin[j] = cmin[j] - border;
+    mmax[j] = cmax[j] + border;
+  }
   double dmin[3] = {mmin[0], mmin[1], mmin[2]}, dmax[3] = {mmax[0], mmax[1], mmax[2]};
   if (const XmlNode* sd = par->child("simulationdomain")) {
     const char* ax = "xyz";
@@ -608,7 +626,11 @@ bool load_case(const std::string& casedir, const std::string& casename, Case& c,
       if (dmin[j] > mmin[j] || dmax[j] < mmax[j]) { err = "domain limits are not valid"; return false; }
     }
   }
-  for (int j = 0; j < 3; j++) { p.maprealposmin[j] = dmin[j]; p.maprealposmax[j] = dmax[j]; }
+  // ResizeMapLimits applies the domain to non-periodic axes only (JSph.cpp:1473-1475)
+  for (int j = 0; j < 3; j++) {
+    p.maprealposmin[j] = p.peri[j] ? mmin[j] : dmin[j];
+    p.maprealposmax[j] = p.peri[j] ? mmax[j] : dmax[j];
+  }
   return true;
 }
 

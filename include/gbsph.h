@@ -64,6 +64,8 @@ typedef struct {
   double maprealposmin[3], maprealposmax[3];
   int tshift;                 /* Shifting: 0 none, 1 NoBound, 2 NoFixed, 3 Full */
   float shiftcoef, shifttfs;  /* ShiftCoef (default -2), ShiftTFS (0: no free-surface threshold) */
+  int peri[3];                /* periodic axes x, y, z (JSph.cpp:815-826) */
+  double periinc[9];          /* per axis k, its increment (XPeriodicIncY ...); the own component is set by config */
 } gbsph_params;
 
 /* Derived constants of a case: the members of JSph / StCteSph the hot path
@@ -79,6 +81,9 @@ typedef struct {
   unsigned mapcells[3], domcells[3], domcellcode;
   int tshift;
   float shiftcoef, shifttfs;
+  int peri[3];                /* periodic axes */
+  double periinc[9];          /* PeriXinc, PeriYinc, PeriZinc (JSph.cpp:2186-2188) */
+  double mapposmax[3];        /* Map_PosMax: MapRealPosMax + KernelSize on periodic axes */
 } gbsph_consts;
 
 /* Cell-division summary (JCellDivGpuSingle members, JCellDivGpu.h). */

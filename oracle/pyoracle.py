@@ -28,6 +28,7 @@ class OrcParams(C.Structure):
         ("dtini", C.c_double), ("dtmin", C.c_double),
         ("maprealposmin", C.c_double * 3), ("maprealposmax", C.c_double * 3),
         ("tshift", C.c_int), ("shiftcoef", C.c_float), ("shifttfs", C.c_float),
+        ("peri", C.c_int * 3), ("periinc", C.c_double * 9),
     ]
 
 
@@ -48,6 +49,7 @@ class OrcCtes(C.Structure):
         ("domposmin", C.c_double * 3), ("domrealposmin", C.c_double * 3), ("domrealposmax", C.c_double * 3),
         ("mapcells", C.c_uint * 3), ("domcells", C.c_uint * 3), ("domcellcode", C.c_uint),
         ("tshift", C.c_int), ("shiftcoef", C.c_float), ("shifttfs", C.c_float),
+        ("peri", C.c_int * 3), ("periinc", C.c_double * 9), ("mapposmax", C.c_double * 3),
     ]
 
 
@@ -64,6 +66,7 @@ class OrcDiv(C.Structure):
         ("bounddividecellmin", C.c_uint * 3), ("bounddividecellmax", C.c_uint * 3),
         ("npbignore", C.c_uint), ("npbout", C.c_uint), ("npfout", C.c_uint), ("npboutignore", C.c_uint),
         ("npfoutignore", C.c_uint), ("npfinal", C.c_uint), ("npbfinal", C.c_uint),
+        ("npb2", C.c_uint), ("npf2", C.c_uint),
     ]
 
 
@@ -73,7 +76,7 @@ _SIG = {
     "orc_calc_cellcode": (C.c_uint, [C.c_uint, C.c_uint, C.c_uint]),
     "orc_load_dcell": (None, [C.POINTER(OrcCtes), C.c_uint, P, P, P]),
     "orc_compute_press": (C.c_float, [C.POINTER(OrcCtes), C.c_float]),
-    "orc_divide": (C.c_int, [C.POINTER(OrcCtes), C.POINTER(OrcDiv), C.c_uint, C.c_uint, C.c_int, P, P, P, P, P,
+    "orc_divide": (C.c_int, [C.POINTER(OrcCtes), C.POINTER(OrcDiv), C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_int, P, P, P, P, P,
                              C.c_uint]),
     "orc_interaction_forces": (None, [C.POINTER(OrcCtes), C.POINTER(OrcDiv), P, C.c_uint, C.c_uint, C.c_uint, P, P,
                                       P, P, P, P, P, P, C.POINTER(C.c_float), C.c_int, P]),

@@ -141,10 +141,20 @@ int orc_config(const orc_params* p, orc_ctes* c) {
   c->movlimit = c->scell * 0.9f;
   for (int k = 0; k < 3; k++) {
     c->maprealposmin[k] = p->maprealposmin[k];
-    c->maprealsize[k] = p->maprealposmax[k] - p->maprealposmin[k];
     c->maprealposmax[k] = p->maprealposmax[k];
-    c->mapposmin[k] = p->maprealposmin[k];
-    const double mapsize = p->maprealposmax[k] - p->maprealposmin[k];
+    c->maprealsize[k] = p->maprealposmax[k] - p->maprealposmin[k];
+    c->peri[k] = p->peri[k] != 0;
+  }
+  /* periodic increments: the own component is -MapRealSize (JSph.cpp:2186-2188) */
+  for (int k = 0; k < 3; k++)
+    for (int j = 0; j < 3; j++)
+      c->periinc[3 * k + j] = c->peri[k] ? (j == k ? -c->maprealsize[k] : p->periinc[3 * k + j]) : 0.0;
+  /* Map_PosMin/Max: a KernelSize halo on periodic axes (JSph.cpp:2190-2194);
+     ConfigCellDivision (JSph.cpp:1877-1886) */
+  for (int k = 0; k < 3; k++) {
+    c->mapposmin[k] = c->peri[k] ? c->maprealposmin[k] - (double)c->kernelsize : c->maprealposmin[k];
+    c->mapposmax[k] = c->peri[k] ? c->maprealposmax[k] + (double)c->kernelsize : c->maprealposmax[k];
+    const double mapsize = c->mapposmax[k] - c->mapposmin[k];
     c->mapcells[k] = (unsigned)ceil(mapsize / c->scell);
   }
   /* SelecDomain(0,Map_Cells) (JSph.cpp:1901-1944) */
@@ -152,12 +162,11 @@ int orc_config(const orc_params* p, orc_ctes* c) {
     c->domcells[k] = c->mapcells[k];
     c->domposmin[k] = c->mapposmin[k] + (0 * c->scell);
     double dmax = c->mapposmin[k] + (c->mapcells[k] * c->scell);
-    const double mapmax = p->maprealposmax[k];
-    if (dmax > mapmax) dmax = mapmax;
+    if (dmax > c->mapposmax[k]) dmax = c->mapposmax[k];
     c->domrealposmin[k] = c->domposmin[k];
     c->domrealposmax[k] = dmax;
-    if (c->domrealposmax[k] > p->maprealposmax[k]) c->domrealposmax[k] = p->maprealposmax[k];
-    if (c->domrealposmin[k] < p->maprealposmin[k]) c->domrealposmin[k] = p->maprealposmin[k];
+    if (c->domrealposmax[k] > c->maprealposmax[k]) c->domrealposmax[k] = c->maprealposmax[k];
+    if (c->domrealposmin[k] < c->maprealposmin[k]) c->domrealposmin[k] = c->maprealposmin[k];
   }
   c->domcellcode = orc_calc_cellcode(c->domcells[0] + 1, c->domcells[1] + 1, c->domcells[2] + 1);
   return c->domcellcode ? 0 : -1;
@@ -206,23 +215,36 @@ static void limits_cell(const orc_ctes* c, unsigned n, unsigned pini, const unsi
   }
 }
 
-static void calc_domain_part(const orc_ctes* c, unsigned n, unsigned pini, const unsigned* dcell, const uint16_t* code,
-                             unsigned cellmin[3], unsigned cellmax[3]) {
-  /* CalcCellDomainBound / CalcCellDomainFluid with n2=0 (JCellDivCpu.cpp:295-345) */
+static void calc_domain_part(const orc_ctes* c, unsigned n, unsigned pini, unsigned n2, unsigned pini2,
+                             const unsigned* dcell, const uint16_t* code, unsigned cellmin[3], unsigned cellmax[3]) {
+  /* CalcCellDomainBound / CalcCellDomainFluid (JCellDivCpu.cpp:295-345): the
+     second range holds the periodic copies */
   unsigned cmin[3], cmax[3];
   limits_cell(c, n, pini, dcell, code, cmin, cmax);
   for (int k = 0; k < 3; k++) {
     cellmin[k] = (cmin[0] > cmax[0] ? c->domcells[k] : cmin[k]);
     cellmax[k] = (cmin[0] > cmax[0] ? 0 : cmax[k]);
   }
+  if (n2) {
+    limits_cell(c, n2, pini2, dcell, code, cmin, cmax);
+    const int empty = cmin[0] > cmax[0];
+    for (int k = 0; k < 3; k++) {
+      const unsigned a = empty ? c->domcells[k] : cmin[k], b = empty ? 0 : cmax[k];
+      if (a < cellmin[k]) cellmin[k] = a;
+      if (b > cellmax[k]) cellmax[k] = b;
+    }
+  }
 }
 
-int orc_divide(const orc_ctes* c, orc_div* d, unsigned npb, unsigned npf, int boundchanged,
-               const unsigned* dcell, const uint16_t* code,
+int orc_divide(const orc_ctes* c, orc_div* d, unsigned npb, unsigned npf, unsigned npbper, unsigned npfper,
+               int boundchanged, const unsigned* dcell, const uint16_t* code,
                unsigned* cellpart, unsigned* sortpart, unsigned* begincell, unsigned begincell_cap) {
-  /* JCellDivCpuSingle::Divide (JCellDivCpuSingle.cpp:280-350) */
+  /* JCellDivCpuSingle::Divide (JCellDivCpuSingle.cpp:280-350); npbper/npfper
+     periodic copies follow the npb+npf particles */
   d->dividefull = 0;
-  d->npb1 = npb; d->npf1 = npf; d->nptot = npb + npf;
+  d->npb1 = npb; d->npf1 = npf; d->npb2 = npbper; d->npf2 = npfper;
+  d->nptot = npb + npf + npbper + npfper;
+  if (c->peri[0] || c->peri[1] || c->peri[2]) boundchanged = 1;
   d->npbout = d->npfout = d->npboutignore = d->npfoutignore = 0;
   d->npfinal = d->npbfinal = 0;
   d->npbignore = 0;
@@ -236,7 +258,7 @@ int orc_divide(const orc_ctes* c, orc_div* d, unsigned npb, unsigned npf, int bo
   /* CalcCellDomain (JCellDivCpuSingle.cpp:45-71) */
   unsigned celbmin[3], celbmax[3], celfmin[3], celfmax[3];
   if (!d->boundlimitok) {
-    calc_domain_part(c, d->npb1, 0, dcell, code, celbmin, celbmax);
+    calc_domain_part(c, d->npb1, 0, d->npb2, d->npb1 + d->npf1, dcell, code, celbmin, celbmax);
     d->boundlimitok = 1;
     memcpy(d->boundlimitcellmin, celbmin, sizeof(celbmin));
     memcpy(d->boundlimitcellmax, celbmax, sizeof(celbmax));
@@ -244,7 +266,7 @@ int orc_divide(const orc_ctes* c, orc_div* d, unsigned npb, unsigned npf, int bo
     memcpy(celbmin, d->boundlimitcellmin, sizeof(celbmin));
     memcpy(celbmax, d->boundlimitcellmax, sizeof(celbmax));
   }
-  calc_domain_part(c, d->npf1, d->npb1, dcell, code, celfmin, celfmax);
+  calc_domain_part(c, d->npf1, d->npb1, d->npf2, d->npb1 + d->npf1 + d->npb2, dcell, code, celfmin, celfmax);
   /* MergeMapCellBoundFluid (JCellDivCpuSingle.cpp:85-101) */
   {
     const unsigned sd = (unsigned)c->cellmode_div;
@@ -339,7 +361,7 @@ int orc_divide(const orc_ctes* c, orc_div* d, unsigned npb, unsigned npf, int bo
   d->npboutignore = begincell[d->boxboundoutignore + 1] - begincell[d->boxboundoutignore];
   d->npfoutignore = begincell[d->boxfluidoutignore + 1] - begincell[d->boxfluidoutignore];
   d->npfinal = d->nptot - d->npbout - d->npfout - d->npboutignore - d->npfoutignore;
-  d->npbfinal = d->npb1 - d->npboutignore;
+  d->npbfinal = d->npb1 + d->npb2 - d->npboutignore;
   if (d->npbout != 0 && d->dividefull) d->npbfinal = UINT_MAX;
   return 0;
 }
@@ -662,6 +684,7 @@ struct orc_sim {
   orc_div d;
   int nthreads;
   unsigned cap, np, npb, npbok, casenbound;
+  unsigned npbper, npfper; /* periodic copies made by the last RunPeriodic */
   double *pos, *pospre;
   float *velrho, *velrhopre, *velrhom1;
   unsigned *idp, *dcell;
@@ -743,6 +766,99 @@ void orc_sim_destroy(orc_sim* s) {
   free(s);
 }
 
+/* Grows every per-particle array to hold n particles (ResizeParticlesSizeData). */
+static void ensure_cap(orc_sim* s, unsigned n) {
+  if (n <= s->cap) return;
+  const unsigned cap = n + n / 4 + 64;
+#define GROW(T, ARR, W) do { T* q_ = (T*)calloc((size_t)(W) * cap + 1, sizeof(T)); \
+    memcpy(q_, (ARR), sizeof(T) * (W) * (size_t)s->cap); free(ARR); (ARR) = q_; } while (0)
+  GROW(double, s->pos, 3); GROW(double, s->pospre, 3);
+  GROW(float, s->velrho, 4); GROW(float, s->velrhopre, 4); GROW(float, s->velrhom1, 4);
+  GROW(unsigned, s->idp, 1); GROW(unsigned, s->dcell, 1); GROW(uint16_t, s->code, 1);
+  GROW(float, s->boundnor, 3); GROW(float, s->tau, 6); GROW(float, s->strain, 6);
+  GROW(float, s->ace, 3); GROW(float, s->ar, 1); GROW(float, s->shiftpos, 4);
+  GROW(unsigned, s->cellpart, 1); GROW(unsigned, s->sortpart, 1);
+#undef GROW
+  free(s->scratch);
+  s->scratch = xmalloc(sizeof(double) * 6 * cap);
+  s->cap = cap;
+}
+
+/* JSphCpuSingle::RunPeriodic (JSphCpuSingle.cpp:416-504) with PeriodicMakeList
+ * and PeriodicDuplicate* (JSphCpuSingle.cpp:210-356): the periodic copies of
+ * the last divide are marked to be ignored; every particle within reach of a
+ * periodic face gets a copy moved by the increment, appended after the np
+ * particles, boundary copies then fluid ones, axis by axis (copies made for
+ * one axis are themselves copied for the next). */
+static void run_periodic(orc_sim* s) {
+  const orc_ctes* c = &s->c;
+  for (unsigned p = 0; p < s->np; p++)
+    if (codespecial(s->code[p]) == ORC_CODE_PERIODIC)
+      s->code[p] = (uint16_t)((s->code[p] & ~ORC_CODE_MASKSPECIAL) | ORC_CODE_OUTIGNORE);
+  const unsigned npb0 = s->npb, npf0 = s->np - s->npb;
+  s->npbper = s->npfper = 0;
+  s->boundchanged = 1;
+  unsigned* list = NULL;
+  for (int ctype = 0; ctype < 2; ctype++) {
+    const unsigned pini = ctype ? npb0 : 0, num = ctype ? npf0 : npb0;
+    for (int cper = 0; cper < 3; cper++) {
+      if (!c->peri[cper]) continue;
+      const double* inc = c->periinc + 3 * cper;
+      for (int cblock = 0; cblock < 2; cblock++) {
+        const unsigned nper = ctype ? s->npfper : s->npbper;
+        const unsigned pini2 = cblock ? pini : s->np - nper, num2 = cblock ? num : nper;
+        if (!num2) continue;
+        /* PeriodicMakeList */
+        list = (unsigned*)realloc(list, sizeof(unsigned) * 2 * (size_t)num2 + 1);
+        unsigned count = 0;
+        for (unsigned p2 = pini2; p2 < pini2 + num2; p2++) {
+          if (codespecial(s->code[p2]) > ORC_CODE_PERIODIC) continue;
+          const double* ps = s->pos + 3 * (size_t)p2;
+          for (int sgn = 0; sgn < 2; sgn++) {
+            double q[3];
+            for (int k = 0; k < 3; k++) q[k] = sgn ? ps[k] - inc[k] : ps[k] + inc[k];
+            if (c->mapposmin[0] <= q[0] && c->mapposmin[1] <= q[1] && c->mapposmin[2] <= q[2] &&
+                q[0] < c->mapposmax[0] && q[1] < c->mapposmax[1] && q[2] < c->mapposmax[2])
+              list[count++] = sgn ? (p2 | 0x80000000u) : p2;
+          }
+        }
+        /* PeriodicDuplicateSymplectic / PeriodicDuplicateVerlet / Normals */
+        ensure_cap(s, s->np + count);
+        for (unsigned i = 0; i < count; i++) {
+          const unsigned pnew = s->np + i, rp = list[i], pcopy = rp & 0x7fffffffu;
+          const int inverse = rp >= 0x80000000u;
+          double ps[3];
+          for (int k = 0; k < 3; k++) ps[k] = s->pos[3 * (size_t)pcopy + k];
+          ps[0] += (inverse ? -inc[0] : inc[0]);
+          ps[1] += (inverse ? -inc[1] : inc[1]);
+          ps[2] += (inverse ? -inc[2] : inc[2]);
+          unsigned cx = (unsigned)((ps[0] - c->domposmin[0]) / c->scell);
+          unsigned cy = (unsigned)((ps[1] - c->domposmin[1]) / c->scell);
+          unsigned cz = (unsigned)((ps[2] - c->domposmin[2]) / c->scell);
+          cx = (cx <= c->domcells[0] ? cx : c->domcells[0]);
+          cy = (cy <= c->domcells[1] ? cy : c->domcells[1]);
+          cz = (cz <= c->domcells[2] ? cz : c->domcells[2]);
+          for (int k = 0; k < 3; k++) s->pos[3 * (size_t)pnew + k] = ps[k];
+          s->dcell[pnew] = dcel_cell(c->domcellcode, cx, cy, cz);
+          s->idp[pnew] = s->idp[pcopy];
+          s->code[pnew] = (uint16_t)((s->code[pcopy] & ~ORC_CODE_MASKSPECIAL) | ORC_CODE_PERIODIC);
+          memcpy(s->velrho + 4 * (size_t)pnew, s->velrho + 4 * (size_t)pcopy, sizeof(float) * 4);
+          if (c->tstep == ORC_STEP_VERLET) memcpy(s->velrhom1 + 4 * (size_t)pnew, s->velrhom1 + 4 * (size_t)pcopy, sizeof(float) * 4);
+          else if (s->pre_active) {
+            memcpy(s->pospre + 3 * (size_t)pnew, s->pospre + 3 * (size_t)pcopy, sizeof(double) * 3);
+            memcpy(s->velrhopre + 4 * (size_t)pnew, s->velrhopre + 4 * (size_t)pcopy, sizeof(float) * 4);
+          }
+          if (c->tvisco == ORC_VISCO_LAMINARSPS) memcpy(s->tau + 6 * (size_t)pnew, s->tau + 6 * (size_t)pcopy, sizeof(float) * 6);
+          if (c->tboundary == ORC_BC_MDBC) memcpy(s->boundnor + 3 * (size_t)pnew, s->boundnor + 3 * (size_t)pcopy, sizeof(float) * 3);
+        }
+        s->np += count;
+        if (!ctype) s->npbper += count; else s->npfper += count;
+      }
+    }
+  }
+  free(list);
+}
+
 #define SORT_ARRAY(T, ARR, W)                                                            \
   do {                                                                                   \
     T* tmp_ = (T*)s->scratch;                                                            \
@@ -753,8 +869,10 @@ void orc_sim_destroy(orc_sim* s) {
 
 /* JSphCpuSingle::RunCellDivide (JSphCpuSingle.cpp:510-590), no periodicity. */
 int orc_sim_run_cell_divide(orc_sim* s) {
-  const unsigned npf = s->np - s->npb;
-  int r = orc_divide(&s->c, &s->d, s->npb, npf, s->boundchanged, s->dcell, s->code, s->cellpart, s->sortpart,
+  s->npbper = s->npfper = 0;
+  if (s->c.peri[0] || s->c.peri[1] || s->c.peri[2]) run_periodic(s);
+  const unsigned npf = s->np - s->npb - s->npbper - s->npfper;
+  int r = orc_divide(&s->c, &s->d, s->npb, npf, s->npbper, s->npfper, s->boundchanged, s->dcell, s->code, s->cellpart, s->sortpart,
                      s->begincell, s->begincell_cap);
   if (r) return r;
   const unsigned n = s->d.nptot;
@@ -815,12 +933,39 @@ static void update_pos(const orc_ctes* c, const double* rpos0, double movx, doub
   const int outmov = (fabsf((float)movx) > c->movlimit || fabsf((float)movy) > c->movlimit ||
                       fabsf((float)movz) > c->movlimit);
   double rx = rpos0[0] + movx, ry = rpos0[1] + movy, rz = rpos0[2] + movz;
-  const double dx = rx - c->maprealposmin[0];
-  const double dy = ry - c->maprealposmin[1];
-  const double dz = rz - c->maprealposmin[2];
-  const int out = (dx != dx || dy != dy || dz != dz || dx < 0 || dy < 0 || dz < 0 || dx >= c->maprealsize[0] ||
-                   dy >= c->maprealsize[1] || dz >= c->maprealsize[2]);
+  double dx = rx - c->maprealposmin[0];
+  double dy = ry - c->maprealposmin[1];
+  double dz = rz - c->maprealposmin[2];
+  int out = (dx != dx || dy != dy || dz != dz || dx < 0 || dy < 0 || dz < 0 || dx >= c->maprealsize[0] ||
+             dy >= c->maprealsize[1] || dz >= c->maprealsize[2]);
+  const int periactive = c->peri[0] || c->peri[1] || c->peri[2];
+  if (periactive && out) {
+    /* back into the domain across a periodic face (JSphCpu.cpp:1477-1494) */
+    const double* inc = c->periinc;
+    if (c->peri[0]) {
+      if (dx < 0) { dx -= inc[0]; dy -= inc[1]; dz -= inc[2]; }
+      if (dx >= c->maprealsize[0]) { dx += inc[0]; dy += inc[1]; dz += inc[2]; }
+    }
+    if (c->peri[1]) {
+      if (dy < 0) { dx -= inc[3]; dy -= inc[4]; dz -= inc[5]; }
+      if (dy >= c->maprealsize[1]) { dx += inc[3]; dy += inc[4]; dz += inc[5]; }
+    }
+    if (c->peri[2]) {
+      if (dz < 0) { dx -= inc[6]; dy -= inc[7]; dz -= inc[8]; }
+      if (dz >= c->maprealsize[2]) { dx += inc[6]; dy += inc[7]; dz += inc[8]; }
+    }
+    const int outx = !c->peri[0] && (dx < 0 || dx >= c->maprealsize[0]);
+    const int outy = !c->peri[1] && (dy < 0 || dy >= c->maprealsize[1]);
+    const int outz = !c->peri[2] && (dz < 0 || dz >= c->maprealsize[2]);
+    out = outx || outy || outz;
+    rx = dx + c->maprealposmin[0]; ry = dy + c->maprealposmin[1]; rz = dz + c->maprealposmin[2];
+  }
   pos[3 * (size_t)p] = rx; pos[3 * (size_t)p + 1] = ry; pos[3 * (size_t)p + 2] = rz;
+  if (periactive && !(outrho || outmov || out)) {
+    dx = rx - c->domposmin[0];
+    dy = ry - c->domposmin[1];
+    dz = rz - c->domposmin[2];
+  }
   if (outrho || outmov || out) {
     uint16_t rcode = code[p];
     const uint16_t base = (uint16_t)(rcode & ~ORC_CODE_MASKSPECIAL);
@@ -838,6 +983,7 @@ static void update_pos(const orc_ctes* c, const double* rpos0, double movx, doub
 /* JSphCpu::ComputeSymplecticPre (JSphCpu.cpp:1687-1844). */
 int orc_sim_symplectic_pre(orc_sim* s, double dt) {
   const orc_ctes* c = &s->c;
+  const int periactive = c->peri[0] || c->peri[1] || c->peri[2];
   const double dt05 = dt * .5;
   const int np = (int)s->np, npb = (int)s->npb;
   memcpy(s->pospre, s->pos, sizeof(double) * 3 * (size_t)np);
@@ -879,6 +1025,8 @@ int orc_sim_symplectic_pre(orc_sim* s, double dt) {
   for (int p = npb; p < np; p++) {
     const uint16_t rcode = s->code[p];
     const int outrho = (codespecial(rcode) == ORC_CODE_OUTRHO);
+    /* periodic copies are not moved (JSphCpu.cpp:1816-1817, 2000-2001) */
+    if (periactive && !outrho && codespecial(rcode) != ORC_CODE_NORMAL) continue;
     if (codetype(rcode) == ORC_CODE_TYPE_FLUID)
       update_pos(c, s->pospre + 3 * (size_t)p, mov[3 * (size_t)p], mov[3 * (size_t)p + 1], mov[3 * (size_t)p + 2],
                  outrho, (unsigned)p, s->pos, s->dcell, s->code);
@@ -930,6 +1078,7 @@ void orc_sim_set_shiftpos(orc_sim* s, const float* in) {
 /* JSphCpu::ComputeSymplecticCorr (JSphCpu.cpp:1850-2029). */
 int orc_sim_symplectic_cor(orc_sim* s, double dt) {
   const orc_ctes* c = &s->c;
+  const int periactive = c->peri[0] || c->peri[1] || c->peri[2];
   const double dt05 = dt * .5;
   const int np = (int)s->np, npb = (int)s->npb;
   for (int p = 0; p < npb; p++) {
@@ -972,6 +1121,8 @@ int orc_sim_symplectic_cor(orc_sim* s, double dt) {
   for (int p = npb; p < np; p++) {
     const uint16_t rcode = s->code[p];
     const int outrho = (codespecial(rcode) == ORC_CODE_OUTRHO);
+    /* periodic copies are not moved (JSphCpu.cpp:1816-1817, 2000-2001) */
+    if (periactive && !outrho && codespecial(rcode) != ORC_CODE_NORMAL) continue;
     if (codetype(rcode) == ORC_CODE_TYPE_FLUID)
       update_pos(c, s->pospre + 3 * (size_t)p, mov[3 * (size_t)p], mov[3 * (size_t)p + 1], mov[3 * (size_t)p + 2],
                  outrho, (unsigned)p, s->pos, s->dcell, s->code);

@@ -72,6 +72,9 @@ typedef struct {
   unsigned mapcells[3], domcells[3], domcellcode;
   int tshift;
   float shiftcoef, shifttfs;
+  int peri[3];
+  double periinc[9];
+  double mapposmax[3];
 } orc_ctes;
 
 /* Raw case parameters (what the run XML carries) from which orc_config derives
@@ -86,6 +89,8 @@ typedef struct {
   double maprealposmin[3], maprealposmax[3];
   int tshift;
   float shiftcoef, shifttfs;
+  int peri[3];
+  double periinc[9];
 } orc_params;
 
 /* Cell-division state: JCellDivCpu/JCellDivCpuSingle members. */
@@ -99,6 +104,7 @@ typedef struct {
   unsigned boundlimitcellmin[3], boundlimitcellmax[3];
   unsigned bounddividecellmin[3], bounddividecellmax[3];
   unsigned npbignore, npbout, npfout, npboutignore, npfoutignore, npfinal, npbfinal;
+  unsigned npb2, npf2; /* periodic copies of boundary and fluid particles after npb1+npf1 */
 } orc_div;
 
 /* Host-side simulation state held by the oracle (JSphCpuSingle arrays). */
@@ -112,7 +118,8 @@ void orc_load_dcell(const orc_ctes* c, unsigned n, const uint16_t* code, const d
 float orc_compute_press(const orc_ctes* c, float rho);
 
 /* ---- neighbour list (cell division) ---- */
-int orc_divide(const orc_ctes* c, orc_div* d, unsigned npb, unsigned npf, int boundchanged,
+int orc_divide(const orc_ctes* c, orc_div* d, unsigned npb, unsigned npf, unsigned npbper, unsigned npfper,
+               int boundchanged,
                const unsigned* dcell, const uint16_t* code,
                unsigned* cellpart, unsigned* sortpart, unsigned* begincell, unsigned begincell_cap);
 

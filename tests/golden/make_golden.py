@@ -47,6 +47,9 @@ CASES = {
                                      extra_params={"Shifting": 3, "ShiftCoef": -2, "ShiftTFS": 2.75}), 12),
     "shiftnb_d04": (lambda: cg.spec_c1(dp=0.04, name="shiftnb_d04", step_algorithm=1, verlet_steps=5,
                                        init_vel=0.05, seed=31, extra_params={"Shifting": 1}), 12),
+    # periodic in x: a channel whose fluid moves at 2 m/s across the periodic faces
+    "peri_d04": (lambda: cg.spec_c1(dp=0.04, name="peri_d04", tank=(0.8, 0.4, 0.3), column=(0.8, 0.4, 0.2),
+                                    periodic_x=True, init_vel_x=2.0, init_vel=0.02, seed=37), 30),
 }
 
 # A sloshing tank: the walls move through a chain of movements -- sinusoidal
