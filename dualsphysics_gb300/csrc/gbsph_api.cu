@@ -94,6 +94,7 @@ int check_device_errors(gbsph_ctx* ctx) {
   CK(cudaStreamSynchronize(ctx->stream), "sync");
   if (derr & GB_ERR_BOUNDOUT) return set_err(ctx, GBSPH_EBOUND_OUT, "boundary particles left the domain");
   if (derr & GB_ERR_CELLCAP) return set_err(ctx, GBSPH_ECAPACITY, "cell domain exceeds the allocated cells");
+  if (derr & GB_ERR_PERICAP) return set_err(ctx, GBSPH_ECAPACITY, "the periodic copies exceed the particle capacity");
   if (serr & GB_ERR_NANDT) return set_err(ctx, GBSPH_ENAN_DT, "the computed dt is NaN or infinity");
   return GBSPH_OK;
 }

@@ -27,6 +27,8 @@
 #define GB_ERR_CELLCAP 2u
 #define GB_ERR_NANDT 4u
 #define GB_ERR_PARTOUT 8u   // a particle of the initial state lies outside the domain
+#define GB_ERR_PERICAP 16u  // the periodic copies do not fit the capacity
+#define GB_CODE_PERIODIC 0x2000u
 
 // Device-resident cell-division state (JCellDivGpuSingle members).
 struct DivState {
@@ -46,6 +48,11 @@ struct DivState {
   unsigned boundchanged;
   unsigned error;
   unsigned nctt_cap;
+  // periodic conditions (RunPeriodic): copies of boundary (npb2) and fluid
+  // (npf2) particles appended after the npb1+npf1 particles, the counts the
+  // copying started from, and the group being copied (source range, first
+  // new index, number of copies)
+  unsigned npb2, npf2, peri_npb0, peri_npf0, peri_pini, peri_num, peri_base, peri_count;
 };
 
 // Device-resident step scalars (JSph members Symplectic*, Dt*, AceMax ...).
@@ -207,6 +214,11 @@ struct MotionStep {
 // Launchers implemented in the .cu files (host side).
 namespace gbk {
 void load_dcell(const gbsph_consts& c, const DevArrays& a, unsigned n, cudaStream_t s);  // sets GB_ERR_PARTOUT in DivState::error
+// RunPeriodic (JSphCpuSingle.cpp:416-504): marks the last copies to be ignored
+// and appends new periodic copies; divide() runs it first when an axis is
+// periodic.  blockcounts holds gb_div_up(cap, 256) + 1 entries.
+void run_periodic(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned* blockcounts, cudaStream_t s,
+                  unsigned long long* nlaunch);
 void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses, cudaStream_t s, unsigned long long* nlaunch);
 // Stable sort of n <= sort_noalloc_max_keys() keys of nbits bits on the static
 // work area (work = its device address, from sort_noalloc_address on the

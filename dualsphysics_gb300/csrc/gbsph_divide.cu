@@ -46,11 +46,14 @@ __global__ void k_load_dcell(gbsph_consts c, DevArrays a, unsigned n) {
 }
 
 // Start of a divide: reset the limit reductions (JCellDivCpuSingle.cpp:284-305).
-__global__ void k_div_begin(DivState* d) {
+// With periodic conditions the boundary always counts as changed
+// (RunPeriodic sets BoundChanged, JSphCpuSingle.cpp:433): its copies are made
+// anew before every divide.
+__global__ void k_div_begin(DivState* d, int periactive) {
   d->nptot = d->np;
   d->npb1 = d->npb;
   d->npbout = d->npfout = d->npboutignore = d->npfoutignore = 0;
-  if (d->boundchanged) {
+  if (d->boundchanged || periactive) {
     d->boundlimitok = d->bounddivideok = 0;
     for (int k = 0; k < 3; k++) d->blmin[k] = d->blmax[k] = d->bdmin[k] = d->bdmax[k] = 0;
   }
@@ -62,9 +65,12 @@ __global__ void k_div_begin(DivState* d) {
 
 // LimitsCellBound/LimitsCellFluid (JCellDivCpu.cpp:256-345) as a block
 // reduction followed by one atomic per block and axis.
+// The arrays hold up to four segments: npb1 boundary, npf1 fluid, then the
+// npb2 boundary and npf2 fluid periodic copies.
 __global__ void k_limits(unsigned dcc, DevArrays a) {
   DivState* d = a.div;
   const unsigned np = d->nptot, npb = d->npb1;
+  const unsigned e1 = np - d->npb2 - d->npf2, e2 = e1 + d->npb2;  // [e1, e2): boundary copies
   const bool dobound = !d->boundlimitok;
   unsigned fmn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, fmx[3] = {0, 0, 0};
   unsigned bmn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, bmx[3] = {0, 0, 0};
@@ -73,7 +79,7 @@ __global__ void k_limits(unsigned dcc, DevArrays a) {
     if ((a.code[p] & GB_CODE_MASKSPECIAL) < GB_CODE_OUTIGNORE) {
       const unsigned cel = a.dcell[p];
       const unsigned v[3] = {gb_cx(dcc, cel), gb_cy(dcc, cel), gb_cz(dcc, cel)};
-      if (p >= npb) {
+      if (p >= npb && (p < e1 || p >= e2)) {
         for (int k = 0; k < 3; k++) { fmn[k] = min(fmn[k], v[k]); fmx[k] = max(fmx[k], v[k]); }
       } else {
         for (int k = 0; k < 3; k++) { bmn[k] = min(bmn[k], v[k]); bmx[k] = max(bmx[k], v[k]); }
@@ -350,7 +356,7 @@ __global__ void k_div_counts(DevArrays a) {
   d->npboutignore = bc[d->boxboundoutignore + 1] - bc[d->boxboundoutignore];
   d->npfoutignore = bc[d->boxfluidoutignore + 1] - bc[d->boxfluidoutignore];
   d->npfinal = d->nptot - d->npbout - d->npfout - d->npboutignore - d->npfoutignore;
-  d->npbfinal = d->npb1 - d->npboutignore;
+  d->npbfinal = d->npb1 + d->npb2 - d->npboutignore;
   if (d->npbout) d->error |= GB_ERR_BOUNDOUT;
   d->np = d->npfinal;
   d->npb = d->npbfinal;
@@ -401,6 +407,154 @@ __global__ void k_reorder(gbsph_consts c, DevArrays a) {
   a.pscell[p] = ps;
 }
 
+
+// ---- periodic conditions (JSphCpuSingle::RunPeriodic, JSphCpuSingle.cpp:416-504) ----
+// Every particle within reach of a periodic face gets a copy moved by the
+// axis increment, appended after the np particles in the order the reference's
+// PeriodicMakeList gives (JSphCpuSingle.cpp:210-252): by source index, the
+// copy by +inc before the one by -inc.  For each (type, axis, block) group a
+// count kernel sums the copies of 256-particle tiles, one block scans the tile
+// sums and reserves the room, and the duplicate kernel re-derives its tile's
+// copies and writes them at the scanned offsets.  All counts stay on the
+// device.
+
+// PeriodicIgnore (JSphCpuSingle.cpp:186-203): the copies of the last divide
+// are ignored from now on; the counts the copying starts from.
+__global__ void k_peri_begin(DevArrays a) {
+  DivState* d = a.div;
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p == 0) {
+    d->peri_npb0 = d->npb;
+    d->peri_npf0 = d->np - d->npb;
+    d->npb2 = d->npf2 = 0;
+  }
+  if (p < d->np) {
+    const unsigned code = a.code[p];
+    if ((code & GB_CODE_MASKSPECIAL) == GB_CODE_PERIODIC)
+      a.code[p] = (uint16_t)((code & ~GB_CODE_MASKSPECIAL) | GB_CODE_OUTIGNORE);
+  }
+}
+
+// Range of a group: the copies made so far of this type (cblock 0), or the
+// particles of this type present before the copying (cblock 1).
+__device__ __forceinline__ void peri_range(const DivState* d, int ctype, int cblock, unsigned& pini, unsigned& num) {
+  if (cblock) {
+    pini = ctype ? d->peri_npb0 : 0;
+    num = ctype ? d->peri_npf0 : d->peri_npb0;
+  } else {
+    num = ctype ? d->npf2 : d->npb2;
+    pini = d->np - num;
+  }
+}
+
+// Copies of particle p: bit 0 for +inc, bit 1 for -inc, each kept when it
+// falls inside [Map_PosMin, Map_PosMax); particles already excluded get none.
+__device__ __forceinline__ unsigned peri_flags(const gbsph_consts& c, const DevArrays& a, unsigned p, int axis) {
+  if ((a.code[p] & GB_CODE_MASKSPECIAL) > GB_CODE_PERIODIC) return 0u;
+  const double* inc = c.periinc + 3 * axis;
+  const double x = a.px[p], y = a.py[p], z = a.pz[p];
+  unsigned f = 0;
+  {
+    const double qx = __dadd_rn(x, inc[0]), qy = __dadd_rn(y, inc[1]), qz = __dadd_rn(z, inc[2]);
+    if (c.mapposmin[0] <= qx && c.mapposmin[1] <= qy && c.mapposmin[2] <= qz && qx < c.mapposmax[0] &&
+        qy < c.mapposmax[1] && qz < c.mapposmax[2])
+      f |= 1u;
+  }
+  {
+    const double qx = __dsub_rn(x, inc[0]), qy = __dsub_rn(y, inc[1]), qz = __dsub_rn(z, inc[2]);
+    if (c.mapposmin[0] <= qx && c.mapposmin[1] <= qy && c.mapposmin[2] <= qz && qx < c.mapposmax[0] &&
+        qy < c.mapposmax[1] && qz < c.mapposmax[2])
+      f |= 2u;
+  }
+  return f;
+}
+
+// Copies per 256-particle tile of the group's range.
+__global__ void k_peri_count(gbsph_consts c, DevArrays a, int ctype, int cblock, int axis, unsigned* __restrict__ tiles) {
+  unsigned pini, num;
+  peri_range(a.div, ctype, cblock, pini, num);
+  const unsigned i = blockIdx.x * kDivBlock + threadIdx.x;
+  const unsigned n = i < num ? __popc(peri_flags(c, a, pini + i, axis)) : 0u;
+  unsigned tot;
+  block_exclusive_scan(n, &tot);
+  if (threadIdx.x == 0) tiles[blockIdx.x] = tot;
+}
+
+// Exclusive scan of the tile counts (one block); reserves the room for the
+// group's copies after np, or flags GB_ERR_PERICAP and makes none.
+__global__ void k_peri_scan(DevArrays a, int ctype, int cblock, unsigned* __restrict__ tiles, unsigned ntiles,
+                            unsigned cap) {
+  const unsigned chunk = gb_div_up(ntiles, blockDim.x);
+  const unsigned b = threadIdx.x * chunk, e = min(ntiles, b + chunk);
+  unsigned sum = 0;
+  for (unsigned i = b; i < e; i++) sum += tiles[i];
+  unsigned total;
+  unsigned run = block_exclusive_scan(sum, &total);
+  for (unsigned i = b; i < e; i++) {
+    const unsigned v = tiles[i];
+    tiles[i] = run;
+    run += v;
+  }
+  if (threadIdx.x == 0) {
+    DivState* d = a.div;
+    unsigned pini, num;
+    peri_range(d, ctype, cblock, pini, num);
+    d->peri_pini = pini;
+    d->peri_num = num;
+    d->peri_base = d->np;
+    if ((unsigned long long)d->np + total > cap) {
+      d->error |= GB_ERR_PERICAP;
+      d->peri_count = 0;
+    } else {
+      d->peri_count = total;
+      d->np += total;
+      if (ctype) d->npf2 += total;
+      else d->npb2 += total;
+    }
+  }
+}
+
+// PeriodicDuplicatePos / PeriodicDuplicateSymplectic / PeriodicDuplicateVerlet /
+// PeriodicDuplicateNormals (JSphCpuSingle.cpp:258-380): the copy takes every
+// array of its source (the PRE arrays and VelrhoM1 included, which the
+// reference copies only while they are live), its position moved by the
+// increment, the cell of that position clamped to the domain, and the code
+// marked periodic.
+template <bool withsps, bool withnor>
+__global__ void k_peri_dup(gbsph_consts c, DevArrays a, int axis, const unsigned* __restrict__ tiles) {
+  const DivState* d = a.div;
+  const unsigned num = d->peri_num;
+  const unsigned i = blockIdx.x * kDivBlock + threadIdx.x;
+  const unsigned pcopy = d->peri_pini + i;
+  const unsigned f = (i < num && d->peri_count) ? peri_flags(c, a, pcopy, axis) : 0u;
+  const unsigned off = block_exclusive_scan(__popc(f), nullptr);
+  if (!f) return;
+  unsigned pnew = d->peri_base + tiles[blockIdx.x] + off;
+  const double* inc = c.periinc + 3 * axis;
+  const double x = a.px[pcopy], y = a.py[pcopy], z = a.pz[pcopy];
+  const unsigned code = (a.code[pcopy] & ~GB_CODE_MASKSPECIAL) | GB_CODE_PERIODIC;
+  const double sc = (double)c.scell;
+  for (int sgn = 0; sgn < 2; sgn++) {
+    if (!(f & (1u << sgn))) continue;
+    const double qx = sgn ? __dadd_rn(x, -inc[0]) : __dadd_rn(x, inc[0]);
+    const double qy = sgn ? __dadd_rn(y, -inc[1]) : __dadd_rn(y, inc[1]);
+    const double qz = sgn ? __dadd_rn(z, -inc[2]) : __dadd_rn(z, inc[2]);
+    const unsigned cx = min((unsigned)__ddiv_rn(__dsub_rn(qx, c.domposmin[0]), sc), c.domcells[0]);
+    const unsigned cy = min((unsigned)__ddiv_rn(__dsub_rn(qy, c.domposmin[1]), sc), c.domcells[1]);
+    const unsigned cz = min((unsigned)__ddiv_rn(__dsub_rn(qz, c.domposmin[2]), sc), c.domcells[2]);
+    a.px[pnew] = qx; a.py[pnew] = qy; a.pz[pnew] = qz;
+    a.dcell[pnew] = gb_cell(c.domcellcode, cx, cy, cz);
+    a.idp[pnew] = a.idp[pcopy];
+    a.code[pnew] = (uint16_t)code;
+    a.velrho[pnew] = a.velrho[pcopy];
+    a.qx[pnew] = a.qx[pcopy]; a.qy[pnew] = a.qy[pcopy]; a.qz[pnew] = a.qz[pcopy];
+    a.velrhopre[pnew] = a.velrhopre[pcopy];
+    if (withsps) { a.taua[pnew] = a.taua[pcopy]; a.taub[pnew] = a.taub[pcopy]; }
+    if (withnor) a.boundnor[pnew] = a.boundnor[pcopy];
+    pnew++;
+  }
+}
+
 template <typename T>
 inline void swp(T*& x, T*& y) {
   T* t = x;
@@ -417,14 +571,46 @@ void load_dcell(const gbsph_consts& c, const DevArrays& a, unsigned n, cudaStrea
   k_load_dcell<<<gb_div_up(n, kDivBlock), kDivBlock, 0, s>>>(c, a, n);
 }
 
-// JSphGpuSingle::RunCellDivide without periodic conditions.  `cap` is the
+void run_periodic(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned* tiles, cudaStream_t s,
+                  unsigned long long* nlaunch) {
+  const unsigned ntiles = gb_div_up(cap, kDivBlock);
+  const bool withsps = (c.tvisco == GBSPH_VISCO_LAMINARSPS);
+  const bool withnor = (c.tboundary == GBSPH_BC_MDBC);
+  unsigned long long n = 1;
+  k_peri_begin<<<ntiles, kDivBlock, 0, s>>>(a);
+  for (int ctype = 0; ctype < 2; ctype++) {
+    bool first = true;
+    for (int axis = 0; axis < 3; axis++) {
+      if (!c.peri[axis]) continue;
+      // before the first axis there are no copies of this type to copy again
+      for (int cblock = first ? 1 : 0; cblock < 2; cblock++) {
+        k_peri_count<<<ntiles, kDivBlock, 0, s>>>(c, a, ctype, cblock, axis, tiles);
+        k_peri_scan<<<1, 1024, 0, s>>>(a, ctype, cblock, tiles, ntiles, cap);
+        if (withsps) {
+          if (withnor) k_peri_dup<true, true><<<ntiles, kDivBlock, 0, s>>>(c, a, axis, tiles);
+          else k_peri_dup<true, false><<<ntiles, kDivBlock, 0, s>>>(c, a, axis, tiles);
+        } else {
+          if (withnor) k_peri_dup<false, true><<<ntiles, kDivBlock, 0, s>>>(c, a, axis, tiles);
+          else k_peri_dup<false, false><<<ntiles, kDivBlock, 0, s>>>(c, a, axis, tiles);
+        }
+        n += 3;
+      }
+      first = false;
+    }
+  }
+  if (nlaunch) *nlaunch += n;
+}
+
+// JSphGpuSingle::RunCellDivide: RunPeriodic first when an axis is periodic.  `cap` is the
 // particle capacity (grids are sized by it; kernels read the live counts from
 // DivState).  The reorder swaps the cur/alt array pairs in `a`.
 void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses, cudaStream_t s,
             unsigned long long* nlaunch) {
   const unsigned dcc = c.domcellcode;
   const unsigned grid_p = gb_div_up(cap, kDivBlock);
-  k_div_begin<<<1, 1, 0, s>>>(a.div);
+  const bool periactive = c.peri[0] || c.peri[1] || c.peri[2];
+  if (periactive) run_periodic(c, a, cap, a.hist, s, nlaunch);
+  k_div_begin<<<1, 1, 0, s>>>(a.div, periactive ? 1 : 0);
   k_limits<<<min(grid_p, 152u * 8u), kDivBlock, 0, s>>>(dcc, a);
   k_div_setup<<<1, 1, 0, s>>>(c, a.div);
   k_presort<<<grid_p, kDivBlock, 0, s>>>(dcc, a);

@@ -39,16 +39,20 @@ class PartWriter {
     std::vector<double> pos;
     std::vector<float> velrho;
     std::vector<unsigned> idp;
+    std::vector<uint16_t> code;
     unsigned part = 0, step = 0, np = 0;
     double t = 0, dtn = 0;
   };
 
-  PartWriter(const std::string& dirout, const gbio::Case& cs) : dirout_(dirout), cs_(cs), th_([this] { loop(); }) {
+  // cap: the particles the device may hold (periodic copies included)
+  PartWriter(const std::string& dirout, const gbio::Case& cs, unsigned cap)
+      : dirout_(dirout), cs_(cs), th_([this] { loop(); }) {
     std::lock_guard<std::mutex> lk(mu_);
     for (auto& b : bufs_) {
-      b.pos.resize(3 * (size_t)cs.np);
-      b.velrho.resize(4 * (size_t)cs.np);
-      b.idp.resize(cs.np);
+      b.pos.resize(3 * (size_t)cap);
+      b.velrho.resize(4 * (size_t)cap);
+      b.idp.resize(cap);
+      b.code.resize(cap);
       free_.push_back(&b);
     }
   }
@@ -102,6 +106,19 @@ class PartWriter {
         todo_.erase(todo_.begin());
       }
       const auto t0 = std::chrono::steady_clock::now();
+      // only normal particles are saved, not periodic copies (GetParticlesData
+      // with onlynormal, JSphCpu.cpp:366-424)
+      unsigned n = 0;
+      for (unsigned p = 0; p < j->np; p++) {
+        if (j->code[p] & 0xe000u) continue;
+        if (n != p) {
+          for (int k = 0; k < 3; k++) j->pos[3 * (size_t)n + k] = j->pos[3 * (size_t)p + k];
+          for (int k = 0; k < 4; k++) j->velrho[4 * (size_t)n + k] = j->velrho[4 * (size_t)p + k];
+          j->idp[n] = j->idp[p];
+        }
+        n++;
+      }
+      j->np = n;
       std::string e;
       const bool ok = gbio::save_part(dirout_, cs_, j->part, j->t, j->step, j->dtn, j->np, j->pos.data(),
                                       j->velrho.data(), j->idp.data(), e);
@@ -186,7 +203,9 @@ int main(int argc, char** argv) {
     return 0;
   }
   gbsph_ctx* ctx = nullptr;
-  int rc = gbsph_create(&c, cs.np, device, &ctx);
+  // room for the periodic copies: each periodic axis can copy every particle once
+  const unsigned cap = cs.np * (1u + (c.peri[0] ? 1u : 0u) + (c.peri[1] ? 1u : 0u) + (c.peri[2] ? 1u : 0u));
+  int rc = gbsph_create(&c, cap, device, &ctx);
   if (rc != GBSPH_OK) return fail("gbsph_create", "code " + std::to_string(rc));
   rc = gbsph_upload(ctx, cs.np, cs.npb, cs.pos.data(), cs.velrho.data(), cs.idp.data(), cs.code.data(),
                     cs.boundnor.empty() ? nullptr : cs.boundnor.data());
@@ -205,14 +224,14 @@ int main(int argc, char** argv) {
   std::printf("Case %s: %u particles (%u boundary, %u fluid), h=%g, dp=%g\n", casename.c_str(), cs.np, cs.npb,
               cs.np - cs.npb, cs.params.h, cs.params.dp);
   gbsph_divinfo di;
-  PartWriter writer(dirout, cs);
+  PartWriter writer(dirout, cs, cap);
   auto save_part = [&](unsigned part, double t, unsigned step, double dtn) -> bool {
     if (!save) return true;
     const std::string werr = writer.error();
     if (!werr.empty()) { err = werr; return false; }
     if (gbsph_get_divinfo(ctx, &di, nullptr, 0, nullptr, nullptr) != GBSPH_OK) return false;
     PartWriter::Job* j = writer.acquire();
-    if (gbsph_download(ctx, j->pos.data(), j->velrho.data(), j->idp.data(), nullptr, nullptr) != GBSPH_OK) {
+    if (gbsph_download(ctx, j->pos.data(), j->velrho.data(), j->idp.data(), j->code.data(), nullptr) != GBSPH_OK) {
       writer.release(j);
       return false;
     }

@@ -22,18 +22,36 @@ constexpr int kUpdBlock = 256;
 __device__ __forceinline__ double dadd(double x, double y) { return __dadd_rn(x, y); }
 __device__ __forceinline__ double dmul(double x, double y) { return __dmul_rn(x, y); }
 
-// UpdatePos (JSphCpu.cpp:1464-1516) without periodic conditions.
+// UpdatePos (JSphCpu.cpp:1464-1516).  With periodic conditions a particle
+// that left the real domain across a periodic face comes back by the axis
+// increment, and cells are taken from DomPosMin.
 __device__ __forceinline__ void update_pos(const gbsph_consts& c, const DevArrays& a, unsigned p, double rx, double ry,
                                            double rz, double movx, double movy, double movz, bool outrho,
                                            double rsc) {
   const bool outmov = (fabsf(gb_d2f(movx)) > c.movlimit || fabsf(gb_d2f(movy)) > c.movlimit ||
                        fabsf(gb_d2f(movz)) > c.movlimit);
   rx = dadd(rx, movx); ry = dadd(ry, movy); rz = dadd(rz, movz);
-  const double dx = __dsub_rn(rx, c.maprealposmin[0]);
-  const double dy = __dsub_rn(ry, c.maprealposmin[1]);
-  const double dz = __dsub_rn(rz, c.maprealposmin[2]);
-  const bool out = gb_outside(dx, c.maprealsize[0]) || gb_outside(dy, c.maprealsize[1]) ||
-                   gb_outside(dz, c.maprealsize[2]);
+  double dx = __dsub_rn(rx, c.maprealposmin[0]);
+  double dy = __dsub_rn(ry, c.maprealposmin[1]);
+  double dz = __dsub_rn(rz, c.maprealposmin[2]);
+  bool out = gb_outside(dx, c.maprealsize[0]) || gb_outside(dy, c.maprealsize[1]) ||
+             gb_outside(dz, c.maprealsize[2]);
+  const bool periactive = c.peri[0] || c.peri[1] || c.peri[2];
+  if (periactive && out) {
+    for (int k = 0; k < 3; k++) {
+      if (!c.peri[k]) continue;
+      const double* inc = c.periinc + 3 * k;
+      const double dk = k == 0 ? dx : (k == 1 ? dy : dz);
+      if (dk < 0) { dx = __dsub_rn(dx, inc[0]); dy = __dsub_rn(dy, inc[1]); dz = __dsub_rn(dz, inc[2]); }
+      const double dk2 = k == 0 ? dx : (k == 1 ? dy : dz);
+      if (dk2 >= c.maprealsize[k]) { dx = dadd(dx, inc[0]); dy = dadd(dy, inc[1]); dz = dadd(dz, inc[2]); }
+    }
+    const bool outx = !c.peri[0] && (dx < 0 || dx >= c.maprealsize[0]);
+    const bool outy = !c.peri[1] && (dy < 0 || dy >= c.maprealsize[1]);
+    const bool outz = !c.peri[2] && (dz < 0 || dz >= c.maprealsize[2]);
+    out = outx || outy || outz;
+    rx = dadd(dx, c.maprealposmin[0]); ry = dadd(dy, c.maprealposmin[1]); rz = dadd(dz, c.maprealposmin[2]);
+  }
   a.px[p] = rx; a.py[p] = ry; a.pz[p] = rz;
   if (outrho || outmov || out) {
     const unsigned rcode = a.code[p];
@@ -41,6 +59,9 @@ __device__ __forceinline__ void update_pos(const gbsph_consts& c, const DevArray
     a.code[p] = (uint16_t)(base | (out ? GB_CODE_OUTPOS : (outrho ? GB_CODE_OUTRHO : GB_CODE_OUTMOV)));
     a.dcell[p] = 0xffffffffu;
   } else {
+    if (periactive) {
+      dx = __dsub_rn(rx, c.domposmin[0]); dy = __dsub_rn(ry, c.domposmin[1]); dz = __dsub_rn(rz, c.domposmin[2]);
+    }
     const double sc = (double)c.scell;
     const unsigned cx = gb_cellidx(dx, sc, rsc), cy = gb_cellidx(dy, sc, rsc), cz = gb_cellidx(dz, sc, rsc);
     a.dcell[p] = gb_cell(c.domcellcode, cx, cy, cz);
@@ -81,7 +102,8 @@ __global__ void k_sym_pre(gbsph_consts c, DevArrays a, const double* dtp, double
     code = (rcode & ~GB_CODE_MASKSPECIAL) | GB_CODE_OUTRHO;
     a.code[p] = (uint16_t)code;
   }
-  if ((code & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID)
+  // periodic copies are not moved (JSphCpu.cpp:1816): the next divide replaces them
+  if ((code & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID && (code & GB_CODE_MASKSPECIAL) != GB_CODE_PERIODIC)
     update_pos(c, a, p, x, y, z, dx, dy, dz, (code & GB_CODE_MASKSPECIAL) == GB_CODE_OUTRHO, rsc);
 }
 
@@ -119,6 +141,7 @@ __global__ void k_sym_cor(gbsph_consts c, DevArrays a, const double* dtp, double
     a.code[p] = (uint16_t)code;
   }
   a.velrho[p] = make_float4(vx, vy, vz, rhonew);
+  if ((code & GB_CODE_MASKSPECIAL) == GB_CODE_PERIODIC) return;  // JSphCpu.cpp:2000
   if ((code & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID)
     update_pos(c, a, p, a.qx[p], a.qy[p], a.qz[p], dx, dy, dz, (code & GB_CODE_MASKSPECIAL) == GB_CODE_OUTRHO, rsc);
   else {
@@ -257,7 +280,8 @@ __global__ void k_run_shifting(gbsph_consts c, DevArrays a, const double* __rest
 }
 
 // CalcRidp (JSphCpu.cpp:2099-2127) over the npb boundary particles: the
-// current index of each moving particle by id (ridp preset to UINT_MAX).
+// current index of each moving particle by id (ridp preset to UINT_MAX);
+// periodic copies share their source's id and are left out.
 // Thread 0 also marks the boundary changed when some object is active
 // (JSphCpu::RunMotion sets BoundChanged, JSphCpu.cpp:2196).
 __global__ void k_motion_ridp(DevArrays a, const MotionStep* __restrict__ hdr, unsigned idmin, unsigned nmoving,
@@ -266,7 +290,7 @@ __global__ void k_motion_ridp(DevArrays a, const MotionStep* __restrict__ hdr, u
   if (p == 0 && hdr->active) a.div->boundchanged = 1;
   if (p >= a.div->npb) return;
   const unsigned rel = a.idp[p] - idmin;
-  if (rel < nmoving) ridp[rel] = p;
+  if (rel < nmoving && (a.code[p] & GB_CODE_MASKSPECIAL) == GB_CODE_NORMAL) ridp[rel] = p;
 }
 
 // MatrixMulPoint: rows 1..3 of a 4x4 matrix times (x, y, z, 1).

@@ -29,6 +29,22 @@ from ._lib import (DivInfo, GbsphError, INTERSTEP_SYMCORRECTOR, INTERSTEP_SYMPRE
 from .case import CaseData, load_case
 
 
+CODE_MASKSPECIAL = 0xE000
+
+
+def default_capacity(cd: CaseData) -> int:
+    """Particles to allocate for a case: its particles, plus room for the
+    periodic copies (each periodic axis can copy every particle once)."""
+    nperi = sum(1 for k in cd.params.peri if k)
+    return int(cd.np * (1 + nperi))
+
+
+def normal_rows(code: np.ndarray) -> np.ndarray:
+    """Rows whose code is normal (CODE_IsNormal): particles of the case, not
+    their periodic copies."""
+    return (code & CODE_MASKSPECIAL) == 0
+
+
 class GbSphSingle:
     def __init__(self, device: int = 0):
         self.device = device
@@ -70,7 +86,7 @@ class GbSphSingle:
         self.case = cd
         self.consts = config(cd.params)
         self.close()
-        cap = int(capacity or cd.np)
+        cap = int(capacity or default_capacity(cd))
         self._check(lib().gbsph_create(C.byref(self.consts), cap, self.device, C.byref(self.ctx)), "gbsph_create")
         self._check(lib().gbsph_upload(self.ctx, cd.np, cd.npb, ptr(cd.pos), ptr(cd.velrho), ptr(cd.idp),
                                        ptr(cd.code), ptr(cd.boundnor)), "gbsph_upload")
@@ -244,6 +260,10 @@ class GbSphSingle:
         """Writes data/Part_%04u.bi4 (JSph::SaveData / JPartDataBi4, JSph.cpp:3062-3110)."""
         cd = self.case
         st = self.download()
+        # only the particles of the case are saved, not their periodic copies
+        # (GetParticlesData with onlynormal, JSphCpu.cpp:366-424)
+        keep = normal_rows(st["code"])
+        st = {k: v[keep] for k, v in st.items()}
         order = np.argsort(st["idp"], kind="stable")
         dtl, dtn, t = self.step_dt()
         nmov = sum(c for _, c in cd.motion["objects"]) if cd.motion else 0

@@ -36,7 +36,8 @@ def _write_case(tmp_path, name):
     return spec.name
 
 
-@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "sps_d04", "verlet_d04", "lam_d04", "half_d04", "mov_d04"])
+@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "sps_d04", "verlet_d04", "lam_d04", "half_d04", "mov_d04",
+                                  "peri_d04"])
 def test_driver_case_summary_matches_python_loader(tmp_path, name):
     import make_golden
     cn = _write_case(tmp_path, name)
@@ -87,7 +88,7 @@ def _parts(dirout):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "mov_d04"])
+@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "mov_d04", "peri_d04"])
 def test_driver_parts_equal_python_run(tmp_path, name):
     """gbsph_run and GbSphSingle.Run step the same case to the same end time
     and write bit-identical particle data in every Part file."""
@@ -101,6 +102,7 @@ def test_driver_parts_equal_python_run(tmp_path, name):
     s = GbSphSingle(0)
     res = s.Run(str(tmp_path), cn, p_out, time_max=tmax)
     s.close()
+    ncase = load_case(str(tmp_path), cn).np
     dp, pp = _parts(d_out), _parts(p_out)
     assert dp == pp and len(dp) >= 2, (dp, pp)
     for f in dp:
@@ -112,6 +114,9 @@ def test_driver_parts_equal_python_run(tmp_path, name):
         assert pa.get("Step") == pb.get("Step") and pa.get("TimeStep") == pb.get("TimeStep")
         for arr in ("Idp", "Vel", "Rhop"):
             np.testing.assert_array_equal(pa.array(arr), pb.array(arr), err_msg=f"{f}: {arr}")
+        # each particle of the case at most once: periodic copies are not saved
+        idp = pa.array("Idp")
+        assert len(np.unique(idp)) == len(idp) <= ncase
         posname = "Posd" if "Posd" in pa.arrays else "Pos"
         np.testing.assert_array_equal(pa.array(posname), pb.array(posname), err_msg=f"{f}: {posname}")
     assert res["steps"] > 0
