@@ -82,6 +82,47 @@ def test_driver_rejects_unknown_option_and_missing_case(tmp_path):
     assert r.returncode == 1 and "usage" in r.stderr
 
 
+def _info(tmp_path, name, *opts):
+    cn = _write_case(tmp_path, name)
+    out = subprocess.run([_driver(), str(tmp_path / cn), str(tmp_path / "out"), "-info", *opts],
+                         capture_output=True, text=True, timeout=120)
+    return out
+
+
+def test_driver_command_line_overrides_case_parameters(tmp_path):
+    """The reference's run options override the XML parameters as
+    JSph::LoadConfigCommands does (JSph.cpp:876-995); words are case-insensitive."""
+    base = json.loads(_info(tmp_path, "mdbc_d04").stdout)
+    assert (base["tstep"], base["tboundary"], base["tvisco"], base["tdensity"]) == (2, 2, 1, 2)
+    r = _info(tmp_path, "mdbc_d04", "-gpu", "-Verlet:7", "-dbc", "-viscolamsps:1e-6", "-viscoboundfactor:0.5",
+              "-ddt:1", "-cfl:0.1", "-rhopout:800:1200", "-stable", "-nortimes", "-svtimers:0", "-svpips:1:50")
+    assert r.returncode == 0, r.stderr
+    i = json.loads(r.stdout)
+    assert (i["tstep"], i["verletsteps"], i["tboundary"], i["tvisco"], i["tdensity"]) == (1, 7, 1, 2, 1)
+    assert np.float32(i["visco"]) == np.float32(1e-6) and i["viscoboundfactor"] == 0.5
+    assert i["ddtvalue"] == base["ddtvalue"] and i["cflnumber"] == 0.1
+    assert (i["rhopoutmin"], i["rhopoutmax"]) == (800.0, 1200.0)
+    # -ddt:0 drops the diffusion value; -ddtvalue sets it; -ddt on a case without one takes 0.1
+    i = json.loads(_info(tmp_path, "mdbc_d04", "-ddt:0").stdout)
+    assert (i["tdensity"], i["ddtvalue"]) == (0, 0.0)
+    i = json.loads(_info(tmp_path, "mdbc_d04", "-ddt:3", "-ddtvalue:0.2").stdout)
+    assert (i["tdensity"], np.float32(i["ddtvalue"])) == (3, np.float32(0.2))
+    i = json.loads(_info(tmp_path, "dbc_d04", "-CELLMODE:H", "-symplectic", "-wendland").stdout)
+    assert i["cellmode_div"] == 2 and i["tstep"] == 2
+
+
+@pytest.mark.parametrize("opt", ["-viscoart:11", "-ddt:4", "-ddtvalue:2", "-cfl:0", "-svpips:3", "-cubic", "-cpu",
+                                 "-mdbc_noslip", "-sv:vtk", "-cellmode:x"])
+def test_driver_rejects_invalid_options(tmp_path, opt):
+    r = _info(tmp_path, "dbc_d04", opt)
+    assert r.returncode == 1 and "*** Exception: options" in r.stderr
+
+
+def test_driver_mdbc_needs_normals(tmp_path):
+    r = _info(tmp_path, "dbc_d04", "-mdbc")
+    assert r.returncode == 1 and "normals" in r.stderr
+
+
 def _parts(dirout):
     d = os.path.join(dirout, "data")
     return sorted(f for f in os.listdir(d) if f.startswith("Part_") and f.endswith(".bi4"))
@@ -120,3 +161,27 @@ def test_driver_parts_equal_python_run(tmp_path, name):
         posname = "Posd" if "Posd" in pa.arrays else "Pos"
         np.testing.assert_array_equal(pa.array(posname), pb.array(posname), err_msg=f"{f}: {posname}")
     assert res["steps"] > 0
+
+
+@pytest.mark.gpu
+def test_driver_pips_summary_and_csv(tmp_path):
+    """-svpips:2:<n> samples the interaction count every n steps and at the
+    last, prints the reference's summary lines and writes PIPS.csv."""
+    cn = _write_case(tmp_path, "dbc_d04")
+    out = str(tmp_path / "out")
+    r = subprocess.run([_driver(), str(tmp_path / cn), out, "-nsteps:12", "-sv:none", "-svpips:2:5"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert "GPIPS" in r.stdout and "Total particle interactions (f+b)" in r.stdout
+    rows = open(os.path.join(out, "PIPS.csv")).read().strip().split("\n")
+    assert rows[0].startswith("Time [s];RunTime [s];Nstep;RealFluid")
+    steps = [int(x.split(";")[2]) for x in rows[1:]]
+    assert steps == [0, 5, 10, 12]
+    # the count of a sample equals a direct count of the same state at step 0
+    s = GbSphSingle(0)
+    s.setup(load_case(str(tmp_path), cn))
+    p = s.pips()
+    s.close()
+    first = rows[1].split(";")
+    assert (int(first[3]), int(first[4]), int(first[5]), int(first[6])) == \
+        (p["real_fluid"], p["real_bound"], p["checked_fluid"], p["checked_bound"])
