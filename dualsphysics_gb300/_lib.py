@@ -105,6 +105,14 @@ MOV_TYPES = {"wait": 1, "mvrect": 2, "mvrectace": 3, "mvrot": 4, "mvrotace": 5, 
              "mvnull": 8}
 
 
+TUNE_CANDIDATES = 4
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("best", C.c_int), ("variant", C.c_int * TUNE_CANDIDATES), ("bsize", C.c_int * TUNE_CANDIDATES),
+                ("ms", C.c_float * TUNE_CANDIDATES)]
+
+
 class Maxes(C.Structure):
     _fields_ = [("acemax", C.c_double), ("velmax", C.c_float), ("viscdtmax", C.c_float)]
 
@@ -136,6 +144,13 @@ SIGNATURES = {
     "gbsph_launch_count": (C.c_ulonglong, [P]),
     "gbsph_stream": (P, [P]),
     "gbsph_set_option": (C.c_int, [P, C.c_int, C.c_int]),
+    "gbsph_tune_forces": (C.c_int, [P, C.c_int, C.POINTER(TuneResult)]),
+    "gbsph_ensemble_create": (C.c_int, [C.c_uint, C.POINTER(P), C.POINTER(P)]),
+    "gbsph_ensemble_destroy": (None, [P]),
+    "gbsph_ensemble_last_error": (C.c_char_p, [P]),
+    "gbsph_ensemble_run": (C.c_int, [P, C.c_uint, C.c_int]),
+    "gbsph_ensemble_sync": (C.c_int, [P]),
+    "gbsph_ensemble_launches_per_step": (C.c_ulonglong, [P]),
     "gbsph_graph_prepare": (C.c_int, [P, C.c_uint]),
     "gbsph_profile": (C.c_int, [P, C.c_uint]),
     "gbsph_profile_read": (C.c_int, [P, P, C.c_uint, C.POINTER(C.c_uint)]),

@@ -469,10 +469,9 @@ int gbsph_verlet(gbsph_ctx* ctx, double dt) {
 // JSph::CalcMotion at the start of a Symplectic step (JSphGpuSingle.cpp:787):
 // the host advances the motion over [time, time+SymplecticDtPre] and copies
 // the step's motion table to the device.
-static int motion_prepare(gbsph_ctx* ctx) {
-  StepState st;
-  CK(cudaMemcpyAsync(&st, ctx->a.st, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream), "motion dt");
-  CK(cudaStreamSynchronize(ctx->stream), "motion sync");
+// Advances the motion over the step that starts at st.time with st.dtpre and
+// copies its table to the device on stream s.
+static int motion_table(gbsph_ctx* ctx, const StepState& st, cudaStream_t s) {
   const unsigned n = ctx->mot_nobj;
   std::vector<gbsph_motion_data> md(n);
   const int rc = gbsph_motion_process(ctx->motion, st.time, st.dtpre, md.data());
@@ -496,8 +495,15 @@ static int motion_prepare(gbsph_ctx* ctx) {
     for (int c = 0; c < 12; c++) o[k].mat[c] = md[k].mat[c];
   }
   // pageable source: the copy has read it when the call returns
-  CK(cudaMemcpyAsync(ctx->mot_buf, h.data(), h.size(), cudaMemcpyHostToDevice, ctx->stream), "motion table");
+  CK(cudaMemcpyAsync(ctx->mot_buf, h.data(), h.size(), cudaMemcpyHostToDevice, s), "motion table");
   return GBSPH_OK;
+}
+
+static int motion_prepare(gbsph_ctx* ctx) {
+  StepState st;
+  CK(cudaMemcpyAsync(&st, ctx->a.st, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream), "motion dt");
+  CK(cudaStreamSynchronize(ctx->stream), "motion sync");
+  return motion_table(ctx, st, ctx->stream);
 }
 
 int gbsph_set_motion(gbsph_ctx* ctx, gbsph_motion* m) {
@@ -999,6 +1005,251 @@ int gbsph_set_option(gbsph_ctx* ctx, int key, int value) {
   else return set_err(ctx, GBSPH_EINVAL, "unknown option %d", key);
   reset_graph(ctx);
   return GBSPH_OK;
+}
+
+// ---- autotuner ------------------------------------------------------------
+// Times the fluid-row kernel configurations on the context's current state
+// (between steps) and keeps the fastest: the warp-queued rounds kernel, and the
+// one-thread-per-row kernel at 64, 128 and 256 threads per block.  The launches
+// only rewrite the interaction outputs, which the next step recomputes.
+int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (reps < 1) reps = 1;
+  CK(cudaSetDevice(ctx->device), "set device");
+  static const int cand[GBSPH_TUNE_CANDIDATES][2] = {{0, 128}, {1, 64}, {1, 128}, {1, 256}};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  int best = 0;
+  float tbest = 0;
+  gbsph_tune_result r{};
+  for (int k = 0; k < GBSPH_TUNE_CANDIDATES; k++) {
+    const int var = cand[k][0], bs = cand[k][1];
+    gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, ctx->stream, nullptr, nullptr, nullptr);  // warm-up
+    cudaEventRecord(e0, ctx->stream);
+    for (int i = 0; i < reps; i++) gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, ctx->stream, nullptr, nullptr, nullptr);
+    cudaEventRecord(e1, ctx->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return cuda_check(ctx, e, "tune");
+    }
+    ms /= (float)reps;
+    r.ms[k] = ms;
+    r.variant[k] = var;
+    r.bsize[k] = bs;
+    if (k == 0 || ms < tbest) { tbest = ms; best = k; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  r.best = best;
+  ctx->forces_variant = cand[best][0];
+  ctx->forces_bsize = cand[best][1];
+  reset_graph(ctx);
+  if (out) *out = r;
+  return GBSPH_OK;
+}
+
+}  // extern "C"
+
+// ---- ensembles --------------------------------------------------------------
+// Independent cases on one device advanced together: every case keeps its own
+// arrays, stream and adaptive dt; one step of all of them is captured as one
+// CUDA graph whose branches (one per case) run concurrently, and the graph is
+// replayed.  Moving cases have their motions advanced on the host between
+// replays (one read-back of all their step states, one upload each).
+struct gbsph_ensemble {
+  std::vector<gbsph_ctx*> cases;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<cudaEvent_t> ev;        // [0] fork/done, [1+i] case i
+  cudaGraphExec_t exec = nullptr;
+  std::vector<unsigned> parity;       // each case's pointer parity at capture
+  std::vector<unsigned long long> nl; // each case's launches per captured step
+  std::string err;
+};
+
+namespace {
+
+int ens_err(gbsph_ensemble* e, int code, const std::string& msg) {
+  if (e) e->err = msg;
+  return code;
+}
+
+int ens_cuda(gbsph_ensemble* e, cudaError_t c, const char* what) {
+  if (c != cudaSuccess) return ens_err(e, GBSPH_ECUDA, std::string(what) + ": " + cudaGetErrorString(c));
+  return GBSPH_OK;
+}
+
+// prior work on every case stream before the ensemble stream's next work
+int ens_order_in(gbsph_ensemble* e) {
+  for (size_t i = 0; i < e->cases.size(); i++) {
+    if (int rc = ens_cuda(e, cudaEventRecord(e->ev[1 + i], e->cases[i]->stream), "order")) return rc;
+    if (int rc = ens_cuda(e, cudaStreamWaitEvent(e->stream, e->ev[1 + i], 0), "order")) return rc;
+  }
+  return GBSPH_OK;
+}
+
+// the ensemble's work before later work on every case stream
+int ens_order_out(gbsph_ensemble* e) {
+  if (int rc = ens_cuda(e, cudaEventRecord(e->ev[0], e->stream), "order")) return rc;
+  for (gbsph_ctx* c : e->cases)
+    if (int rc = ens_cuda(e, cudaStreamWaitEvent(c->stream, e->ev[0], 0), "order")) return rc;
+  return GBSPH_OK;
+}
+
+// RunMotion input of every moving case for the coming step
+int ens_motion(gbsph_ensemble* e) {
+  std::vector<StepState> st(e->cases.size());
+  bool any = false;
+  for (size_t i = 0; i < e->cases.size(); i++) {
+    gbsph_ctx* c = e->cases[i];
+    if (!c->motion) continue;
+    any = true;
+    if (int rc = ens_cuda(e, cudaMemcpyAsync(&st[i], c->a.st, sizeof(StepState), cudaMemcpyDeviceToHost, e->stream),
+                          "motion dt"))
+      return rc;
+  }
+  if (!any) return GBSPH_OK;
+  if (int rc = ens_cuda(e, cudaStreamSynchronize(e->stream), "motion sync")) return rc;
+  for (size_t i = 0; i < e->cases.size(); i++) {
+    gbsph_ctx* c = e->cases[i];
+    if (!c->motion) continue;
+    if (int rc = motion_table(c, st[i], e->stream)) return ens_err(e, rc, "case " + std::to_string(i) + ": " + c->err);
+  }
+  return GBSPH_OK;
+}
+
+int ens_capture(gbsph_ensemble* e) {
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  e->exec = nullptr;
+  const size_t n = e->cases.size();
+  std::vector<DevArrays> a0(n);
+  std::vector<unsigned> s0(n);
+  std::vector<unsigned long long> l0(n);
+  e->parity.assign(n, 0);
+  e->nl.assign(n, 0);
+  if (int rc = ens_cuda(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal), "capture")) return rc;
+  cudaEventRecord(e->ev[0], e->stream);
+  int rc = GBSPH_OK;
+  size_t ncap = 0;  // cases whose host state was saved
+  for (size_t i = 0; i < n && !rc; i++) {
+    gbsph_ctx* c = e->cases[i];
+    a0[i] = c->a; s0[i] = c->swaps; l0[i] = c->launches;
+    ncap = i + 1;
+    e->parity[i] = c->swaps & 1u;
+    cudaStreamWaitEvent(c->stream, e->ev[0], 0);
+    rc = enqueue_step(c);
+    if (rc) rc = ens_err(e, rc, "case " + std::to_string(i) + ": " + c->err);
+    cudaEventRecord(e->ev[1 + i], c->stream);
+    cudaStreamWaitEvent(e->stream, e->ev[1 + i], 0);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+  // the capture recorded the work without running it: restore the pointer state
+  for (size_t i = 0; i < ncap; i++) {
+    gbsph_ctx* c = e->cases[i];
+    e->nl[i] = c->launches - l0[i];
+    c->a = a0[i]; c->swaps = s0[i]; c->launches = l0[i];
+  }
+  if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+  if (int r2 = ens_cuda(e, ce, "end capture")) return r2;
+  const cudaError_t ie = cudaGraphInstantiate(&e->exec, g, 0);
+  cudaGraphDestroy(g);
+  return ens_cuda(e, ie, "instantiate");
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbsph_ensemble_create(unsigned n, gbsph_ctx* const* ctxs, gbsph_ensemble** out) {
+  if (!out || !ctxs || n == 0) return GBSPH_EINVAL;
+  *out = nullptr;
+  for (unsigned i = 0; i < n; i++) {
+    if (!ctxs[i] || !ctxs[i]->uploaded) return GBSPH_ESTATE;
+    if (ctxs[i]->device != ctxs[0]->device) return GBSPH_EINVAL;
+    for (unsigned j = 0; j < i; j++) if (ctxs[j] == ctxs[i]) return GBSPH_EINVAL;
+  }
+  gbsph_ensemble* e = new gbsph_ensemble();
+  e->cases.assign(ctxs, ctxs + n);
+  e->device = ctxs[0]->device;
+  e->ev.assign(n + 1, nullptr);
+  bool ok = cudaSetDevice(e->device) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) == cudaSuccess;
+  for (unsigned i = 0; ok && i <= n; i++) ok = cudaEventCreateWithFlags(&e->ev[i], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    gbsph_ensemble_destroy(e);
+    return GBSPH_ECUDA;
+  }
+  *out = e;
+  return GBSPH_OK;
+}
+
+void gbsph_ensemble_destroy(gbsph_ensemble* e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  for (cudaEvent_t v : e->ev) if (v) cudaEventDestroy(v);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+const char* gbsph_ensemble_last_error(const gbsph_ensemble* e) { return e ? e->err.c_str() : "null ensemble"; }
+
+int gbsph_ensemble_run(gbsph_ensemble* e, unsigned nsteps, int use_graph) {
+  if (!e) return GBSPH_EINVAL;
+  if (int rc = ens_cuda(e, cudaSetDevice(e->device), "set device")) return rc;
+  bool sym = true;
+  for (gbsph_ctx* c : e->cases) sym = sym && c->c.tstep == GBSPH_STEP_SYMPLECTIC;
+  if (!use_graph || !sym) {
+    // every case on its own stream: the streams run concurrently
+    for (unsigned k = 0; k < nsteps; k++)
+      for (size_t i = 0; i < e->cases.size(); i++) {
+        gbsph_ctx* c = e->cases[i];
+        int rc = c->motion ? motion_prepare(c) : GBSPH_OK;
+        if (!rc) rc = enqueue_step(c);
+        if (rc) return ens_err(e, rc, "case " + std::to_string(i) + ": " + c->err);
+      }
+    for (size_t i = 0; i < e->cases.size(); i++)
+      if (int rc = ens_cuda(e, cudaGetLastError(), "run")) return rc;
+    return GBSPH_OK;
+  }
+  bool valid = e->exec != nullptr;
+  for (size_t i = 0; valid && i < e->cases.size(); i++) valid = (e->cases[i]->swaps & 1u) == e->parity[i];
+  if (!valid)
+    if (int rc = ens_capture(e)) return rc;
+  if (int rc = ens_order_in(e)) return rc;
+  for (unsigned k = 0; k < nsteps; k++) {
+    if (int rc = ens_motion(e)) return rc;
+    if (int rc = ens_cuda(e, cudaGraphLaunch(e->exec, e->stream), "graph launch")) return rc;
+    for (size_t i = 0; i < e->cases.size(); i++) {
+      e->cases[i]->swaps += 2;  // two divides per Symplectic step: parity unchanged
+      e->cases[i]->launches += e->nl[i];
+    }
+  }
+  return ens_order_out(e);
+}
+
+int gbsph_ensemble_sync(gbsph_ensemble* e) {
+  if (!e) return GBSPH_EINVAL;
+  if (int rc = ens_cuda(e, cudaStreamSynchronize(e->stream), "sync")) return rc;
+  for (size_t i = 0; i < e->cases.size(); i++) {
+    gbsph_ctx* c = e->cases[i];
+    if (int rc = ens_cuda(e, cudaStreamSynchronize(c->stream), "sync")) return rc;
+    if (int rc = check_device_errors(c)) return ens_err(e, rc, "case " + std::to_string(i) + ": " + c->err);
+  }
+  return GBSPH_OK;
+}
+
+unsigned long long gbsph_ensemble_launches_per_step(const gbsph_ensemble* e) {
+  unsigned long long n = 0;
+  if (e) for (unsigned long long v : e->nl) n += v;
+  return n;
 }
 
 }  // extern "C"

@@ -156,7 +156,7 @@ __device__ __forceinline__ void fluid_pass(const gbsph_consts& c, const DevArray
 }
 
 template <int tvisco, int tdensity, bool tshift>
-__global__ void __launch_bounds__(128) k_forces_fluid(gbsph_consts c, DevArrays a) {
+__global__ void __launch_bounds__(256) k_forces_fluid(gbsph_consts c, DevArrays a) {
   const DivState& d = *a.div;
   const unsigned np = d.np, npb = d.npb;
   const unsigned p1 = npb + blockIdx.x * blockDim.x + threadIdx.x;
@@ -824,9 +824,10 @@ __global__ void k_pips(gbsph_consts c, DevArrays a) {
 }
 
 template <int tvisco, int tdensity, bool tshift>
-void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s) {
-  if (variant == 1) {
-    k_forces_fluid<tvisco, tdensity, tshift><<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, cudaStream_t s) {
+  if (variant == 1) {  // one thread per row: any block size of 64, 128 or 256
+    const unsigned bs = (bsize == 64 || bsize == 256) ? (unsigned)bsize : 128u;
+    k_forces_fluid<tvisco, tdensity, tshift><<<gb_div_up(cap, bs), bs, 0, s>>>(c, a);
     return;
   }
   const PairK k = make_pairk(c);
@@ -843,18 +844,18 @@ void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int v
 }
 
 template <int tvisco, int tdensity>
-void launch_fluid_s(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s) {
-  if (c.tshift) launch_fluid<tvisco, tdensity, true>(c, a, cap, variant, s);
-  else launch_fluid<tvisco, tdensity, false>(c, a, cap, variant, s);
+void launch_fluid_s(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, cudaStream_t s) {
+  if (c.tshift) launch_fluid<tvisco, tdensity, true>(c, a, cap, variant, bsize, s);
+  else launch_fluid<tvisco, tdensity, false>(c, a, cap, variant, bsize, s);
 }
 
 template <int tvisco>
-void launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s) {
+void launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, cudaStream_t s) {
   switch (c.tdensity) {
-    case GBSPH_DDT_NONE: launch_fluid_s<tvisco, GBSPH_DDT_NONE>(c, a, cap, variant, s); break;
-    case GBSPH_DDT_DDT: launch_fluid_s<tvisco, GBSPH_DDT_DDT>(c, a, cap, variant, s); break;
-    case GBSPH_DDT_DDT2: launch_fluid_s<tvisco, GBSPH_DDT_DDT2>(c, a, cap, variant, s); break;
-    default: launch_fluid_s<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, variant, s); break;
+    case GBSPH_DDT_NONE: launch_fluid_s<tvisco, GBSPH_DDT_NONE>(c, a, cap, variant, bsize, s); break;
+    case GBSPH_DDT_DDT: launch_fluid_s<tvisco, GBSPH_DDT_DDT>(c, a, cap, variant, bsize, s); break;
+    case GBSPH_DDT_DDT2: launch_fluid_s<tvisco, GBSPH_DDT_DDT2>(c, a, cap, variant, bsize, s); break;
+    default: launch_fluid_s<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, variant, bsize, s); break;
   }
 }
 
@@ -864,7 +865,6 @@ namespace gbk {
 
 void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, cudaStream_t s,
             unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin, cudaEvent_t ev_fluid_end) {
-  (void)bsize;
   cudaMemsetAsync(&a.st->acemax2, 0, 3 * sizeof(unsigned), s);
   k_forces_bound<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
   // inside a stream capture the records must be external nodes so that every
@@ -874,9 +874,9 @@ void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, 
   const unsigned ev_flags = cap_st == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (ev_fluid_begin) cudaEventRecordWithFlags(ev_fluid_begin, s, ev_flags);
   switch (c.tvisco) {
-    case GBSPH_VISCO_ARTIFICIAL: launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, variant, s); break;
-    case GBSPH_VISCO_LAMINAR: launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, variant, s); break;
-    default: launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, variant, s); break;
+    case GBSPH_VISCO_ARTIFICIAL: launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, variant, bsize, s); break;
+    case GBSPH_VISCO_LAMINAR: launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, variant, bsize, s); break;
+    default: launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, variant, bsize, s); break;
   }
   if (ev_fluid_end) cudaEventRecordWithFlags(ev_fluid_end, s, ev_flags);
   if (nlaunch) *nlaunch += 2;

@@ -349,8 +349,46 @@ unsigned long long gbsph_launch_count(const gbsph_ctx* ctx);
 void* gbsph_stream(gbsph_ctx* ctx);
 /* Kernel options (autotuner hook).  key 1 = fluid-row kernel of
  * gbsph_forces: 0 (default) per-lane neighbour queues evaluated in rounds,
- * 1 one thread per particle with no queue.  key 0 is accepted and ignored. */
+ * 1 one thread per particle with no queue.  key 0 = threads per block of the
+ * one-thread-per-particle kernel (64, 128 or 256; the queued kernel uses 128).
+ * The reference fixes 128 threads per block (JSphGpu.cpp, BlockSizes). */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
+
+/* Autotuner (no reference counterpart).  Times each fluid-row kernel
+ * configuration -- the queued kernel, and the one-thread-per-particle kernel at
+ * 64, 128 and 256 threads per block -- over `reps` launches on the context's
+ * current state, between steps, and keeps the fastest.  The launches rewrite
+ * only the interaction outputs, which the next step recomputes.  The two
+ * kernels sum a row's neighbours in different orders: results stay within the
+ * FP32 criterion of each other, not bit-identical. */
+#define GBSPH_TUNE_CANDIDATES 4
+typedef struct {
+  int best;                              /* index of the configuration kept */
+  int variant[GBSPH_TUNE_CANDIDATES];    /* gbsph_set_option key 1 */
+  int bsize[GBSPH_TUNE_CANDIDATES];      /* gbsph_set_option key 0 */
+  float ms[GBSPH_TUNE_CANDIDATES];       /* mean time of one fluid-row pass */
+} gbsph_tune_result;
+int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out);
+
+/* Ensembles (no reference counterpart: the reference runs one case per
+ * process, JSphGpuSingle::Run, JSphGpuSingle.cpp:950-1010).  Independent,
+ * uploaded contexts of one device advanced together: each keeps its own
+ * arrays, dt and motion; one Symplectic step of every case is captured as one
+ * CUDA graph with a concurrent branch per case and replayed.  Cases with a
+ * motion have it advanced on the host between replays.  If any case uses
+ * Verlet, or use_graph is 0, the steps are issued on the cases' own streams,
+ * which run concurrently.  The contexts stay owned by the caller and must
+ * outlive the ensemble; work the caller issues on a case after
+ * gbsph_ensemble_run is ordered after the ensemble's. */
+typedef struct gbsph_ensemble gbsph_ensemble;
+int gbsph_ensemble_create(unsigned n, gbsph_ctx* const* ctxs, gbsph_ensemble** out);
+void gbsph_ensemble_destroy(gbsph_ensemble* e);
+const char* gbsph_ensemble_last_error(const gbsph_ensemble* e);
+int gbsph_ensemble_run(gbsph_ensemble* e, unsigned nsteps, int use_graph);
+/* Waits for the ensemble and checks every case's device error word. */
+int gbsph_ensemble_sync(gbsph_ensemble* e);
+/* Kernel launches one replay of the ensemble graph holds (0 before the first). */
+unsigned long long gbsph_ensemble_launches_per_step(const gbsph_ensemble* e);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,122 @@
+"""Batched ensembles and the autotuner (no reference counterpart: the
+reference runs one case per process).
+
+* CPU: the seeded draw of the cases (ranges, determinism), a sloshing case
+  loads with its motion.
+* GPU: one graph replay steps every case exactly as the case's own step does
+  (bit-identical states against each case run alone, with and without the
+  graph, moving cases included); the autotuner keeps the fastest candidate and
+  the block size of the per-row kernel leaves results bit-identical.
+"""
+import numpy as np
+import pytest
+
+from dualsphysics_gb300.ensemble import ensemble_specs, load_ensemble_case
+
+SMALL = dict(count_range=(3000, 12000))
+
+
+def test_ensemble_draw_is_seeded_and_in_range():
+    a, b = ensemble_specs(64, seed=5), ensemble_specs(64, seed=5)
+    assert [x.spec for x in a] == [x.spec for x in b]
+    assert ensemble_specs(8, seed=6)[0].spec != a[0].spec
+    for ec in a:
+        assert all(0.5 <= v <= 2.0 for v in ec.spec.tank)
+        fill = np.prod(ec.spec.column) / np.prod(ec.spec.tank)
+        assert 0.2 <= fill <= 0.6
+        assert 20_000 <= ec.target <= 2_000_000
+        if ec.sloshing:
+            m = ec.spec.motion[0]
+            assert m["type"] == "mvrectsinu" and 0 <= m["ampl"][0] <= 0.05 and 0.5 <= m["freq"][0] <= 2.0
+    assert 0 < sum(ec.sloshing for ec in a) < 64
+
+
+def test_sloshing_case_loads_with_its_motion(tmp_path):
+    ec = next(e for e in ensemble_specs(16, seed=3, **SMALL) if e.sloshing)
+    cd = load_ensemble_case(ec, str(tmp_path))
+    assert cd.motion and cd.motion["movements"][0]["type"] == "mvrectsinu"
+    assert cd.motion["objects"] == [(0, cd.npb)]
+
+
+def _cases(n, seed):
+    from dualsphysics_gb300.sph import GbSphSingle
+    specs = ensemble_specs(n, seed=seed, **SMALL)
+    cds = [load_ensemble_case(ec) for ec in specs]
+    return specs, cds
+
+
+def _sims(cds):
+    from dualsphysics_gb300.sph import GbSphSingle
+    out = []
+    for cd in cds:
+        s = GbSphSingle(0)
+        s.setup(cd)
+        out.append(s)
+    return out
+
+
+def _same(a, b, what):
+    sa, sb = a.download(), b.download()
+    for k in ("idp", "code", "dcell", "pos", "velrho"):
+        np.testing.assert_array_equal(sa[k], sb[k], err_msg=f"{what}: {k}")
+    assert a.step_dt() == b.step_dt(), what
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_ensemble_steps_equal_each_case_alone(use_graph):
+    from dualsphysics_gb300.ensemble import Ensemble
+    specs, cds = _cases(6, seed=11)
+    assert any(ec.sloshing for ec in specs) and not all(ec.sloshing for ec in specs)
+    ens_sims, alone = _sims(cds), _sims(cds)
+    e = Ensemble(ens_sims)
+    e.run(3, use_graph=use_graph)
+    e.run(4, use_graph=use_graph)   # a second call replays the same graph
+    e.sync()
+    if use_graph:
+        assert e.launches_per_step() > 0
+    for s in alone:
+        s.RunSteps(7, use_graph=True)
+    for k, (a, b) in enumerate(zip(ens_sims, alone)):
+        _same(a, b, f"case {k}")
+    # work issued on a case after the ensemble is ordered after it
+    ens_sims[0].RunSteps(1, use_graph=False)
+    alone[0].RunSteps(1, use_graph=False)
+    _same(ens_sims[0], alone[0], "after the ensemble")
+    e.close()
+    for s in ens_sims + alone:
+        s.close()
+
+
+@pytest.mark.gpu
+def test_autotuner_keeps_the_fastest_candidate():
+    from dualsphysics_gb300.ensemble import tune
+    _, cds = _cases(2, seed=12)
+    (s,) = _sims(cds[:1])
+    r = tune(s, reps=2)
+    assert len(r["ms"]) == 4 and all(m > 0 for m in r["ms"])
+    assert r["ms"][r["best"]] == min(r["ms"])
+    assert [(v, b) for v, b in zip(r["variant"], r["bsize"])] == [(0, 128), (1, 64), (1, 128), (1, 256)]
+    # the tuned context steps as one set to the same configuration by hand
+    (t,) = _sims(cds[:1])
+    t.set_option(1, r["variant"][r["best"]])
+    t.set_option(0, r["bsize"][r["best"]])
+    s.RunSteps(5, use_graph=True)
+    t.RunSteps(5, use_graph=True)
+    _same(s, t, "tuned vs set by hand")
+    s.close()
+    t.close()
+
+
+@pytest.mark.gpu
+def test_per_row_kernel_block_size_leaves_results_identical():
+    _, cds = _cases(1, seed=13)
+    sims = _sims(cds * 3)
+    for s, bs in zip(sims, (64, 128, 256)):
+        s.set_option(1, 1)
+        s.set_option(0, bs)
+        s.RunSteps(6, use_graph=True)
+    _same(sims[0], sims[1], "64 vs 128")
+    _same(sims[1], sims[2], "128 vs 256")
+    for s in sims:
+        s.close()
