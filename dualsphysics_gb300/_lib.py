@@ -151,6 +151,16 @@ SIGNATURES = {
     "gbsph_ensemble_run": (C.c_int, [P, C.c_uint, C.c_int]),
     "gbsph_ensemble_sync": (C.c_int, [P]),
     "gbsph_ensemble_launches_per_step": (C.c_ulonglong, [P]),
+    "gbsph_closure_set": (C.c_int, [P, P, C.c_float]),
+    "gbsph_closure_features": (C.c_int, [P, P]),
+    "gbsph_closure_fallbacks": (C.c_int, [P, C.POINTER(C.c_ulonglong)]),
+    "gbsph_mlp_create": (C.c_int, [C.c_int, P, C.POINTER(P)]),
+    "gbsph_mlp_destroy": (None, [P]),
+    "gbsph_mlp_set_data": (C.c_int, [P, P, P, C.c_uint]),
+    "gbsph_mlp_grad": (C.c_int, [P, C.c_uint, C.c_uint, P, P]),
+    "gbsph_mlp_train": (C.c_int, [P, C.c_uint, C.c_uint, C.c_float, P]),
+    "gbsph_mlp_infer": (C.c_int, [P, P, C.c_uint, P]),
+    "gbsph_mlp_params": (C.c_int, [P, P, P]),
     "gbsph_graph_prepare": (C.c_int, [P, C.c_uint]),
     "gbsph_profile": (C.c_int, [P, C.c_uint]),
     "gbsph_profile_read": (C.c_int, [P, P, C.c_uint, C.POINTER(C.c_uint)]),

@@ -1,0 +1,315 @@
+"""Learned closure for coarse runs (no reference counterpart).
+
+A 16-64-64-64-3 tanh MLP (BF16 weights, FP32 accumulation) adds a per-particle
+correction to the fluid accelerations of a coarse run.  It is trained on data
+the method generates itself:
+
+* a fine run (spacing dp) of the dam break with the box obstacle;
+* at snapshot times, its fluid particles whose initial lattice indices are
+  all even are exactly the particles of the coarse case (spacing 2 dp): the
+  fine state restricted to them, with the coarse case's own walls, is a
+  coarse state;
+* the target of each coarse particle is (fine acceleration - coarse
+  acceleration of the restricted state) / |g|, the inputs are the closure
+  features of the restricted state (``gbsph_closure_features``).
+
+Training, inference and the correction inside the step run in the library's
+own kernels (``gbsph_mlp_*``, ``gbsph_closure_set``); the plain method is the
+fallback (per particle, when the correction exceeds ``limit`` x |ace|) and the
+judge (the fine run's probe pressures).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import tempfile
+import time
+
+import numpy as np
+
+from . import casegen as cg
+from ._lib import GbsphError, INTERSTEP_SYMPREDICTOR, lib, ptr
+from .case import load_case
+from .sph import GbSphSingle
+
+NFEAT = 16
+NHID = 64
+NOUT = 3
+NPARAMS = NHID * NFEAT + NHID + 2 * (NHID * NHID + NHID) + NOUT * NHID + NOUT
+TANK_HEIGHT = 0.6   # room for columns up to 0.5 m
+
+
+def layer_slices():
+    """(W, b) slices of the flat parameter vector, layers 0..3."""
+    out, o = [], 0
+    for nin, nout in ((NFEAT, NHID), (NHID, NHID), (NHID, NHID), (NHID, NOUT)):
+        w = slice(o, o + nin * nout)
+        o += nin * nout
+        b = slice(o, o + nout)
+        o += nout
+        out.append((w, b, nout, nin))
+    assert o == NPARAMS
+    return out
+
+
+def init_params(seed: int = 0, out_scale: float = 0.1) -> np.ndarray:
+    """Glorot-uniform weights, zero biases; the output layer scaled down so the
+    untrained correction is small."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(NPARAMS, np.float32)
+    for k, (w, b, nout, nin) in enumerate(layer_slices()):
+        lim = math.sqrt(6.0 / (nin + nout)) * (out_scale if k == 3 else 1.0)
+        p[w] = rng.uniform(-lim, lim, nout * nin).astype(np.float32)
+    return p
+
+
+def to_bf16(p: np.ndarray) -> np.ndarray:
+    """Round-to-nearest-even BF16 bit patterns of float32 values."""
+    u = np.ascontiguousarray(p, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+    return r
+
+
+def from_bf16(b: np.ndarray) -> np.ndarray:
+    return (np.asarray(b, np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+class Trainer:
+    """gbsph_mlp: data on the device, FP32 master weights + BF16 copy, Adam."""
+
+    def __init__(self, params: np.ndarray, device: int = 0):
+        self.m = C.c_void_p()
+        p = np.ascontiguousarray(params, np.float32)
+        rc = lib().gbsph_mlp_create(device, ptr(p), C.byref(self.m))
+        if rc:
+            raise GbsphError(rc, "gbsph_mlp_create")
+
+    def _check(self, rc, what):
+        if rc:
+            raise GbsphError(rc, what)
+
+    def set_data(self, x: np.ndarray, t: np.ndarray) -> None:
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        assert x.shape[1] == NFEAT and t.shape == (x.shape[0], NOUT)
+        self._check(lib().gbsph_mlp_set_data(self.m, ptr(x), ptr(t), x.shape[0]), "gbsph_mlp_set_data")
+        self.n = x.shape[0]
+
+    def grad(self, first: int = 0, n: int | None = None) -> tuple[np.ndarray, float]:
+        n = self.n - first if n is None else n
+        g = np.empty(NPARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        self._check(lib().gbsph_mlp_grad(self.m, first, n, ptr(g), ptr(loss)), "gbsph_mlp_grad")
+        return g, float(loss[0])
+
+    def train(self, epochs: int, batch: int, lr: float) -> np.ndarray:
+        loss = np.empty(epochs, np.float32)
+        self._check(lib().gbsph_mlp_train(self.m, epochs, batch, lr, ptr(loss)), "gbsph_mlp_train")
+        return loss
+
+    def infer(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.empty((x.shape[0], NOUT), np.float32)
+        self._check(lib().gbsph_mlp_infer(self.m, ptr(x), x.shape[0], ptr(y)), "gbsph_mlp_infer")
+        return y
+
+    def params(self) -> tuple[np.ndarray, np.ndarray]:
+        master = np.empty(NPARAMS, np.float32)
+        w = np.empty(NPARAMS, np.uint16)
+        self._check(lib().gbsph_mlp_params(self.m, ptr(master), ptr(w)), "gbsph_mlp_params")
+        return master, w
+
+    def close(self):
+        if self.m:
+            lib().gbsph_mlp_destroy(self.m)
+            self.m = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def attach(sim: GbSphSingle, w_bf16: np.ndarray | None, limit: float = 0.2) -> None:
+    """Turns the closure on (or off with None) for every later step of `sim`."""
+    w = None if w_bf16 is None else np.ascontiguousarray(w_bf16, np.uint16)
+    sim._check(lib().gbsph_closure_set(sim.ctx, ptr(w), float(limit)), "gbsph_closure_set")
+
+
+def fallbacks(sim: GbSphSingle) -> int:
+    n = C.c_ulonglong()
+    sim._check(lib().gbsph_closure_fallbacks(sim.ctx, C.byref(n)), "gbsph_closure_fallbacks")
+    return int(n.value)
+
+
+def features(sim: GbSphSingle) -> np.ndarray:
+    """Closure features of the fluid rows (after Interaction_Forces)."""
+    info = sim.divinfo()
+    out = np.empty((info["np"] - info["npb"], NFEAT), np.float32)
+    sim._check(lib().gbsph_closure_features(sim.ctx, ptr(out)), "gbsph_closure_features")
+    return out
+
+
+# ---- the paired fine / coarse data --------------------------------------------
+def spec(dp: float, height: float, name: str) -> cg.CaseSpec:
+    """The dam break with the box obstacle and mDBC (the C2 geometry), a
+    column of the given height, in a tank raised to TANK_HEIGHT."""
+    return cg.spec_c2(dp=dp, name=name, tank=(1.6, 0.67, TANK_HEIGHT), column=(0.4, 0.67, height), hswl=height)
+
+
+def _load(s: cg.CaseSpec):
+    tmp = tempfile.mkdtemp(prefix="gbclos_")
+    cg.write_case(cg.make_dam_break(s), tmp)
+    return load_case(tmp, s.name)
+
+
+def lattice_key(pos: np.ndarray, dp: float) -> np.ndarray:
+    """(k, j, i) lattice indices of initial fluid positions, as one sortable key."""
+    idx = np.rint(pos / dp).astype(np.int64)
+    return (idx[:, 2] * 100000 + idx[:, 1]) * 100000 + idx[:, 0], idx
+
+
+class Pair:
+    """A fine case and its coarse twin (spacing x2); maps fine fluid ids to
+    coarse fluid rows."""
+
+    def __init__(self, height: float, dp_fine: float = 0.01, tag: str = "P"):
+        self.height = height
+        self.fine = _load(spec(dp_fine, height, f"{tag}F"))
+        self.coarse = _load(spec(2 * dp_fine, height, f"{tag}C"))
+        f, c = self.fine, self.coarse
+        fpos = f.pos[f.npb:]
+        _, idx = lattice_key(fpos, dp_fine)
+        even = np.all(idx % 2 == 0, axis=1)
+        fkey, _ = lattice_key(fpos[even] / 2.0, dp_fine)
+        ckey, _ = lattice_key(c.pos[c.npb:], 2 * dp_fine)
+        # coarse fluid row r <- the fine fluid particle with the same lattice point
+        order_f = np.argsort(fkey)
+        order_c = np.argsort(ckey)
+        if len(fkey) != len(ckey) or not np.array_equal(fkey[order_f], ckey[order_c]):
+            raise ValueError("fine and coarse lattices do not nest")
+        fine_ids = f.idp[f.npb:][np.nonzero(even)[0]]
+        self.coarse_row_fine_id = np.empty(len(ckey), np.int64)
+        self.coarse_row_fine_id[order_c] = fine_ids[order_f]
+
+    def coarse_state(self, fst: dict):
+        """The coarse case with its fluid rows taken from the fine state
+        `fst` (download of the fine run), or None if one left the domain."""
+        c = self.coarse
+        where = np.full(int(fst["idp"].max()) + 1, -1, np.int64)
+        where[fst["idp"]] = np.arange(len(fst["idp"]))
+        rows = where[self.coarse_row_fine_id]
+        if (rows < 0).any():
+            return None
+        import copy
+        cd = copy.copy(c)
+        cd.pos = c.pos.copy()
+        cd.velrho = c.velrho.copy()
+        cd.pos[c.npb:] = fst["pos"][rows]
+        cd.velrho[c.npb:] = fst["velrho"][rows]
+        return cd, rows
+
+
+def paired_samples(heights, dp_fine: float = 0.01, t_end: float = 0.3, n_snap: int = 10,
+                   device: int = 0, log=None) -> tuple[np.ndarray, np.ndarray, dict]:
+    """Features and targets over fine runs of the given column heights,
+    restricted to the coarse particles at n_snap times in (0, t_end]."""
+    xs, ts, meta = [], [], {"snapshots": 0, "fine_steps": 0, "fine_s": 0.0}
+    g = 9.81
+    for hk, h in enumerate(heights):
+        pair = Pair(h, dp_fine, tag=f"H{hk}")
+        fine = GbSphSingle(device)
+        fine.setup(pair.fine)
+        tnext = t_end / n_snap
+        t0 = time.perf_counter()
+        while True:
+            fine.RunSteps(1, use_graph=True)
+            meta["fine_steps"] += 1
+            t = fine.step_dt()[2]
+            if t < tnext:
+                continue
+            tnext += t_end / n_snap
+            # fine accelerations of this state
+            fine.MdbcBoundCorrection(INTERSTEP_SYMPREDICTOR)
+            fine.Interaction_Forces(INTERSTEP_SYMPREDICTOR)
+            fst = fine.download()
+            face, _ = fine.forces()
+            got = pair.coarse_state(fst)
+            if got is not None:
+                cd, rows = got
+                cs = GbSphSingle(device)
+                cs.setup(cd)
+                cs.MdbcBoundCorrection(INTERSTEP_SYMPREDICTOR)
+                cs.Interaction_Forces(INTERSTEP_SYMPREDICTOR)
+                cst = cs.download()
+                cace, _ = cs.forces()
+                x = features(cs)
+                cs.close()
+                crow = cst["idp"][cst["idp"] >= cd.npb] - cd.npb    # coarse fluid row of each feature row
+                fnow = rows[crow]                                   # its fine particle in fst
+                tgt = (face[fnow] - cace[cd.npb:cd.npb + len(crow)]) / g
+                ok = np.isfinite(x).all(axis=1) & np.isfinite(tgt).all(axis=1)
+                xs.append(x[ok])
+                ts.append(tgt[ok].astype(np.float32))
+                meta["snapshots"] += 1
+            if t >= t_end - 1e-12:
+                break
+        meta["fine_s"] += time.perf_counter() - t0
+        fine.close()
+        if log:
+            log(f"height {h:.3f}: {sum(len(x) for x in xs)} samples")
+    return np.concatenate(xs), np.concatenate(ts), meta
+
+
+# ---- evaluation against the fine run ---------------------------------------------
+def probe_mesh(h: float):
+    """Pressure probes on the obstacle's upstream face, 1.5 h off it: 8 points
+    from z = 0.02 to 0.16 m on the face's centre line."""
+    x = cg.OBSTACLE_C2[0] - 1.5 * h
+    y = cg.OBSTACLE_C2[1] + cg.OBSTACLE_C2[3] / 2   # (x0, y0, sx, sy, sz)
+    return dict(ptref=(x, y, 0.02), vec1=(0.0, 0.0, 1.0), vec2=(1.0, 0.0, 0.0), vec3=(0.0, 1.0, 0.0),
+                dis=(0.14, 0.0, 0.0), dispt=(0.02, 0.0, 0.0))
+
+
+def run_with_probes(cd, t_end: float, dt_probe: float, w_bf16=None, limit: float = 0.2, device: int = 0,
+                    mesh_h: float | None = None) -> dict:
+    """Runs a case to t_end, sampling the probes every dt_probe; returns the
+    probe pressures, their times and the wall time of the stepping alone."""
+    from .gauges import GaugeSystem
+    s = GbSphSingle(device)
+    s.setup(cd)
+    if w_bf16 is not None:
+        attach(s, w_bf16, limit)
+    gs = GaugeSystem(s)
+    m = probe_mesh(mesh_h if mesh_h is not None else cd.params.h)
+    gs.AddGaugeMesh("probes", **m)
+    times, press = [], []
+    tnext, t, wall, nsteps = dt_probe, 0.0, 0.0, 0
+    while t < t_end:
+        s.sync()
+        t0 = time.perf_counter()
+        s.RunSteps(1, use_graph=True)
+        t = s.step_dt()[2]
+        wall += time.perf_counter() - t0
+        nsteps += 1
+        if t >= tnext:
+            tnext += dt_probe
+            gs.CalculeGpu(t)
+            times.append(t)
+            press.append(gs.Pressure(gs.GetResult("probes")["rhop"]))
+    out = {"t": np.array(times), "p": np.array(press), "wall_s": wall, "steps": nsteps,
+           "np": cd.np, "fallbacks": fallbacks(s) if w_bf16 is not None else 0}
+    s.close()
+    return out
+
+
+def probe_error(run: dict, ref: dict) -> float:
+    """RMS difference of the probe pressures against the reference run, the
+    reference interpolated to the run's sample times (Pa)."""
+    n = min(len(run["t"]), len(ref["t"]))
+    if n == 0:
+        return float("nan")
+    pr = np.stack([np.interp(run["t"][:n], ref["t"], ref["p"][:, k]) for k in range(ref["p"].shape[1])], axis=1)
+    return float(np.sqrt(np.mean((run["p"][:n] - pr) ** 2)))

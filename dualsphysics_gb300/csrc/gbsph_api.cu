@@ -9,6 +9,7 @@
 // into a CUDA graph and replayed.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -57,6 +58,12 @@ struct gbsph_ctx {
   void* mot_buf = nullptr;
   std::vector<char> mot_host;
   void* gauge_buf = nullptr;  // gauge inputs and results (grown on demand)
+  // learned closure: BF16 weights, the feature rows (cap x 16), the fallback counter
+  void* clos_w = nullptr;
+  float* clos_feat = nullptr;
+  unsigned* clos_nfb = nullptr;
+  float clos_limit = 0.2f;
+  bool clos_on = false;
   size_t gauge_bytes = 0;
   std::string err;
 };
@@ -175,6 +182,11 @@ int do_forces(gbsph_ctx* ctx) {
   }
   gbk::forces(ctx->c, ctx->a, ctx->cap, ctx->forces_bsize, ctx->forces_variant, ctx->stream, &ctx->launches, e0, e1);
   if (ctx->c.tvisco == GBSPH_VISCO_LAMINARSPS) gbk::sps_tau(ctx->c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
+  if (ctx->clos_on) {  // the learned correction of the fluid accelerations
+    gbk::closure_features(ctx->c, ctx->a, ctx->cap, ctx->clos_feat, ctx->stream, &ctx->launches);
+    gbk::closure_apply(ctx->c, ctx->a, ctx->cap, ctx->clos_w, ctx->clos_feat, ctx->clos_limit, ctx->clos_nfb,
+                       ctx->stream, &ctx->launches);
+  }
   return cuda_check(ctx, cudaGetLastError(), "forces");
 }
 
@@ -276,6 +288,9 @@ void gbsph_destroy(gbsph_ctx* ctx) {
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->gauge_buf) cudaFree(ctx->gauge_buf);
   if (ctx->mot_buf) cudaFree(ctx->mot_buf);
+  if (ctx->clos_w) cudaFree(ctx->clos_w);
+  if (ctx->clos_feat) cudaFree(ctx->clos_feat);
+  if (ctx->clos_nfb) cudaFree(ctx->clos_nfb);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -1250,6 +1265,231 @@ unsigned long long gbsph_ensemble_launches_per_step(const gbsph_ensemble* e) {
   unsigned long long n = 0;
   if (e) for (unsigned long long v : e->nl) n += v;
   return n;
+}
+
+// ---- learned closure ----------------------------------------------------------
+static int closure_alloc(gbsph_ctx* ctx) {
+  if (ctx->clos_feat) return GBSPH_OK;
+  CK(gbk::closure_init(), "closure init");
+  if (cudaMalloc(&ctx->clos_feat, sizeof(float) * GBSPH_CLOSURE_FEATURES * (size_t)ctx->cap) != cudaSuccess ||
+      cudaMalloc(&ctx->clos_w, sizeof(uint16_t) * GBSPH_CLOSURE_PARAMS) != cudaSuccess ||
+      cudaMalloc(&ctx->clos_nfb, sizeof(unsigned)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, GBSPH_ENOMEM, "closure buffers");
+  }
+  CK(cudaMemsetAsync(ctx->clos_nfb, 0, sizeof(unsigned), ctx->stream), "closure");
+  return GBSPH_OK;
+}
+
+int gbsph_closure_set(gbsph_ctx* ctx, const uint16_t* w_bf16, float limit) {
+  if (!ctx) return GBSPH_EINVAL;
+  CK(cudaSetDevice(ctx->device), "set device");
+  reset_graph(ctx);
+  if (!w_bf16) {
+    ctx->clos_on = false;
+    return GBSPH_OK;
+  }
+  if (!(limit >= 0)) return set_err(ctx, GBSPH_EINVAL, "closure limit must be >= 0");
+  if (int rc = closure_alloc(ctx)) return rc;
+  CK(cudaMemcpyAsync(ctx->clos_w, w_bf16, sizeof(uint16_t) * GBSPH_CLOSURE_PARAMS, cudaMemcpyHostToDevice,
+                     ctx->stream), "closure weights");
+  CK(cudaStreamSynchronize(ctx->stream), "closure weights");
+  ctx->clos_limit = limit;
+  ctx->clos_on = true;
+  return GBSPH_OK;
+}
+
+int gbsph_closure_features(gbsph_ctx* ctx, float* out) {
+  if (!ctx || !ctx->uploaded || !out) return set_err(ctx, GBSPH_EINVAL, "closure_features");
+  CK(cudaSetDevice(ctx->device), "set device");
+  if (int rc = closure_alloc(ctx)) return rc;
+  DivState ds;
+  CK(cudaMemcpyAsync(&ds, ctx->a.div, sizeof(ds), cudaMemcpyDeviceToHost, ctx->stream), "div");
+  gbk::closure_features(ctx->c, ctx->a, ctx->cap, ctx->clos_feat, ctx->stream, &ctx->launches);
+  CK(cudaStreamSynchronize(ctx->stream), "features");
+  CK(cudaMemcpy(out, ctx->clos_feat, sizeof(float) * GBSPH_CLOSURE_FEATURES * (size_t)(ds.np - ds.npb),
+                cudaMemcpyDeviceToHost), "features");
+  return check_device_errors(ctx);
+}
+
+int gbsph_closure_fallbacks(gbsph_ctx* ctx, unsigned long long* n) {
+  if (!ctx || !n) return GBSPH_EINVAL;
+  unsigned v = 0;
+  if (ctx->clos_nfb) {
+    CK(cudaMemcpyAsync(&v, ctx->clos_nfb, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream), "fallbacks");
+    CK(cudaStreamSynchronize(ctx->stream), "fallbacks");
+  }
+  *n = v;
+  return GBSPH_OK;
+}
+
+}  // extern "C"
+
+// Trainer: device copies of the data, FP32 master weights with their BF16
+// copy, Adam moments, the gradient and per-epoch losses.
+struct gbsph_mlp {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  float* master = nullptr;   // GBSPH_CLOSURE_PARAMS
+  void* w = nullptr;         // BF16 copy
+  float *grad = nullptr, *m = nullptr, *v = nullptr, *loss = nullptr;
+  unsigned nloss = 0;
+  float *x = nullptr, *t = nullptr;
+  unsigned n = 0;
+  unsigned long long adam_t = 0;
+};
+
+extern "C" {
+
+int gbsph_mlp_create(int device, const float* params, gbsph_mlp** out) {
+  if (!params || !out) return GBSPH_EINVAL;
+  *out = nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) return GBSPH_ECUDA;
+  if (gbk::closure_init() != cudaSuccess) return GBSPH_ECUDA;
+  gbsph_mlp* m = new gbsph_mlp();
+  m->device = device;
+  const size_t P = GBSPH_CLOSURE_PARAMS;
+  bool ok = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaMalloc(&m->master, 4 * P) == cudaSuccess && cudaMalloc(&m->w, 2 * P) == cudaSuccess &&
+            cudaMalloc(&m->grad, 4 * P) == cudaSuccess && cudaMalloc(&m->m, 4 * P) == cudaSuccess &&
+            cudaMalloc(&m->v, 4 * P) == cudaSuccess;
+  if (ok) {
+    ok = cudaMemcpy(m->master, params, 4 * P, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(m->grad, 0, 4 * P) == cudaSuccess && cudaMemset(m->m, 0, 4 * P) == cudaSuccess &&
+         cudaMemset(m->v, 0, 4 * P) == cudaSuccess;
+    if (ok) gbk::to_bf16(m->master, m->w, (int)P, m->stream);
+    ok = ok && cudaStreamSynchronize(m->stream) == cudaSuccess;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    gbsph_mlp_destroy(m);
+    return GBSPH_ENOMEM;
+  }
+  *out = m;
+  return GBSPH_OK;
+}
+
+void gbsph_mlp_destroy(gbsph_mlp* m) {
+  if (!m) return;
+  cudaSetDevice(m->device);
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  void* bufs[] = {m->master, m->w, m->grad, m->m, m->v, m->loss, m->x, m->t};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+int gbsph_mlp_set_data(gbsph_mlp* m, const float* x, const float* t, unsigned n) {
+  if (!m || !x || !t || !n) return GBSPH_EINVAL;
+  if (cudaSetDevice(m->device) != cudaSuccess) return GBSPH_ECUDA;
+  cudaStreamSynchronize(m->stream);
+  if (m->x) cudaFree(m->x);
+  if (m->t) cudaFree(m->t);
+  m->x = m->t = nullptr;
+  m->n = 0;
+  if (cudaMalloc(&m->x, sizeof(float) * GBSPH_CLOSURE_FEATURES * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&m->t, sizeof(float) * 3 * (size_t)n) != cudaSuccess) {
+    cudaGetLastError();
+    return GBSPH_ENOMEM;
+  }
+  if (cudaMemcpy(m->x, x, sizeof(float) * GBSPH_CLOSURE_FEATURES * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(m->t, t, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess)
+    return GBSPH_ECUDA;
+  m->n = n;
+  return GBSPH_OK;
+}
+
+static int mlp_loss_buf(gbsph_mlp* m, unsigned n) {
+  if (m->nloss >= n) return GBSPH_OK;
+  if (m->loss) cudaFree(m->loss);
+  m->loss = nullptr;
+  m->nloss = 0;
+  if (cudaMalloc(&m->loss, sizeof(float) * n) != cudaSuccess) {
+    cudaGetLastError();
+    return GBSPH_ENOMEM;
+  }
+  m->nloss = n;
+  return GBSPH_OK;
+}
+
+int gbsph_mlp_grad(gbsph_mlp* m, unsigned first, unsigned n, float* grad, float* loss) {
+  if (!m || !grad || !n || (unsigned long long)first + n > m->n) return GBSPH_EINVAL;
+  if (cudaSetDevice(m->device) != cudaSuccess) return GBSPH_ECUDA;
+  if (int rc = mlp_loss_buf(m, 1)) return rc;
+  cudaMemsetAsync(m->grad, 0, sizeof(float) * GBSPH_CLOSURE_PARAMS, m->stream);
+  cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream);
+  gbk::mlp_grad(m->w, m->x + (size_t)first * GBSPH_CLOSURE_FEATURES, m->t + (size_t)first * 3, n, m->grad, m->loss,
+                m->stream);
+  if (cudaStreamSynchronize(m->stream) != cudaSuccess) return GBSPH_ECUDA;
+  if (cudaMemcpy(grad, m->grad, sizeof(float) * GBSPH_CLOSURE_PARAMS, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GBSPH_ECUDA;
+  if (loss && cudaMemcpy(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) return GBSPH_ECUDA;
+  cudaMemsetAsync(m->grad, 0, sizeof(float) * GBSPH_CLOSURE_PARAMS, m->stream);
+  return cudaStreamSynchronize(m->stream) == cudaSuccess ? GBSPH_OK : GBSPH_ECUDA;
+}
+
+int gbsph_mlp_train(gbsph_mlp* m, unsigned epochs, unsigned batch, float lr, float* loss_per_epoch) {
+  if (!m || !m->n || !batch || !epochs) return GBSPH_EINVAL;
+  if (cudaSetDevice(m->device) != cudaSuccess) return GBSPH_ECUDA;
+  if (int rc = mlp_loss_buf(m, epochs)) return rc;
+  cudaMemsetAsync(m->loss, 0, sizeof(float) * epochs, m->stream);
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const unsigned nb = (m->n + batch - 1) / batch;
+  for (unsigned e = 0; e < epochs; e++) {
+    for (unsigned b = 0; b < nb; b++) {
+      const unsigned first = b * batch, n = std::min(batch, m->n - first);
+      gbk::mlp_grad(m->w, m->x + (size_t)first * GBSPH_CLOSURE_FEATURES, m->t + (size_t)first * 3, n, m->grad,
+                    m->loss + e, m->stream);
+      m->adam_t++;
+      const float bc1 = (float)(1.0 - std::pow((double)b1, (double)m->adam_t));
+      const float bc2 = (float)(1.0 - std::pow((double)b2, (double)m->adam_t));
+      gbk::mlp_adam(m->master, m->w, m->grad, m->m, m->v, lr, b1, b2, eps, bc1, bc2, m->stream);
+    }
+  }
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(m->stream) != cudaSuccess) return GBSPH_ECUDA;
+  if (loss_per_epoch) {
+    std::vector<float> l(epochs);
+    if (cudaMemcpy(l.data(), m->loss, sizeof(float) * epochs, cudaMemcpyDeviceToHost) != cudaSuccess) return GBSPH_ECUDA;
+    for (unsigned e = 0; e < epochs; e++) loss_per_epoch[e] = l[e] / (float)nb;  // mean of the batch losses
+  }
+  return GBSPH_OK;
+}
+
+int gbsph_mlp_infer(gbsph_mlp* m, const float* x, unsigned n, float* y) {
+  if (!m || !x || !y) return GBSPH_EINVAL;
+  if (!n) return GBSPH_OK;
+  if (cudaSetDevice(m->device) != cudaSuccess) return GBSPH_ECUDA;
+  float *dx = nullptr, *dy = nullptr;
+  if (cudaMalloc(&dx, sizeof(float) * GBSPH_CLOSURE_FEATURES * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&dy, sizeof(float) * 3 * (size_t)n) != cudaSuccess) {
+    cudaGetLastError();
+    if (dx) cudaFree(dx);
+    return GBSPH_ENOMEM;
+  }
+  int rc = GBSPH_OK;
+  if (cudaMemcpyAsync(dx, x, sizeof(float) * GBSPH_CLOSURE_FEATURES * (size_t)n, cudaMemcpyHostToDevice, m->stream) !=
+      cudaSuccess)
+    rc = GBSPH_ECUDA;
+  if (!rc) {
+    gbk::mlp_infer(m->w, dx, n, dy, m->stream);
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess ||
+        cudaMemcpy(y, dy, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = GBSPH_ECUDA;
+  }
+  cudaFree(dx);
+  cudaFree(dy);
+  return rc;
+}
+
+int gbsph_mlp_params(gbsph_mlp* m, float* master, uint16_t* w_bf16) {
+  if (!m) return GBSPH_EINVAL;
+  if (cudaSetDevice(m->device) != cudaSuccess || cudaStreamSynchronize(m->stream) != cudaSuccess) return GBSPH_ECUDA;
+  if (master && cudaMemcpy(master, m->master, 4 * GBSPH_CLOSURE_PARAMS, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GBSPH_ECUDA;
+  if (w_bf16 && cudaMemcpy(w_bf16, m->w, 2 * GBSPH_CLOSURE_PARAMS, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GBSPH_ECUDA;
+  return GBSPH_OK;
 }
 
 }  // extern "C"

@@ -219,6 +219,17 @@ void load_dcell(const gbsph_consts& c, const DevArrays& a, unsigned n, cudaStrea
 // periodic.  blockcounts holds gb_div_up(cap, 256) + 1 entries.
 void run_periodic(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned* blockcounts, cudaStream_t s,
                   unsigned long long* nlaunch);
+// learned closure (gbsph_closure.cu)
+cudaError_t closure_init();
+void closure_features(const gbsph_consts& c, const DevArrays& a, unsigned cap, float* feat, cudaStream_t s,
+                      unsigned long long* nlaunch);
+void closure_apply(const gbsph_consts& c, const DevArrays& a, unsigned cap, const void* w_bf16, const float* feat,
+                   float limit, unsigned* nfallback, cudaStream_t s, unsigned long long* nlaunch);
+void mlp_infer(const void* w_bf16, const float* x, unsigned n, float* y, cudaStream_t s);
+void mlp_grad(const void* w_bf16, const float* x, const float* t, unsigned n, float* grad, float* loss, cudaStream_t s);
+void mlp_adam(float* master, void* w_bf16, float* grad, float* m, float* v, float lr, float b1, float b2, float eps,
+              float bc1, float bc2, cudaStream_t s);
+void to_bf16(const float* src, void* dst, int n, cudaStream_t s);
 void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses, cudaStream_t s, unsigned long long* nlaunch);
 // Stable sort of n <= sort_noalloc_max_keys() keys of nbits bits on the static
 // work area (work = its device address, from sort_noalloc_address on the

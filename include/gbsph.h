@@ -390,6 +390,43 @@ int gbsph_ensemble_sync(gbsph_ensemble* e);
 /* Kernel launches one replay of the ensemble graph holds (0 before the first). */
 unsigned long long gbsph_ensemble_launches_per_step(const gbsph_ensemble* e);
 
+/* ---- learned closure (no reference counterpart) -------------------------
+ * A 16-64-64-64-3 tanh MLP with BF16 weights and FP32 accumulation that adds
+ * a per-particle correction g*y to the fluid accelerations of a coarse run.
+ * Its inputs are the GBSPH_CLOSURE_FEATURES features of a fluid row over its
+ * kernel neighbourhood (density, kernel-weighted velocity differences,
+ * pressure-gradient moment, Shepard sum, position divergence, the plain
+ * acceleration, boundary proximity).  Parameters, flat and row-major:
+ * W0[64][16] b0[64] W1[64][64] b1[64] W2[64][64] b2[64] W3[3][64] b3[3]. */
+#define GBSPH_CLOSURE_FEATURES 16
+#define GBSPH_CLOSURE_PARAMS 9603
+/* Attaches the closure to a context (w_bf16 NULL detaches): after every
+ * interaction pass of every later step the correction is added to each fluid
+ * row whose correction norm is at most `limit` x its plain |ace| (the others
+ * keep the plain acceleration, counted by gbsph_closure_fallbacks), and AceMax
+ * is taken over the corrected rows. */
+int gbsph_closure_set(gbsph_ctx* ctx, const uint16_t* w_bf16, float limit);
+/* Features of the fluid rows of the current state ((np-npb) x 16 floats, in the
+ * order gbsph_download returns rows npb..np-1); call after gbsph_forces. */
+int gbsph_closure_features(gbsph_ctx* ctx, float* out);
+int gbsph_closure_fallbacks(gbsph_ctx* ctx, unsigned long long* n);
+
+/* Trainer: the MLP's own forward/backward kernels and Adam on one device.
+ * Data (features x, targets t = 3 per sample) are copied to the device once;
+ * gbsph_mlp_train runs `epochs` passes of mini-batches of `batch` samples in
+ * data order (the caller shuffles), the loss being the mean of (y - t)^2. */
+typedef struct gbsph_mlp gbsph_mlp;
+int gbsph_mlp_create(int device, const float* params, gbsph_mlp** out);
+void gbsph_mlp_destroy(gbsph_mlp* m);
+int gbsph_mlp_set_data(gbsph_mlp* m, const float* x, const float* t, unsigned n);
+/* Gradient (GBSPH_CLOSURE_PARAMS floats) and loss of samples [first, first+n)
+ * at the current weights. */
+int gbsph_mlp_grad(gbsph_mlp* m, unsigned first, unsigned n, float* grad, float* loss);
+int gbsph_mlp_train(gbsph_mlp* m, unsigned epochs, unsigned batch, float lr, float* loss_per_epoch);
+int gbsph_mlp_infer(gbsph_mlp* m, const float* x, unsigned n, float* y);
+/* FP32 master weights and their BF16 copy (either may be NULL). */
+int gbsph_mlp_params(gbsph_mlp* m, float* master, uint16_t* w_bf16);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,186 @@
+"""The learned closure (no reference counterpart): its MLP kernels against the
+FP64 oracle (oracle/closure_oracle.py), its features against a brute-force
+restatement, its use inside the step, and what a trained network gains.
+
+* CPU: the oracle's gradient against central finite differences; BF16
+  rounding against torch's; the parameter count against the header; the
+  fine/coarse lattices nest.
+* GPU: forward (BF16 weights, FP32 accumulation) and gradient against the
+  oracle evaluated with the same BF16 weights; Adam training of a smooth
+  target; the features of a case against the oracle; a zero correction and
+  an always-rejected correction leave the run bit-identical to the plain one
+  (the second counted as fallbacks); a network trained on paired runs of
+  three column heights lowers the acceleration error of a fourth, held-out
+  height against its fine run.
+"""
+import os
+import re
+import sys
+
+import numpy as np
+import pytest
+
+import goldens as G
+from dualsphysics_gb300 import closure as cl
+
+sys.path.insert(0, os.path.join(G.ROOT, "oracle"))
+import closure_oracle as co  # noqa: E402
+
+
+def _rand_data(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0, 1, (n, cl.NFEAT)).astype(np.float32)
+    x[:, 13:] = 0
+    t = np.stack([np.sin(x[:, 0]) * 0.5, x[:, 1] * x[:, 2] * 0.3, np.tanh(x[:, 3] - x[:, 4])], 1).astype(np.float32)
+    return x, t
+
+
+def test_parameter_count_matches_header():
+    h = open(os.path.join(G.ROOT, "include", "gbsph.h")).read()
+    assert int(re.search(r"#define GBSPH_CLOSURE_PARAMS (\d+)", h).group(1)) == cl.NPARAMS == 9603
+    assert int(re.search(r"#define GBSPH_CLOSURE_FEATURES (\d+)", h).group(1)) == cl.NFEAT
+
+
+def test_oracle_gradient_against_finite_differences():
+    x, t = _rand_data(7, 1)
+    p = cl.init_params(3, out_scale=1.0).astype(np.float64)
+    _, g = co.loss_and_grad(p, x, t)
+    rng = np.random.default_rng(2)
+    for i in rng.choice(cl.NPARAMS, 40, replace=False):
+        e = np.zeros_like(p)
+        e[i] = 1e-6
+        fd = (co.loss_and_grad(p + e, x, t)[0] - co.loss_and_grad(p - e, x, t)[0]) / 2e-6
+        assert abs(fd - g[i]) <= 1e-7 + 1e-5 * abs(g[i]), i
+
+
+def test_bf16_rounding_matches_torch():
+    torch = pytest.importorskip("torch")
+    v = np.random.default_rng(0).normal(0, 3, 5000).astype(np.float32)
+    v[:4] = [0.0, -0.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8]   # ties to even
+    ours = cl.to_bf16(v)
+    ref = torch.from_numpy(v).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16)
+    np.testing.assert_array_equal(ours, ref)
+
+
+def test_fine_and_coarse_lattices_nest():
+    pair = cl.Pair(0.25, dp_fine=0.04, tag="N")
+    c = pair.coarse
+    assert len(pair.coarse_row_fine_id) == c.np - c.npb
+    f = pair.fine
+    fp = f.pos[pair.coarse_row_fine_id]
+    np.testing.assert_allclose(fp, c.pos[c.npb:], atol=1e-12)
+
+
+# ---- GPU ------------------------------------------------------------------
+@pytest.mark.gpu
+def test_mlp_forward_and_gradient_match_oracle():
+    x, t = _rand_data(3000, 4)
+    p = cl.init_params(5, out_scale=1.0)
+    tr = cl.Trainer(p)
+    tr.set_data(x, t)
+    pb = cl.from_bf16(cl.to_bf16(p)).astype(np.float64)      # the weights the kernels use
+    master, w = tr.params()
+    np.testing.assert_array_equal(master, p)
+    np.testing.assert_array_equal(w, cl.to_bf16(p))
+    y = tr.infer(x)
+    yo = co.forward(pb, x)[-1]
+    assert np.abs(y - yo).max() <= 2e-5 * max(1.0, np.abs(yo).max())
+    g, loss = tr.grad()
+    lo, go = co.loss_and_grad(pb, x, t)
+    assert loss == pytest.approx(lo, rel=1e-5)
+    assert np.abs(g - go).max() <= 1e-4 * np.abs(go).max()
+    # a sub-range of the data
+    g2, _ = tr.grad(100, 500)
+    _, go2 = co.loss_and_grad(pb, x[100:600], t[100:600])
+    assert np.abs(g2 - go2).max() <= 1e-4 * np.abs(go2).max()
+    tr.close()
+
+
+@pytest.mark.gpu
+def test_adam_training_fits_a_smooth_target():
+    x, t = _rand_data(20000, 6)
+    tr = cl.Trainer(cl.init_params(7))
+    tr.set_data(x, t)
+    loss = tr.train(epochs=40, batch=512, lr=2e-3)
+    assert np.isfinite(loss).all() and loss[-1] < 0.1 * loss[0]
+    master, w = tr.params()
+    np.testing.assert_array_equal(w, cl.to_bf16(master))       # the BF16 copy follows the master weights
+    tr.close()
+
+
+@pytest.mark.gpu
+def test_features_match_oracle():
+    from dualsphysics_gb300 import _lib
+    from dualsphysics_gb300.sph import GbSphSingle
+    cd = G.load_generated("mdbc_d04")
+    s = GbSphSingle(0)
+    s.setup(cd)
+    s.MdbcBoundCorrection(_lib.INTERSTEP_SYMPREDICTOR)
+    s.Interaction_Forces(_lib.INTERSTEP_SYMPREDICTOR)
+    f = cl.features(s)
+    st = s.download()
+    ace, _ = s.forces()
+    c = s.consts
+    s.close()
+    # the pressure every kernel uses: the Tait EOS in FP32 (rho/rho0 rounded to float)
+    x = (st["velrho"][:, 3] / np.float32(c.rhopzero)).astype(np.float32)
+    press = np.float32(c.cteb) * ((x.astype(np.float64) ** c.gamma).astype(np.float32) - np.float32(1.0))
+    fo = co.features(st["pos"], st["velrho"], cd.npb, c, press)
+    fo[:, 9:12] = ace[cd.npb:] / np.linalg.norm(np.asarray(c.gravity[:], np.float64))
+    assert f.shape == fo.shape and np.isfinite(f).all()
+    scale = np.maximum(np.abs(fo).max(axis=0), 1e-3)
+    err = np.abs(f - fo).max(axis=0) / scale
+    assert err.max() < 2e-4, err
+    assert np.all(f[:, 13:] == 0)
+
+
+def _run(cd, n, w=None, limit=0.2):
+    from dualsphysics_gb300.sph import GbSphSingle
+    s = GbSphSingle(0)
+    s.setup(cd)
+    if w is not None:
+        cl.attach(s, w, limit)
+    s.RunSteps(n, use_graph=True)
+    st = s.download()
+    nfb = cl.fallbacks(s) if w is not None else 0
+    dt = s.step_dt()
+    s.close()
+    return st, nfb, dt
+
+
+@pytest.mark.gpu
+def test_zero_and_rejected_corrections_leave_the_run_unchanged():
+    cd = G.load_generated("mdbc_d04")
+    base, _, dt0 = _run(cd, 6)
+    zero = cl.to_bf16(np.zeros(cl.NPARAMS, np.float32))
+    st, nfb, dt = _run(cd, 6, zero)
+    for k in ("idp", "pos", "velrho"):
+        np.testing.assert_array_equal(st[k], base[k], err_msg=k)
+    assert nfb == 0 and dt == dt0
+    big = np.zeros(cl.NPARAMS, np.float32)
+    big[-3:] = 1000.0                                          # output bias: 1000 g, always above 0.2 |ace|
+    st, nfb, dt = _run(cd, 6, cl.to_bf16(big))
+    for k in ("idp", "pos", "velrho"):
+        np.testing.assert_array_equal(st[k], base[k], err_msg=k)
+    assert nfb == 6 * 2 * (cd.np - cd.npb) and dt == dt0    # every fluid row, two passes per step
+
+
+@pytest.mark.gpu
+def test_trained_closure_lowers_the_held_out_acceleration_error():
+    """Paired data of three column heights (fine dp 0.02, coarse 0.04);
+    trained on them, the network lowers the coarse acceleration error of a
+    fourth height against its fine run."""
+    xs, ts, meta = cl.paired_samples([0.22, 0.28, 0.34], dp_fine=0.02, t_end=0.12, n_snap=4)
+    xh, th, _ = cl.paired_samples([0.31], dp_fine=0.02, t_end=0.12, n_snap=4)
+    assert meta["snapshots"] == 12 and len(xs) > 5000
+    rng = np.random.default_rng(0)
+    o = rng.permutation(len(xs))
+    tr = cl.Trainer(cl.init_params(1))
+    tr.set_data(xs[o], ts[o])
+    loss = tr.train(epochs=60, batch=1024, lr=1e-3)
+    assert loss[-1] < loss[0]
+    yh = tr.infer(xh)
+    plain = float(np.mean(th ** 2))                  # the coarse run's error with no correction
+    learned = float(np.mean((th - yh) ** 2))
+    assert learned < 0.8 * plain, (learned, plain)
+    tr.close()
