@@ -262,6 +262,62 @@ def run_ensemble(args, local: int = 0):
     print(json.dumps(line))
 
 
+def run_closure(args, local: int = 0):
+    """Learned closure (--workload closure): paired fine (dp 0.01) / coarse
+    (dp 0.02) data over seeded column heights, training on the GPU, then on a
+    held-out height the probe pressures on the obstacle face and the surge
+    front of the coarse run with and without the closure and of the fine run,
+    each against a finer judge run (dp 0.005), with the wall time of each run."""
+    from dualsphysics_gb300 import closure as cl
+    rng = np.random.default_rng(args.clos_seed)
+    heights = [float(h) for h in np.sort(rng.uniform(0.2, 0.5, args.clos_heights))]
+    held, t_end, dtp = args.clos_held, args.clos_tend, 0.005
+    t0 = time.perf_counter()
+    xs, ts, meta = cl.paired_samples(heights, dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
+    t_data = time.perf_counter() - t0
+    order = rng.permutation(len(xs))
+    tr = cl.Trainer(cl.init_params(args.clos_seed), local)
+    tr.set_data(xs[order], ts[order])
+    t1 = time.perf_counter()
+    loss = tr.train(args.clos_epochs, 1024, 1e-3)
+    t_train = time.perf_counter() - t1
+    _, w = tr.params()
+    xh, th, _ = cl.paired_samples([held], dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
+    yh = tr.infer(xh)
+    tr.close()
+    coarse = cl._load(cl.spec(0.02, held, "HeldC"))
+    hc = coarse.params.h
+    judge = cl.run_with_probes(cl._load(cl.spec(0.005, held, "HeldJ")), t_end, dtp, device=local, mesh_h=hc)
+    fine = cl.run_with_probes(cl._load(cl.spec(0.01, held, "HeldF")), t_end, dtp, device=local, mesh_h=hc)
+    plain = cl.run_with_probes(coarse, t_end, dtp, device=local, mesh_h=hc)
+    learned = cl.run_with_probes(coarse, t_end, dtp, w_bf16=w, limit=0.2, device=local, mesh_h=hc)
+    err = {k: cl.probe_error(r, judge) for k, r in (("fine_dp0.01", fine), ("coarse_plain", plain),
+                                                      ("coarse_learned", learned))}
+    werr = {k: cl.probe_error(r, judge, window=0.02) for k, r in (("fine_dp0.01", fine), ("coarse_plain", plain),
+                                                                    ("coarse_learned", learned))}
+    ferr = {k: cl.front_error(r, judge) for k, r in (("fine_dp0.01", fine), ("coarse_plain", plain),
+                                                       ("coarse_learned", learned))}
+    speed = fine["wall_s"] / learned["wall_s"]
+    line = {"metric": "learned vs plain time-to-accuracy (probe pressure on the obstacle face)",
+            "value": speed, "unit": "x (fine dp=0.01 wall time / learned coarse wall time)", "n_gpus": 1,
+            "higher_is_better": True, "data": "synthetic", "dtype": "bf16 weights, f32 accumulate",
+            "config": {"workload": f"dam break with box obstacle, mDBC, tank height {cl.TANK_HEIGHT} m; held-out "
+                                   f"column {held} m; {t_end} s; judge dp=0.005",
+                       "train_heights": len(heights), "snapshots_per_height": args.clos_snaps,
+                       "samples": int(len(xs)), "epochs": args.clos_epochs},
+            "probe_rmse_pa": err, "probe_rmse_pa_20ms_means": werr, "front_rmse_m": ferr,
+            "wall_s": {"judge_dp0.005": judge["wall_s"], "fine_dp0.01": fine["wall_s"],
+                       "coarse_plain": plain["wall_s"], "coarse_learned": learned["wall_s"]},
+            "particles": {"judge": judge["np"], "fine": fine["np"], "coarse": plain["np"]},
+            "target_met": bool(err["coarse_learned"] <= err["fine_dp0.01"] and speed >= 5.0),
+            "learned_vs_plain_probe_error": err["coarse_learned"] / err["coarse_plain"],
+            "apriori_heldout_mse": {"plain": float(np.mean(th ** 2)), "learned": float(np.mean((th - yh) ** 2))},
+            "train": {"loss_first": float(loss[0]), "loss_last": float(loss[-1]), "data_s": t_data,
+                      "train_s": t_train, "fine_steps": meta["fine_steps"]},
+            "fallback_rows": learned["fallbacks"]}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -276,8 +332,15 @@ def main():
                     help="the reference's -cellmode run option: cells of 2h (default) or h")
     ap.add_argument("--variant", type=int, default=None,
                     help="fluid-row kernel: 0 queued rounds, 1 one thread per particle")
-    ap.add_argument("--workload", default="c2", choices=["c2", "ensemble"],
-                    help="c2: the dam break with obstacle (default); ensemble: the batched cases")
+    ap.add_argument("--workload", default="c2", choices=["c2", "ensemble", "closure"],
+                    help="c2: the dam break with obstacle (default); ensemble: the batched cases; "
+                         "closure: the learned closure against fine runs")
+    ap.add_argument("--clos-heights", type=int, default=32)
+    ap.add_argument("--clos-snaps", type=int, default=8)
+    ap.add_argument("--clos-epochs", type=int, default=25)
+    ap.add_argument("--clos-held", type=float, default=0.3)
+    ap.add_argument("--clos-tend", type=float, default=0.3)
+    ap.add_argument("--clos-seed", type=int, default=5)
     ap.add_argument("--ens-cases", type=int, default=64)
     ap.add_argument("--ens-seed", type=int, default=1)
     ap.add_argument("--ens-scale", type=float, default=1.0, help="scales every case's particle count")
@@ -300,9 +363,9 @@ def main():
             dist.destroy_process_group()
         return
 
-    if args.workload == "ensemble":
+    if args.workload in ("ensemble", "closure"):
         if rank == 0:
-            run_ensemble(args, local)
+            (run_ensemble if args.workload == "ensemble" else run_closure)(args, local)
         if dist:
             dist.destroy_process_group()
         return

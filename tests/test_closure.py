@@ -69,6 +69,13 @@ def test_fine_and_coarse_lattices_nest():
     f = pair.fine
     fp = f.pos[pair.coarse_row_fine_id]
     np.testing.assert_allclose(fp, c.pos[c.npb:], atol=1e-12)
+    # every fine fluid particle in one block of at most 8, whose corner it shares the cell of
+    cnt = np.bincount(pair.fine_block, minlength=c.np - c.npb)
+    assert cnt.sum() == f.np - f.npb and cnt.min() >= 1 and cnt.max() == 8
+    st = {"idp": f.idp, "pos": f.pos, "velrho": f.velrho}
+    m, n = pair.block_mean(st, f.pos)
+    assert np.array_equal(n, cnt)
+    assert np.abs(m[:, :] - c.pos[c.npb:]).max() <= 0.5 * 0.04 + 1e-12
 
 
 # ---- GPU ------------------------------------------------------------------
