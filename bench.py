@@ -150,13 +150,25 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def make_case(dp: float, cellmode: str = "full"):
+def make_case(dp: float, cellmode: str = "full", workload: str = "c2"):
+    """c2: the dam break with the box obstacle and mDBC (tank 1.6x0.67x0.4 m);
+    c3: the large plain run, the geometry scaled x4 (tank 6.4x2.68x1.6 m, a
+    1.6x2.68x0.6 m column, DBC walls)."""
     from dualsphysics_gb300 import casegen as cg
     from dualsphysics_gb300.case import load_case
     tmp = tempfile.mkdtemp(prefix="gbbench_")
-    spec = cg.spec_c2(dp=dp, name="DamC2")
+    name = "DamC3" if workload == "c3" else "DamC2"
+    spec = cg.spec_c3(dp=dp, name=name) if workload == "c3" else cg.spec_c2(dp=dp, name=name)
     cg.write_case(cg.make_dam_break(spec), tmp)
-    return load_case(tmp, "DamC2", cellmode)
+    return load_case(tmp, name, cellmode)
+
+
+def workload_text(args) -> str:
+    if args.workload == "c3":
+        return (f"large plain dam break (tank 6.4x2.68x1.6 m, column 1.6x2.68x0.6 m), DBC walls, dp={args.dp}, "
+                f"Symplectic, Wendland, artificial visc 0.01, DDT2 0.1")
+    return (f"3-D dam break (tank 1.6x0.67x0.4 m, column 0.4x0.67x0.3 m), mDBC + 0.12x0.12x0.45 m box obstacle, "
+            f"dp={args.dp}, Symplectic, Wendland, artificial visc 0.01, DDT2 0.1")
 
 
 def cpu_baseline(cd, stride: int, steps: int = 1):
@@ -188,7 +200,7 @@ def run_reference(args, cd, rank):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 positions)", "data": "synthetic",
-            "config": {"workload": f"3-D dam break, mDBC + box obstacle, dp={args.dp}", "particles": cd.np,
+            "config": {"workload": workload_text(args), "particles": cd.np,
                        "fluid": cd.nfluid, "boundary": cd.npb, "l2": "inputs larger than L2"},
             "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
                              "sample": f"oracle step with 1/{stride} of the interaction rows per step, "
@@ -332,9 +344,10 @@ def main():
                     help="the reference's -cellmode run option: cells of 2h (default) or h")
     ap.add_argument("--variant", type=int, default=None,
                     help="fluid-row kernel: 0 queued rounds, 1 one thread per particle")
-    ap.add_argument("--workload", default="c2", choices=["c2", "ensemble", "closure"],
-                    help="c2: the dam break with obstacle (default); ensemble: the batched cases; "
-                         "closure: the learned closure against fine runs")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "ensemble", "closure"],
+                    help="c2: the dam break with obstacle (default); c3: the large plain run (dp 0.004, "
+                         "~49 M particles); ensemble: the batched cases; closure: the learned closure against "
+                         "fine runs")
     ap.add_argument("--clos-heights", type=int, default=32)
     ap.add_argument("--clos-snaps", type=int, default=8)
     ap.add_argument("--clos-epochs", type=int, default=25)
@@ -346,6 +359,10 @@ def main():
     ap.add_argument("--ens-scale", type=float, default=1.0, help="scales every case's particle count")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload == "c3" and args.dp == 0.0025:
+        args.dp = 0.004
+    if args.workload == "c3" and args.cpu_stride == 16:
+        args.cpu_stride = 128   # a bounded CPU sample of the 49 M-particle state
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -358,7 +375,7 @@ def main():
 
     if args.impl == "reference":
         if rank == 0:
-            run_reference(args, make_case(args.dp, args.cellmode), rank)
+            run_reference(args, make_case(args.dp, args.cellmode, args.workload), rank)
         if dist:
             dist.destroy_process_group()
         return
@@ -373,7 +390,7 @@ def main():
     from dualsphysics_gb300 import _lib
     from dualsphysics_gb300.sph import GbSphSingle
 
-    cd = make_case(args.dp, args.cellmode)
+    cd = make_case(args.dp, args.cellmode, args.workload)
     K, W = args.steps, args.warmup
     s = GbSphSingle(local)
     s.setup(cd)
@@ -455,9 +472,7 @@ def main():
             "metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": t_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (f64 positions and integration)", "data": "synthetic",
-            "config": {"workload": f"3-D dam break (tank 1.6x0.67x0.4 m, column 0.4x0.67x0.3 m), mDBC + "
-                                   f"0.12x0.12x0.45 m box obstacle, dp={args.dp}, Symplectic, Wendland, "
-                                   f"artificial visc 0.01, DDT2 0.1",
+            "config": {"workload": workload_text(args),
                        "particles": cd.np, "fluid": cd.nfluid, "boundary": cd.npb, "cellmode": args.cellmode,
                        "parallelism": "replicas only" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (no flush)"},
