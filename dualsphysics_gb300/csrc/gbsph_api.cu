@@ -190,6 +190,12 @@ int do_forces(gbsph_ctx* ctx) {
   return cuda_check(ctx, cudaGetLastError(), "forces");
 }
 
+}  // namespace
+extern "C" {
+static int motion_table(gbsph_ctx* ctx, const StepState& st, cudaStream_t s);  // defined with the motion entries
+}
+namespace {
+
 // Bytes of the device motion table before the ridp array.
 size_t motion_table_bytes(unsigned nobj) { return 256 + 256 * ((sizeof(MotionObjDev) * nobj + 255) / 256); }
 
@@ -221,12 +227,27 @@ int enqueue_step(gbsph_ctx* ctx) {
     if (c.tboundary == GBSPH_BC_MDBC) gbk::mdbc(c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
     if (int rc = do_forces(ctx)) return rc;
     gbk::dtvariable(c, ctx->a, 2, ctx->stream, &ctx->launches);
+    if (ctx->motion) {
+      // CalcMotion(dt) with the dt this step just computed (JSphCpuSingle.cpp:
+      // 879): read back, advance the motion on the host, upload its table
+      StepState st;
+      CK(cudaMemcpyAsync(&st, ctx->a.st, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream), "motion dt");
+      CK(cudaStreamSynchronize(ctx->stream), "motion sync");
+      st.dtpre = st.dt_var;
+      if (int rc = motion_table(ctx, st, ctx->stream)) return rc;
+    }
     if (c.tshift) gbk::run_shifting(c, ctx->a, ctx->cap, &ctx->a.st->dt_var, 1.0, ctx->stream, &ctx->launches);
     ctx->verletstep++;
     const int euler = !(ctx->verletstep < c.verletsteps);
     if (euler) ctx->verletstep = 0;
     gbk::verlet_step(c, ctx->a, ctx->cap, &ctx->a.st->dt_var, euler, ctx->stream, &ctx->launches);
     gbk::step_end(ctx->a, 0, ctx->stream, &ctx->launches);
+    if (ctx->motion) {  // RunMotion(dt), before the divide that ends the step
+      char* mb = (char*)ctx->mot_buf;
+      gbk::motion_move(c, ctx->a, (const MotionStep*)mb, (const MotionObjDev*)(mb + 256), ctx->mot_nobj,
+                       (unsigned*)(mb + motion_table_bytes(ctx->mot_nobj)), ctx->mot_idmin, ctx->mot_nmoving,
+                       ctx->cap, ctx->stream, &ctx->launches);
+    }
   }
   return do_divide(ctx);
 }
@@ -531,7 +552,6 @@ int gbsph_set_motion(gbsph_ctx* ctx, gbsph_motion* m) {
   ctx->motion = nullptr;
   ctx->mot_nobj = ctx->mot_idmin = ctx->mot_nmoving = 0;
   if (!m) return GBSPH_OK;
-  if (ctx->c.tstep != GBSPH_STEP_SYMPLECTIC) return set_err(ctx, GBSPH_EINVAL, "moving boundaries need Symplectic");
   const unsigned n = gbmotion::object_count(m);
   const gbsph_motion_object* info = gbmotion::objects(m);
   unsigned long long lo = ~0ull, hi = 0;
@@ -557,7 +577,7 @@ int gbsph_set_motion(gbsph_ctx* ctx, gbsph_motion* m) {
 
 int gbsph_step(gbsph_ctx* ctx) {
   if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
-  if (ctx->motion)
+  if (ctx->motion && ctx->c.tstep == GBSPH_STEP_SYMPLECTIC)  // Verlet advances it inside the step
     if (int rc = motion_prepare(ctx)) return rc;
   return enqueue_step(ctx);
 }
@@ -569,7 +589,7 @@ int gbsph_run(gbsph_ctx* ctx, unsigned nsteps, int use_graph) {
   // divide and a host-side Euler counter) run eagerly.
   if (!use_graph || ctx->c.tstep != GBSPH_STEP_SYMPLECTIC) {
     for (unsigned i = 0; i < nsteps; i++) {
-      if (ctx->motion)
+      if (ctx->motion && ctx->c.tstep == GBSPH_STEP_SYMPLECTIC)
         if (int rc = motion_prepare(ctx)) return rc;
       if (int rc = enqueue_step(ctx)) return rc;
     }
@@ -1226,7 +1246,7 @@ int gbsph_ensemble_run(gbsph_ensemble* e, unsigned nsteps, int use_graph) {
     for (unsigned k = 0; k < nsteps; k++)
       for (size_t i = 0; i < e->cases.size(); i++) {
         gbsph_ctx* c = e->cases[i];
-        int rc = c->motion ? motion_prepare(c) : GBSPH_OK;
+        int rc = (c->motion && c->c.tstep == GBSPH_STEP_SYMPLECTIC) ? motion_prepare(c) : GBSPH_OK;
         if (!rc) rc = enqueue_step(c);
         if (rc) return ens_err(e, rc, "case " + std::to_string(i) + ": " + c->err);
       }

@@ -338,8 +338,10 @@ int gbsph_motion_process(gbsph_motion* m, double timestep, double dt, gbsph_moti
  * the host, and after the step's update moves the objects' particles
  * (position by UpdatePos, velocity set to the motion's, normals rotated by a
  * matrix motion) and marks the boundary changed, so the next divide is full.
- * gbsph_run's multi-step graph (mode 2) is not used with a motion.  Verlet
- * steps with a motion are not supported (GBSPH_EINVAL).  The motion stays
+ * gbsph_run's multi-step graph (mode 2) is not used with a motion.  A Verlet
+ * step advances the motion inside the step, with the dt it has just computed
+ * (one read-back of the step state), so Verlet steps with a motion are not
+ * captured in graphs.  The motion stays
  * owned by the caller and must outlive the attachment. */
 int gbsph_set_motion(gbsph_ctx* ctx, gbsph_motion* m);
 

@@ -188,7 +188,9 @@ class OracleCpu : public JSphCpuSingle{
     DumpState("s1"); DumpDivide("s1");
   }
 
-  // First Verlet step piece by piece (ComputeStep_Ver, JSphCpuSingle.cpp:873-892).
+  // First Verlet step piece by piece (ComputeStep_Ver, JSphCpuSingle.cpp:873-892;
+  // with moving boundaries, CalcMotion after DtVariable and RunMotion after
+  // the update, as the Run loop does, JSphCpuSingle.cpp:1191-1194).
   void FirstStepVerlet(){
     Meta("s0");
     DumpState("s0"); DumpDivide("s0");
@@ -199,12 +201,14 @@ class OracleCpu : public JSphCpuSingle{
     Interaction_Forces(InterStep);
     DumpForces("s0pred");
     const double dt=DtVariable(true);
+    if(CaseNmoving){ CalcMotion(dt); DumpMotion(dt); }
     char tx[256]; sprintf(tx,"dt=%.17g\ndt_p=%.17g\n",dt,dt);
     Meta("s0pred",tx);
     ShiftAndDump(dt,"s0predsh");
     ComputeVerlet(dt);
     PosInteraction_Forces();
     DumpState("s0pre");
+    if(CaseNmoving)RunMotion(dt);
     TimeStep+=dt; Nstep++;
     RunCellDivide(true);
     DtList.push_back(dt);

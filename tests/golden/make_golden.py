@@ -41,6 +41,7 @@ CASES = {
     "ddt2f_d04": (lambda: cg.spec_c2(dp=0.04, name="ddt2f_d04", density_dt=3, init_vel=0.02, seed=17), 10),
     "half_d04": (lambda: cg.spec_c1(dp=0.04, name="half_d04", init_vel=0.02, seed=19), 10, ["-cellmode:half"]),
     "mov_d04": (lambda: spec_moving(), 20),
+    "movv_d04": (lambda: spec_moving(name="movv_d04", step_algorithm=1, verlet_steps=5, seed=41), 20),
     # standard shifting: Full with the free-surface threshold (Symplectic), and
     # NoBound without it (Verlet)
     "shift_d04": (lambda: cg.spec_c1(dp=0.04, name="shift_d04", init_vel=0.05, seed=29,
@@ -66,9 +67,9 @@ MOVING_TANK = [
 ]
 
 
-def spec_moving():
-    return cg.spec_c1(dp=0.04, name="mov_d04", motion=MOVING_TANK, posmin_x="default - 0.1",
-                      posmax_x="default + 0.1", init_vel=0.02, seed=23)
+def spec_moving(name: str = "mov_d04", seed: int = 23, **kw):
+    return cg.spec_c1(dp=0.04, name=name, motion=MOVING_TANK, posmin_x="default - 0.1",
+                      posmax_x="default + 0.1", init_vel=0.02, seed=seed, **kw)
 
 
 GAUGE_CASES = ("dbc_d04", "mdbc_d04")

@@ -11,9 +11,10 @@ application to the moving particles (RunMotion: MoveLinBound / MoveMatBound).
   MATRIX_ATOL (a few ulps).  Semantics of events, chaining and rotations on
   hand-made motions; the loader reads moving blocks and the motion XML.
 * GPU: the sloshing-tank case stepped with its motion matches the
-  reference's run: dt of every step, the moving particles' positions (the
-  motion is independent of the flow, up to the dt it is given) and velocities,
-  and the whole state within the multi-step tolerance.
+  reference's run, with Symplectic and with Verlet (tests/golden/movv_d04.npz):
+  dt of every step, the moving particles' positions (the motion is
+  independent of the flow, up to the dt it is given) and velocities, and the
+  whole state within the multi-step tolerance.
 """
 import ctypes as C
 
@@ -43,10 +44,11 @@ def _process(m, nobj, t, dt):
     return rc, out
 
 
-def test_host_motion_matches_reference_dump():
-    cd = G.load_generated("mov_d04")
-    g = G.golden("mov_d04")["motion"]
-    assert len(g) == G.case_nsteps("mov_d04") + 1
+@pytest.mark.parametrize("name", ["mov_d04", "movv_d04"])
+def test_host_motion_matches_reference_dump(name):
+    cd = G.load_generated(name)
+    g = G.golden(name)["motion"]
+    assert len(g) == G.case_nsteps(name) + 1
     m = _motion(cd.motion)
     kinds = set()
     for r in g:
@@ -139,10 +141,13 @@ def test_loader_reads_moving_blocks_and_motion():
 
 # ---- GPU ------------------------------------------------------------------
 @pytest.mark.gpu
-def test_moving_tank_matches_reference_run():
+@pytest.mark.parametrize("name", ["mov_d04", "movv_d04"])
+def test_moving_tank_matches_reference_run(name):
+    """Symplectic (mov_d04) and Verlet (movv_d04, the motion advanced inside
+    the step with the dt the step computes)."""
     from dualsphysics_gb300.sph import GbSphSingle
-    g = G.golden("mov_d04")
-    cd = G.load_generated("mov_d04")
+    g = G.golden(name)
+    cd = G.load_generated(name)
     s = GbSphSingle(0)
     s.setup(cd)
     n = len(g["dtlist"])
