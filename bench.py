@@ -150,6 +150,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def replica_throughput(ms: float, K: int, dist=None, world: int = 1) -> tuple[float, float]:
+    """N independent replicas (one per rank, no data-path collective): each
+    rank timed its own K steps in `ms`; the job took as long as the slowest
+    rank (a MAX all-reduce over the ranks), and the whole-job value is
+    world * K steps over that time.  Returns (t_max in ms, steps/s)."""
+    t_max = ms
+    if dist is not None and world > 1:
+        import torch
+        tt = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    return t_max, world * K / (t_max / 1e3)
+
+
 def make_case(dp: float, cellmode: str = "full", workload: str = "c2"):
     """c2: the dam break with the box obstacle and mDBC (tank 1.6x0.67x0.4 m);
     c3: the large plain run, the geometry scaled x4 (tank 6.4x2.68x1.6 m, a
@@ -415,13 +429,7 @@ def main():
     launches = s.launch_count() - l0
     kms = s.profile_read()
     s.profile(0)
-    t_max = ms
-    if dist:
-        import torch
-        tt = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    steps_per_s = world * K / (t_max / 1e3)
+    t_max, steps_per_s = replica_throughput(ms, K, dist, world)
     pis_per_step = 2.0 * (pi["real_fluid"] + pi["real_bound"])
     info = s.divinfo()
     # roofline of the fluid Interaction_Forces kernel
