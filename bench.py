@@ -301,16 +301,13 @@ def run_closure(args, local: int = 0):
     t0 = time.perf_counter()
     xs, ts, meta = cl.paired_samples(heights, dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
     t_data = time.perf_counter() - t0
-    order = rng.permutation(len(xs))
-    tr = cl.Trainer(cl.init_params(args.clos_seed), local)
-    tr.set_data(xs[order], ts[order])
     t1 = time.perf_counter()
-    loss = tr.train(args.clos_epochs, 1024, 1e-3)
+    p, w, loss = cl.train_closure(xs, ts, epochs=args.clos_epochs, seed=args.clos_seed, device=local)
     t_train = time.perf_counter() - t1
-    _, w = tr.params()
     xh, th, _ = cl.paired_samples([held], dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
-    yh = tr.infer(xh)
-    tr.close()
+    ev = cl.Trainer(cl.from_bf16(w), local)     # the deployed BF16 weights
+    yh = ev.infer(xh)
+    ev.close()
     coarse = cl._load(cl.spec(0.02, held, "HeldC"))
     hc = coarse.params.h
     judge = cl.run_with_probes(cl._load(cl.spec(0.005, held, "HeldJ")), t_end, dtp, device=local, mesh_h=hc)
@@ -364,7 +361,7 @@ def main():
                          "fine runs")
     ap.add_argument("--clos-heights", type=int, default=32)
     ap.add_argument("--clos-snaps", type=int, default=8)
-    ap.add_argument("--clos-epochs", type=int, default=25)
+    ap.add_argument("--clos-epochs", type=int, default=40)
     ap.add_argument("--clos-held", type=float, default=0.3)
     ap.add_argument("--clos-tend", type=float, default=0.3)
     ap.add_argument("--clos-seed", type=int, default=5)

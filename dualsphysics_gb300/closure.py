@@ -136,6 +136,47 @@ class Trainer:
             pass
 
 
+def fold_standardisation(p: np.ndarray, mu_x, sd_x, sd_t) -> np.ndarray:
+    """Parameters of a network trained on standardised data ((x - mu_x)/sd_x
+    in, t/sd_t out) rewritten to take raw features and give raw targets: the
+    input scaling goes into W0 and b0, the output scaling into W3 and b3."""
+    q = np.array(p, np.float64)
+    (w0, b0, _, _), _, _, (w3, b3, _, _) = layer_slices()
+    W0 = q[w0].reshape(NHID, NFEAT) / sd_x[None, :]
+    q[b0] = q[b0] - W0 @ mu_x
+    q[w0] = W0.ravel()
+    q[w3] = (q[w3].reshape(NOUT, NHID) * sd_t[:, None]).ravel()
+    q[b3] = q[b3] * sd_t
+    return q.astype(np.float32)
+
+
+def train_closure(x: np.ndarray, t: np.ndarray, epochs: int = 40, batch: int = 1024, lr: float = 1e-3,
+                  seed: int = 0, device: int = 0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Trains on standardised features and targets (zero mean and unit
+    variance per column; constant columns left as they are), in a seeded
+    shuffled order, and returns the folded FP32 parameters, their BF16 bits
+    and the per-epoch losses (in standardised units)."""
+    x = np.asarray(x, np.float32)
+    t = np.asarray(t, np.float32)
+    mu = x.mean(axis=0).astype(np.float64)
+    sd = x.std(axis=0).astype(np.float64)
+    const = sd < 1e-6
+    mu[const], sd[const] = 0.0, 1.0
+    st = np.maximum(t.std(axis=0).astype(np.float64), 1e-6)
+    order = np.random.default_rng(seed).permutation(len(x))
+    xs = ((x[order] - mu) / sd).astype(np.float32)
+    ts = (t[order] / st).astype(np.float32)
+    tr = Trainer(init_params(seed), device)
+    try:
+        tr.set_data(xs, ts)
+        loss = tr.train(epochs, batch, lr)
+        master, _ = tr.params()
+    finally:
+        tr.close()
+    p = fold_standardisation(master, mu, sd, st)
+    return p, to_bf16(p), loss
+
+
 def attach(sim: GbSphSingle, w_bf16: np.ndarray | None, limit: float = 0.2) -> None:
     """Turns the closure on (or off with None) for every later step of `sim`."""
     w = None if w_bf16 is None else np.ascontiguousarray(w_bf16, np.uint16)

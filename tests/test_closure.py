@@ -62,6 +62,17 @@ def test_bf16_rounding_matches_torch():
     np.testing.assert_array_equal(ours, ref)
 
 
+def test_standardisation_folds_into_the_first_and_last_layers():
+    rng = np.random.default_rng(3)
+    x = rng.normal(2.0, 5.0, (50, cl.NFEAT))
+    mu, sd = x.mean(0), x.std(0) + 0.5
+    st = np.array([2.0, 0.5, 3.0])
+    p = cl.init_params(4, out_scale=1.0)
+    y_std = co.forward(p.astype(np.float64), (x - mu) / sd)[-1] * st
+    y_raw = co.forward(cl.fold_standardisation(p, mu, sd, st).astype(np.float64), x)[-1]
+    np.testing.assert_allclose(y_raw, y_std, rtol=2e-5, atol=2e-5 * np.abs(y_std).max())
+
+
 def test_fine_and_coarse_lattices_nest():
     pair = cl.Pair(0.25, dp_fine=0.04, tag="N")
     c = pair.coarse
@@ -180,12 +191,9 @@ def test_trained_closure_lowers_the_held_out_acceleration_error():
     xs, ts, meta = cl.paired_samples([0.22, 0.28, 0.34], dp_fine=0.02, t_end=0.12, n_snap=4)
     xh, th, _ = cl.paired_samples([0.31], dp_fine=0.02, t_end=0.12, n_snap=4)
     assert meta["snapshots"] == 12 and len(xs) > 5000
-    rng = np.random.default_rng(0)
-    o = rng.permutation(len(xs))
-    tr = cl.Trainer(cl.init_params(1))
-    tr.set_data(xs[o], ts[o])
-    loss = tr.train(epochs=60, batch=1024, lr=1e-3)
+    p, w, loss = cl.train_closure(xs, ts, epochs=60, seed=1)
     assert loss[-1] < loss[0]
+    tr = cl.Trainer(cl.from_bf16(w))           # the folded BF16 weights the step would use
     yh = tr.infer(xh)
     plain = float(np.mean(th ** 2))                  # the coarse run's error with no correction
     learned = float(np.mean((th - yh) ** 2))
