@@ -80,6 +80,10 @@ class CaseSpec:
     # declares XPeriodicIncY=0; init_vel_x gives the fluid a uniform x velocity
     periodic_x: bool = False
     init_vel_x: float = 0.0
+    # periodic in y as well (or alone): no walls on the y sides, the fluid fills
+    # the period [0, Ly), YPeriodicIncX=0; init_vel_y a uniform y velocity
+    periodic_y: bool = False
+    init_vel_y: float = 0.0
 
 
 @dataclass
@@ -118,10 +122,10 @@ def make_dam_break(spec: CaseSpec) -> Case:
     dp = spec.dp
     nx, ny, nz = (_nsteps(v, dp) for v in spec.tank)
     # --- walls: lattice i in [-3,nx+3], j in [-3,ny+3], k in [-3,nz] minus interior
-    if spec.periodic_x:  # one period [0, nx*dp) of floor and side walls
-        wl = _lattice((0, nx - 1), (-3, ny + 3), (-3, nz))
-    else:
-        wl = _lattice((-3, nx + 3), (-3, ny + 3), (-3, nz))
+    # one period [0, n*dp) of the walls along each periodic axis
+    wx = (0, nx - 1) if spec.periodic_x else (-3, nx + 3)
+    wy = (0, ny - 1) if spec.periodic_y else (-3, ny + 3)
+    wl = _lattice(wx, wy, (-3, nz))
     inside = ((wl[:, 0] >= 0) & (wl[:, 0] <= nx) & (wl[:, 1] >= 0) & (wl[:, 1] <= ny) & (wl[:, 2] >= 0))
     wall = wl[~inside].astype(np.float64) * dp
     # --- obstacle: solid lattice block on the floor
@@ -135,6 +139,8 @@ def make_dam_break(spec: CaseSpec) -> Case:
     fx, fy, fz = (_nsteps(v, dp) for v in spec.column)
     if spec.periodic_x:
         fx = nx - 1
+    if spec.periodic_y:
+        fy = ny - 1
     fl = _lattice((0, fx), (0, fy), (0, fz)).astype(np.float64) * dp
     if spec.obstacle is not None and len(obst):
         lo, hi = obst.min(axis=0) - 0.5 * dp, obst.max(axis=0) + 0.5 * dp
@@ -201,6 +207,8 @@ def make_dam_break(spec: CaseSpec) -> Case:
         vel[npb:] = rng.uniform(-spec.init_vel, spec.init_vel, size=(nf, 3)).astype(np.float32)
     if spec.init_vel_x and nf:
         vel[npb:, 0] += np.float32(spec.init_vel_x)
+    if spec.init_vel_y and nf:
+        vel[npb:, 1] += np.float32(spec.init_vel_y)
     return Case(spec=spec, pos=pos, vel=vel, rhop=rhop.astype(np.float32),
                 idp=np.arange(n, dtype=np.uint32), code=code, boundnor=boundnor, blocks=blocks,
                 npb=npb, h=h, b=b, mass=mass)
@@ -256,6 +264,8 @@ def write_case(case: Case, dirpath: str) -> tuple[str, str]:
         params.pop("SlipMode")
     if s.periodic_x:
         params["XPeriodicIncY"] = 0
+    if s.periodic_y:
+        params["YPeriodicIncX"] = 0
     params.update(s.extra_params)
     lines = ['<?xml version="1.0" encoding="UTF-8" ?>',
              '<case app="dualsphysics_gb300.casegen">',

@@ -363,8 +363,13 @@ int main(int argc, char** argv) {
     return 0;
   }
   gbsph_ctx* ctx = nullptr;
-  // room for the periodic copies: each periodic axis can copy every particle once
-  const unsigned cap = cs.np * (1u + (c.peri[0] ? 1u : 0u) + (c.peri[1] ? 1u : 0u) + (c.peri[2] ? 1u : 0u));
+  // room for the periodic copies: at most 2^k - 1 per particle over k periodic
+  // axes, and the copies of the last divide are still held while the new ones
+  // are made
+  const unsigned nperi = (c.peri[0] ? 1u : 0u) + (c.peri[1] ? 1u : 0u) + (c.peri[2] ? 1u : 0u);
+  const unsigned long long capl = (unsigned long long)cs.np * (1ull + 2ull * ((1ull << nperi) - 1ull));
+  if (capl > 0x7fffffffull) return fail("gbsph_create", "the periodic copies would not fit 2^31 particles");
+  const unsigned cap = (unsigned)capl;
   int rc = gbsph_create(&c, cap, device, &ctx);
   if (rc != GBSPH_OK) return fail("gbsph_create", "code " + std::to_string(rc));
   rc = gbsph_upload(ctx, cs.np, cs.npb, cs.pos.data(), cs.velrho.data(), cs.idp.data(), cs.code.data(),

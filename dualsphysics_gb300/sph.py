@@ -34,9 +34,12 @@ CODE_MASKSPECIAL = 0xE000
 
 def default_capacity(cd: CaseData) -> int:
     """Particles to allocate for a case: its particles, plus room for the
-    periodic copies (each periodic axis can copy every particle once)."""
+    periodic copies.  A particle has at most 2^k - 1 copies over k periodic
+    axes (one per axis and per combination of axes, the period being longer
+    than twice the kernel size), and while RunPeriodic appends the new copies
+    the copies of the last divide are still in the arrays: np * (1 + 2 (2^k - 1))."""
     nperi = sum(1 for k in cd.params.peri if k)
-    return int(cd.np * (1 + nperi))
+    return int(cd.np * (1 + 2 * ((1 << nperi) - 1)))
 
 
 def normal_rows(code: np.ndarray) -> np.ndarray:

@@ -51,6 +51,11 @@ CASES = {
     # periodic in x: a channel whose fluid moves at 2 m/s across the periodic faces
     "peri_d04": (lambda: cg.spec_c1(dp=0.04, name="peri_d04", tank=(0.8, 0.4, 0.3), column=(0.8, 0.4, 0.2),
                                     periodic_x=True, init_vel_x=2.0, init_vel=0.02, seed=37), 30),
+    # periodic in x and y: a floor only, the fluid moving diagonally across both
+    # pairs of faces; copies made for x are copied again for y
+    "perixy_d04": (lambda: cg.spec_c1(dp=0.04, name="perixy_d04", tank=(0.6, 0.4, 0.3), column=(0.6, 0.4, 0.2),
+                                      periodic_x=True, periodic_y=True, init_vel_x=1.5, init_vel_y=-1.0,
+                                      init_vel=0.02, seed=43), 30),
 }
 
 # A sloshing tank: the walls move through a chain of movements -- sinusoidal

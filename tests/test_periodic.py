@@ -39,7 +39,8 @@ def test_periodic_configuration_matches_reference():
 
 def test_default_capacity_and_normal_rows():
     cd = G.load_generated("peri_d04")
-    assert default_capacity(cd) == 2 * cd.np
+    assert default_capacity(cd) == 3 * cd.np
+    assert default_capacity(G.load_generated("perixy_d04")) == 7 * G.load_generated("perixy_d04").np
     assert default_capacity(G.load_generated("dbc_d04")) == G.load_generated("dbc_d04").np
     code = np.array([0x1800, 0x3800, 0x0000, 0x2000, 0x5800], np.uint16)
     assert normal_rows(code).tolist() == [True, False, True, False, False]
@@ -56,11 +57,21 @@ def test_reference_run_wraps_particles():
 
 
 # ---- GPU ------------------------------------------------------------------
+def _wrapped(pos, pos0, size):
+    """Particles that crossed a periodic face: moved by more than half a period."""
+    d = np.abs(pos - pos0)
+    return np.any(d[:, :2] > 0.5 * np.asarray(size[:2]), axis=1)
+
+
 @pytest.mark.gpu
-def test_periodic_channel_matches_reference_run():
+@pytest.mark.parametrize("name", ["peri_d04", "perixy_d04"])
+def test_periodic_channel_matches_reference_run(name):
+    """x-periodic channel, and the xy-periodic box whose copies made for x
+    are copied again for y."""
     from dualsphysics_gb300.sph import GbSphSingle
-    g = G.golden("peri_d04")
-    cd = G.load_generated("peri_d04")
+    g = G.golden(name)
+    cd = G.load_generated(name)
+    size = list(_lib.config(cd.params).maprealsize)
     s = GbSphSingle(0)
     s.setup(cd)
     dts = []
@@ -80,16 +91,22 @@ def test_periodic_channel_matches_reference_run():
     np.testing.assert_array_equal(st["idp"][keep][o1], g["end_idp"][rkeep][o2])
     pos, rpos = st["pos"][keep][o1], g["end_pos"][rkeep][o2]
     vr, rvr = st["velrho"][keep][o1], g["end_velrho"][rkeep][o2]
-    wrapped = pos[:, 0] < cd.pos[:, 0] - 0.5
-    assert wrapped.sum() > 0 and (wrapped == (rpos[:, 0] < cd.pos[:, 0] - 0.5)).all()
+    wrapped = _wrapped(pos, cd.pos, size)
+    assert wrapped.sum() > 0 and (wrapped == _wrapped(rpos, cd.pos, size)).all()
     np.testing.assert_allclose(pos, rpos, atol=1e-6)
     np.testing.assert_allclose(vr[:, :3], rvr[:, :3], atol=2e-3)
     np.testing.assert_allclose(vr[:, 3], rvr[:, 3], rtol=1e-4)
-    # each copy sits one period away from its source
+    # each copy sits whole periods away from its source, along the periodic axes
     cp = ~keep
     src = {i: p for i, p in zip(st["idp"][keep], st["pos"][keep])}
-    d = np.array([st["pos"][k] - src[i] for k, i in zip(np.nonzero(cp)[0], st["idp"][cp])])
-    assert np.allclose(np.abs(d[:, 0]), 0.8, atol=1e-12) and np.abs(d[:, 1:]).max() < 1e-12
+    d = np.abs(np.array([st["pos"][k] - src[i] for k, i in zip(np.nonzero(cp)[0], st["idp"][cp])]))
+    for k in range(2):
+        on = cd.params.peri[k] != 0
+        ok = (d[:, k] < 1e-12) | (on & (np.abs(d[:, k] - size[k]) < 1e-12))
+        assert ok.all(), k
+    assert (d[:, 2] < 1e-12).all() and (d[:, :2].max(axis=1) > 0).all()
+    if name == "perixy_d04":   # copies of copies: one period along x and one along y
+        assert ((np.abs(d[:, 0] - size[0]) < 1e-12) & (np.abs(d[:, 1] - size[1]) < 1e-12)).any()
 
 
 @pytest.mark.gpu
