@@ -658,7 +658,28 @@ __global__ void __launch_bounds__(128) k_mdbc(gbsph_consts c, DevArrays a) {
   if (p1 >= d.npbok) return;
   const float4 bn = a.boundnor[p1];
   if (bn.x == 0.f && bn.y == 0.f && bn.z == 0.f) return;
-  const double gx = a.px[p1] + (double)bn.x, gy = a.py[p1] + (double)bn.y, gz = a.pz[p1] + (double)bn.z;
+  double gx = a.px[p1] + (double)bn.x, gy = a.py[p1] + (double)bn.y, gz = a.pz[p1] + (double)bn.z;
+  // the ghost node taken back into the domain across periodic faces
+  // (UpdatePeriodicPos, JSphCpu_mdbc.cpp:50, JSph.cpp:2079-2101)
+  if (c.peri[0] || c.peri[1] || c.peri[2]) {
+    double dx = __dsub_rn(gx, c.maprealposmin[0]), dy = __dsub_rn(gy, c.maprealposmin[1]),
+           dz = __dsub_rn(gz, c.maprealposmin[2]);
+    const bool out = dx != dx || dy != dy || dz != dz || dx < 0 || dy < 0 || dz < 0 || dx >= c.maprealsize[0] ||
+                     dy >= c.maprealsize[1] || dz >= c.maprealsize[2];
+    if (out) {
+      for (int k = 0; k < 3; k++) {
+        if (!c.peri[k]) continue;
+        const double* inc = c.periinc + 3 * k;
+        if ((k == 0 ? dx : k == 1 ? dy : dz) < 0) {
+          dx = __dsub_rn(dx, inc[0]); dy = __dsub_rn(dy, inc[1]); dz = __dsub_rn(dz, inc[2]);
+        }
+        if ((k == 0 ? dx : k == 1 ? dy : dz) >= c.maprealsize[k]) {
+          dx = __dadd_rn(dx, inc[0]); dy = __dadd_rn(dy, inc[1]); dz = __dadd_rn(dz, inc[2]);
+        }
+      }
+      gx = __dadd_rn(dx, c.maprealposmin[0]); gy = __dadd_rn(dy, c.maprealposmin[1]); gz = __dadd_rn(dz, c.maprealposmin[2]);
+    }
+  }
   const double sc = (double)c.scell;
   // cell of the ghost node, truncated toward zero as int() does (JCellSearch_inline.h:59-61)
   const int gcx = (int)((gx - c.domposmin[0]) / sc), gcy = (int)((gy - c.domposmin[1]) / sc),

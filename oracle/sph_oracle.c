@@ -526,6 +526,24 @@ static float mdbc_solve(const double A[4][4], float rhop1, const float grad[3], 
   return (rhofinal != FLT_MAX ? rhofinal : rhopzero);
 }
 
+/* JSph::UpdatePeriodicPos (JSph.cpp:2079-2101): a position outside the real
+ * domain comes back across the periodic faces by the axis increments. */
+static void update_periodic_pos(const orc_ctes* c, double p[3]) {
+  double dx = p[0] - c->maprealposmin[0], dy = p[1] - c->maprealposmin[1], dz = p[2] - c->maprealposmin[2];
+  const int out = (dx != dx || dy != dy || dz != dz || dx < 0 || dy < 0 || dz < 0 || dx >= c->maprealsize[0] ||
+                   dy >= c->maprealsize[1] || dz >= c->maprealsize[2]);
+  if (!out) return;
+  for (int k = 0; k < 3; k++) {
+    if (!c->peri[k]) continue;
+    const double* inc = c->periinc + 3 * k;
+    if ((k == 0 ? dx : k == 1 ? dy : dz) < 0) { dx -= inc[0]; dy -= inc[1]; dz -= inc[2]; }
+    if ((k == 0 ? dx : k == 1 ? dy : dz) >= c->maprealsize[k]) { dx += inc[0]; dy += inc[1]; dz += inc[2]; }
+  }
+  p[0] = dx + c->maprealposmin[0];
+  p[1] = dy + c->maprealposmin[1];
+  p[2] = dz + c->maprealposmin[2];
+}
+
 void orc_mdbc_correction(const orc_ctes* c, const orc_div* d, const unsigned* begincell, unsigned n,
                          const double* pos, const uint16_t* code, const float* boundnor, float* velrho,
                          int nthreads) {
@@ -537,7 +555,9 @@ void orc_mdbc_correction(const orc_ctes* c, const orc_div* d, const unsigned* be
     const float* bn = boundnor + 3 * (size_t)p1;
     if (bn[0] == 0 && bn[1] == 0 && bn[2] == 0) continue;
     const double* ps = pos + 3 * (size_t)p1;
-    const double gp[3] = {ps[0] + (double)bn[0], ps[1] + (double)bn[1], ps[2] + (double)bn[2]};
+    double gp[3] = {ps[0] + (double)bn[0], ps[1] + (double)bn[1], ps[2] + (double)bn[2]};
+    /* the ghost node taken back into the domain (JSphCpu_mdbc.cpp:50) */
+    if (c->peri[0] || c->peri[1] || c->peri[2]) update_periodic_pos(c, gp);
     float rhop1 = 0;
     float grad[3] = {0, 0, 0};
     double A[4][4];

@@ -53,6 +53,12 @@ CASES = {
                                     periodic_x=True, init_vel_x=2.0, init_vel=0.02, seed=37), 30),
     # periodic in x and y: a floor only, the fluid moving diagonally across both
     # pairs of faces; copies made for x are copied again for y
+    # the channel with Verlet (periodic copies are moved by the update), and with mDBC (copies carry their normals)
+    "periv_d04": (lambda: cg.spec_c1(dp=0.04, name="periv_d04", tank=(0.8, 0.4, 0.3), column=(0.8, 0.4, 0.2),
+                                     periodic_x=True, init_vel_x=2.0, init_vel=0.02, seed=47, step_algorithm=1,
+                                     verlet_steps=5), 30),
+    "perim_d04": (lambda: cg.spec_c1(dp=0.04, name="perim_d04", tank=(0.8, 0.4, 0.3), column=(0.8, 0.4, 0.2),
+                                     periodic_x=True, init_vel_x=2.0, init_vel=0.02, seed=53, boundary="mdbc"), 30),
     "perixy_d04": (lambda: cg.spec_c1(dp=0.04, name="perixy_d04", tank=(0.6, 0.4, 0.3), column=(0.6, 0.4, 0.2),
                                       periodic_x=True, periodic_y=True, init_vel_x=1.5, init_vel_y=-1.0,
                                       init_vel=0.02, seed=43), 30),
