@@ -59,6 +59,10 @@ CASES = {
                                      verlet_steps=5), 30),
     "perim_d04": (lambda: cg.spec_c1(dp=0.04, name="perim_d04", tank=(0.8, 0.4, 0.3), column=(0.8, 0.4, 0.2),
                                      periodic_x=True, init_vel_x=2.0, init_vel=0.02, seed=53, boundary="mdbc"), 30),
+    # the channel with standard shifting (sums over copies near the faces)
+    "peris_d04": (lambda: cg.spec_c1(dp=0.04, name="peris_d04", tank=(0.8, 0.4, 0.3), column=(0.8, 0.4, 0.2),
+                                     periodic_x=True, init_vel_x=2.0, init_vel=0.02, seed=59,
+                                     extra_params={"Shifting": 3, "ShiftCoef": -2, "ShiftTFS": 2.75}), 30),
     "perixy_d04": (lambda: cg.spec_c1(dp=0.04, name="perixy_d04", tank=(0.6, 0.4, 0.3), column=(0.6, 0.4, 0.2),
                                       periodic_x=True, periodic_y=True, init_vel_x=1.5, init_vel_y=-1.0,
                                       init_vel=0.02, seed=43), 30),
