@@ -279,6 +279,8 @@ def run_ensemble(args, local: int = 0):
             "speedup_vs_sequential": t_seq / t_graph,
             "launches_per_replay": ens.launches_per_step(),
             "tuner": {"choices": [[t["variant"][t["best"]], t["bsize"][t["best"]]] for t in tuned],
+                      "sort_bits": [t["sort_bits"] for t in tuned],
+                      "sort_ms_8_11": [[round(x, 4) for x in t["sort_ms"]] for t in tuned],
                       "candidates": [[v, b] for v, b in zip(tuned[0]["variant"], tuned[0]["bsize"])],
                       "ms": [[round(x, 4) for x in t["ms"]] for t in tuned]},
             "clocks": clk.summary()}

@@ -31,7 +31,8 @@ struct gbsph_ctx {
   void* arena = nullptr;
   size_t arena_bytes = 0;
   DevArrays a;
-  unsigned npasses = 1;
+  unsigned keybits = 8;   // bits of the largest box key (2 Nct + 6)
+  int sort_bits = 8;      // digit width of the radix sort passes (8 or 11)
   unsigned nctt_cap = 0;
   bool uploaded = false;
   int verletstep = 0;
@@ -147,7 +148,7 @@ size_t layout(gbsph_ctx* ctx, void* base) {
   a.keys = k.take<unsigned>(n); a.keys2 = k.take<unsigned>(n);
   a.vals = k.take<unsigned>(n); a.vals2 = k.take<unsigned>(n);
   const size_t ntiles = (n + 2047) / 2048;
-  a.hist = k.take<unsigned>(ntiles * 256 + 256 + 1);  // tile counts + digit totals
+  a.hist = k.take<unsigned>(ntiles * 2048 + 2048 + 1);  // tile counts + digit totals, digits of up to 11 bits
   a.begincell = k.take<unsigned>(ctx->nctt_cap + 1);
   a.div = k.take<DivState>(1);
   a.st = k.take<StepState>(1);
@@ -168,7 +169,7 @@ void reset_graph(gbsph_ctx* ctx) {
 }
 
 int do_divide(gbsph_ctx* ctx) {
-  gbk::divide(ctx->c, ctx->a, ctx->cap, ctx->npasses, ctx->stream, &ctx->launches);
+  gbk::divide(ctx->c, ctx->a, ctx->cap, ctx->keybits, ctx->sort_bits, ctx->stream, &ctx->launches);
   ctx->swaps++;
   return cuda_check(ctx, cudaGetLastError(), "divide");
 }
@@ -278,8 +279,13 @@ int gbsph_create(const gbsph_consts* c, unsigned capacity, int device, gbsph_ctx
   ctx->nctt_cap = (unsigned)(2ull * maxnct + 6);
   unsigned bits = 1;
   while ((1ull << bits) < ctx->nctt_cap) bits++;
-  ctx->npasses = (bits + 7) / 8;
+  ctx->keybits = bits;
   if (cudaSetDevice(device) != cudaSuccess) {
+    delete ctx;
+    return GBSPH_ECUDA;
+  }
+  if (gbk::sort_init() != cudaSuccess) {
+    cudaGetLastError();
     delete ctx;
     return GBSPH_ECUDA;
   }
@@ -1037,9 +1043,51 @@ int gbsph_set_option(gbsph_ctx* ctx, int key, int value) {
   if (!ctx) return GBSPH_EINVAL;
   if (key == 0) ctx->forces_bsize = value;
   else if (key == 1) ctx->forces_variant = value;
+  else if (key == 2) {
+    if (value != 8 && value != 11) return set_err(ctx, GBSPH_EINVAL, "sort digits of 8 or 11 bits");
+    ctx->sort_bits = value;
+  }
   else return set_err(ctx, GBSPH_EINVAL, "unknown option %d", key);
   reset_graph(ctx);
   return GBSPH_OK;
+}
+
+// Times `reps` cell divisions of the current state with each digit width of
+// the radix sort (8 and 11 bits: 11 takes fewer passes for keys of 12 to 22
+// bits, with 8x larger histograms) and keeps the faster.  A division of a
+// divided state gives the same particle order, except for periodic copies,
+// which are made anew.
+int gbsph_tune_sort(gbsph_ctx* ctx, int reps, int* best_bits, float* ms) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (reps < 1) reps = 1;
+  CK(cudaSetDevice(ctx->device), "set device");
+  reset_graph(ctx);
+  const int cand[2] = {8, 11};
+  float t[2] = {0, 0};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  int rc = GBSPH_OK;
+  for (int k = 0; k < 2 && !rc; k++) {
+    ctx->sort_bits = cand[k];
+    rc = do_divide(ctx);  // warm-up
+    cudaEventRecord(e0, ctx->stream);
+    for (int i = 0; i < reps && !rc; i++) rc = do_divide(ctx);
+    cudaEventRecord(e1, ctx->stream);
+    if (!rc) {
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&t[k], e0, e1);
+      if (e != cudaSuccess) rc = cuda_check(ctx, e, "tune sort");
+    }
+    t[k] /= (float)reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  ctx->sort_bits = t[1] < t[0] ? 11 : 8;
+  if (best_bits) *best_bits = ctx->sort_bits;
+  if (ms) { ms[0] = t[0]; ms[1] = t[1]; }
+  return check_device_errors(ctx);
 }
 
 // ---- autotuner ------------------------------------------------------------

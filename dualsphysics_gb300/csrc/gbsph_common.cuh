@@ -230,7 +230,12 @@ void mlp_grad(const void* w_bf16, const float* x, const float* t, unsigned n, fl
 void mlp_adam(float* master, void* w_bf16, float* grad, float* m, float* v, float lr, float b1, float b2, float eps,
               float bc1, float bc2, cudaStream_t s);
 void to_bf16(const float* src, void* dst, int n, cudaStream_t s);
-void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses, cudaStream_t s, unsigned long long* nlaunch);
+// keybits: bits of the largest box key; radixbits: digit width of the sort
+// passes, 8 or 11 (11 needs sort_init first: its scatter takes 80 KB of
+// shared memory)
+void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned keybits, int radixbits, cudaStream_t s,
+            unsigned long long* nlaunch);
+cudaError_t sort_init();
 // Stable sort of n <= sort_noalloc_max_keys() keys of nbits bits on the static
 // work area (work = its device address, from sort_noalloc_address on the
 // current device).

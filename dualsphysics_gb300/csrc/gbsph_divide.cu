@@ -19,8 +19,9 @@ constexpr int kDivBlock = 256;
 constexpr int kSortBlock = 256;
 constexpr int kSortItems = 8;                       // items per thread per tile
 constexpr int kSortTile = kSortBlock * kSortItems;  // 2048 keys per tile
-constexpr int kRadixBits = 8;
+constexpr int kRadixBits = 8;        // digit width of the no-alloc sort and the default
 constexpr int kRadix = 1 << kRadixBits;
+constexpr int kRadixBitsWide = 11;   // the other digit width the divide can use
 
 // LoadDcellParticles (JSph.cpp:1794-1817): cell of every particle.
 __global__ void k_load_dcell(gbsph_consts c, DevArrays a, unsigned n) {
@@ -195,8 +196,10 @@ __global__ void k_presort(unsigned dcc, DevArrays a) {
 
 // ---- stable LSD radix sort of (key,value) over [ini, nptot) ------------------
 // Tile histograms, stored digit-major: hist[digit*ntiles + tile].
+template <int RB>
 __global__ void k_rs_hist(const unsigned* __restrict__ keys, unsigned* __restrict__ hist, const DivState* d,
                           unsigned ntiles_cap, int shift) {
+  constexpr int kRadix = 1 << RB;
   __shared__ unsigned sh[kRadix];
   const unsigned ini = d->ini, n = d->nptot - d->ini;
   const unsigned ntiles = gb_div_up(n, kSortTile);
@@ -259,11 +262,21 @@ __global__ void k_rs_scan_cols(unsigned* __restrict__ hist, unsigned* __restrict
   if (threadIdx.x == 0) tot[blockIdx.x] = total;
 }
 
-// Exclusive scan of the digit totals (one block of kRadix threads).
+// Exclusive scan of the 2^RB digit totals (one block; each thread owns
+// 2^RB / blockDim.x consecutive digits).
+template <int RB>
 __global__ void k_rs_scan_digits(unsigned* __restrict__ tot) {
-  const unsigned v = tot[threadIdx.x];
-  const unsigned e = block_exclusive_scan(v, nullptr);
-  tot[threadIdx.x] = e;
+  constexpr int kRadix = 1 << RB;
+  const int chunk = kRadix / (int)blockDim.x;
+  const int b = threadIdx.x * chunk;
+  unsigned sum = 0;
+  for (int i = 0; i < chunk; i++) sum += tot[b + i];
+  unsigned run = block_exclusive_scan(sum, nullptr);
+  for (int i = 0; i < chunk; i++) {
+    const unsigned v = tot[b + i];
+    tot[b + i] = run;
+    run += v;
+  }
 }
 
 // Stable scatter: within a tile, items keep their index order per digit.
@@ -271,14 +284,21 @@ __global__ void k_rs_scan_digits(unsigned* __restrict__ tot) {
 // each warp ranks its 32 items with __match_any_sync, per-digit warp counts are
 // prefixed across warps in warp order, and a running per-digit offset carries
 // the order from one round to the next.
+// Shared memory (dynamic): s_off, s_tot and s_wc below.
+template <int RB>
+constexpr size_t scatter_smem() { return sizeof(unsigned) * ((size_t)(2 + kSortBlock / 32) << RB); }
+
+template <int RB>
 __global__ void __launch_bounds__(kSortBlock) k_rs_scatter(const unsigned* __restrict__ kin, const unsigned* __restrict__ vin,
                                                            unsigned* __restrict__ kout, unsigned* __restrict__ vout,
                                                            const unsigned* __restrict__ hist, const DivState* d,
                                                            unsigned ntiles_cap, int shift) {
+  constexpr int kRadix = 1 << RB;
   constexpr int kWarps = kSortBlock / 32;
-  __shared__ unsigned s_off[kRadix];          // running output offset of each digit for this tile
-  __shared__ unsigned s_tot[kRadix];          // per-digit count of the current round
-  __shared__ unsigned s_wc[kWarps][kRadix];   // per-warp counts, then exclusive prefix across warps
+  extern __shared__ unsigned s_rs[];
+  unsigned* s_off = s_rs;                                        // running output offset of each digit for this tile
+  unsigned* s_tot = s_off + kRadix;                              // per-digit count of the current round
+  unsigned(*s_wc)[kRadix] = (unsigned(*)[kRadix])(s_tot + kRadix);  // per-warp counts, then prefix across warps
   const unsigned ini = d->ini, n = d->nptot - d->ini;
   const unsigned ntiles = gb_div_up(n, kSortTile);
   const unsigned tile = blockIdx.x;
@@ -555,6 +575,18 @@ __global__ void k_peri_dup(gbsph_consts c, DevArrays a, int axis, const unsigned
   }
 }
 
+// One LSD pass of RB-bit digits: tile histograms, their scan per digit, the
+// digit totals' scan, the stable scatter.
+template <int RB>
+void sort_pass(const unsigned* kin, const unsigned* vin, unsigned* kout, unsigned* vout, unsigned* hist,
+               const DivState* d, unsigned ntiles_cap, int shift, cudaStream_t s) {
+  constexpr int R = 1 << RB;
+  k_rs_hist<RB><<<ntiles_cap, kSortBlock, 0, s>>>(kin, hist, d, ntiles_cap, shift);
+  k_rs_scan_cols<<<R, 256, 0, s>>>(hist, hist + (size_t)R * ntiles_cap, ntiles_cap);
+  k_rs_scan_digits<RB><<<1, R < 1024 ? R : 1024, 0, s>>>(hist + (size_t)R * ntiles_cap);
+  k_rs_scatter<RB><<<ntiles_cap, kSortBlock, scatter_smem<RB>(), s>>>(kin, vin, kout, vout, hist, d, ntiles_cap, shift);
+}
+
 template <typename T>
 inline void swp(T*& x, T*& y) {
   T* t = x;
@@ -565,6 +597,11 @@ inline void swp(T*& x, T*& y) {
 }  // namespace
 
 namespace gbk {
+
+cudaError_t sort_init() {
+  return cudaFuncSetAttribute(k_rs_scatter<kRadixBitsWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)scatter_smem<kRadixBitsWide>());
+}
 
 void load_dcell(const gbsph_consts& c, const DevArrays& a, unsigned n, cudaStream_t s) {
   if (!n) return;
@@ -604,7 +641,7 @@ void run_periodic(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned* t
 // JSphGpuSingle::RunCellDivide: RunPeriodic first when an axis is periodic.  `cap` is the
 // particle capacity (grids are sized by it; kernels read the live counts from
 // DivState).  The reorder swaps the cur/alt array pairs in `a`.
-void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses, cudaStream_t s,
+void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned keybits, int radixbits, cudaStream_t s,
             unsigned long long* nlaunch) {
   const unsigned dcc = c.domcellcode;
   const unsigned grid_p = gb_div_up(cap, kDivBlock);
@@ -619,12 +656,12 @@ void divide(const gbsph_consts& c, DevArrays& a, unsigned cap, unsigned npasses,
   unsigned* vin = a.vals;
   unsigned* kout = a.keys2;
   unsigned* vout = a.vals2;
+  const int rb = radixbits == kRadixBitsWide ? kRadixBitsWide : kRadixBits;
+  const unsigned npasses = gb_div_up(keybits, (unsigned)rb);
   for (unsigned pass = 0; pass < npasses; pass++) {
-    const int shift = (int)(pass * kRadixBits);
-    k_rs_hist<<<ntiles_cap, kSortBlock, 0, s>>>(kin, a.hist, a.div, ntiles_cap, shift);
-    k_rs_scan_cols<<<kRadix, 256, 0, s>>>(a.hist, a.hist + (size_t)kRadix * ntiles_cap, ntiles_cap);
-    k_rs_scan_digits<<<1, kRadix, 0, s>>>(a.hist + (size_t)kRadix * ntiles_cap);
-    k_rs_scatter<<<ntiles_cap, kSortBlock, 0, s>>>(kin, vin, kout, vout, a.hist, a.div, ntiles_cap, shift);
+    const int shift = (int)(pass * rb);
+    if (rb == kRadixBitsWide) sort_pass<kRadixBitsWide>(kin, vin, kout, vout, a.hist, a.div, ntiles_cap, shift, s);
+    else sort_pass<kRadixBits>(kin, vin, kout, vout, a.hist, a.div, ntiles_cap, shift, s);
     swp(kin, kout);
     swp(vin, vout);
   }
@@ -730,10 +767,7 @@ void sort_noalloc(unsigned char* work, const unsigned* keys, unsigned n, unsigne
     const int shift = (int)(pass * kRadixBits);
     unsigned* kout = (pass & 1) ? keys_b : keys_a;
     unsigned* vout = (pass & 1) ? vals_a : vals_b;
-    k_rs_hist<<<ntiles, kSortBlock, 0, s>>>(kin, hist, d, ntiles, shift);
-    k_rs_scan_cols<<<kRadix, 256, 0, s>>>(hist, hist + (size_t)kRadix * ntiles, ntiles);
-    k_rs_scan_digits<<<1, kRadix, 0, s>>>(hist + (size_t)kRadix * ntiles);
-    k_rs_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, hist, d, ntiles, shift);
+    sort_pass<kRadixBits>(kin, vin, kout, vout, hist, d, ntiles, shift, s);
     kin = kout;
     vin = vout;
   }

@@ -104,7 +104,12 @@ class Ensemble:
 
 
 def tune(sim: GbSphSingle, reps: int = 3) -> dict:
-    """Runs the autotuner on one case; returns the timings and the choice."""
+    """Runs the autotuners on one case (fluid-row kernel, then the sort's
+    digit width); returns the timings and the choices."""
     r = TuneResult()
     sim._check(lib().gbsph_tune_forces(sim.ctx, reps, C.byref(r)), "gbsph_tune_forces")
-    return {"best": r.best, "variant": list(r.variant), "bsize": list(r.bsize), "ms": list(r.ms)}
+    bits = C.c_int()
+    ms = (C.c_float * 2)()
+    sim._check(lib().gbsph_tune_sort(sim.ctx, reps, C.byref(bits), ms), "gbsph_tune_sort")
+    return {"best": r.best, "variant": list(r.variant), "bsize": list(r.bsize), "ms": list(r.ms),
+            "sort_bits": bits.value, "sort_ms": list(ms)}

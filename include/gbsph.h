@@ -353,7 +353,8 @@ void* gbsph_stream(gbsph_ctx* ctx);
  * gbsph_forces: 0 (default) per-lane neighbour queues evaluated in rounds,
  * 1 one thread per particle with no queue.  key 0 = threads per block of the
  * one-thread-per-particle kernel (64, 128 or 256; the queued kernel uses 128).
- * The reference fixes 128 threads per block (JSphGpu.cpp, BlockSizes). */
+ * The reference fixes 128 threads per block (JSphGpu.cpp, BlockSizes).
+ * key 2 = digit width of the divide's radix sort, 8 (default) or 11 bits. */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
 
 /* Autotuner (no reference counterpart).  Times each fluid-row kernel
@@ -371,6 +372,12 @@ typedef struct {
   float ms[GBSPH_TUNE_CANDIDATES];       /* mean time of one fluid-row pass */
 } gbsph_tune_result;
 int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out);
+/* Autotuner of the cell division: times `reps` divisions of the current state
+ * (between steps) with radix-sort digits of 8 and of 11 bits and keeps the
+ * faster (gbsph_set_option key 2).  Both give the same sort order; the
+ * periodic copies of the state are made anew.  ms receives the two mean
+ * times (may be NULL). */
+int gbsph_tune_sort(gbsph_ctx* ctx, int reps, int* best_bits, float* ms);
 
 /* Ensembles (no reference counterpart: the reference runs one case per
  * process, JSphGpuSingle::Run, JSphGpuSingle.cpp:950-1010).  Independent,

@@ -120,3 +120,47 @@ def test_per_row_kernel_block_size_leaves_results_identical():
     _same(sims[1], sims[2], "128 vs 256")
     for s in sims:
         s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["dbc_d04", "mdbc_d04", "peri_d04"])
+def test_sort_digit_width_leaves_the_order_unchanged(name):
+    """The divide's radix sort with 11-bit digits (fewer passes) gives the
+    same stable order as with 8-bit digits: identical runs."""
+    import goldens as G
+    from dualsphysics_gb300.sph import GbSphSingle
+    cd = G.load_generated(name)
+    a, b = GbSphSingle(0), GbSphSingle(0)
+    a.setup(cd)
+    b.setup(cd)
+    b.set_option(2, 11)
+    b.RunCellDivide()                       # a divide of a divided state: the same order
+    a.RunCellDivide()
+    _same(a, b, "re-divided")
+    a.RunSteps(6, use_graph=True)
+    b.RunSteps(6, use_graph=True)
+    _same(a, b, name)
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_sort_tuner_keeps_a_valid_width_and_the_run():
+    import ctypes as C
+    import goldens as G
+    from dualsphysics_gb300._lib import lib
+    from dualsphysics_gb300.sph import GbSphSingle
+    cd = G.load_generated("dbc_d04")
+    a, b = GbSphSingle(0), GbSphSingle(0)
+    a.setup(cd)
+    b.setup(cd)
+    bits = C.c_int()
+    ms = np.zeros(2, np.float32)
+    assert lib().gbsph_tune_sort(b.ctx, 3, C.byref(bits), ms.ctypes.data_as(C.c_void_p)) == 0
+    assert bits.value in (8, 11) and (ms > 0).all() and ms[0 if bits.value == 8 else 1] == ms.min()
+    assert lib().gbsph_set_option(b.ctx, 2, 9) != 0           # only 8 or 11
+    a.RunSteps(5, use_graph=True)
+    b.RunSteps(5, use_graph=True)
+    _same(a, b, "tuned sort")
+    a.close()
+    b.close()
