@@ -357,6 +357,7 @@ def main():
                     help="the reference's -cellmode run option: cells of 2h (default) or h")
     ap.add_argument("--variant", type=int, default=None,
                     help="fluid-row kernel: 0 queued rounds, 1 one thread per particle")
+    ap.add_argument("--no-tune", action="store_true", help="keep the 8-bit sort digits (no sort autotuning)")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "ensemble", "closure"],
                     help="c2: the dam break with obstacle (default); c3: the large plain run (dp 0.004, "
                          "~49 M particles); ensemble: the batched cases; closure: the learned closure against "
@@ -407,6 +408,12 @@ def main():
     K, W = args.steps, args.warmup
     s = GbSphSingle(local)
     s.setup(cd)
+    # the sort autotuner (outside the timed region; both digit widths give the
+    # same particle order, so the run is unchanged)
+    import ctypes as C
+    sort_bits, sort_ms = C.c_int(8), (C.c_float * 2)()
+    if not args.no_tune:
+        s._check(_lib.lib().gbsph_tune_sort(s.ctx, 3, C.byref(sort_bits), sort_ms), "gbsph_tune_sort")
     if args.variant is not None:
         s.set_option(1, args.variant)
     pi = s.pips()
@@ -450,6 +457,7 @@ def main():
         t0 = time.perf_counter()
         e = GbSphSingle(local)
         e.setup(pcd)
+        e.set_option(2, sort_bits.value)   # the tuned sort width, set as a caller would
         if args.variant is not None:
             e.set_option(1, args.variant)
         for _ in range(K):
@@ -481,6 +489,8 @@ def main():
             "dtype": "f32 (f64 positions and integration)", "data": "synthetic",
             "config": {"workload": workload_text(args),
                        "particles": cd.np, "fluid": cd.nfluid, "boundary": cd.npb, "cellmode": args.cellmode,
+                       "sort_digit_bits": sort_bits.value,
+                       "sort_divide_ms_8_11": [round(float(x), 4) for x in sort_ms] if not args.no_tune else None,
                        "parallelism": "replicas only" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (no flush)"},
             "particle_interactions_per_s": steps_per_s * pis_per_step,
