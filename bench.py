@@ -479,9 +479,16 @@ def main():
                          f"full step time extrapolated"}
     clks = clk.summary()
     traffic = _dram_traffic(args.dp)
-    fp32_peak = None
+    fp32_nominal = None
     if clks.get("sm_mhz"):
-        fp32_peak = _sm_count(local) * FP32_LANES_PER_SM * 2 * clks["sm_mhz"] * 1e6 / 1e12
+        fp32_nominal = _sm_count(local) * FP32_LANES_PER_SM * 2 * clks["sm_mhz"] * 1e6 / 1e12
+    # the measured FP32 rate: FFMA microbenchmark on this device, after the timed region
+    import ctypes as C
+    ff = C.c_float()
+    fp32_peak = float(ff.value) if _lib.lib().gbsph_ffma_peak(local, C.byref(ff)) == 0 and ff.value > 0 else None
+    fp32_src = "measured: FFMA microbenchmark (gbsph_ffma_peak), best of 5 launches"
+    if fp32_peak is None:
+        fp32_peak, fp32_src = fp32_nominal, "nominal FFMA rate (SMs x 128 lanes x 2 FLOP) at the sampled SM clock"
     if rank == 0:
         line = {
             "metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -505,7 +512,7 @@ def main():
             "roofline_fp32": {"achieved_tflops": flops_launch / (kavg / 1e3) / 1e12, "peak_tflops": fp32_peak,
                               "frac": flops_launch / (kavg / 1e3) / 1e12 / fp32_peak if fp32_peak else None,
                               "model": "80 FLOP per real fluid-row pair",
-                              "peak_source": "nominal FFMA rate (SMs x 128 lanes x 2 FLOP) at the sampled SM clock"},
+                              "peak_source": fp32_src, "nominal_tflops": fp32_nominal},
             "clocks": clks,
             "gpu_launches": int(launches),
             "e2e": e2e,

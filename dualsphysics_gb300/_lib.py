@@ -146,6 +146,7 @@ SIGNATURES = {
     "gbsph_set_option": (C.c_int, [P, C.c_int, C.c_int]),
     "gbsph_tune_forces": (C.c_int, [P, C.c_int, C.POINTER(TuneResult)]),
     "gbsph_tune_sort": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), P]),
+    "gbsph_ffma_peak": (C.c_int, [C.c_int, C.POINTER(C.c_float)]),
     "gbsph_ensemble_create": (C.c_int, [C.c_uint, C.POINTER(P), C.POINTER(P)]),
     "gbsph_ensemble_destroy": (None, [P]),
     "gbsph_ensemble_last_error": (C.c_char_p, [P]),

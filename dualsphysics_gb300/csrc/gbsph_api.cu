@@ -1561,3 +1561,56 @@ int gbsph_mlp_params(gbsph_mlp* m, float* master, uint16_t* w_bf16) {
 }
 
 }  // extern "C"
+
+// ---- FP32 peak ------------------------------------------------------------------
+// FFMA microbenchmark for the FP32 roofline denominator: every thread runs 8
+// independent fused multiply-add chains; the best of a few timed launches
+// gives the issue-limited FP32 rate of the device at its current clock.
+namespace {
+__global__ void k_ffma_peak(float* out, int iters, float a, float b) {
+  float x[8];
+  for (int k = 0; k < 8; k++) x[k] = (float)(threadIdx.x + k) * 1e-3f;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) x[k] = fmaf(x[k], a, b);
+    }
+  }
+  float s = 0;
+  for (int k = 0; k < 8; k++) s += x[k];
+  if (s == -1.f) out[blockIdx.x] = s;  // keeps the chains live
+}
+}  // namespace
+
+extern "C" int gbsph_ffma_peak(int device, float* tflops) {
+  if (!tflops) return GBSPH_EINVAL;
+  if (cudaSetDevice(device) != cudaSuccess) return GBSPH_ECUDA;
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return GBSPH_ECUDA;
+  const int threads = 256, blocks = nsm * 8, iters = 2048;
+  float* out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaMalloc(&out, sizeof(float) * blocks) != cudaSuccess) return GBSPH_ENOMEM;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  k_ffma_peak<<<blocks, threads>>>(out, iters, 0.999999f, 1e-6f);  // warm-up
+  for (int rep = 0; rep < 5; rep++) {
+    cudaEventRecord(e0);
+    k_ffma_peak<<<blocks, threads>>>(out, iters, 0.999999f, 1e-6f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms > 0 && ms < best) best = ms;
+  }
+  const cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return GBSPH_ECUDA;
+  const double flop = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+  *tflops = (float)(flop / (best * 1e-3) / 1e12);
+  return GBSPH_OK;
+}

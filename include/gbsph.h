@@ -399,6 +399,11 @@ int gbsph_ensemble_sync(gbsph_ensemble* e);
 /* Kernel launches one replay of the ensemble graph holds (0 before the first). */
 unsigned long long gbsph_ensemble_launches_per_step(const gbsph_ensemble* e);
 
+/* FP32 roofline denominator (no reference counterpart): an FFMA
+ * microbenchmark, 8 independent chains per thread on 8 blocks of 256 threads
+ * per SM, best of 5 launches; TFLOP/s at the device's current clock. */
+int gbsph_ffma_peak(int device, float* tflops);
+
 /* ---- learned closure (no reference counterpart) -------------------------
  * A 16-64-64-64-3 tanh MLP with BF16 weights and FP32 accumulation that adds
  * a per-particle correction g*y to the fluid accelerations of a coarse run.
