@@ -300,11 +300,14 @@ def run_closure(args, local: int = 0):
     rng = np.random.default_rng(args.clos_seed)
     heights = [float(h) for h in np.sort(rng.uniform(0.2, 0.5, args.clos_heights))]
     held, t_end, dtp = args.clos_held, args.clos_tend, 0.005
+    val = heights[3::8]                                   # 4 of 32 heights validate (early stopping)
+    train = [h for h in heights if h not in val]
     t0 = time.perf_counter()
-    xs, ts, meta = cl.paired_samples(heights, dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
+    xs, ts, meta = cl.paired_samples(train, dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
+    xv, tv, _ = cl.paired_samples(val, dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
     t_data = time.perf_counter() - t0
     t1 = time.perf_counter()
-    p, w, loss = cl.train_closure(xs, ts, epochs=args.clos_epochs, seed=args.clos_seed, device=local)
+    p, w, loss = cl.train_closure(xs, ts, epochs=args.clos_epochs, seed=args.clos_seed, device=local, xv=xv, tv=tv)
     t_train = time.perf_counter() - t1
     xh, th, _ = cl.paired_samples([held], dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
     ev = cl.Trainer(cl.from_bf16(w), local)     # the deployed BF16 weights
@@ -328,7 +331,8 @@ def run_closure(args, local: int = 0):
             "higher_is_better": True, "data": "synthetic", "dtype": "bf16 weights, f32 accumulate",
             "config": {"workload": f"dam break with box obstacle, mDBC, tank height {cl.TANK_HEIGHT} m; held-out "
                                    f"column {held} m; {t_end} s; judge dp=0.005",
-                       "train_heights": len(heights), "snapshots_per_height": args.clos_snaps,
+                       "train_heights": len(train), "validation_heights": len(val),
+                       "snapshots_per_height": args.clos_snaps,
                        "samples": int(len(xs)), "epochs": args.clos_epochs},
             "probe_rmse_pa": err, "probe_rmse_pa_20ms_means": werr, "front_rmse_m": ferr,
             "wall_s": {"judge_dp0.005": judge["wall_s"], "fine_dp0.01": fine["wall_s"],

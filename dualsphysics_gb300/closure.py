@@ -151,11 +151,15 @@ def fold_standardisation(p: np.ndarray, mu_x, sd_x, sd_t) -> np.ndarray:
 
 
 def train_closure(x: np.ndarray, t: np.ndarray, epochs: int = 40, batch: int = 1024, lr: float = 1e-3,
-                  seed: int = 0, device: int = 0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+                  seed: int = 0, device: int = 0, xv: np.ndarray | None = None, tv: np.ndarray | None = None,
+                  check_every: int = 5) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     """Trains on standardised features and targets (zero mean and unit
     variance per column; constant columns left as they are), in a seeded
     shuffled order, and returns the folded FP32 parameters, their BF16 bits
-    and the per-epoch losses (in standardised units)."""
+    and the per-epoch losses (in standardised units).  With validation data
+    (xv, tv: runs not trained on), the weights kept are those of the
+    `check_every`-epoch checkpoint with the lowest validation error (early
+    stopping), the untrained network's included."""
     x = np.asarray(x, np.float32)
     t = np.asarray(t, np.float32)
     mu = x.mean(axis=0).astype(np.float64)
@@ -169,8 +173,21 @@ def train_closure(x: np.ndarray, t: np.ndarray, epochs: int = 40, batch: int = 1
     tr = Trainer(init_params(seed), device)
     try:
         tr.set_data(xs, ts)
-        loss = tr.train(epochs, batch, lr)
-        master, _ = tr.params()
+        if xv is None:
+            loss = tr.train(epochs, batch, lr)
+            master, _ = tr.params()
+        else:
+            xvs = ((np.asarray(xv, np.float32) - mu) / sd).astype(np.float32)
+            tvs = (np.asarray(tv, np.float32) / st).astype(np.float32)
+            master, _ = tr.params()
+            best = float(np.mean((tr.infer(xvs) - tvs) ** 2))
+            losses = []
+            for _ in range(max(1, epochs // check_every)):
+                losses.append(tr.train(check_every, batch, lr))
+                v = float(np.mean((tr.infer(xvs) - tvs) ** 2))
+                if v < best:
+                    best, (master, _) = v, tr.params()
+            loss = np.concatenate(losses)
     finally:
         tr.close()
     p = fold_standardisation(master, mu, sd, st)
