@@ -84,6 +84,9 @@ class CaseSpec:
     # the period [0, Ly), YPeriodicIncX=0; init_vel_y a uniform y velocity
     periodic_y: bool = False
     init_vel_y: float = 0.0
+    # cross increment of the x periodicity: a particle leaving through x = Lx
+    # comes back at x = 0 shifted by this much in y (XPeriodicIncY)
+    peri_inc_y: float = 0.0
 
 
 @dataclass
@@ -263,7 +266,7 @@ def write_case(case: Case, dirpath: str) -> tuple[str, str]:
     if s.boundary != "mdbc":
         params.pop("SlipMode")
     if s.periodic_x:
-        params["XPeriodicIncY"] = 0
+        params["XPeriodicIncY"] = s.peri_inc_y
     if s.periodic_y:
         params["YPeriodicIncX"] = 0
     params.update(s.extra_params)

@@ -63,6 +63,10 @@ CASES = {
     "peris_d04": (lambda: cg.spec_c1(dp=0.04, name="peris_d04", tank=(0.8, 0.4, 0.3), column=(0.8, 0.4, 0.2),
                                      periodic_x=True, init_vel_x=2.0, init_vel=0.02, seed=59,
                                      extra_params={"Shifting": 3, "ShiftCoef": -2, "ShiftTFS": 2.75}), 30),
+    # the channel with a cross increment: copies and wrapped particles shift by 0.08 m in y
+    "perishear_d04": (lambda: cg.spec_c1(dp=0.04, name="perishear_d04", tank=(0.8, 0.4, 0.3),
+                                         column=(0.8, 0.4, 0.2), periodic_x=True, peri_inc_y=0.08, init_vel_x=2.0,
+                                         init_vel=0.02, seed=61), 30),
     "perixy_d04": (lambda: cg.spec_c1(dp=0.04, name="perixy_d04", tank=(0.6, 0.4, 0.3), column=(0.6, 0.4, 0.2),
                                       periodic_x=True, periodic_y=True, init_vel_x=1.5, init_vel_y=-1.0,
                                       init_vel=0.02, seed=43), 30),
