@@ -2,6 +2,7 @@
 obstacle at dp=0.0025 m (~5.2M fluid + ~1.5M boundary particles).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference] [--dp DP]
+    python bench.py --workload c3|ensemble|closure   (the other measured workloads)
 
 A step is one Symplectic step (predictor + corrector interaction passes, two
 cell divisions, mDBC correction, dt reduction) of the whole particle set.
