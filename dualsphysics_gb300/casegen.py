@@ -84,6 +84,10 @@ class CaseSpec:
     # the period [0, Ly), YPeriodicIncX=0; init_vel_y a uniform y velocity
     periodic_y: bool = False
     init_vel_y: float = 0.0
+    # periodic in z: no floor, the fluid fills the period [0, Lz) and falls
+    # through the bottom face back in at the top (ZPeriodicIncX=0)
+    periodic_z: bool = False
+    init_vel_z: float = 0.0
     # cross increment of the x periodicity: a particle leaving through x = Lx
     # comes back at x = 0 shifted by this much in y (XPeriodicIncY)
     peri_inc_y: float = 0.0
@@ -128,7 +132,7 @@ def make_dam_break(spec: CaseSpec) -> Case:
     # one period [0, n*dp) of the walls along each periodic axis
     wx = (0, nx - 1) if spec.periodic_x else (-3, nx + 3)
     wy = (0, ny - 1) if spec.periodic_y else (-3, ny + 3)
-    wl = _lattice(wx, wy, (-3, nz))
+    wl = _lattice(wx, wy, (0, nz - 1) if spec.periodic_z else (-3, nz))
     inside = ((wl[:, 0] >= 0) & (wl[:, 0] <= nx) & (wl[:, 1] >= 0) & (wl[:, 1] <= ny) & (wl[:, 2] >= 0))
     wall = wl[~inside].astype(np.float64) * dp
     # --- obstacle: solid lattice block on the floor
@@ -144,6 +148,8 @@ def make_dam_break(spec: CaseSpec) -> Case:
         fx = nx - 1
     if spec.periodic_y:
         fy = ny - 1
+    if spec.periodic_z:
+        fz = nz - 1
     fl = _lattice((0, fx), (0, fy), (0, fz)).astype(np.float64) * dp
     if spec.obstacle is not None and len(obst):
         lo, hi = obst.min(axis=0) - 0.5 * dp, obst.max(axis=0) + 0.5 * dp
@@ -212,6 +218,8 @@ def make_dam_break(spec: CaseSpec) -> Case:
         vel[npb:, 0] += np.float32(spec.init_vel_x)
     if spec.init_vel_y and nf:
         vel[npb:, 1] += np.float32(spec.init_vel_y)
+    if spec.init_vel_z and nf:
+        vel[npb:, 2] += np.float32(spec.init_vel_z)
     return Case(spec=spec, pos=pos, vel=vel, rhop=rhop.astype(np.float32),
                 idp=np.arange(n, dtype=np.uint32), code=code, boundnor=boundnor, blocks=blocks,
                 npb=npb, h=h, b=b, mass=mass)
@@ -269,6 +277,8 @@ def write_case(case: Case, dirpath: str) -> tuple[str, str]:
         params["XPeriodicIncY"] = s.peri_inc_y
     if s.periodic_y:
         params["YPeriodicIncX"] = 0
+    if s.periodic_z:
+        params["ZPeriodicIncX"] = 0
     params.update(s.extra_params)
     lines = ['<?xml version="1.0" encoding="UTF-8" ?>',
              '<case app="dualsphysics_gb300.casegen">',

@@ -67,6 +67,9 @@ CASES = {
     "perishear_d04": (lambda: cg.spec_c1(dp=0.04, name="perishear_d04", tank=(0.8, 0.4, 0.3),
                                          column=(0.8, 0.4, 0.2), periodic_x=True, peri_inc_y=0.08, init_vel_x=2.0,
                                          init_vel=0.02, seed=61), 30),
+    # periodic in z: side walls only, the fluid falls through the bottom face and comes back at the top
+    "periz_d04": (lambda: cg.spec_c1(dp=0.04, name="periz_d04", tank=(0.4, 0.4, 0.4), column=(0.4, 0.4, 0.4),
+                                     periodic_z=True, init_vel_z=-2.0, init_vel=0.02, seed=67), 30),
     "perixy_d04": (lambda: cg.spec_c1(dp=0.04, name="perixy_d04", tank=(0.6, 0.4, 0.3), column=(0.6, 0.4, 0.2),
                                       periodic_x=True, periodic_y=True, init_vel_x=1.5, init_vel_y=-1.0,
                                       init_vel=0.02, seed=43), 30),

@@ -18,7 +18,7 @@ from dualsphysics_gb300.case import load_case  # noqa: E402
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 CASE_NAMES = ["dbc_d04", "mdbc_d04", "jit_d04", "vel_d04", "verlet_d04", "sps_d04", "lam_d04", "ddt2f_d04", "half_d04",
-              "shift_d04", "shiftnb_d04", "peri_d04", "perixy_d04", "periv_d04", "perim_d04", "peris_d04", "perishear_d04"]
+              "shift_d04", "shiftnb_d04", "peri_d04", "perixy_d04", "periv_d04", "perim_d04", "peris_d04", "perishear_d04", "periz_d04"]
 SHIFT_CASES = ["shift_d04", "shiftnb_d04", "peris_d04"]
 FLT_MAX = float(np.finfo(np.float32).max)
 
