@@ -335,8 +335,8 @@ def write_case(case: Case, dirpath: str) -> tuple[str, str]:
 
 
 # ---------------------------------------------------------------------------
-# The dam-break workloads (geometry actually generated is recorded by
-# counting the particles; see the design doc for the counts).
+# The dam-break workloads (the particle counts of the generated geometry are
+# those the generator produces, counted after generation).
 # ---------------------------------------------------------------------------
 OBSTACLE_C2 = (0.9, 0.24, 0.12, 0.12, 0.45)
 

@@ -284,7 +284,7 @@ int gbsph_create(const gbsph_consts* c, unsigned capacity, int device, gbsph_ctx
     delete ctx;
     return GBSPH_ECUDA;
   }
-  if (gbk::sort_init() != cudaSuccess) {
+  if (gbk::sort_init() != cudaSuccess || gbk::forces_init(*c) != cudaSuccess) {
     cudaGetLastError();
     delete ctx;
     return GBSPH_ECUDA;

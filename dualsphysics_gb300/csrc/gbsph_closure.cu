@@ -189,11 +189,11 @@ __global__ void __launch_bounds__(kMlpBlock) k_closure_apply(gbsph_consts c, Dev
       nfb++;
     }
     if (lane == 0) a.acear[p1] = ac;
-    amax2 = fmaxf(amax2, ac.x * ac.x + ac.y * ac.y + ac.z * ac.z);
+    amax2 = gb_fmax_nan(amax2, ac.x * ac.x + ac.y * ac.y + ac.z * ac.z + 0.f * ac.w);
     __syncwarp();
   }
   if (lane == 0) {
-    if (amax2 > 0) gb_atomic_max_nonneg(&a.st->acemax2, amax2);
+    if (!(amax2 <= 0.f)) gb_atomic_max_nonneg(&a.st->acemax2, amax2);
     if (nfb && nfallback) atomicAdd(nfallback, nfb);
   }
 }

@@ -96,9 +96,29 @@ __device__ __forceinline__ unsigned gb_cell(unsigned dcc, unsigned cx, unsigned 
   return (cx << ((dcc >> 10) & 31)) | (cy << ((dcc >> 15) & 31)) | cz;
 }
 
-// float max via the bit pattern of a non-negative float
+// float max via the bit pattern of a non-negative float; a NaN (positive or
+// negative) has a larger bit pattern than every finite float and stays
 __device__ __forceinline__ void gb_atomic_max_nonneg(unsigned* addr, float v) {
   atomicMax(addr, __float_as_uint(v));
+}
+
+// max of the dt maxima that keeps a NaN (fmaxf drops it): a NaN in a fluid
+// row's sums reaches the dt, which then reports GB_ERR_NANDT
+__device__ __forceinline__ float gb_fmax_nan(float a, float b) { return (a != a || a > b) ? a : b; }
+
+// Warp maxima of the dt quantities (NaN kept), one atomic per warp; values
+// that are not above zero are not written (the maxima start at zero).
+__device__ __forceinline__ void gb_warp_maxes(StepState* st, float acemax2, float visc, float vel2) {
+  for (int o = 16; o; o >>= 1) {
+    acemax2 = gb_fmax_nan(acemax2, __shfl_xor_sync(0xffffffffu, acemax2, o));
+    visc = gb_fmax_nan(visc, __shfl_xor_sync(0xffffffffu, visc, o));
+    vel2 = gb_fmax_nan(vel2, __shfl_xor_sync(0xffffffffu, vel2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (!(acemax2 <= 0.f)) gb_atomic_max_nonneg(&st->acemax2, acemax2);
+    if (!(visc <= 0.f)) gb_atomic_max_nonneg(&st->viscdt, visc);
+    if (!(vel2 <= 0.f)) gb_atomic_max_nonneg(&st->velmax2, vel2);
+  }
 }
 
 // Pressure from density: Tait/Monaghan EOS B*((rho/rho0)^gamma-1)
@@ -249,6 +269,11 @@ void stage_upload(const DevArrays& a, const double* stage, const float* nor3, un
 void stage_download(const DevArrays& a, double* stage, unsigned n, cudaStream_t s);
 void sort_noalloc(unsigned char* work, const unsigned* keys, unsigned n, unsigned nbits, unsigned* perm,
                   unsigned* sorted_keys, cudaStream_t s);
+// Raises the shared-memory limit of the staged fluid-row kernels that the
+// constants `c` select (call once per context, before any stream capture).
+cudaError_t forces_init(const gbsph_consts& c);
+// variant: 0 warp-queued rounds, 1 one thread per row (block size bsize),
+// 2 cell-tiled staged (ring of 8 chunks), 3 cell-tiled staged (ring of 4)
 void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, cudaStream_t s, unsigned long long* nlaunch,
             cudaEvent_t ev_fluid_begin = nullptr, cudaEvent_t ev_fluid_end = nullptr);
 void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch);

@@ -187,21 +187,13 @@ __global__ void __launch_bounds__(256) k_forces_fluid(gbsph_consts c, DevArrays 
       a.straina[p1] = make_float4(ff.s0 + fb.s0, ff.s1 + fb.s1, ff.s2 + fb.s2, ff.s3 + fb.s3);
       a.strainb[p1] = make_float2(ff.s4 + fb.s4, ff.s5 + fb.s5);
     }
-    acemax2 = ax * ax + ay * ay + az * az;
+    // a NaN density rate makes the maximum NaN (x + 0 * ar is x otherwise)
+    acemax2 = ax * ax + ay * ay + az * az + 0.f * ar;
     visc = fmaxf(ff.visc, fb.visc);
     vel2 = vr1.x * vr1.x + vr1.y * vr1.y + vr1.z * vr1.z;
   }
   // block reduction of the maxima, one atomic per block
-  for (int o = 16; o; o >>= 1) {
-    acemax2 = fmaxf(acemax2, __shfl_xor_sync(0xffffffffu, acemax2, o));
-    visc = fmaxf(visc, __shfl_xor_sync(0xffffffffu, visc, o));
-    vel2 = fmaxf(vel2, __shfl_xor_sync(0xffffffffu, vel2, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (acemax2 > 0) gb_atomic_max_nonneg(&a.st->acemax2, acemax2);
-    if (visc > 0) gb_atomic_max_nonneg(&a.st->viscdt, visc);
-    if (vel2 > 0) gb_atomic_max_nonneg(&a.st->velmax2, vel2);
-  }
+  gb_warp_maxes(a.st, acemax2, visc, vel2);
 }
 
 // ---- fluid rows, production kernel ----------------------------------------
@@ -273,21 +265,27 @@ PairK make_pairk(const gbsph_consts& c) {
 __device__ __forceinline__ float gb_rcp(float x) { return __fdividef(1.f, x); }
 
 
-template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift>
-__device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k, const DevArrays& a,
-                                           float4 e, float4 vr2, float p2press, float4 vr1,
-                                           float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
-                                           float massp2, PairAcc& r) {
+// The pair terms of fluid row i and neighbour j, given dr = r_i - r_j, the
+// neighbour's velrho and pressure, its SPS tau/rho^2 (read only for Laminar+SPS
+// fluid neighbours) and whether it is a fixed boundary particle (read only by
+// the NoFixed shifting mode).  With guard0 a pair closer than ALMOSTZERO
+// (r^2 < 1e-18, a particle and itself) adds nothing, as the reference's
+// neighbour test leaves it out (JSphCpu.cpp:826).
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, bool guard0 = false>
+__device__ __forceinline__ void pair_core(const gbsph_consts& c, const PairK& k, float drx, float dry, float drz,
+                                          float4 vr2, float p2press, float4 ta2, float2 tb2, bool nbfixed,
+                                          float4 vr1, float p1press, float inv_rho1, float4 ta1, float2 tb1,
+                                          float vfac, float massp2, PairAcc& r) {
   // fluid neighbours (boundp2=false) are summed without their mass, which the
   // caller applies once to the pass's sums; the continuity sum leaves out rho1
   const float m2 = boundp2 ? massp2 : 1.f;
-  const unsigned p2 = __float_as_uint(e.w);
-  const float drx = e.x, dry = e.y, drz = e.z;
   const float rr2 = drx * drx + dry * dry + drz * drz;
+  const bool real = !guard0 || rr2 >= GB_ALMOSTZERO;
   const float rinv = rsqrtf(rr2);
   const float qq = rr2 * rinv * k.hinv;
   const float wqq1 = 1.f - 0.5f * qq;
-  const float fac = c.bwenh * wqq1 * wqq1 * wqq1;
+  const float fac0 = c.bwenh * wqq1 * wqq1 * wqq1;
+  const float fac = real ? fac0 : 0.f;  // every term carries fac (or fr)
   const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
   const float inv_rho2 = gb_rcp(vr2.w);
   // momentum
@@ -300,13 +298,13 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
   if (tdensity == GBSPH_DDT_DDT && r.delta != FLT_MAX) {
     const float visc_densi = k.ddt_kc * (vr1.w * inv_rho2 - 1.f) * inv_r2eta;
     const float dot3 = drx * frx + dry * fry + drz * frz;
-    r.delta = (boundp2 && c.tboundary == GBSPH_BC_DBC) ? FLT_MAX : r.delta + visc_densi * dot3 * m2;
+    r.delta = (boundp2 && c.tboundary == GBSPH_BC_DBC && real) ? FLT_MAX : r.delta + visc_densi * dot3 * m2;
   }
   if (tdensity == GBSPH_DDT_DDT2 || (tdensity == GBSPH_DDT_DDT2FULL && !boundp2)) {
     // the fluid neighbours are visited first, so only the boundary pass can
     // meet the veto (and it sets it: DDT2 leaves particles next to the boundary out)
     if (boundp2) {
-      r.delta = FLT_MAX;
+      if (real) r.delta = FLT_MAX;
     } else {
       const float t = c.ddtgz * drz;
       float drho;
@@ -321,7 +319,7 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
   // shifting sums (JSphCpu.cpp:942-950), fluid ones without the mass
   if (tshift && r.sh0 != FLT_MAX) {
     const float massrho = m2 * inv_rho2;
-    const bool noshift = boundp2 && (c.tshift == 1 || (c.tshift == 2 && (a.code[p2] & GB_CODE_MASKTYPE) == 0u));
+    const bool noshift = boundp2 && real && (c.tshift == 1 || (c.tshift == 2 && nbfixed));
     r.sh0 = noshift ? FLT_MAX : r.sh0 + massrho * frx;
     r.sh1 += massrho * fry;
     r.sh2 += massrho * frz;
@@ -330,7 +328,7 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
   // viscosity
   const float dot = drx * dvx + dry * dvy + drz * dvz;
   const float dot_rr2 = dot * inv_r2eta;
-  r.visc = fmaxf(dot_rr2, r.visc);
+  r.visc = fmaxf(real ? dot_rr2 : 0.f, r.visc);
   if (tvisco == GBSPH_VISCO_ARTIFICIAL) {
     // applied for approaching pairs (dot < 0); evaluated for every pair and
     // selected, since nearly every warp has lanes on both sides of the test
@@ -345,8 +343,6 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
     if (tvisco == GBSPH_VISCO_LAMINARSPS) {
       float t0 = ta1.x, t1 = ta1.y, t2 = ta1.z, t3 = ta1.w, t4 = tb1.x, t5 = tb1.y;
       if (!boundp2) {
-        const float4 ta2 = a.taua[p2];
-        const float2 tb2 = a.taub[p2];
         t0 += ta2.x; t1 += ta2.y; t2 += ta2.z; t3 += ta2.w; t4 += tb2.x; t5 += tb2.y;
       }
       r.ax += m2 * (t0 * frx + t1 * fry + t2 * frz);
@@ -358,6 +354,23 @@ __device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k
       dv = dvz * volp2; r.s2 += dv * frx; r.s4 += dv * fry; r.s5 += dv * frz;
     }
   }
+}
+
+// A queued entry e = (dr, neighbour index): the neighbour's SPS tau and code
+// are read from global memory where the pair terms need them.
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift>
+__device__ __forceinline__ void pair_fluid(const gbsph_consts& c, const PairK& k, const DevArrays& a,
+                                           float4 e, float4 vr2, float p2press, float4 vr1,
+                                           float p1press, float inv_rho1, float4 ta1, float2 tb1, float vfac,
+                                           float massp2, PairAcc& r) {
+  const unsigned p2 = __float_as_uint(e.w);
+  float4 ta2 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 tb2 = make_float2(0.f, 0.f);
+  if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ta2 = a.taua[p2]; tb2 = a.taub[p2]; }
+  bool nbfixed = false;
+  if (tshift && boundp2) nbfixed = (a.code[p2] & GB_CODE_MASKTYPE) == 0u;
+  pair_core<tvisco, tdensity, boundp2, ddtgen, tshift>(c, k, e.x, e.y, e.z, vr2, p2press, ta2, tb2, nbfixed, vr1,
+                                                        p1press, inv_rho1, ta1, tb1, vfac, massp2, r);
 }
 
 // One round: every lane evaluates up to two of its oldest queued pairs, with
@@ -536,20 +549,308 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, Pair
       a.strainb[p1] = make_float2(ff.s4, ff.s5);
     }
     if (tshift) a.shiftpos[p1] = make_float4(ff.sh0, ff.sh1, ff.sh2, ff.sh3);
-    acemax2 = ax * ax + ay * ay + az * az;
+    // a NaN density rate makes the maximum NaN (x + 0 * ar is x otherwise)
+    acemax2 = ax * ax + ay * ay + az * az + 0.f * ar;
     visc = ff.visc;
     vel2 = vr1.x * vr1.x + vr1.y * vr1.y + vr1.z * vr1.z;
   }
-  for (int o = 16; o; o >>= 1) {
-    acemax2 = fmaxf(acemax2, __shfl_xor_sync(0xffffffffu, acemax2, o));
-    visc = fmaxf(visc, __shfl_xor_sync(0xffffffffu, visc, o));
-    vel2 = fmaxf(vel2, __shfl_xor_sync(0xffffffffu, vel2, o));
+  gb_warp_maxes(a.st, acemax2, visc, vel2);
+}
+
+// ---- fluid rows, cell-tiled staged kernel ----------------------------------
+// A warp takes 32 consecutive fluid rows (targets).  The candidate neighbours
+// of its targets are the particles of the neighbour boxes, which in the sorted
+// order form one contiguous range per row of boxes (JCellSearch_inline.h:33-84):
+// for the targets of one row of cells (y, z) the candidates are the
+// (2sd+1)^2 box rows around it, each over the x range of the targets' cells
+// widened by sd.  These ranges, taken as one stream, are staged 32 candidates
+// (a chunk) at a time through a per-warp ring of R chunks in shared memory.
+// A chunk draws kTSeg consecutive candidates from each of 32/kTSeg equal
+// parts of the stream, so that every chunk samples the whole neighbourhood and
+// the targets' hits arrive at similar rates; each lane stages one candidate
+// with coalesced float4 loads (pscell, velrho), its position moved into the
+// frame of one cell of the group.  The distance checks read the staged
+// positions as broadcasts (structure of arrays, four candidates a load) and
+// evaluate two candidates per packed f32x2 instruction; each lane's hits in a
+// chunk form a 32-bit mask.  The pair terms then run in rounds in which every
+// lane evaluates its next hit, reading the neighbour from shared memory; a
+// round is taken when every target of the row group has a hit pending, or
+// when the ring slot about to be refilled still holds one.  A candidate of the
+// widened ranges that lies outside a target's own 27 (or 125) boxes is more
+// than 2h away from it and fails the check, so the pairs are those of the
+// per-target walk; the summation order per target is the order of the stream.
+constexpr int kTBlock = 128;
+constexpr int kTSeg = 8;             // consecutive candidates a chunk takes from each part of the stream
+constexpr float kFarAway = 1.0e18f;  // position of an empty ring slot: fails every check
+
+template <int tvisco, bool tshift, int R>
+struct TileLayout {
+  static constexpr bool sps = tvisco == GBSPH_VISCO_LAMINARSPS;
+  // per slot: frame position + pressure (16), velrho (16), negated frame
+  // position as three arrays (12), hit mask (4), [tau a, tau b (24)], [fixed flag (4)]
+  static constexpr size_t per_warp = (size_t)R * 32 * (16 + 16 + 12 + 4 + (sps ? 24 : 0) + (tshift ? 4 : 0));
+  static constexpr size_t bytes = per_warp * (kTBlock / 32);
+};
+
+struct TileRing {
+  float4* sa;      // frame position (x, y, z) + pressure, R*32
+  float4* sb;      // velrho, R*32
+  float* nx;       // -x, -y, -z of the frame position, R*32 each
+  float* ny;
+  float* nz;
+  unsigned* sm;    // hit masks [R][32]
+  float4* st;      // SPS tau a
+  float2* stb;     // SPS tau b
+  unsigned* sc;    // 1: fixed boundary particle (NoFixed shifting)
+};
+
+// Pending hits of a lane: `cur` holds the unconsumed hits of chunk `cc`;
+// chunks cc+1 .. cnext-1 have their masks in the ring.  With nothing pending,
+// cc = cnext (the lane waits for the next chunk).
+template <int R>
+__device__ __forceinline__ void tile_refill(const TileRing& ring, unsigned& cur, unsigned& cc, unsigned cnext,
+                                            int lane) {
+  while (cur == 0u && cc + 1u < cnext) {
+    cc++;
+    cur = ring.sm[(cc & (R - 1)) * 32 + lane];
   }
-  if ((threadIdx.x & 31) == 0) {
-    if (acemax2 > 0) gb_atomic_max_nonneg(&a.st->acemax2, acemax2);
-    if (visc > 0) gb_atomic_max_nonneg(&a.st->viscdt, visc);
-    if (vel2 > 0) gb_atomic_max_nonneg(&a.st->velmax2, vel2);
+  if (cur == 0u) cc = cnext;
+}
+
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, int R>
+__device__ __forceinline__ void tile_round(const gbsph_consts& c, const PairK& k, const TileRing& ring,
+                                           unsigned& cur, unsigned& cc, unsigned cnext, float fx, float fy,
+                                           float fz, float4 vr1, float p1press, float inv_rho1, float4 ta1,
+                                           float2 tb1, float vfac, float massp2, PairAcc& r, int lane) {
+  if (cur != 0u) {
+    const unsigned slot = ((cc & (R - 1)) << 5) | (unsigned)(__ffs(cur) - 1);
+    cur &= cur - 1u;
+    const float4 q = ring.sa[slot];
+    const float4 vr2 = ring.sb[slot];
+    float4 ta2 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 tb2 = make_float2(0.f, 0.f);
+    if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ta2 = ring.st[slot]; tb2 = ring.stb[slot]; }
+    const bool nbfixed = (tshift && boundp2) ? ring.sc[slot] != 0u : false;
+    pair_core<tvisco, tdensity, boundp2, ddtgen, tshift, true>(c, k, fx - q.x, fy - q.y, fz - q.z, vr2, q.w, ta2,
+                                                                tb2, nbfixed, vr1, p1press, inv_rho1, ta1, tb1, vfac,
+                                                                massp2, r);
+    tile_refill<R>(ring, cur, cc, cnext, lane);
   }
+}
+
+// Hit bits of four staged candidates (positions negated, structure of arrays)
+// for the lane at (fx, fy, fz): two candidates per packed instruction.
+__device__ __forceinline__ unsigned tile_check4(float2 fxx, float2 fyy, float2 fzz, float4 x, float4 y, float4 z,
+                                                float ks2, int q) {
+  const float2 dx0 = __fadd2_rn(fxx, make_float2(x.x, x.y)), dx1 = __fadd2_rn(fxx, make_float2(x.z, x.w));
+  const float2 dy0 = __fadd2_rn(fyy, make_float2(y.x, y.y)), dy1 = __fadd2_rn(fyy, make_float2(y.z, y.w));
+  const float2 dz0 = __fadd2_rn(fzz, make_float2(z.x, z.y)), dz1 = __fadd2_rn(fzz, make_float2(z.z, z.w));
+  float2 r0 = __fmul2_rn(dx0, dx0), r1 = __fmul2_rn(dx1, dx1);
+  r0 = __ffma2_rn(dy0, dy0, r0);
+  r1 = __ffma2_rn(dy1, dy1, r1);
+  r0 = __ffma2_rn(dz0, dz0, r0);
+  r1 = __ffma2_rn(dz1, dz1, r1);
+  return ((r0.x <= ks2 ? 1u : 0u) | (r0.y <= ks2 ? 2u : 0u) | (r1.x <= ks2 ? 4u : 0u) | (r1.y <= ks2 ? 8u : 0u)) << q;
+}
+
+// One pass of the warp's fluid rows over the fluid (boundp2=false) or boundary
+// (boundp2=true) boxes.  cx, cy, cz: the lane's cell in the trimmed domain.
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, int R>
+__device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k, const DevArrays& a,
+                                          const DivState& d, const TileRing& ring, bool active, int cx, int cy,
+                                          int cz, float4 ps1, float4 vr1, float inv_rho1, float4 ta1, float2 tb1,
+                                          PairAcc& r) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned cellinit = boundp2 ? 0u : d.boxfluid;
+  const float scell = c.scell, ks2 = c.kernelsize2;
+  const float vfac = boundp2 ? k.vfac_b : k.vfac_f;
+  const float massp2 = boundp2 ? c.massbound : c.massfluid;
+  const int sd = c.cellmode_div;
+  const int ncx = (int)d.ncx, ncy = (int)d.ncy, ncz = (int)d.ncz;
+  const unsigned dcc = c.domcellcode, cmin0 = d.cellmin[0];
+  unsigned cnext = 0u, cc = 0u, cur = 0u;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  unsigned remaining = __ballot_sync(FULL, active);
+  while (remaining) {
+    // the targets in the row of cells of the lowest remaining lane
+    const int leader = __ffs(remaining) - 1;
+    const int rx = __shfl_sync(FULL, cx, leader), ry = __shfl_sync(FULL, cy, leader),
+              rz = __shfl_sync(FULL, cz, leader);
+    const bool ing = active && cy == ry && cz == rz;
+    const unsigned grp = __ballot_sync(FULL, ing);
+    remaining &= ~grp;
+    const int xmin = __reduce_min_sync(FULL, ing ? cx : 0x7fffffff);
+    const int xmax = __reduce_max_sync(FULL, ing ? cx : -1);
+    const int x0 = max(xmin - sd, 0), x1 = min(xmax + sd, ncx - 1);
+    const int y0 = max(ry - sd, 0), y1 = min(ry + sd, ncy - 1);
+    const int z0 = max(rz - sd, 0), z1 = min(rz + sd, ncz - 1);
+    const int nyr = y1 - y0 + 1, nrows = nyr * (z1 - z0 + 1);  // at most 25
+    // lane w < nrows holds box row w: first candidate, count, end in the stream
+    unsigned rb = 0u, rlen = 0u;
+    int rdy = 0, rdz = 0;
+    if (lane < nrows) {
+      const int y = y0 + lane % nyr, z = z0 + lane / nyr;
+      const unsigned rowbase = cellinit + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+      rb = a.begincell[rowbase + (unsigned)x0];
+      rlen = a.begincell[rowbase + (unsigned)x1 + 1u] - rb;
+      rdy = y - ry;
+      rdz = z - rz;
+    }
+    unsigned incl = rlen;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const unsigned total = __shfl_sync(FULL, incl, 31);
+    if (total == 0u) continue;
+    const unsigned rbase = rb - (incl - rlen);  // candidate index = rbase + stream position
+    if (ing) {  // the lane's position in the frame of cell (rx, ry, rz)
+      fx = ps1.x + (float)(cx - rx) * scell;
+      fy = ps1.y;
+      fz = ps1.z;
+    }
+    const float2 fxx = make_float2(fx, fx), fyy = make_float2(fy, fy), fzz = make_float2(fz, fz);
+    const unsigned gmask = ing ? FULL : 0u;
+    // this lane stages stream position s = part*plen + chunk*kTSeg + (lane % kTSeg)
+    const unsigned nch = (total + 31u) >> 5, plen = nch * kTSeg;
+    unsigned s = (unsigned)(lane / kTSeg) * plen + (unsigned)(lane % kTSeg);
+    int row = 0;  // the box row holding s: the rows whose end is <= s come before it
+    for (int w = 0; w < nrows; w++) row += __shfl_sync(FULL, incl, w) <= s ? 1 : 0;
+    unsigned rend = __shfl_sync(FULL, incl, min(row, 31));
+    const unsigned send = min((unsigned)(lane / kTSeg + 1) * plen, total);  // end of this lane's part
+    for (unsigned ch = 0; ch < nch; ch++, s += kTSeg) {
+      for (;;) {  // advance to the row holding s (rows may be empty)
+        const bool adv = s < send && s >= rend;
+        if (!__any_sync(FULL, adv)) break;
+        row += adv ? 1 : 0;
+        rend = __shfl_sync(FULL, incl, min(row, 31));
+      }
+      const bool has = s < send;
+      const int rowc = min(row, 31);
+      const unsigned jb = __shfl_sync(FULL, rbase, rowc);
+      const int dyj = __shfl_sync(FULL, rdy, rowc), dzj = __shfl_sync(FULL, rdz, rowc);
+      float4 ps2 = make_float4(kFarAway, kFarAway, kFarAway, 0.f), vr2 = make_float4(0.f, 0.f, 0.f, 1.f);
+      float4 ta2 = make_float4(0.f, 0.f, 0.f, 0.f);
+      float2 tb2 = make_float2(0.f, 0.f);
+      unsigned fixed = 0u;
+      if (has) {
+        const unsigned j = jb + s;
+        ps2 = a.pscell[j];
+        vr2 = a.velrho[j];
+        const int dxj = (int)(gb_cx(dcc, a.dcell[j]) - cmin0) - rx;
+        if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ta2 = a.taua[j]; tb2 = a.taub[j]; }
+        if (tshift && boundp2) fixed = (a.code[j] & GB_CODE_MASKTYPE) == 0u ? 1u : 0u;
+        ps2.x += (float)dxj * scell;
+        ps2.y += (float)dyj * scell;
+        ps2.z += (float)dzj * scell;
+      }
+      // the ring slot of this chunk must hold no pending hit of chunk cnext - R
+      while (__any_sync(FULL, cur != 0u && cc + (unsigned)R <= cnext))
+        tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, ps1.w,
+                                                                 inv_rho1, ta1, tb1, vfac, massp2, r, lane);
+      const unsigned base = (cnext & (R - 1)) << 5;
+      ring.sa[base + lane] = ps2;
+      ring.sb[base + lane] = vr2;
+      ring.nx[base + lane] = -ps2.x;
+      ring.ny[base + lane] = -ps2.y;
+      ring.nz[base + lane] = -ps2.z;
+      if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ring.st[base + lane] = ta2; ring.stb[base + lane] = tb2; }
+      if (tshift && boundp2) ring.sc[base + lane] = fixed;
+      __syncwarp();
+      // distance checks: four staged candidates per broadcast load
+      unsigned m = 0u;
+#pragma unroll
+      for (int q = 0; q < 32; q += 4) {
+        const float4 xq = *(const float4*)(ring.nx + base + q);
+        const float4 yq = *(const float4*)(ring.ny + base + q);
+        const float4 zq = *(const float4*)(ring.nz + base + q);
+        m |= tile_check4(fxx, fyy, fzz, xq, yq, zq, ks2, q);
+      }
+      m &= gmask;
+      ring.sm[base + lane] = m;
+      if (cc == cnext) cur = m;
+      cnext++;
+      if (cur == 0u) cc = cnext;
+      // rounds while every target of the row group has a pending hit
+      while (__ballot_sync(FULL, ing && cur != 0u) == grp)
+        tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, ps1.w,
+                                                                 inv_rho1, ta1, tb1, vfac, massp2, r, lane);
+    }
+  }
+  while (__any_sync(FULL, cur != 0u))
+    tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, ps1.w,
+                                                             inv_rho1, ta1, tb1, vfac, massp2, r, lane);
+  __syncwarp();  // the next pass reuses the ring
+}
+
+template <int tvisco, int tdensity, bool ddtgen, bool tshift, int R>
+__global__ void __launch_bounds__(kTBlock) k_forces_fluid_t(gbsph_consts c, PairK k, DevArrays a) {
+  extern __shared__ float4 tile_smem[];
+  using L = TileLayout<tvisco, tshift, R>;
+  const DivState& d = *a.div;
+  const unsigned np = d.np, npb = d.npb;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned p1 = npb + blockIdx.x * kTBlock + threadIdx.x;
+  const bool active = p1 < np;
+  if (__all_sync(0xffffffffu, !active)) return;
+  char* wbase = (char*)tile_smem + (size_t)warp * L::per_warp;
+  TileRing ring;
+  ring.sa = (float4*)wbase;
+  ring.sb = ring.sa + R * 32;
+  ring.nx = (float*)(ring.sb + R * 32);
+  ring.ny = ring.nx + R * 32;
+  ring.nz = ring.ny + R * 32;
+  ring.sm = (unsigned*)(ring.nz + R * 32);
+  ring.st = L::sps ? (float4*)(ring.sm + R * 32) : nullptr;
+  ring.stb = L::sps ? (float2*)(ring.st + R * 32) : nullptr;
+  ring.sc = tshift ? (unsigned*)(L::sps ? (void*)(ring.stb + R * 32) : (void*)(ring.sm + R * 32)) : nullptr;
+  float4 ps1 = make_float4(0, 0, 0, 0), vr1 = make_float4(0, 0, 0, 1);
+  float4 ta1 = make_float4(0, 0, 0, 0);
+  float2 tb1 = make_float2(0, 0);
+  int cx = 0, cy = 0, cz = 0;
+  if (active) {
+    ps1 = a.pscell[p1];
+    vr1 = a.velrho[p1];
+    if (tvisco == GBSPH_VISCO_LAMINARSPS) { ta1 = a.taua[p1]; tb1 = a.taub[p1]; }
+    const unsigned dcc = c.domcellcode, cel = a.dcell[p1];
+    cx = (int)gb_cx(dcc, cel) - (int)d.cellmin[0];
+    cy = (int)gb_cy(dcc, cel) - (int)d.cellmin[1];
+    cz = (int)gb_cz(dcc, cel) - (int)d.cellmin[2];
+  }
+  (void)lane;
+  const float inv_rho1 = gb_rcp(vr1.w);
+  PairAcc ff = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  tile_pass<tvisco, tdensity, false, ddtgen, tshift, R>(c, k, a, d, ring, active, cx, cy, cz, ps1, vr1, inv_rho1, ta1,
+                                                         tb1, ff);
+  {  // the fluid-neighbour sums carry no mass yet
+    const float mf = c.massfluid;
+    ff.ax *= mf; ff.ay *= mf; ff.az *= mf; ff.ar *= mf; ff.delta *= mf;
+    if (tdensity == GBSPH_DDT_DDT2 || tdensity == GBSPH_DDT_DDT2FULL) ff.delta *= k.ddt_kc;
+    ff.s0 *= mf; ff.s1 *= mf; ff.s2 *= mf; ff.s3 *= mf; ff.s4 *= mf; ff.s5 *= mf;
+    if (tshift) { ff.sh0 *= mf; ff.sh1 *= mf; ff.sh2 *= mf; ff.sh3 *= mf; }
+  }
+  tile_pass<tvisco, tdensity, true, ddtgen, tshift, R>(c, k, a, d, ring, active, cx, cy, cz, ps1, vr1, inv_rho1, ta1,
+                                                        tb1, ff);
+  ff.ar *= vr1.w;  // the rho1 factor of every continuity term
+  float acemax2 = 0, visc = 0, vel2 = 0;
+  if (active) {
+    float ar = ff.ar;
+    if (tdensity != GBSPH_DDT_NONE && ff.delta != FLT_MAX) ar += ff.delta;
+    const float ax = ff.ax, ay = ff.ay, az = ff.az;
+    a.acear[p1] = make_float4(ax, ay, az, ar);
+    if (tvisco == GBSPH_VISCO_LAMINARSPS) {
+      a.straina[p1] = make_float4(ff.s0, ff.s1, ff.s2, ff.s3);
+      a.strainb[p1] = make_float2(ff.s4, ff.s5);
+    }
+    if (tshift) a.shiftpos[p1] = make_float4(ff.sh0, ff.sh1, ff.sh2, ff.sh3);
+    // a NaN density rate makes the maximum NaN (x + 0 * ar is x otherwise)
+    acemax2 = ax * ax + ay * ay + az * az + 0.f * ar;
+    visc = ff.visc;
+    vel2 = vr1.x * vr1.x + vr1.y * vr1.y + vr1.z * vr1.z;
+  }
+  gb_warp_maxes(a.st, acemax2, visc, vel2);
 }
 
 // Bound rows (JSphCpu.cpp:633-703): continuity and visc from fluid neighbours.
@@ -600,14 +901,7 @@ __global__ void __launch_bounds__(128) k_forces_bound(gbsph_consts c, DevArrays 
     }
     a.acear[p1] = make_float4(0.f, 0.f, 0.f, arp1);
   }
-  for (int o = 16; o; o >>= 1) {
-    visc = fmaxf(visc, __shfl_xor_sync(0xffffffffu, visc, o));
-    vel2 = fmaxf(vel2, __shfl_xor_sync(0xffffffffu, vel2, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (visc > 0) gb_atomic_max_nonneg(&a.st->viscdt, visc);
-    if (vel2 > 0) gb_atomic_max_nonneg(&a.st->velmax2, vel2);
-  }
+  gb_warp_maxes(a.st, 0.f, visc, vel2);
 }
 
 // JSphCpu::ComputeSpsTau (JSphCpu.cpp:1279-1309) for fluid particles.
@@ -844,39 +1138,74 @@ __global__ void k_pips(gbsph_consts c, DevArrays a) {
   }
 }
 
+// The staged kernel with a ring of R chunks; with prepare set, only raises its
+// dynamic shared-memory limit (done once per context, outside any capture).
+template <int tvisco, int tdensity, bool ddtgen, bool tshift, int R>
+cudaError_t launch_tiled(const gbsph_consts& c, const PairK& k, const DevArrays& a, unsigned cap, bool prepare,
+                         cudaStream_t s) {
+  using L = TileLayout<tvisco, tshift, R>;
+  if (prepare)
+    return cudaFuncSetAttribute(k_forces_fluid_t<tvisco, tdensity, ddtgen, tshift, R>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes);
+  k_forces_fluid_t<tvisco, tdensity, ddtgen, tshift, R><<<gb_div_up(cap, kTBlock), kTBlock, L::bytes, s>>>(c, k, a);
+  return cudaSuccess;
+}
+
+template <int tvisco, int tdensity, bool ddtgen, bool tshift>
+cudaError_t launch_fluid_g(const gbsph_consts& c, const PairK& k, const DevArrays& a, unsigned cap, int variant,
+                           bool prepare, cudaStream_t s) {
+  if (variant == 2 || prepare) {
+    const cudaError_t e = launch_tiled<tvisco, tdensity, ddtgen, tshift, 8>(c, k, a, cap, prepare, s);
+    if (variant == 2 || e != cudaSuccess) return e;
+  }
+  if (variant == 3 || prepare) return launch_tiled<tvisco, tdensity, ddtgen, tshift, 4>(c, k, a, cap, prepare, s);
+  k_forces_fluid_q<tvisco, tdensity, ddtgen, tshift><<<gb_div_up(cap, kQBlock), kQBlock, 0, s>>>(c, k, a);
+  return cudaSuccess;
+}
+
 template <int tvisco, int tdensity, bool tshift>
-void launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, cudaStream_t s) {
-  if (variant == 1) {  // one thread per row: any block size of 64, 128 or 256
+cudaError_t launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, bool prepare,
+                         cudaStream_t s) {
+  if (variant == 1 && !prepare) {  // one thread per row: any block size of 64, 128 or 256
     const unsigned bs = (bsize == 64 || bsize == 256) ? (unsigned)bsize : 128u;
     k_forces_fluid<tvisco, tdensity, tshift><<<gb_div_up(cap, bs), bs, 0, s>>>(c, a);
-    return;
+    return cudaSuccess;
   }
   const PairK k = make_pairk(c);
-  const unsigned grid = gb_div_up(cap, kQBlock);
   if constexpr (tdensity == GBSPH_DDT_DDT2 || tdensity == GBSPH_DDT_DDT2FULL) {
     // the series form of the hydrostatic term holds for |ddtgz*drz| < 0.05 and
     // |drz| <= 2h for every pair; otherwise the general power form is compiled in
-    if (!(fabsf(c.ddtgz) * c.kernelsize < 0.049f)) {
-      k_forces_fluid_q<tvisco, tdensity, true, tshift><<<grid, kQBlock, 0, s>>>(c, k, a);
-      return;
-    }
+    if (!(fabsf(c.ddtgz) * c.kernelsize < 0.049f))
+      return launch_fluid_g<tvisco, tdensity, true, tshift>(c, k, a, cap, variant, prepare, s);
   }
-  k_forces_fluid_q<tvisco, tdensity, false, tshift><<<grid, kQBlock, 0, s>>>(c, k, a);
+  return launch_fluid_g<tvisco, tdensity, false, tshift>(c, k, a, cap, variant, prepare, s);
 }
 
 template <int tvisco, int tdensity>
-void launch_fluid_s(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, cudaStream_t s) {
-  if (c.tshift) launch_fluid<tvisco, tdensity, true>(c, a, cap, variant, bsize, s);
-  else launch_fluid<tvisco, tdensity, false>(c, a, cap, variant, bsize, s);
+cudaError_t launch_fluid_s(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize,
+                           bool prepare, cudaStream_t s) {
+  if (c.tshift) return launch_fluid<tvisco, tdensity, true>(c, a, cap, variant, bsize, prepare, s);
+  return launch_fluid<tvisco, tdensity, false>(c, a, cap, variant, bsize, prepare, s);
 }
 
 template <int tvisco>
-void launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, cudaStream_t s) {
+cudaError_t launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize,
+                           bool prepare, cudaStream_t s) {
   switch (c.tdensity) {
-    case GBSPH_DDT_NONE: launch_fluid_s<tvisco, GBSPH_DDT_NONE>(c, a, cap, variant, bsize, s); break;
-    case GBSPH_DDT_DDT: launch_fluid_s<tvisco, GBSPH_DDT_DDT>(c, a, cap, variant, bsize, s); break;
-    case GBSPH_DDT_DDT2: launch_fluid_s<tvisco, GBSPH_DDT_DDT2>(c, a, cap, variant, bsize, s); break;
-    default: launch_fluid_s<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, variant, bsize, s); break;
+    case GBSPH_DDT_NONE: return launch_fluid_s<tvisco, GBSPH_DDT_NONE>(c, a, cap, variant, bsize, prepare, s);
+    case GBSPH_DDT_DDT: return launch_fluid_s<tvisco, GBSPH_DDT_DDT>(c, a, cap, variant, bsize, prepare, s);
+    case GBSPH_DDT_DDT2: return launch_fluid_s<tvisco, GBSPH_DDT_DDT2>(c, a, cap, variant, bsize, prepare, s);
+    default: return launch_fluid_s<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, variant, bsize, prepare, s);
+  }
+}
+
+cudaError_t launch_fluid_v(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize,
+                           bool prepare, cudaStream_t s) {
+  switch (c.tvisco) {
+    case GBSPH_VISCO_ARTIFICIAL:
+      return launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, variant, bsize, prepare, s);
+    case GBSPH_VISCO_LAMINAR: return launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, variant, bsize, prepare, s);
+    default: return launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, variant, bsize, prepare, s);
   }
 }
 
@@ -894,13 +1223,14 @@ void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, 
   if (ev_fluid_begin || ev_fluid_end) cudaStreamIsCapturing(s, &cap_st);
   const unsigned ev_flags = cap_st == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (ev_fluid_begin) cudaEventRecordWithFlags(ev_fluid_begin, s, ev_flags);
-  switch (c.tvisco) {
-    case GBSPH_VISCO_ARTIFICIAL: launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, variant, bsize, s); break;
-    case GBSPH_VISCO_LAMINAR: launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, variant, bsize, s); break;
-    default: launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, variant, bsize, s); break;
-  }
+  launch_fluid_v(c, a, cap, variant, bsize, false, s);
   if (ev_fluid_end) cudaEventRecordWithFlags(ev_fluid_end, s, ev_flags);
   if (nlaunch) *nlaunch += 2;
+}
+
+cudaError_t forces_init(const gbsph_consts& c) {
+  DevArrays a{};
+  return launch_fluid_v(c, a, 0, 2, 128, true, nullptr);
 }
 
 void sps_tau(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch) {

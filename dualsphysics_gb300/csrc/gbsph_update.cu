@@ -197,8 +197,10 @@ __global__ void k_dtvar(gbsph_consts c, StepState* st, int which) {
   const double h = (double)c.kernelh;
   const double dt1 = (acemax ? sqrt(h / acemax) : DBL_MAX);
   const double vm = (double)velmax * 10.;
-  const double dt2 = h / ((c.cs0 > vm ? c.cs0 : vm) + h * (double)viscdt);
-  double dt = c.cflnumber * (dt1 < dt2 ? dt1 : dt2);
+  // std::max(Cs0, vm) and std::min(dt1, dt2) as the reference writes them: the
+  // same values for numbers, and a NaN dt1 (from a NaN AceMax) is kept
+  const double dt2 = h / ((c.cs0 < vm ? vm : c.cs0) + h * (double)viscdt);
+  double dt = c.cflnumber * (dt2 < dt1 ? dt2 : dt1);
   if (isnan(dt) || isinf(dt)) {
     st->error |= GB_ERR_NANDT;
     dt = c.dtmin;

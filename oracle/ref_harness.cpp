@@ -12,6 +12,7 @@
 //
 //   ref_harness <casedir> <casename> <outdir> <nsteps_after_first> <threads>
 //==============================================================================
+#include <chrono>
 #include "JSphCpuSingle.h"
 #include "JSphCfgRun.h"
 #include "JDsGaugeSystem.h"
@@ -353,6 +354,26 @@ class OracleCpu : public JSphCpuSingle{
     }
     fclose(o);
   }
+  // Timing (timing.txt: "<nsteps>"): steps as the Run loop does, wall clock
+  // around the steps only (the case is loaded and divided before); writes
+  // "steps <n> seconds <t> np <np>" to timing_out.txt.
+  void RunTiming(const std::string& infile){
+    FILE* f=fopen(infile.c_str(),"r");
+    if(!f)return;
+    unsigned nsteps=0;
+    if(fscanf(f,"%u",&nsteps)!=1){ fclose(f); return; }
+    fclose(f);
+    const auto t0=std::chrono::steady_clock::now();
+    for(unsigned c=0;c<nsteps;c++){
+      const double stepdt=ComputeStep();
+      RunCellDivide(true);
+      TimeStep+=stepdt; Nstep++;
+    }
+    const double sec=std::chrono::duration<double>(std::chrono::steady_clock::now()-t0).count();
+    FILE* o=fopen((Out+"/timing_out.txt").c_str(),"w");
+    fprintf(o,"steps %u seconds %.6f np %u\n",nsteps,sec,Np);
+    fclose(o);
+  }
 };
 
 int main(int argc,char** argv){
@@ -383,7 +404,8 @@ int main(int argc,char** argv){
     OracleCpu sph;
     sph.Out=outdir;
     sph.Prepare(AppInfo.GetFullName(),&cfg,log);
-    if(fun::FileExists(casedir+"/series.txt"))sph.RunSeries(casedir+"/series.txt");
+    if(fun::FileExists(casedir+"/timing.txt"))sph.RunTiming(casedir+"/timing.txt");
+    else if(fun::FileExists(casedir+"/series.txt"))sph.RunSeries(casedir+"/series.txt");
     else{
       if(sph.IsSymplectic())sph.FirstStepDetailed();
       else sph.FirstStepVerlet();

@@ -86,3 +86,56 @@ def test_single_fluid_particle():
     _compare(st, o)
     f = st["idp"] == cd.npb
     assert st["velrho"][f, 2][0] < 0                          # falling
+
+
+# ---- failure detection (faults made on the host: no GPU fault is involved) ----
+def test_nan_in_the_state_is_reported_as_nan_dt():
+    """A NaN velocity uploaded in one fluid particle: its neighbours' density
+    rates are NaN after the first interaction, the maximum behind dt keeps the
+    NaN, and the step reports GBSPH_ENAN_DT (the reference's check of a NaN or
+    infinite dt, JSphCpu.cpp:2053-2060, JSphGpu.cpp:1122-1131)."""
+    from dualsphysics_gb300 import _lib
+    from dualsphysics_gb300.sph import GbSphSingle
+    cd = copy.copy(G.load_generated("dbc_d04"))
+    cd.velrho = cd.velrho.copy()
+    k = cd.npb + (cd.np - cd.npb) // 2                      # a fluid particle inside the column
+    cd.velrho[k, 0] = np.nan
+    s = GbSphSingle(0)
+    s.setup(cd)
+    with pytest.raises(_lib.GbsphError) as e:
+        s.ComputeStep()
+        s.step_dt()
+    assert e.value.code == -3 and "NaN" in str(e.value)
+    s.close()
+    # the same state without the NaN steps normally
+    cd.velrho[k, 0] = 0.0
+    s = GbSphSingle(0)
+    s.setup(cd)
+    s.ComputeStep()
+    assert np.isfinite(s.step_dt()[0])
+    s.close()
+
+
+def test_moving_boundary_driven_out_of_the_map_is_reported():
+    """A moving tank driven upwards at 5 m/s by a uniform rectilinear motion
+    (mvrect) leaves the map through its top: the divide after the step that
+    moved boundary particles out reports GBSPH_EBOUND_OUT (the reference's
+    "boundary particles out" exception, JSph.cpp:2837)."""
+    from dualsphysics_gb300 import _lib
+    from dualsphysics_gb300.sph import GbSphSingle
+    cd = copy.copy(G.load_generated("mov_d04"))
+    nb = cd.npb
+    cd.motion = {"objects": [(0, nb)],
+                 "movements": [{"obj": 0, "next": 0, "angdegrees": True, "type": "mvrect", "id": 1,
+                                "duration": 100.0, "vel": (0.0, 0.0, 5.0)}],
+                 "events": [(0, 1, 0.0, -1.0)]}
+    s = GbSphSingle(0)
+    s.setup(cd)
+    steps = 0
+    with pytest.raises(_lib.GbsphError) as e:
+        for steps in range(1, 4001):
+            s.ComputeStep()
+            s.step_dt()
+    assert e.value.code == -4 and "boundary" in str(e.value)
+    assert steps > 1                                          # the tank first moved inside the map
+    s.close()

@@ -82,9 +82,10 @@ def test_forces_within_tolerance(name):
 
 @pytest.mark.parametrize("name", ["dbc_d04", "vel_d04", "sps_d04", "mdbc_d04", "lam_d04", "ddt2f_d04", "half_d04",
                                   "shift_d04", "shiftnb_d04"])
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_forces_variants_within_tolerance(name, variant):
-    """Both fluid-row kernels: queued rounds (0), one thread per particle (1)."""
+    """Every fluid-row kernel: queued rounds (0), one thread per particle (1),
+    cell-tiled staged with a ring of 8 (2) or 4 (3) chunks."""
     cd = G.load_generated(name)
     s = _gpu(cd)
     s.set_option(1, variant)
