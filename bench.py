@@ -2,7 +2,7 @@
 obstacle at dp=0.0025 m (~5.2M fluid + ~1.5M boundary particles).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference] [--dp DP]
-    python bench.py --workload c3|ensemble|closure   (the other measured workloads)
+    python bench.py --workload c3|c3err|ensemble|closure   (the other measured workloads)
 
 A step is one Symplectic step (predictor + corrector interaction passes, two
 cell divisions, mDBC correction, dt reduction) of the whole particle set.
@@ -16,15 +16,17 @@ cell divisions, mDBC correction, dt reduction) of the whole particle set.
   launch bracketed by CUDA events inside the timed region.  Algorithmic bytes
   per launch: 52 B per fluid row (pscell, velrho, dcell read; acear written)
   plus 32 B per boundary particle (read once as a neighbour); ``traffic`` is
-  the DRAM bytes per launch from the ncu capture summarised in
-  profiles/k_forces_fluid_q_c2_dram.md.  The kernel is issue-bound, so its HBM
+  the DRAM bytes per launch that ncu measured for that kernel on this
+  workload (DRAM_TRAFFIC below, with the capture it comes from).  The kernel is issue-bound, so its HBM
   fraction is small by construction; ``roofline_fp32`` states the same
   launches against the FP32 FLOP model (80 FLOP per real fluid-row pair) and
   the nominal FFMA rate at the sampled SM clock, and ``gather_gbs`` the
   neighbour bytes the checks read through L1/L2 (32 B per checked neighbour).
 * ``cpu_baseline``: the oracle (CPU restatement of the reference step, OpenMP
-  on all host cores) timed on a bounded sample of the same state.
-* ``--impl reference``: the oracle port on the host cores as the reference arm.
+  on all host cores), in its timing build, timed over full steps of the same
+  state.
+* ``--impl reference``: the same timed oracle on the host cores as the
+  reference arm (the reference's own solver does not build on the GPU host).
 Inputs (~1.5 GB of particle arrays) are larger than L2 (129 MB).
 """
 from __future__ import annotations
@@ -51,21 +53,19 @@ BYTES_PER_BOUND_NEIGHBOUR = 32.0  # pscell + velrho of a boundary particle, read
 FP32_LANES_PER_SM = 128     # FFMA lanes per SM (2 FLOP each per clock)
 
 
-def _dram_traffic(dp: float):
-    """DRAM bytes per fluid-row launch from the committed ncu summary, when it
-    was captured on this workload."""
-    try:
-        vals = {}
-        with open(os.path.join(ROOT, "profiles", "k_forces_fluid_q_c2_dram.md")) as f:
-            for line in f:
-                if ":" in line and line.split(":")[0] in ("traffic_bytes_per_launch", "traffic_dp"):
-                    k, v = line.split(":", 1)
-                    vals[k] = float(v)
-        if abs(vals.get("traffic_dp", -1) - dp) < 1e-12:
-            return vals.get("traffic_bytes_per_launch")
-    except OSError:
-        pass
-    return None
+# DRAM bytes per launch of the fluid-row kernels on the C2 workload (dp =
+# 0.0025 m), from one ncu capture each (dram__bytes_read.sum +
+# dram__bytes_write.sum, --clock-control none), summarised in profiles/:
+# variant -> (kernel, bytes per launch, dp of the capture)
+DRAM_TRAFFIC = {0: ("k_forces_fluid_q", 269218560.0, 0.0025)}
+# the fluid-row kernel of each variant (gbsph_set_option key 1)
+KERNEL_NAME = {0: "k_forces_fluid_q", 1: "k_forces_fluid", 2: "k_forces_fluid_t (ring of 8 chunks)",
+               3: "k_forces_fluid_t (ring of 4 chunks)"}
+
+
+def _dram_traffic(variant: int, dp: float):
+    v = DRAM_TRAFFIC.get(variant)
+    return v[1] if v and abs(v[2] - dp) < 1e-12 else None
 
 
 def _pinned(shape, dtype):
@@ -179,50 +179,122 @@ def make_case(dp: float, cellmode: str = "full", workload: str = "c2"):
 
 
 def workload_text(args) -> str:
-    if args.workload == "c3":
+    if args.workload in ("c3", "c3err"):
         return (f"large plain dam break (tank 6.4x2.68x1.6 m, column 1.6x2.68x0.6 m), DBC walls, dp={args.dp}, "
                 f"Symplectic, Wendland, artificial visc 0.01, DDT2 0.1")
     return (f"3-D dam break (tank 1.6x0.67x0.4 m, column 0.4x0.67x0.3 m), mDBC + 0.12x0.12x0.45 m box obstacle, "
             f"dp={args.dp}, Symplectic, Wendland, artificial visc 0.01, DDT2 0.1")
 
 
-def cpu_baseline(cd, stride: int, steps: int = 1):
-    """Oracle (OpenMP on all host cores) on a bounded sample: every step runs
-    the divides, mDBC and updates in full and the interaction rows p with
-    p % stride == phase; the full-step time is extrapolated as
-    t_step + (stride-1) * t_interaction."""
+def cpu_baseline(cd, steps: int, warmup: int = 0):
+    """The oracle's timing build (OpenMP on all host cores) over `steps` full,
+    unsampled steps of the state `cd` after `warmup` untimed steps; returns
+    (mean seconds per step, threads)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
     po.build()
+    po.use_timing_build()
     ct = po.config(po.params_from(cd.params))
     sim = po.Sim(ct, cd.pos, cd.velrho, cd.idp, cd.code, cd.npb, cd.boundnor)
-    ts = []
-    for k in range(steps):
-        po.lib().orc_set_sampling(stride, k % stride)
+    for _ in range(warmup):
         sim.step()
-        t_inter, t_step = sim.times()
-        ts.append(t_step + (stride - 1) * t_inter)
-    po.lib().orc_set_sampling(1, 0)
-    return float(np.mean(ts)), os.cpu_count()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.step()
+    t = (time.perf_counter() - t0) / max(steps, 1)
+    return t, int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
 
 
 def run_reference(args, cd, rank):
-    stride = args.ref_stride
-    t_warm = [cpu_baseline(cd, stride, 1)[0] for _ in range(min(args.warmup, 1))]
-    del t_warm
-    t, cores = cpu_baseline(cd, stride, args.steps)
+    """The reference arm: full oracle steps (timing build) on the host cores,
+    one untimed warm-up step (a CPU step needs no more), then K timed steps."""
+    warm = min(args.warmup, 1)
+    t, cores = cpu_baseline(cd, args.steps, warm)
     v = 1.0 / t
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "steps": args.steps, "warmup": warm, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 positions)", "data": "synthetic",
             "config": {"workload": workload_text(args), "particles": cd.np,
                        "fluid": cd.nfluid, "boundary": cd.npb, "l2": "inputs larger than L2"},
             "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
-                             "sample": f"oracle step with 1/{stride} of the interaction rows per step, "
-                                       f"full step time extrapolated, {args.steps} steps"},
+                             "sample": f"{args.steps} full oracle steps of the workload (timing build: the "
+                                       f"reference's -O3 -ffast-math), after {warm} warm-up step"},
             "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if rank == 0:
         print(json.dumps(line))
+
+
+def _dt_from(c, acemax, velmax, viscdt):
+    """DtVariable (JSphCpu.cpp:2035-2078) in double from the three maxima."""
+    h = float(c.kernelh)
+    dt1 = np.sqrt(h / acemax) if acemax else np.finfo(np.float64).max
+    dt2 = h / (max(float(c.cs0), velmax * 10.0) + h * viscdt)
+    return max(float(c.cflnumber) * min(dt1, dt2), float(c.dtmin))
+
+
+def run_c3err(args, local: int = 0):
+    """C3 error statement (--workload c3err): the large plain run (49.4 M
+    particles) stepped `--steps` times on the GPU; at the first, middle and
+    last step the state is read back, and the interaction the next step starts
+    with (the predictor's Interaction_Forces and DtVariable) is evaluated both
+    on the GPU and by the oracle in FP64 (and, for comparison, in FP32, the
+    reference's own algorithm and evaluation order) on that same state.
+    Reports, per sample, the scaled errors (|x - x_f64| / conditioning scale)
+    of ace (fluid rows) and ar (all rows) -- maximum, 99.9th percentile and
+    median -- and the relative error of AceMax and of the dt."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    from dualsphysics_gb300 import _lib
+    from dualsphysics_gb300.sph import GbSphSingle
+    po.build()
+    cd = make_case(args.dp, args.cellmode, "c3")
+    s = GbSphSingle(local)
+    s.setup(cd)
+    ct = po.config(po.params_from(cd.params))
+    K = args.steps
+    samples = sorted({0, K // 2, K})
+    out = []
+
+    def errs(x, ref, scale):
+        e = np.abs(np.asarray(x, np.float64) - ref)
+        e = (e.max(axis=1) if e.ndim == 2 else e) / np.maximum(scale, 1e-30)
+        return {"max": float(e.max()), "p99.9": float(np.percentile(e, 99.9)), "median": float(np.median(e))}
+
+    t0 = time.perf_counter()
+    for k in range(K + 1):
+        if k in samples:
+            mx = s.Interaction_Forces(_lib.INTERSTEP_SYMPREDICTOR)
+            dt_gpu = s.DtVariable(False)
+            ace, ar = s.forces()
+            gs = s.download()
+            o = po.Sim(ct, gs["pos"], gs["velrho"], gs["idp"], gs["code"], cd.npb, None)
+            assert np.array_equal(o.state()["idp"], gs["idp"]), "the oracle's divide of the GPU state differs"
+            f64 = po.forces_f64(o)
+            o.interaction()
+            a32, r32 = o.forces()
+            om = o.maxes()
+            npb = o.npb
+            acemax64 = float(np.sqrt((f64["ace"][npb:] ** 2).sum(axis=1).max()))
+            dt64 = _dt_from(ct, acemax64, om["velmax"], f64["viscdt"])
+            out.append({"step": k, "particles": int(o.np),
+                        "ace_gpu": errs(ace[npb:], f64["ace"][npb:], f64["absace"][npb:]),
+                        "ace_oracle_fp32": errs(a32[npb:], f64["ace"][npb:], f64["absace"][npb:]),
+                        "ar_gpu": errs(ar, f64["ar"], f64["absar"]),
+                        "ar_oracle_fp32": errs(r32, f64["ar"], f64["absar"]),
+                        "acemax_rel": abs(mx["acemax"] - acemax64) / acemax64,
+                        "viscdtmax_rel": abs(mx["viscdtmax"] - f64["viscdt"]) / max(f64["viscdt"], 1e-30),
+                        "dt_rel": abs(dt_gpu - dt64) / dt64})
+            del o, f64
+            print(json.dumps(out[-1]), flush=True)
+        if k < K:
+            s.RunSteps(1, use_graph=True)
+    s.close()
+    worst = {q: max(r[q]["max"] for r in out) for q in ("ace_gpu", "ace_oracle_fp32", "ar_gpu", "ar_oracle_fp32")}
+    line = {"metric": "FP32 error against the FP64 oracle, C3 (max over the samples)", "value": worst["ace_gpu"],
+            "unit": "scaled error of ace", "steps": K, "samples": out, "worst": worst,
+            "dt_rel_max": max(r["dt_rel"] for r in out), "wall_s": time.perf_counter() - t0,
+            "config": {"workload": workload_text(args), "particles": cd.np}}
+    print(json.dumps(line))
 
 
 def run_ensemble(args, local: int = 0):
@@ -355,15 +427,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
     ap.add_argument("--dp", type=float, default=0.0025)
-    ap.add_argument("--ref-stride", type=int, default=16)
-    ap.add_argument("--cpu-stride", type=int, default=16)
+    ap.add_argument("--cpu-steps", type=int, default=None,
+                    help="full oracle steps timed for cpu_baseline (default 2; 1 for c3)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cellmode", default="full", choices=["full", "half"],
                     help="the reference's -cellmode run option: cells of 2h (default) or h")
     ap.add_argument("--variant", type=int, default=None,
-                    help="fluid-row kernel: 0 queued rounds, 1 one thread per particle")
+                    help="fluid-row kernel: 0 queued rounds, 1 one thread per particle, 2/3 cell-tiled staged "
+                         "(ring of 8/4 chunks); default: the library's")
     ap.add_argument("--no-tune", action="store_true", help="keep the 8-bit sort digits (no sort autotuning)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "ensemble", "closure"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c3err", "ensemble", "closure"],
                     help="c2: the dam break with obstacle (default); c3: the large plain run (dp 0.004, "
                          "~49 M particles); ensemble: the batched cases; closure: the learned closure against "
                          "fine runs")
@@ -378,10 +451,12 @@ def main():
     ap.add_argument("--ens-scale", type=float, default=1.0, help="scales every case's particle count")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.workload == "c3" and args.dp == 0.0025:
+    if args.workload in ("c3", "c3err") and args.dp == 0.0025:
         args.dp = 0.004
-    if args.workload == "c3" and args.cpu_stride == 16:
-        args.cpu_stride = 128   # a bounded CPU sample of the 49 M-particle state
+    if args.workload == "c3err" and args.steps == 20:
+        args.steps = 200
+    if args.cpu_steps is None:
+        args.cpu_steps = 1 if args.workload == "c3" else 2
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -399,9 +474,9 @@ def main():
             dist.destroy_process_group()
         return
 
-    if args.workload in ("ensemble", "closure"):
+    if args.workload in ("ensemble", "closure", "c3err"):
         if rank == 0:
-            (run_ensemble if args.workload == "ensemble" else run_closure)(args, local)
+            {"ensemble": run_ensemble, "closure": run_closure, "c3err": run_c3err}[args.workload](args, local)
         if dist:
             dist.destroy_process_group()
         return
@@ -421,6 +496,7 @@ def main():
         s._check(_lib.lib().gbsph_tune_sort(s.ctx, 3, C.byref(sort_bits), sort_ms), "gbsph_tune_sort")
     if args.variant is not None:
         s.set_option(1, args.variant)
+    variant = s.get_option(1)
     pi = s.pips()
     s.RunSteps(W, use_graph=True)
     s.sync()
@@ -478,12 +554,12 @@ def main():
         e.close()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        t_cpu, cores = cpu_baseline(cd, args.cpu_stride, 1)
+        t_cpu, cores = cpu_baseline(cd, args.cpu_steps)
         cpu = {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": cores, "kind": "port",
-               "sample": f"one oracle step of the same state with 1/{args.cpu_stride} of the interaction rows, "
-                         f"full step time extrapolated"}
+               "sample": f"{args.cpu_steps} full oracle steps of the same state (timing build: the reference's "
+                         f"-O3 -ffast-math; within 4% of the reference's own solver on C1, same threads)"}
     clks = clk.summary()
-    traffic = _dram_traffic(args.dp)
+    traffic = _dram_traffic(variant, args.dp)
     fp32_nominal = None
     if clks.get("sm_mhz"):
         fp32_nominal = _sm_count(local) * FP32_LANES_PER_SM * 2 * clks["sm_mhz"] * 1e6 / 1e12
@@ -510,7 +586,7 @@ def main():
             "np_after": info["np"],
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": ach / peaks["hbm_gbs"], "traffic": traffic,
-                         "kernel": "k_forces_fluid_q",
+                         "kernel": KERNEL_NAME.get(variant, str(variant)),
                          "model": "52 B per fluid row + 32 B per boundary neighbour per launch",
                          "peak_source": src, "launch_ms": kavg, "launches_timed": int(len(kms)),
                          "gather_gbs": gather_gbs},

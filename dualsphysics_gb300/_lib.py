@@ -105,7 +105,7 @@ MOV_TYPES = {"wait": 1, "mvrect": 2, "mvrectace": 3, "mvrot": 4, "mvrotace": 5, 
              "mvnull": 8}
 
 
-TUNE_CANDIDATES = 4
+TUNE_CANDIDATES = 6
 
 
 class TuneResult(C.Structure):
@@ -144,6 +144,7 @@ SIGNATURES = {
     "gbsph_launch_count": (C.c_ulonglong, [P]),
     "gbsph_stream": (P, [P]),
     "gbsph_set_option": (C.c_int, [P, C.c_int, C.c_int]),
+    "gbsph_get_option": (C.c_int, [P, C.c_int, C.POINTER(C.c_int)]),
     "gbsph_tune_forces": (C.c_int, [P, C.c_int, C.POINTER(TuneResult)]),
     "gbsph_tune_sort": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), P]),
     "gbsph_ffma_peak": (C.c_int, [C.c_int, C.POINTER(C.c_float)]),

@@ -37,7 +37,7 @@ struct gbsph_ctx {
   bool uploaded = false;
   int verletstep = 0;
   unsigned long long launches = 0;
-  int forces_bsize = 128, forces_variant = 0;
+  int forces_bsize = 128, forces_variant = 3;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_parity = -1;  // pointer-swap parity the graph was captured with
@@ -1042,13 +1042,25 @@ void* gbsph_stream(gbsph_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; 
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value) {
   if (!ctx) return GBSPH_EINVAL;
   if (key == 0) ctx->forces_bsize = value;
-  else if (key == 1) ctx->forces_variant = value;
+  else if (key == 1) {
+    if (value < 0 || value > 3) return set_err(ctx, GBSPH_EINVAL, "fluid-row kernel variant %d is not 0..3", value);
+    ctx->forces_variant = value;
+  }
   else if (key == 2) {
     if (value != 8 && value != 11) return set_err(ctx, GBSPH_EINVAL, "sort digits of 8 or 11 bits");
     ctx->sort_bits = value;
   }
   else return set_err(ctx, GBSPH_EINVAL, "unknown option %d", key);
   reset_graph(ctx);
+  return GBSPH_OK;
+}
+
+int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value) {
+  if (!ctx || !value) return GBSPH_EINVAL;
+  if (key == 0) *value = ctx->forces_bsize;
+  else if (key == 1) *value = ctx->forces_variant;
+  else if (key == 2) *value = ctx->sort_bits;
+  else return GBSPH_EINVAL;
   return GBSPH_OK;
 }
 
@@ -1092,14 +1104,16 @@ int gbsph_tune_sort(gbsph_ctx* ctx, int reps, int* best_bits, float* ms) {
 
 // ---- autotuner ------------------------------------------------------------
 // Times the fluid-row kernel configurations on the context's current state
-// (between steps) and keeps the fastest: the warp-queued rounds kernel, and the
-// one-thread-per-row kernel at 64, 128 and 256 threads per block.  The launches
-// only rewrite the interaction outputs, which the next step recomputes.
+// (between steps) and keeps the fastest: the cell-tiled staged kernel with a
+// ring of 4 and of 8 chunks, the warp-queued rounds kernel, and the
+// one-thread-per-row kernel at 64, 128 and 256 threads per block.  The
+// launches only rewrite the interaction outputs, which the next step
+// recomputes.
 int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
   if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
   if (reps < 1) reps = 1;
   CK(cudaSetDevice(ctx->device), "set device");
-  static const int cand[GBSPH_TUNE_CANDIDATES][2] = {{0, 128}, {1, 64}, {1, 128}, {1, 256}};
+  static const int cand[GBSPH_TUNE_CANDIDATES][2] = {{3, 128}, {2, 128}, {0, 128}, {1, 64}, {1, 128}, {1, 256}};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0), "event");
   CK(cudaEventCreate(&e1), "event");

@@ -747,8 +747,19 @@ namespace gbk {
 
 unsigned sort_noalloc_max_keys() { return kNoAllocMaxKeys; }
 
-// Device address of the work area on the current device.
-cudaError_t sort_noalloc_address(void** p) { return cudaGetSymbolAddress(p, g_sort_work); }
+// Device address of the work area on the current device.  The kernels of the
+// no-alloc sort are loaded here as well (cudaFuncGetAttributes loads a
+// function under lazy module loading), so that no later call loads code.
+cudaError_t sort_noalloc_address(void** p) {
+  cudaError_t e = cudaGetSymbolAddress(p, g_sort_work);
+  cudaFuncAttributes fa;
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_na_init);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_rs_hist<kRadixBits>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_rs_scan_cols);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_rs_scan_digits<kRadixBits>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_rs_scatter<kRadixBits>);
+  return e;
+}
 
 void sort_noalloc(unsigned char* work, const unsigned* keys, unsigned n, unsigned nbits, unsigned* perm,
                   unsigned* sorted_keys, cudaStream_t s) {

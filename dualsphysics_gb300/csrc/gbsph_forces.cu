@@ -566,8 +566,10 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, Pair
 // widened by sd.  These ranges, taken as one stream, are staged 32 candidates
 // (a chunk) at a time through a per-warp ring of R chunks in shared memory.
 // A chunk draws kTSeg consecutive candidates from each of 32/kTSeg equal
-// parts of the stream, so that every chunk samples the whole neighbourhood and
-// the targets' hits arrive at similar rates; each lane stages one candidate
+// parts of the stream, and the chunks are taken in a strided order, so that
+// every few chunks sample the whole neighbourhood and the targets' hits
+// arrive at similar rates (a lane whose hits come faster than the others'
+// forces rounds in which the others idle); each lane stages one candidate
 // with coalesced float4 loads (pscell, velrho), its position moved into the
 // frame of one cell of the group.  The distance checks read the staged
 // positions as broadcasts (structure of arrays, four candidates a load) and
@@ -578,9 +580,10 @@ __global__ void __launch_bounds__(kQBlock) k_forces_fluid_q(gbsph_consts c, Pair
 // when the ring slot about to be refilled still holds one.  A candidate of the
 // widened ranges that lies outside a target's own 27 (or 125) boxes is more
 // than 2h away from it and fails the check, so the pairs are those of the
-// per-target walk; the summation order per target is the order of the stream.
+// per-target walk; the summation order per target is the order in which the
+// chunks are taken.
 constexpr int kTBlock = 128;
-constexpr int kTSeg = 8;             // consecutive candidates a chunk takes from each part of the stream
+constexpr int kTSeg = 4;             // consecutive candidates a chunk takes from each part of the stream
 constexpr float kFarAway = 1.0e18f;  // position of an empty ring slot: fails every check
 
 template <int tvisco, bool tshift, int R>
@@ -713,22 +716,36 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
     }
     const float2 fxx = make_float2(fx, fx), fyy = make_float2(fy, fy), fzz = make_float2(fz, fz);
     const unsigned gmask = ing ? FULL : 0u;
-    // this lane stages stream position s = part*plen + chunk*kTSeg + (lane % kTSeg)
+    // Chunk ch (taken in the order ch = i * stride mod nch, a stride near
+    // 0.618 nch and coprime with it, so that consecutive chunks lie far apart
+    // in every part of the stream) has this lane stage stream position
+    // s = part * plen + ch * kTSeg + lane % kTSeg.
     const unsigned nch = (total + 31u) >> 5, plen = nch * kTSeg;
-    unsigned s = (unsigned)(lane / kTSeg) * plen + (unsigned)(lane % kTSeg);
-    int row = 0;  // the box row holding s: the rows whose end is <= s come before it
-    for (int w = 0; w < nrows; w++) row += __shfl_sync(FULL, incl, w) <= s ? 1 : 0;
-    unsigned rend = __shfl_sync(FULL, incl, min(row, 31));
+    unsigned stride = max(1u, (unsigned)__float2uint_rn(0.6180339887f * (float)nch));
+    for (;;) {  // the smallest stride from there that is coprime with nch
+      unsigned u = stride, v = nch;
+      while (v) { const unsigned t = u % v; u = v; v = t; }
+      if (u == 1u) break;
+      stride++;
+    }
+    const unsigned pbase = (unsigned)(lane / kTSeg) * plen + (unsigned)(lane % kTSeg);
     const unsigned send = min((unsigned)(lane / kTSeg + 1) * plen, total);  // end of this lane's part
-    for (unsigned ch = 0; ch < nch; ch++, s += kTSeg) {
-      for (;;) {  // advance to the row holding s (rows may be empty)
-        const bool adv = s < send && s >= rend;
-        if (!__any_sync(FULL, adv)) break;
-        row += adv ? 1 : 0;
-        rend = __shfl_sync(FULL, incl, min(row, 31));
+    unsigned ch = 0u;
+    for (unsigned i = 0; i < nch; i++, ch = (ch + stride >= nch) ? ch + stride - nch : ch + stride) {
+      const unsigned s = pbase + ch * kTSeg;
+      // the box row holding s: the number of rows whose end is <= s
+      int lo = 0, hi = nrows;
+#pragma unroll
+      for (int it = 0; it < 5; it++) {
+        const int mid = (lo + hi) >> 1;
+        const bool le = __shfl_sync(FULL, incl, mid & 31) <= s;
+        if (lo < hi) {
+          if (le) lo = mid + 1;
+          else hi = mid;
+        }
       }
       const bool has = s < send;
-      const int rowc = min(row, 31);
+      const int rowc = min(lo, 31);
       const unsigned jb = __shfl_sync(FULL, rbase, rowc);
       const int dyj = __shfl_sync(FULL, rdy, rowc), dzj = __shfl_sync(FULL, rdz, rowc);
       float4 ps2 = make_float4(kFarAway, kFarAway, kFarAway, 0.f), vr2 = make_float4(0.f, 0.f, 0.f, 1.f);

@@ -248,9 +248,15 @@ class GbSphSingle:
         return ms.value
 
     def set_option(self, key: int, value: int) -> None:
-        """Kernel options: key 1 = fluid-row kernel (0 queued rounds, 1 one
-        thread per particle)."""
+        """Kernel options: key 1 = fluid-row kernel (3 cell-tiled with a ring of
+        4 chunks, the default; 2 the same with 8; 0 queued rounds; 1 one thread
+        per particle), key 0 = block size of kernel 1, key 2 = sort digit bits."""
         self._check(lib().gbsph_set_option(self.ctx, key, value), "set_option")
+
+    def get_option(self, key: int) -> int:
+        v = C.c_int()
+        self._check(lib().gbsph_get_option(self.ctx, key, C.byref(v)), "get_option")
+        return v.value
 
     def graph_prepare(self, nsteps: int) -> None:
         self._check(lib().gbsph_graph_prepare(self.ctx, nsteps), "graph_prepare")

@@ -211,16 +211,23 @@ int gbsph_elapsed(gbsph_ctx* ctx, unsigned a, unsigned b, float* ms);
  * or free during the call -- a host application that owns a pre-sized device
  * pool, or a latency-bound caller that cannot absorb the device
  * synchronisation of cudaFree.
- *   d_keys: n keys in device memory, nbits significant bits (1..32);
+ *   d_keys: n keys in device memory, nbits significant bits (1..32); bits
+ *           above nbits are not looked at, so keys that have some leave the
+ *           order undefined;
  *   d_perm: receives, for each sorted slot, the index of its key (ties keep
  *           the input order); d_sorted_keys (may be NULL) the sorted keys.
  * n is limited to GBSPH_SORT_NOALLOC_MAX_KEYS; larger n returns
  * GBSPH_ECAPACITY with a message in gbsph_last_error.  The work runs on the
  * context stream; the results are ready when that stream reaches them.  The
- * first call for a device looks the work area up (cudaGetSymbolAddress with
- * that device current) and should come before any stream capture.  There is
- * one work area per process and device: calls that overlap in time (from two
- * threads or two streams) race on it and must be serialised by the caller. */
+ * first call for a device (any n, 0 included) looks the work area up
+ * (cudaGetSymbolAddress with that device current) and loads the sort's
+ * kernels, so it may itself take memory for code; make it once, as a warm-up,
+ * before relying on the no-allocation property and before any stream capture.
+ * The address is kept for the life of the process: after cudaDeviceReset (or
+ * any teardown of the device's primary context) it is stale, and this entry
+ * must not be called again in that process.  There is one work area per
+ * process and device: calls that overlap in time (from two threads or two
+ * streams) race on it and must be serialised by the caller. */
 #define GBSPH_SORT_NOALLOC_MAX_KEYS 262144u
 int gbsph_sort_keys_noalloc(gbsph_ctx* ctx, const unsigned* d_keys, unsigned n, unsigned nbits, unsigned* d_perm,
                             unsigned* d_sorted_keys);
@@ -350,21 +357,27 @@ unsigned long long gbsph_launch_count(const gbsph_ctx* ctx);
 /* CUDA stream of the context (as void*), for callers that order their own work. */
 void* gbsph_stream(gbsph_ctx* ctx);
 /* Kernel options (autotuner hook).  key 1 = fluid-row kernel of
- * gbsph_forces: 0 (default) per-lane neighbour queues evaluated in rounds,
- * 1 one thread per particle with no queue.  key 0 = threads per block of the
- * one-thread-per-particle kernel (64, 128 or 256; the queued kernel uses 128).
- * The reference fixes 128 threads per block (JSphGpu.cpp, BlockSizes).
- * key 2 = digit width of the divide's radix sort, 8 (default) or 11 bits. */
+ * gbsph_forces: 3 (default) cell-tiled: the neighbour cells' particles staged
+ * through a shared-memory ring of 4 chunks of 32, distance checks on the
+ * staged copies, pair terms in rounds; 2 the same with a ring of 8 chunks;
+ * 0 per-lane neighbour queues evaluated in rounds; 1 one thread per particle
+ * with no queue.  key 0 = threads per block of the one-thread-per-particle
+ * kernel (64, 128 or 256; the other kernels use 128).  The reference fixes
+ * 128 threads per block (JSphGpu.cpp, BlockSizes).  key 2 = digit width of
+ * the divide's radix sort, 8 (default) or 11 bits. */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
+/* The current value of an option of gbsph_set_option (no reference counterpart). */
+int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value);
 
 /* Autotuner (no reference counterpart).  Times each fluid-row kernel
- * configuration -- the queued kernel, and the one-thread-per-particle kernel at
- * 64, 128 and 256 threads per block -- over `reps` launches on the context's
- * current state, between steps, and keeps the fastest.  The launches rewrite
- * only the interaction outputs, which the next step recomputes.  The two
- * kernels sum a row's neighbours in different orders: results stay within the
- * FP32 criterion of each other, not bit-identical. */
-#define GBSPH_TUNE_CANDIDATES 4
+ * configuration -- the cell-tiled kernel with rings of 4 and 8 chunks, the
+ * queued kernel, and the one-thread-per-particle kernel at 64, 128 and 256
+ * threads per block -- over `reps` launches on the context's current state,
+ * between steps, and keeps the fastest.  The launches rewrite only the
+ * interaction outputs, which the next step recomputes.  The kernels sum a
+ * row's neighbours in different orders: results stay within the FP32
+ * criterion of each other, not bit-identical. */
+#define GBSPH_TUNE_CANDIDATES 6
 typedef struct {
   int best;                              /* index of the configuration kept */
   int variant[GBSPH_TUNE_CANDIDATES];    /* gbsph_set_option key 1 */

@@ -36,6 +36,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--threads", type=int, default=os.cpu_count())
     ap.add_argument("--workload", default="c1", choices=["c1", "c2"])
+    ap.add_argument("--build", default="timing", choices=["timing", "checker"],
+                    help="the oracle build timed: the timing build (bench.py's CPU legs) or the checker")
     args = ap.parse_args()
     from dualsphysics_gb300 import casegen as cg
     from dualsphysics_gb300.case import load_case
@@ -57,6 +59,8 @@ def main():
         os.environ["OMP_NUM_THREADS"] = str(args.threads)
         import pyoracle as po
         po.build()
+        if args.build == "timing":
+            po.use_timing_build()
         cd = load_case(casedir, "Cross")
         sim = po.Sim(po.config(po.params_from(cd.params)), cd.pos, cd.velrho, cd.idp, cd.code, cd.npb, cd.boundnor,
                      nthreads=args.threads)
@@ -64,7 +68,7 @@ def main():
         for _ in range(args.steps):
             sim.step()
         orc_s = time.perf_counter() - t0
-    out = {"workload": args.workload, "dp": args.dp, "particles": ref_np, "steps": args.steps,
+    out = {"workload": args.workload, "dp": args.dp, "particles": ref_np, "steps": args.steps, "build": args.build,
            "threads": args.threads, "reference_steps_per_s": args.steps / ref_s,
            "oracle_steps_per_s": args.steps / orc_s, "oracle_over_reference_time": orc_s / ref_s}
     print(json.dumps(out))

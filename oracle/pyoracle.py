@@ -14,6 +14,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "liboracle.so")
+# the same source built with the reference's optimisation flags and without the
+# conditioning sums (timed by bench.py's CPU legs, never used as a checker)
+TIMING_LIBPATH = os.path.join(HERE, "liboracle_timing.so")
 
 
 class OrcParams(C.Structure):
@@ -119,18 +122,27 @@ _SIG = {
 }
 
 _L = None
+_PATH = LIBPATH
 
 
 def build() -> None:
     subprocess.run(["make", "-s", "-C", HERE], check=True)
 
 
+def use_timing_build() -> None:
+    """Makes this process load the timing build (call before the first use)."""
+    global _PATH
+    if _L is not None and _PATH != TIMING_LIBPATH:
+        raise RuntimeError("the checker build of the oracle is already loaded")
+    _PATH = TIMING_LIBPATH
+
+
 def lib() -> C.CDLL:
     global _L
     if _L is None:
-        if not os.path.exists(LIBPATH):
+        if not os.path.exists(_PATH):
             build()
-        L = C.CDLL(LIBPATH)
+        L = C.CDLL(_PATH)
         for k, (r, a) in _SIG.items():
             f = getattr(L, k)
             f.restype = r

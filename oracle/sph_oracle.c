@@ -552,6 +552,7 @@ void orc_mdbc_correction(const orc_ctes* c, const orc_div* d, const unsigned* be
 #pragma omp parallel for schedule(guided)
 #endif
   for (int p1 = 0; p1 < (int)n; p1++) {
+    if (g_sample_stride > 1 && (p1 % g_sample_stride) != g_sample_phase) continue;  /* rows not sampled keep rho */
     const float* bn = boundnor + 3 * (size_t)p1;
     if (bn[0] == 0 && bn[1] == 0 && bn[2] == 0) continue;
     const double* ps = pos + 3 * (size_t)p1;

@@ -280,6 +280,48 @@ def test_c1_full_size_divide_and_forces():
     G.assert_fp32_parity(ar, r32, f64["ar"], f64["absar"], "ar")
 
 
+def test_c2_full_size_divide_mdbc_and_forces():
+    """The benched configuration at its size: C2 (dp=0.0025, 7,093,601
+    particles, mDBC walls and the box obstacle).  The first divide is
+    bit-exact (order, cells, BeginCell); the mDBC densities and the forces of
+    every 64th row (the oracle's row sampling: a full C2 pass of the FP64
+    oracle takes minutes) meet the criteria of the small cases."""
+    import bench
+    cd = bench.make_case(0.0025)
+    assert cd.np == 7093601
+    s = _gpu(cd)
+    o = _oracle(cd)
+    gs, os_ = s.download(), o.state()
+    for k in ("idp", "dcell", "code"):
+        np.testing.assert_array_equal(gs[k], os_[k], err_msg=k)
+    np.testing.assert_array_equal(s.divinfo(True)["begincell"], o.begincell())
+    stride = 64
+    po.lib().orc_set_sampling(stride, 0)
+    try:
+        s.MdbcBoundCorrection(_lib.INTERSTEP_SYMPREDICTOR)
+        o.mdbc(False)
+        gvr = s.download()["velrho"]
+        nb = o.npbok
+        rows = np.arange(0, nb, stride)
+        np.testing.assert_allclose(gvr[rows, 3], o.state()["velrho"][rows, 3], rtol=2e-6)
+        o.set_state(None, gvr)  # identical inputs for the force comparison
+        s.Interaction_Forces(_lib.INTERSTEP_SYMPREDICTOR)
+        ace, ar = s.forces()
+        f64 = po.forces_f64(o)
+        o.interaction()
+        a32, r32 = o.forces()
+    finally:
+        po.lib().orc_set_sampling(1, 0)
+    npb, n = o.npb, o.np
+    fl = np.arange(npb + (-npb) % stride, n, stride)       # sampled fluid rows
+    bd = np.arange(0, npb, stride)                           # sampled boundary rows
+    assert len(fl) > 80000 and len(bd) > 25000
+    G.assert_fp32_parity(ace[fl], a32[fl], f64["ace"][fl], f64["absace"][fl], "ace")
+    G.assert_fp32_parity(ar[fl], r32[fl], f64["ar"][fl], f64["absar"][fl], "ar (fluid rows)")
+    G.assert_fp32_parity(ar[bd], r32[bd], f64["ar"][bd], f64["absar"][bd], "ar (boundary rows)")
+    s.close()
+
+
 def test_invalid_arguments_are_reported():
     cd = G.load_generated("dbc_d04")
     s = GbSphSingle(0)

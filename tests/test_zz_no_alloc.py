@@ -90,3 +90,38 @@ def test_noalloc_sort_refuses_what_it_cannot_do():
     p, _ = _noalloc_sort(s, torch, np.array([3, 1, 2, 1], np.uint32), 2)
     np.testing.assert_array_equal(p, [1, 3, 2, 0])
     s.close()
+
+
+def test_noalloc_sort_synthetic_sizes_and_no_device_allocation():
+    """Against numpy's stable argsort at the edges of the work area: n = 0, 1,
+    one 2048-key tile, and the maximum with many equal keys; after a warm-up
+    call, further calls leave the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    s, _, _, _ = _divided(G.load_generated("dbc_d04"))
+    rng = np.random.default_rng(7)
+    _noalloc_sort(s, torch, np.array([5, 1], np.uint32), 3)      # warm-up (work area + kernels)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for n, nbits in ((0, 8), (1, 8), (2048, 13), (_lib.SORT_NOALLOC_MAX_KEYS, 10)):
+        keys = rng.integers(0, 1 << nbits, size=n, dtype=np.uint64).astype(np.uint32)
+        if n == _lib.SORT_NOALLOC_MAX_KEYS:
+            keys = (keys % 97).astype(np.uint32)   # many ties
+        d_keys = torch.from_numpy(keys.view(np.int32)).cuda() if n else torch.zeros(1, dtype=torch.int32,
+                                                                                       device="cuda")
+        d_perm = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
+        d_sorted = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
+        for _ in range(2):
+            rc = _lib.lib().gbsph_sort_keys_noalloc(s.ctx, C.c_void_p(d_keys.data_ptr()), n, nbits,
+                                                    C.c_void_p(d_perm.data_ptr()), C.c_void_p(d_sorted.data_ptr()))
+            assert rc == 0, _lib.lib().gbsph_last_error(s.ctx)
+            s.sync()
+            assert torch.cuda.mem_get_info()[0] == free_before      # the call allocated nothing
+            if n:
+                ref = np.argsort(keys, kind="stable").astype(np.uint32)
+                np.testing.assert_array_equal(d_perm.cpu().numpy().view(np.uint32)[:n], ref)
+                np.testing.assert_array_equal(d_sorted.cpu().numpy().view(np.uint32)[:n], keys[ref])
+        del d_keys, d_perm, d_sorted
+    assert free0 > 0
+    s.close()
