@@ -145,6 +145,7 @@ SIGNATURES = {
     "gbsph_stream": (P, [P]),
     "gbsph_set_option": (C.c_int, [P, C.c_int, C.c_int]),
     "gbsph_get_option": (C.c_int, [P, C.c_int, C.POINTER(C.c_int)]),
+    "gbsph_set_step_state": (C.c_int, [P, C.c_double, C.c_double]),
     "gbsph_tune_forces": (C.c_int, [P, C.c_int, C.POINTER(TuneResult)]),
     "gbsph_tune_sort": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), P]),
     "gbsph_ffma_peak": (C.c_int, [C.c_int, C.POINTER(C.c_float)]),

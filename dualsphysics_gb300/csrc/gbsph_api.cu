@@ -754,6 +754,21 @@ int gbsph_elapsed(gbsph_ctx* ctx, unsigned a, unsigned b, float* ms) {
   return GBSPH_OK;
 }
 
+int gbsph_set_step_state(gbsph_ctx* ctx, double time, double dtpre) {
+  if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
+  if (!(time >= 0) || !(dtpre >= 0) || std::isinf(time) || std::isinf(dtpre))
+    return set_err(ctx, GBSPH_EINVAL, "invalid restart time %g or dt %g", time, dtpre);
+  CK(cudaSetDevice(ctx->device), "set device");
+  StepState st;
+  CK(cudaMemcpyAsync(&st, ctx->a.st, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream), "step state");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  st.time = time;
+  if (dtpre > 0) st.dtpre = dtpre;
+  CK(cudaMemcpyAsync(ctx->a.st, &st, sizeof(st), cudaMemcpyHostToDevice, ctx->stream), "step state");
+  CK(cudaStreamSynchronize(ctx->stream), "sync");
+  return GBSPH_OK;
+}
+
 int gbsph_step_dt(gbsph_ctx* ctx, double* dt_last, double* dt_next, double* time) {
   if (!ctx) return GBSPH_EINVAL;
   StepState st;

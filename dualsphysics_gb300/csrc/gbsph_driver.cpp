@@ -2,7 +2,7 @@
 // (JSphGpuSingle.cpp:950-1010) over the gbsph C ABI.
 //
 //   gbsph_run <casedir>/<casename> <dirout> [-nsteps:N] [-tmax:T] [-tout:T] [-sv:none|bi4]
-//             [-cellmode:full|half] [-nograph] [-device:D] [-info]
+//             [-partbegin:N[:first] dir] [-cellmode:full|half] [-nograph] [-device:D] [-info]
 //
 // Loads the run XML and Case.bi4 (LoadConfig + LoadCaseParticles), derives the
 // constants, uploads the particles, then steps until TimeMax (or N steps)
@@ -164,6 +164,10 @@ struct RunOptions {
   bool rhopout = false;
   float rhopoutmin = 0, rhopoutmax = 0;
   unsigned pipsmode = 0, pipssteps = 100;
+  // restart (-partbegin:begin[:first] dir, JSphCfgRun): the Part to begin
+  // from, the number of the first Part written, the directory of the Part
+  unsigned partbegin = 0, partbeginfirst = 0;
+  std::string partbegindir;
 };
 
 std::string upper(std::string t) {
@@ -227,6 +231,11 @@ std::string parse_option(const std::string& arg, RunOptions& o) {
   // accepted without effect: stable summation is the only mode here, run times
   // and timers are printed in the summary
   else if (word == "STABLE" || word == "NORTIMES" || word == "SVTIMERS") { (void)enabled; }
+  else if (word == "PARTBEGIN") {
+    if (opt1.empty() || std::atol(opt1.c_str()) <= 0) return bad;
+    o.partbegin = (unsigned)std::atol(opt1.c_str());
+    o.partbeginfirst = opt2.empty() ? 0u : (unsigned)std::atol(opt2.c_str());
+  }
   else if (word == "NOGRAPH") o.graph = false;
   else if (word == "DEVICE") o.device = std::atoi(full.c_str());
   else if (word == "INFO") o.info = true;
@@ -314,7 +323,8 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "usage: %s <casedir>/<casename> <dirout> [-gpu[:id]] [-symplectic|-verlet[:steps]] "
                          "[-dbc|-mdbc] [-viscoart:v|-viscolam:v|-viscolamsps:v] [-viscoboundfactor:v] [-ddt:0-3] "
                          "[-ddtvalue:v] [-rhopout:min:max] [-cfl:v] [-tmax:T] [-tout:T] [-nsteps:N] [-sv:none|binx] "
-                         "[-svpips:0-2[:steps]] [-cellmode:full|half] [-stable] [-nortimes] [-svtimers] [-nograph] "
+                         "[-svpips:0-2[:steps]] [-partbegin:N[:first] dir] [-cellmode:full|half] [-stable] [-nortimes] "
+                         "[-svtimers] [-nograph] "
                          "[-device:D] [-info]\n", argv[0]);
     return 1;
   }
@@ -323,6 +333,10 @@ int main(int argc, char** argv) {
   for (int i = 3; i < argc; i++) {
     const std::string e = parse_option(argv[i], o);
     if (!e.empty()) return fail("options", e);
+    if (o.partbegin && o.partbegindir.empty()) {  // -partbegin:begin[:first] takes the directory next
+      if (i + 1 >= argc) return fail("options", "-partbegin needs the directory of the Part files");
+      o.partbegindir = argv[++i];
+    }
   }
   const long nsteps = o.nsteps;
   double tmax = o.tmax;
@@ -339,6 +353,15 @@ int main(int argc, char** argv) {
   if (!err.empty()) return fail("LoadCase", err);
   gbsph_consts c;
   if (gbsph_config(&cs.params, &c) != GBSPH_OK) return fail("ConfigConstants", "invalid case constants");
+  // restart from a Part file (JPartsLoad4::LoadParticles, JSph::InitRun):
+  // with first = 0 the run's clock starts at 0, otherwise at the Part's time;
+  // SymplecticDtPre is the Part's
+  double t_ini = 0, dtpre_ini = 0, part_time = 0;
+  if (o.partbegin) {
+    if (!cs.mot_objs.empty()) return fail("LoadCase", "a restart with moving boundaries is not supported");
+    if (!gbio::load_part(o.partbegindir, o.partbegin, cs, part_time, dtpre_ini, err)) return fail("LoadPart", err);
+    t_ini = o.partbeginfirst ? part_time : 0.0;
+  }
   if (info) {
     // case summary as JSON (host only: no device is touched)
     std::printf("{\"np\": %u, \"npb\": %u, \"h\": %.17g, \"b\": %.17g, \"dp\": %.17g, \"maprealposmin\": "
@@ -347,7 +370,8 @@ int main(int argc, char** argv) {
                 "\"tstep\": %d, \"tdensity\": %d, \"tvisco\": %d, \"idsum\": %.17g, \"possum\": %.17g, "
                 "\"rhosum\": %.17g, \"norsum\": %.17g, \"codesum\": %.17g, \"nmoving\": %u, \"nmovements\": %u, "
                 "\"nevents\": %u, \"verletsteps\": %d, \"visco\": %.9g, \"viscoboundfactor\": %.9g, "
-                "\"ddtvalue\": %.9g, \"cflnumber\": %.17g, \"rhopoutmin\": %.9g, \"rhopoutmax\": %.9g}\n",
+                "\"ddtvalue\": %.9g, \"cflnumber\": %.17g, \"rhopoutmin\": %.9g, \"rhopoutmax\": %.9g, "
+                "\"parttime\": %.17g, \"timeini\": %.17g, \"dtpre\": %.17g}\n",
                 cs.np, cs.npb, cs.params.h, cs.params.b, cs.params.dp, cs.params.maprealposmin[0],
                 cs.params.maprealposmin[1], cs.params.maprealposmin[2], cs.params.maprealposmax[0],
                 cs.params.maprealposmax[1], cs.params.maprealposmax[2], c.kernelsize2, c.cs0, c.domcellcode,
@@ -359,7 +383,7 @@ int main(int argc, char** argv) {
                 [&] { double s = 0; for (uint16_t v : cs.code) s += v; return s; }(), cs.nmoving,
                 (unsigned)cs.movs.size(), (unsigned)cs.evts.size(), cs.params.verletsteps, cs.params.visco,
                 cs.params.viscoboundfactor, cs.params.ddtvalue, cs.params.cflnumber, cs.params.rhopoutmin,
-                cs.params.rhopoutmax);
+                cs.params.rhopoutmax, part_time, t_ini, dtpre_ini);
     return 0;
   }
   gbsph_ctx* ctx = nullptr;
@@ -375,6 +399,11 @@ int main(int argc, char** argv) {
   rc = gbsph_upload(ctx, cs.np, cs.npb, cs.pos.data(), cs.velrho.data(), cs.idp.data(), cs.code.data(),
                     cs.boundnor.empty() ? nullptr : cs.boundnor.data());
   if (rc != GBSPH_OK) return fail("gbsph_upload", gbsph_last_error(ctx));
+  if (o.partbegin) {
+    const bool symp = c.tstep == GBSPH_STEP_SYMPLECTIC;
+    rc = gbsph_set_step_state(ctx, t_ini, symp ? dtpre_ini : 0.0);
+    if (rc != GBSPH_OK) return fail("LoadPart", gbsph_last_error(ctx));
+  }
   // moving boundaries: JDsMotion::Init from the case's motion (JSph.cpp:1064-1067)
   gbsph_motion* motion = nullptr;
   if (!cs.mot_objs.empty()) {
@@ -404,9 +433,12 @@ int main(int argc, char** argv) {
     writer.submit(j);
     return true;
   };
-  if (!save_part(0, 0.0, 0, c.dtini)) return fail("SaveData", err.empty() ? gbsph_last_error(ctx) : err);
-  unsigned part = 1, nstep = 0;
-  double t = 0, tnext = tout, dtl = 0, dtn = c.dtini;
+  const double dt_ini = (o.partbegin && dtpre_ini > 0) ? dtpre_ini : c.dtini;
+  const unsigned part_ini = o.partbegin ? o.partbeginfirst : 0u;
+  if (save && !gbio::save_head(dirout, cs, part_ini, err)) return fail("SaveData", err);
+  if (!save_part(part_ini, t_ini, 0, dt_ini)) return fail("SaveData", err.empty() ? gbsph_last_error(ctx) : err);
+  unsigned part = part_ini + 1, nstep = 0;
+  double t = t_ini, tnext = t_ini + tout, dtl = 0, dtn = dt_ini;
   const bool sym = c.tstep == GBSPH_STEP_SYMPLECTIC;
   const auto t0 = std::chrono::steady_clock::now();
   const auto runtime = [&] { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };

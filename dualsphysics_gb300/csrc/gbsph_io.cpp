@@ -540,6 +540,8 @@ bool load_case(const std::string& casedir, const std::string& casename, Case& c,
     if (kind < lastkind) { err = "particle blocks must come as fixed, moving, fluid"; return false; }
     lastkind = kind;
     const unsigned begin = (unsigned)b->getd("begin"), count = (unsigned)b->getd("count");
+    c.blocks.push_back({kind == 2 ? 3 : kind, (unsigned)b->getd("mk"),
+                        (unsigned)b->getd(kind == 2 ? "mkfluid" : "mkbound"), begin, count});
     if (kind == 0) blocks.push_back({false, begin, count, 0x0000u | ifix++});
     else if (kind == 1) {
       blocks.push_back({false, begin, count, 0x0800u | imov++});
@@ -634,6 +636,140 @@ bool load_case(const std::string& casedir, const std::string& casename, Case& c,
   return true;
 }
 
+bool load_part(const std::string& dir, unsigned part, Case& c, double& timestep, double& dtpre, std::string& err) {
+  char fn[64];
+  std::snprintf(fn, sizeof(fn), "/Part_%04u.bi4", part);
+  Bi4Item bd;
+  if (!bi4_read(dir + fn, "JPartDataBi4", bd, err)) return false;
+  char nm[32];
+  std::snprintf(nm, sizeof(nm), "PART_%04u", part);
+  const Bi4Item* pt = bd.item(nm);
+  if (!pt) { err = std::string("no ") + nm + " in " + dir + fn; return false; }
+  const Bi4Value* npok = pt->value("Npok");
+  const Bi4Value* vts = pt->value("TimeStep");
+  const Bi4Value* vdt = pt->value("SymplecticDtPre");
+  const Bi4Array* aidp = pt->array("Idp");
+  const Bi4Array* apos = pt->array("Posd");
+  const Bi4Array* aposf = pt->array("Pos");
+  const Bi4Array* avel = pt->array("Vel");
+  const Bi4Array* arho = pt->array("Rhop");
+  if (!npok || !vts || !aidp || (!apos && !aposf) || !avel || !arho) { err = "Part arrays missing"; return false; }
+  const unsigned n = (unsigned)npok->u;
+  if (aidp->count < n || avel->count < n || arho->count < n || (apos ? apos->count : aposf->count) < n) {
+    err = "Part arrays shorter than Npok";
+    return false;
+  }
+  timestep = vts->num[0];
+  dtpre = vdt ? vdt->num[0] : 0.0;
+  // the case's particles by id (load_case leaves them ordered by id)
+  const std::vector<unsigned> cid = c.idp;
+  const std::vector<uint16_t> ccode = c.code;
+  const std::vector<float> cnor = c.boundnor;
+  const unsigned* idp = (const unsigned*)aidp->data.data();
+  std::vector<unsigned> order(n);
+  for (unsigned k = 0; k < n; k++) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](unsigned x, unsigned y) { return idp[x] < idp[y]; });
+  c.pos.assign(3 * (size_t)n, 0.0);
+  c.velrho.assign(4 * (size_t)n, 0.f);
+  c.idp.assign(n, 0u);
+  c.code.assign(n, 0);
+  if (!cnor.empty()) c.boundnor.assign(3 * (size_t)n, 0.f);
+  unsigned npb = 0;
+  for (unsigned k = 0; k < n; k++) {
+    const unsigned s = order[k], id = idp[s];
+    const auto it = std::lower_bound(cid.begin(), cid.end(), id);
+    if (it == cid.end() || *it != id) { err = "Part holds an id the case does not have"; return false; }
+    if (k && id == c.idp[k - 1]) { err = "Part holds an id twice"; return false; }
+    const size_t ci = (size_t)(it - cid.begin());
+    c.idp[k] = id;
+    c.code[k] = ccode[ci];
+    if (id < c.npb) npb++;
+    for (int j = 0; j < 3; j++) {
+      c.pos[3 * (size_t)k + j] = apos ? ((const double*)apos->data.data())[3 * (size_t)s + j]
+                                      : (double)((const float*)aposf->data.data())[3 * (size_t)s + j];
+      c.velrho[4 * (size_t)k + j] = ((const float*)avel->data.data())[3 * (size_t)s + j];
+      if (!cnor.empty()) c.boundnor[3 * (size_t)k + j] = cnor[3 * ci + j];
+    }
+    c.velrho[4 * (size_t)k + 3] = ((const float*)arho->data.data())[s];
+  }
+  c.np = n;
+  c.npb = npb;
+  return true;
+}
+
+namespace {
+// PeriMode (the periodic axes as bits x=1, y=2, z=4: TpPeriFromPeriActive,
+// JPeriodicDef.h:79) and the increment of each axis
+void set_peri(Bi4Item& it, const gbsph_params& p) {
+  it.set_num("PeriMode", DatInt, (p.peri[0] ? 1 : 0) | (p.peri[1] ? 2 : 0) | (p.peri[2] ? 4 : 0));
+  const double z3[3] = {0, 0, 0};
+  it.set_triple("PeriXinc", DatDouble3, p.peri[0] ? p.periinc : z3);
+  it.set_triple("PeriYinc", DatDouble3, p.peri[1] ? p.periinc + 3 : z3);
+  it.set_triple("PeriZinc", DatDouble3, p.peri[2] ? p.periinc + 6 : z3);
+}
+}  // namespace
+
+bool save_head(const std::string& dirout, const Case& c, unsigned firstpart, std::string& err) {
+  const std::string dd = dirout + "/data";
+  mkdir(dirout.c_str(), 0755);
+  mkdir(dd.c_str(), 0755);
+  const gbsph_params& p = c.params;
+  Bi4Item root;
+  root.name = "JPartDataHead";
+  root.set_num("FmtVersion", DatUint, 180324); root.values.back().second.u = 180324;
+  root.set_text("AppName", "gbsph_run");
+  root.set_text("Date", "???");
+  root.set_text("RunCode", "00000000");
+  root.set_text("CaseName", c.name);
+  root.set_num("Data2d", DatBool, p.simulate2d ? 1 : 0);
+  root.set_num("Data2dPosY", DatDouble, 0);
+  root.set_num("Npiece", DatUint, 1); root.values.back().second.u = 1;
+  root.set_num("FirstPart", DatUint, firstpart); root.values.back().second.u = firstpart;
+  root.set_triple("CasePosMin", DatDouble3, c.caseposmin);
+  root.set_triple("CasePosMax", DatDouble3, c.caseposmax);
+  root.set_num("NpDynamic", DatBool, 0);
+  root.set_num("ReuseIds", DatBool, 0);
+  root.set_triple("MapPosMin", DatDouble3, p.maprealposmin);
+  root.set_triple("MapPosMax", DatDouble3, p.maprealposmax);
+  set_peri(root, p);
+  root.set_num("ViscoType", DatUint, p.tvisco); root.values.back().second.u = (unsigned)p.tvisco;
+  root.set_num("ViscoValue", DatFloat, p.visco);
+  root.set_num("ViscoBoundFactor", DatFloat, p.viscoboundfactor);
+  root.set_num("Symmetry", DatBool, 0);
+  root.set_num("Splitting", DatBool, 0);
+  root.set_num("Dp", DatDouble, p.dp);
+  root.set_num("H", DatDouble, (double)(float)p.h);  // KernelH, a float in the reference
+  root.set_num("B", DatDouble, (double)(float)p.b);  // CteB
+  root.set_num("Gamma", DatDouble, (double)(float)p.gamma);
+  root.set_num("RhopZero", DatDouble, (double)(float)p.rhop0);
+  root.set_num("MassBound", DatDouble, (double)(float)p.massbound);
+  root.set_num("MassFluid", DatDouble, (double)(float)p.massfluid);
+  root.set_triple("Gravity", DatFloat3, p.gravity);
+  root.set_u64("CaseNp", DatUllong, c.np);
+  root.set_u64("CaseNfixed", DatUllong, c.npb - c.nmoving);
+  root.set_u64("CaseNmoving", DatUllong, c.nmoving);
+  root.set_u64("CaseNfloat", DatUllong, 0);
+  root.set_u64("CaseNfluid", DatUllong, c.np - c.npb);
+  Bi4Item mk;
+  mk.name = "MkBlocks";
+  mk.set_num("Count", DatUint, (double)c.blocks.size()); mk.values.back().second.u = c.blocks.size();
+  static const char* tnames[4] = {"Fixed", "Moving", "Floating", "Fluid"};
+  for (size_t k = 0; k < c.blocks.size(); k++) {
+    const Case::Block& b = c.blocks[k];
+    Bi4Item it;
+    char nm[32];
+    std::snprintf(nm, sizeof(nm), "MkBlock_%03u", (unsigned)k);
+    it.name = nm;
+    it.set_text("Type", tnames[b.type & 3]);
+    it.set_num("Mk", DatUint, b.mk); it.values.back().second.u = b.mk;
+    it.set_num("MkType", DatUint, b.mktype); it.values.back().second.u = b.mktype;
+    it.set_num("Count", DatUint, b.count); it.values.back().second.u = b.count;
+    mk.items.push_back(std::move(it));
+  }
+  root.items.push_back(std::move(mk));
+  return bi4_write(dd + "/Part_Head.ibi4", root, err);
+}
+
 bool save_part(const std::string& dirout, const Case& c, unsigned part, double timestep, unsigned step,
                double dtnext, unsigned np, const double* pos, const float* velrho, const unsigned* idp,
                std::string& err) {
@@ -691,11 +827,7 @@ bool save_part(const std::string& dirout, const Case& c, unsigned part, double t
   root.set_num("Data2dPosY", DatDouble, 0);
   root.set_triple("MapPosMin", DatDouble3, p.maprealposmin);
   root.set_triple("MapPosMax", DatDouble3, p.maprealposmax);
-  root.set_num("PeriMode", DatInt, 0);
-  const double z3[3] = {0, 0, 0};
-  root.set_triple("PeriXinc", DatDouble3, z3);
-  root.set_triple("PeriYinc", DatDouble3, z3);
-  root.set_triple("PeriZinc", DatDouble3, z3);
+  set_peri(root, p);
   root.set_num("AxisDiv", DatInt, 0);
   root.set_u64("CaseNp", DatUllong, c.np);
   root.set_u64("CaseNfixed", DatUllong, c.npb - c.nmoving);

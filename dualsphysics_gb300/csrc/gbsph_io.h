@@ -79,6 +79,10 @@ struct Case {
   double time_max = 0, time_out = 0;
   bool savepos_double = false;
   double caseposmin[3] = {0, 0, 0}, caseposmax[3] = {0, 0, 0};
+  // particle blocks of case.execution.particles, in id order (JCaseParts):
+  // type 0 fixed, 1 moving, 3 fluid (TpParticles); mk; mkbound / mkfluid
+  struct Block { int type; unsigned mk, mktype, begin, count; };
+  std::vector<Block> blocks;
   // moving boundaries (case.execution.motion; empty without moving blocks)
   unsigned nmoving = 0;
   std::vector<gbsph_motion_object> mot_objs;
@@ -87,6 +91,18 @@ struct Case {
 };
 
 bool load_case(const std::string& casedir, const std::string& casename, Case& c, std::string& err);
+
+// Restart state from dir/Part_%04u.bi4 (JPartsLoad4::LoadParticles with
+// PartBegin, JPartsLoad4.cpp:164-290): replaces the particle arrays of `c` (a
+// case loaded with load_case) by the Part's, ordered by id, with the codes
+// and boundary normals of the case's particles of the same ids; returns the
+// Part's TimeStep and SymplecticDtPre.
+bool load_part(const std::string& dir, unsigned part, Case& c, double& timestep, double& dtpre, std::string& err);
+
+// Writes dirout/data/Part_Head.ibi4, the run's particle-block and constants
+// header that a restart checks (JSph::ConfigSaveData, JSph.cpp:2732-2748;
+// JPartDataHead::SaveFile, JPartDataHead.cpp:208-272).
+bool save_head(const std::string& dirout, const Case& c, unsigned firstpart, std::string& err);
 
 // Writes dirout/data/Part_%04u.bi4 (JSph::SaveData, JSph.cpp:3062-3110, 3209).
 bool save_part(const std::string& dirout, const Case& c, unsigned part, double timestep, unsigned step,

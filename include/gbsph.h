@@ -160,6 +160,10 @@ int gbsph_run(gbsph_ctx* ctx, unsigned nsteps, int use_graph);
 /* Captures `nsteps` Symplectic steps into one CUDA graph (replayed by
  * gbsph_run(ctx, nsteps, 2)); capture records work without running it. */
 int gbsph_graph_prepare(gbsph_ctx* ctx, unsigned nsteps);
+/* Restart: sets the simulated time (TimeStep) and, for Symplectic, the next
+ * SymplecticDtPre (if dtpre > 0) of an uploaded state, as JSph::InitRun does
+ * when a run begins from a Part file (JSph.cpp:2214-2225, 2363-2364). */
+int gbsph_set_step_state(gbsph_ctx* ctx, double time, double dtpre);
 /* Reads back the dt used by the last step and the next SymplecticDtPre. */
 int gbsph_step_dt(gbsph_ctx* ctx, double* dt_last, double* dt_next, double* time);
 

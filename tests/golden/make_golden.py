@@ -285,10 +285,69 @@ def make_series(name: str, threads: int = 8) -> str:
         return path
 
 
+# restart cases: steps the reference runs before its state is written as a
+# Part file, and steps after the restart
+RESTART = {"dbc_d04": (10, 6)}
+
+
+def _part_writer(tmp: str) -> str:
+    """Builds part_write (tests/golden/part_write.cpp with gbsph_run's Part
+    writer, gbsph_io.cpp: host code only)."""
+    exe = os.path.join(tmp, "part_write")
+    csrc = os.path.join(ROOT, "dualsphysics_gb300", "csrc")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), "-I" + csrc,
+                    os.path.join(OUT, "part_write.cpp"), os.path.join(csrc, "gbsph_io.cpp"), "-o", exe], check=True)
+    return exe
+
+
+def make_restart(name: str, threads: int = 8) -> str:
+    """The reference runs n1 steps; its state is written as Part_0001.bi4 by
+    this library's Part writer; the reference restarts from that file
+    (-partbegin:1:1, its own JPartsLoad4 reader) for n2 steps, and also runs
+    n1 + n2 steps without a restart.  Keeps the Part file, the restarted run's
+    first and last states and dts, and the continuous run's last state."""
+    n1, n2 = RESTART[name]
+    spec_fn = CASES[name][0]
+    with tempfile.TemporaryDirectory() as tmp:
+        casedir = os.path.join(tmp, "case")
+        cg.write_case(cg.make_dam_break(spec_fn()), casedir)
+        outs = {k: os.path.join(tmp, k) for k in ("first", "part", "restart", "cont")}
+        for d in outs.values():
+            os.makedirs(d)
+        # the harness runs a detailed first step, then <nsteps> more
+        run = lambda out, n, extra=(): subprocess.run(
+            [HARNESS, casedir, name, out, str(n - 1), str(threads)] + run_options(name) + list(extra), check=True,
+            stdout=subprocess.DEVNULL)
+        run(outs["first"], n1)
+        subprocess.run([_part_writer(tmp), casedir, name, outs["first"], "end", "1", outs["part"]], check=True)
+        partfile = os.path.join(outs["part"], "data", "Part_0001.bi4")
+        run(outs["restart"], n2, ("-partbegin:1:1", os.path.join(outs["part"], "data")))
+        run(outs["cont"], n1 + n2)
+        arr = {"part_bytes": np.frombuffer(open(partfile, "rb").read(), np.uint8),
+               "first_meta_json": np.frombuffer(json.dumps(_meta(outs["first"], "end")).encode(), np.uint8),
+               "restart_meta_json": np.frombuffer(json.dumps(_meta(outs["restart"], "end")).encode(), np.uint8),
+               "restart_s0_meta_json": np.frombuffer(json.dumps(_meta(outs["restart"], "s0")).encode(), np.uint8),
+               "n1": np.uint32(n1), "n2": np.uint32(n2)}
+        for tag, d, t in (("first", outs["first"], "end"), ("restart_s0", outs["restart"], "s0"),
+                          ("restart", outs["restart"], "end"), ("cont", outs["cont"], "end")):
+            for nm, dt, w in STATE:
+                arr[f"{tag}_{nm}"] = _raw(d, t, nm, dt, w)
+        arr["restart_dtlist"] = np.fromfile(os.path.join(outs["restart"], "end_dtlist.bin"), np.float64)
+        arr["cont_dtlist"] = np.fromfile(os.path.join(outs["cont"], "end_dtlist.bin"), np.float64)
+        path = os.path.join(OUT, f"restart_{name}.npz")
+        np.savez_compressed(path, **arr)
+        return path
+
+
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit(f"reference harness not built: {HARNESS} (make -f oracle/Makefile.ref)")
-    for nm in (sys.argv[1:] or list(CASES) + ["series"]):
+    for nm in (sys.argv[1:] or list(CASES) + ["series", "restart"]):
+        if nm == "restart":
+            for rn in RESTART:
+                p = make_restart(rn)
+                print("restart", rn, os.path.getsize(p), "bytes")
+            continue
         if nm == "series":
             for sn in SERIES:
                 p = make_series(sn)

@@ -185,3 +185,95 @@ def test_driver_pips_summary_and_csv(tmp_path):
     first = rows[1].split(";")
     assert (int(first[3]), int(first[4]), int(first[5]), int(first[6])) == \
         (p["real_fluid"], p["real_bound"], p["checked_fluid"], p["checked_bound"])
+
+
+# ---- restart from a Part file (-partbegin) --------------------------------------
+def _restart_fixture(tmp_path):
+    """The restart fixture (make_golden.py restart): the reference's state after
+    n1 steps written by this library's Part writer, and what the reference did
+    with it.  Returns (fixture, case name, directory holding Part_0001.bi4)."""
+    z = np.load(os.path.join(G.GOLDEN, "restart_dbc_d04.npz"))
+    cn = _write_case(tmp_path, "dbc_d04")
+    d = tmp_path / "part" / "data"
+    d.mkdir(parents=True)
+    (d / "Part_0001.bi4").write_bytes(z["part_bytes"].tobytes())
+    return z, cn, str(d)
+
+
+def _meta(z, key):
+    return json.loads(bytes(z[key]).decode())
+
+
+def test_reference_reads_our_part_file_losslessly():
+    """The reference restarted (-partbegin:1:1, its own JPartsLoad4 reader) from
+    a Part_0001.bi4 and Part_Head.ibi4 written by this library's writers: the
+    state it loaded is the one written, bit for bit, with the Part's time and
+    SymplecticDtPre; its restarted run then ran as its continuous run did."""
+    z = np.load(os.path.join(G.GOLDEN, "restart_dbc_d04.npz"))
+    a, b = np.argsort(z["first_idp"]), np.argsort(z["restart_s0_idp"])
+    np.testing.assert_array_equal(z["first_idp"][a], z["restart_s0_idp"][b])
+    np.testing.assert_array_equal(z["first_pos"][a], z["restart_s0_pos"][b])
+    np.testing.assert_array_equal(z["first_velrho"][a], z["restart_s0_velrho"][b])
+    m1, m0 = _meta(z, "first_meta_json"), _meta(z, "restart_s0_meta_json")
+    assert m0["timestep"] == m1["timestep"] and m0["symplecticdtpre"] == m1["symplecticdtpre"]
+    n2 = int(z["n2"])
+    np.testing.assert_array_equal(z["restart_dtlist"], z["cont_dtlist"][-n2:])
+
+
+def test_driver_reads_the_restart_part(tmp_path):
+    """gbsph_run -partbegin:1:1 <dir> loads the same state from the same file
+    (host only: -info touches no device)."""
+    z, cn, d = _restart_fixture(tmp_path)
+    r = subprocess.run([_driver(), str(tmp_path / cn), str(tmp_path / "out"), "-partbegin:1:1", d, "-info"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    i = json.loads(r.stdout)
+    m1 = _meta(z, "first_meta_json")
+    assert i["np"] == len(z["restart_s0_idp"]) and i["npb"] == int(m1["npb"])
+    assert i["idsum"] == float(z["restart_s0_idp"].astype(np.float64).sum())
+    assert i["possum"] == pytest.approx(float(z["restart_s0_pos"].sum()), rel=1e-12)
+    assert i["rhosum"] == pytest.approx(float(z["restart_s0_velrho"][:, 3].astype(np.float64).sum()), rel=1e-12)
+    assert i["parttime"] == float(m1["timestep"]) == i["timeini"]
+    assert i["dtpre"] == float(m1["symplecticdtpre"])
+    # with first = 0 the run's clock starts at 0 (JSph.cpp:2224-2225)
+    i0 = json.loads(subprocess.run([_driver(), str(tmp_path / cn), str(tmp_path / "out"), "-partbegin:1", d, "-info"],
+                                   capture_output=True, text=True, timeout=120, check=True).stdout)
+    assert i0["timeini"] == 0.0 and i0["parttime"] == i["parttime"]
+    r = subprocess.run([_driver(), str(tmp_path / cn), str(tmp_path / "out"), "-partbegin:2:1", d, "-info"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1 and "LoadPart" in r.stderr            # no Part_0002 there
+    r = subprocess.run([_driver(), str(tmp_path / cn), str(tmp_path / "out"), "-partbegin:1"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1 and "directory" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_restart_matches_reference_restart(tmp_path):
+    """gbsph_run restarted from the same Part file steps as the reference's
+    restarted run: every dt within 1e-5 and the final state within the
+    multi-step tolerance; its first Part is the restart state itself."""
+    z, cn, d = _restart_fixture(tmp_path)
+    n2 = int(z["n2"])
+    out = str(tmp_path / "out")
+    r = subprocess.run([_driver(), str(tmp_path / cn), out, "-partbegin:1:1", d, f"-nsteps:{n2}", "-tout:1e-12",
+                        "-sv:bi4"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    parts = _parts(out)
+    assert parts == ["Part_%04u.bi4" % k for k in range(1, n2 + 2)], parts
+    assert os.path.exists(os.path.join(out, "data", "Part_Head.ibi4"))
+    pts = []
+    for f in parts:
+        root = bi4.read(os.path.join(out, "data", f), "JPartDataBi4")
+        pts.append(root.item([it.name for it in root.items if it.name.startswith("PART_")][0]))
+    m1, mr = _meta(z, "first_meta_json"), _meta(z, "restart_meta_json")
+    times = np.array([p.get("TimeStep") for p in pts])
+    assert times[0] == float(m1["timestep"])
+    np.testing.assert_allclose(np.diff(times), z["restart_dtlist"], rtol=1e-5)
+    assert times[-1] == pytest.approx(float(mr["timestep"]), rel=1e-6)
+    last = pts[-1]
+    idp = last.array("Idp")
+    o1, o2 = np.argsort(idp), np.argsort(z["restart_idp"])
+    np.testing.assert_array_equal(idp[o1], z["restart_idp"][o2])
+    np.testing.assert_allclose(last.array("Posd")[o1], z["restart_pos"][o2], atol=1e-6)
+    np.testing.assert_allclose(last.array("Vel")[o1], z["restart_velrho"][o2, :3], atol=2e-3)
+    np.testing.assert_allclose(last.array("Rhop")[o1], z["restart_velrho"][o2, 3], rtol=1e-4)
