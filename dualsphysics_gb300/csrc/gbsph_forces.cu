@@ -356,6 +356,89 @@ __device__ __forceinline__ void pair_core(const gbsph_consts& c, const PairK& k,
   }
 }
 
+// The pair terms of pair_core arranged for the staged kernel, with fewer
+// operations per pair: every term is linear in the kernel gradient factor, so
+// fac leaves out the constant bwenh, which the caller applies once per row
+// (with the mass of the fluid neighbours; the boundary pass passes
+// massp2 = massbound * bwenh); the pressure and viscosity terms of the
+// momentum share one coefficient of dr, and the continuity term takes
+// v_ij . gradW from the dr . v_ij of the viscosity.  A pair closer than
+// ALMOSTZERO (a particle and itself) adds nothing.
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift>
+__device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k, float drx, float dry, float drz,
+                                          float4 vr2, float p2press, float4 ta2, float2 tb2, bool nbfixed,
+                                          float4 vr1, float p1press, float inv_rho1, float4 ta1, float2 tb1,
+                                          float vfac, float massp2, PairAcc& r) {
+  const float m2 = boundp2 ? massp2 : 1.f;
+  const float rr2 = drx * drx + dry * dry + drz * drz;
+  const bool real = rr2 >= GB_ALMOSTZERO;
+  const float rinv = rsqrtf(rr2);
+  const float qq = rr2 * rinv * k.hinv;
+  const float wqq1 = 1.f - 0.5f * qq;
+  const float fac = real ? wqq1 * wqq1 * wqq1 : 0.f;  // gradW / (bwenh r)
+  const float inv_rho2 = gb_rcp(vr2.w);
+  const float inv_r2eta = gb_rcp(rr2 + c.eta2);
+  const float dvx = vr1.x - vr2.x, dvy = vr1.y - vr2.y, dvz = vr1.z - vr2.z;
+  const float dot = drx * dvx + dry * dvy + drz * dvz;  // r_ij . v_ij
+  const float dot_rr2 = dot * inv_r2eta;
+  r.visc = fmaxf(real ? dot_rr2 : 0.f, r.visc);
+  const float dot3 = fac * rr2;  // r . gradW
+  // momentum: pressure (and artificial viscosity) along dr
+  float coef = -(p1press + p2press) * inv_rho1 * inv_rho2 * m2;
+  if (tvisco == GBSPH_VISCO_ARTIFICIAL) {
+    // applied for approaching pairs (dot < 0); -alpha*cs0*h*dot_rr2 / rhobar
+    // with rhobar = (rho1+rho2)/2 (h and 2 in vfac)
+    coef -= dot < 0 ? (vfac * dot_rr2 * gb_rcp(vr1.w + vr2.w)) * m2 : 0.f;
+  }
+  const float cf = coef * fac;
+  r.ax += cf * drx; r.ay += cf * dry; r.az += cf * drz;
+  // continuity: v_ij . gradW = fac * dot
+  r.ar += (fac * dot) * inv_rho2 * m2;
+  if (tdensity == GBSPH_DDT_DDT && r.delta != FLT_MAX) {
+    const float visc_densi = k.ddt_kc * (vr1.w * inv_rho2 - 1.f) * inv_r2eta;
+    r.delta = (boundp2 && c.tboundary == GBSPH_BC_DBC && real) ? FLT_MAX : r.delta + visc_densi * dot3 * m2;
+  }
+  if (tdensity == GBSPH_DDT_DDT2 || (tdensity == GBSPH_DDT_DDT2FULL && !boundp2)) {
+    if (boundp2) {
+      if (real) r.delta = FLT_MAX;
+    } else {
+      const float t = c.ddtgz * drz;
+      float drho;
+      if (ddtgen && !(fabsf(t) < 0.05f)) drho = c.rhopzero * powf(1.f + t, 1.f / c.gamma) - c.rhopzero;
+      else drho = t * (k.c1 + t * (k.c2 + t * (k.c3 + t * (k.c4 + t * k.c5))));
+      r.delta -= ((vr2.w - vr1.w) - drho) * inv_r2eta * dot3 * inv_rho2;
+    }
+  }
+  if (tshift && r.sh0 != FLT_MAX) {
+    const float massrho = m2 * inv_rho2;
+    const float mf = massrho * fac;
+    const bool noshift = boundp2 && real && (c.tshift == 1 || (c.tshift == 2 && nbfixed));
+    r.sh0 = noshift ? FLT_MAX : r.sh0 + mf * drx;
+    r.sh1 += mf * dry;
+    r.sh2 += mf * drz;
+    r.sh3 -= massrho * dot3;
+  }
+  if (tvisco != GBSPH_VISCO_ARTIFICIAL) {
+    const float temp = vfac * inv_r2eta * gb_rcp(vr1.w + vr2.w);
+    const float vtemp = m2 * temp * dot3;
+    r.ax += vtemp * dvx; r.ay += vtemp * dvy; r.az += vtemp * dvz;
+    if (tvisco == GBSPH_VISCO_LAMINARSPS) {
+      float t0 = ta1.x, t1 = ta1.y, t2 = ta1.z, t3 = ta1.w, t4 = tb1.x, t5 = tb1.y;
+      if (!boundp2) {
+        t0 += ta2.x; t1 += ta2.y; t2 += ta2.z; t3 += ta2.w; t4 += tb2.x; t5 += tb2.y;
+      }
+      const float mfac = m2 * fac;
+      r.ax += mfac * (t0 * drx + t1 * dry + t2 * drz);
+      r.ay += mfac * (t1 * drx + t3 * dry + t4 * drz);
+      r.az += mfac * (t2 * drx + t4 * dry + t5 * drz);
+      const float volp2 = -m2 * inv_rho2 * fac;
+      float dv = dvx * volp2; r.s0 += dv * drx; r.s1 += dv * dry; r.s2 += dv * drz;
+      dv = dvy * volp2; r.s1 += dv * drx; r.s3 += dv * dry; r.s4 += dv * drz;
+      dv = dvz * volp2; r.s2 += dv * drx; r.s4 += dv * dry; r.s5 += dv * drz;
+    }
+  }
+}
+
 // A queued entry e = (dr, neighbour index): the neighbour's SPS tau and code
 // are read from global memory where the pair terms need them.
 template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift>
@@ -634,9 +717,8 @@ __device__ __forceinline__ void tile_round(const gbsph_consts& c, const PairK& k
     float2 tb2 = make_float2(0.f, 0.f);
     if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ta2 = ring.st[slot]; tb2 = ring.stb[slot]; }
     const bool nbfixed = (tshift && boundp2) ? ring.sc[slot] != 0u : false;
-    pair_core<tvisco, tdensity, boundp2, ddtgen, tshift, true>(c, k, fx - q.x, fy - q.y, fz - q.z, vr2, q.w, ta2,
-                                                                tb2, nbfixed, vr1, p1press, inv_rho1, ta1, tb1, vfac,
-                                                                massp2, r);
+    pair_tile<tvisco, tdensity, boundp2, ddtgen, tshift>(c, k, fx - q.x, fy - q.y, fz - q.z, vr2, q.w, ta2, tb2,
+                                                          nbfixed, vr1, p1press, inv_rho1, ta1, tb1, vfac, massp2, r);
     tile_refill<R>(ring, cur, cc, cnext, lane);
   }
 }
@@ -656,6 +738,49 @@ __device__ __forceinline__ unsigned tile_check4(float2 fxx, float2 fyy, float2 f
   return ((r0.x <= ks2 ? 1u : 0u) | (r0.y <= ks2 ? 2u : 0u) | (r1.x <= ks2 ? 4u : 0u) | (r1.y <= ks2 ? 8u : 0u)) << q;
 }
 
+// Minimum / maximum of v over the lanes where `in` holds (an order-preserving
+// integer image of the float, reduced by the warp).
+__device__ __forceinline__ int tile_fkey(float v) {
+  const int i = __float_as_int(v);
+  return i ^ ((i >> 31) & 0x7fffffff);
+}
+__device__ __forceinline__ float tile_fmin(bool in, float v) {
+  const int m = __reduce_min_sync(0xffffffffu, in ? tile_fkey(v) : 0x7fffffff);
+  return __int_as_float(m ^ ((m >> 31) & 0x7fffffff));
+}
+__device__ __forceinline__ float tile_fmax(bool in, float v) {
+  const int m = __reduce_max_sync(0xffffffffu, in ? tile_fkey(v) : (int)0x80000000);
+  return __int_as_float(m ^ ((m >> 31) & 0x7fffffff));
+}
+
+// Checks the full chunk cnext of the ring (four staged candidates per
+// broadcast load), stores every lane's hit mask, then runs rounds while every
+// target of the row group has a hit pending.
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, int R>
+__device__ __forceinline__ void tile_check(const gbsph_consts& c, const PairK& k, const TileRing& ring,
+                                           unsigned& cur, unsigned& cc, unsigned& cnext, float fx, float fy,
+                                           float fz, float2 fxx, float2 fyy, float2 fzz, float ks2, unsigned gmask,
+                                           bool ing, unsigned grp, float4 vr1, float p1press, float inv_rho1,
+                                           float4 ta1, float2 tb1, float vfac, float massp2, PairAcc& r, int lane) {
+  const unsigned base = (cnext & (R - 1)) << 5;
+  unsigned m = 0u;
+#pragma unroll
+  for (int q = 0; q < 32; q += 4) {
+    const float4 xq = *(const float4*)(ring.nx + base + q);
+    const float4 yq = *(const float4*)(ring.ny + base + q);
+    const float4 zq = *(const float4*)(ring.nz + base + q);
+    m |= tile_check4(fxx, fyy, fzz, xq, yq, zq, ks2, q);
+  }
+  m &= gmask;
+  ring.sm[base + lane] = m;
+  if (cc == cnext) cur = m;
+  cnext++;
+  if (cur == 0u) cc = cnext;
+  while (__ballot_sync(0xffffffffu, ing && cur != 0u) == grp)
+    tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, p1press,
+                                                             inv_rho1, ta1, tb1, vfac, massp2, r, lane);
+}
+
 // One pass of the warp's fluid rows over the fluid (boundp2=false) or boundary
 // (boundp2=true) boxes.  cx, cy, cz: the lane's cell in the trimmed domain.
 template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, int R>
@@ -668,7 +793,8 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
   const unsigned cellinit = boundp2 ? 0u : d.boxfluid;
   const float scell = c.scell, ks2 = c.kernelsize2;
   const float vfac = boundp2 ? k.vfac_b : k.vfac_f;
-  const float massp2 = boundp2 ? c.massbound : c.massfluid;
+  // the boundary pass's terms carry their mass and the constant of gradW (pair_tile)
+  const float massp2 = boundp2 ? c.massbound * c.bwenh : c.massfluid;
   const int sd = c.cellmode_div;
   const int ncx = (int)d.ncx, ncy = (int)d.ncy, ncz = (int)d.ncz;
   const unsigned dcc = c.domcellcode, cmin0 = d.cellmin[0];
@@ -716,6 +842,13 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
     }
     const float2 fxx = make_float2(fx, fx), fyy = make_float2(fy, fy), fzz = make_float2(fz, fz);
     const unsigned gmask = ing ? FULL : 0u;
+    // the box of the group's targets: a candidate farther than 2h from it is
+    // no target's neighbour and is not staged (the margin keeps every
+    // candidate the check would accept, whatever the rounding)
+    const float blox = tile_fmin(ing, fx), bloy = tile_fmin(ing, fy), bloz = tile_fmin(ing, fz);
+    const float bhix = tile_fmax(ing, fx), bhiy = tile_fmax(ing, fy), bhiz = tile_fmax(ing, fz);
+    const float ks2m = ks2 * 1.0001f;
+    unsigned fill = 0u;  // entries staged in the open chunk (chunk cnext)
     // Chunk ch (taken in the order ch = i * stride mod nch, a stride near
     // 0.618 nch and coprime with it, so that consecutive chunks lie far apart
     // in every part of the stream) has this lane stage stream position
@@ -763,37 +896,56 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
         ps2.y += (float)dyj * scell;
         ps2.z += (float)dzj * scell;
       }
-      // the ring slot of this chunk must hold no pending hit of chunk cnext - R
-      while (__any_sync(FULL, cur != 0u && cc + (unsigned)R <= cnext))
-        tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, ps1.w,
-                                                                 inv_rho1, ta1, tb1, vfac, massp2, r, lane);
-      const unsigned base = (cnext & (R - 1)) << 5;
-      ring.sa[base + lane] = ps2;
-      ring.sb[base + lane] = vr2;
-      ring.nx[base + lane] = -ps2.x;
-      ring.ny[base + lane] = -ps2.y;
-      ring.nz[base + lane] = -ps2.z;
-      if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ring.st[base + lane] = ta2; ring.stb[base + lane] = tb2; }
-      if (tshift && boundp2) ring.sc[base + lane] = fixed;
-      __syncwarp();
-      // distance checks: four staged candidates per broadcast load
-      unsigned m = 0u;
-#pragma unroll
-      for (int q = 0; q < 32; q += 4) {
-        const float4 xq = *(const float4*)(ring.nx + base + q);
-        const float4 yq = *(const float4*)(ring.ny + base + q);
-        const float4 zq = *(const float4*)(ring.nz + base + q);
-        m |= tile_check4(fxx, fyy, fzz, xq, yq, zq, ks2, q);
+      // keep the candidates near the targets' box; they fill the open chunk
+      // in stream order and run over into the next one
+      bool keep = false;
+      if (has) {
+        const float ex = fmaxf(fmaxf(blox - ps2.x, ps2.x - bhix), 0.f);
+        const float ey = fmaxf(fmaxf(bloy - ps2.y, ps2.y - bhiy), 0.f);
+        const float ez = fmaxf(fmaxf(bloz - ps2.z, ps2.z - bhiz), 0.f);
+        keep = ex * ex + ey * ey + ez * ez <= ks2m;
       }
-      m &= gmask;
-      ring.sm[base + lane] = m;
-      if (cc == cnext) cur = m;
-      cnext++;
-      if (cur == 0u) cc = cnext;
-      // rounds while every target of the row group has a pending hit
-      while (__ballot_sync(FULL, ing && cur != 0u) == grp)
+      const unsigned kb = __ballot_sync(FULL, keep);
+      if (kb == 0u) continue;
+      const unsigned nk = (unsigned)__popc(kb);
+      // the ring slots written must hold no pending hit (of chunk cnext - R,
+      // and of cnext + 1 - R when the entries run over)
+      const unsigned need = fill + nk > 32u ? cnext + 1u : cnext;
+      while (__any_sync(FULL, cur != 0u && cc + (unsigned)R <= need))
         tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, ps1.w,
                                                                  inv_rho1, ta1, tb1, vfac, massp2, r, lane);
+      if (keep) {
+        const unsigned pos = fill + (unsigned)__popc(kb & ((1u << lane) - 1u));
+        const unsigned slot = (((pos < 32u ? cnext : cnext + 1u) & (R - 1)) << 5) | (pos & 31u);
+        ring.sa[slot] = ps2;
+        ring.sb[slot] = vr2;
+        ring.nx[slot] = -ps2.x;
+        ring.ny[slot] = -ps2.y;
+        ring.nz[slot] = -ps2.z;
+        if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ring.st[slot] = ta2; ring.stb[slot] = tb2; }
+        if (tshift && boundp2) ring.sc[slot] = fixed;
+      }
+      fill += nk;
+      if (fill >= 32u) {
+        __syncwarp();
+        tile_check<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, fxx, fyy,
+                                                                 fzz, ks2, gmask, ing, grp, vr1, ps1.w, inv_rho1,
+                                                                 ta1, tb1, vfac, massp2, r, lane);
+        fill -= 32u;
+      }
+    }
+    if (fill) {  // the last chunk of the group: empty slots fail every check
+      const unsigned base = (cnext & (R - 1)) << 5;
+      if ((unsigned)lane >= fill) {
+        ring.nx[base + lane] = -kFarAway;
+        ring.ny[base + lane] = -kFarAway;
+        ring.nz[base + lane] = -kFarAway;
+      }
+      __syncwarp();
+      tile_check<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, fxx, fyy, fzz,
+                                                               ks2, gmask, ing, grp, vr1, ps1.w, inv_rho1, ta1, tb1,
+                                                               vfac, massp2, r, lane);
+      fill = 0u;
     }
   }
   while (__any_sync(FULL, cur != 0u))
@@ -803,7 +955,10 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
 }
 
 template <int tvisco, int tdensity, bool ddtgen, bool tshift, int R>
-__global__ void __launch_bounds__(kTBlock) k_forces_fluid_t(gbsph_consts c, PairK k, DevArrays a) {
+// Six blocks of 128 threads per SM leave up to 80 registers a thread; the
+// Laminar+SPS and shifting cases, with more sums per row, take four.
+__global__ void __launch_bounds__(kTBlock, (tvisco == GBSPH_VISCO_LAMINARSPS || tshift) ? 4 : 6)
+    k_forces_fluid_t(gbsph_consts c, PairK k, DevArrays a) {
   extern __shared__ float4 tile_smem[];
   using L = TileLayout<tvisco, tshift, R>;
   const DivState& d = *a.div;
@@ -841,8 +996,8 @@ __global__ void __launch_bounds__(kTBlock) k_forces_fluid_t(gbsph_consts c, Pair
   PairAcc ff = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   tile_pass<tvisco, tdensity, false, ddtgen, tshift, R>(c, k, a, d, ring, active, cx, cy, cz, ps1, vr1, inv_rho1, ta1,
                                                          tb1, ff);
-  {  // the fluid-neighbour sums carry no mass yet
-    const float mf = c.massfluid;
+  {  // the fluid-neighbour sums carry neither the mass nor the constant of gradW yet
+    const float mf = c.massfluid * c.bwenh;
     ff.ax *= mf; ff.ay *= mf; ff.az *= mf; ff.ar *= mf; ff.delta *= mf;
     if (tdensity == GBSPH_DDT_DDT2 || tdensity == GBSPH_DDT_DDT2FULL) ff.delta *= k.ddt_kc;
     ff.s0 *= mf; ff.s1 *= mf; ff.s2 *= mf; ff.s3 *= mf; ff.s4 *= mf; ff.s5 *= mf;
