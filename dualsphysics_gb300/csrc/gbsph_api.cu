@@ -37,7 +37,7 @@ struct gbsph_ctx {
   bool uploaded = false;
   int verletstep = 0;
   unsigned long long launches = 0;
-  int forces_bsize = 128, forces_variant = 3;
+  int forces_bsize = 128, forces_variant = 2;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_parity = -1;  // pointer-swap parity the graph was captured with
@@ -1120,7 +1120,7 @@ int gbsph_tune_sort(gbsph_ctx* ctx, int reps, int* best_bits, float* ms) {
 // ---- autotuner ------------------------------------------------------------
 // Times the fluid-row kernel configurations on the context's current state
 // (between steps) and keeps the fastest: the cell-tiled staged kernel with a
-// ring of 4 and of 8 chunks, the warp-queued rounds kernel, and the
+// ring of 8 and of 4 chunks, the warp-queued rounds kernel, and the
 // one-thread-per-row kernel at 64, 128 and 256 threads per block.  The
 // launches only rewrite the interaction outputs, which the next step
 // recomputes.
@@ -1128,7 +1128,7 @@ int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
   if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
   if (reps < 1) reps = 1;
   CK(cudaSetDevice(ctx->device), "set device");
-  static const int cand[GBSPH_TUNE_CANDIDATES][2] = {{3, 128}, {2, 128}, {0, 128}, {1, 64}, {1, 128}, {1, 256}};
+  static const int cand[GBSPH_TUNE_CANDIDATES][2] = {{2, 128}, {3, 128}, {0, 128}, {1, 64}, {1, 128}, {1, 256}};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0), "event");
   CK(cudaEventCreate(&e1), "event");

@@ -366,9 +366,9 @@ __device__ __forceinline__ void pair_core(const gbsph_consts& c, const PairK& k,
 // ALMOSTZERO (a particle and itself) adds nothing.
 template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift>
 __device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k, float drx, float dry, float drz,
-                                          float4 vr2, float p2press, float4 ta2, float2 tb2, bool nbfixed,
-                                          float4 vr1, float p1press, float inv_rho1, float4 ta1, float2 tb1,
-                                          float vfac, float massp2, PairAcc& r) {
+                                          float dvx, float dvy, float dvz, float rho2, float p2press, float4 ta2,
+                                          float2 tb2, bool nbfixed, float4 vr1, float p1press, float inv_rho1,
+                                          float4 ta1, float2 tb1, float vfac, float massp2, PairAcc& r) {
   const float m2 = boundp2 ? massp2 : 1.f;
   const float rr2 = drx * drx + dry * dry + drz * drz;
   const bool real = rr2 >= GB_ALMOSTZERO;
@@ -376,9 +376,8 @@ __device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k,
   const float qq = rr2 * rinv * k.hinv;
   const float wqq1 = 1.f - 0.5f * qq;
   const float fac = real ? wqq1 * wqq1 * wqq1 : 0.f;  // gradW / (bwenh r)
-  const float inv_rho2 = gb_rcp(vr2.w);
+  const float inv_rho2 = gb_rcp(rho2);
   const float inv_r2eta = gb_rcp(rr2 + c.eta2);
-  const float dvx = vr1.x - vr2.x, dvy = vr1.y - vr2.y, dvz = vr1.z - vr2.z;
   const float dot = drx * dvx + dry * dvy + drz * dvz;  // r_ij . v_ij
   const float dot_rr2 = dot * inv_r2eta;
   r.visc = fmaxf(real ? dot_rr2 : 0.f, r.visc);
@@ -388,7 +387,7 @@ __device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k,
   if (tvisco == GBSPH_VISCO_ARTIFICIAL) {
     // applied for approaching pairs (dot < 0); -alpha*cs0*h*dot_rr2 / rhobar
     // with rhobar = (rho1+rho2)/2 (h and 2 in vfac)
-    coef -= dot < 0 ? (vfac * dot_rr2 * gb_rcp(vr1.w + vr2.w)) * m2 : 0.f;
+    coef -= dot < 0 ? (vfac * dot_rr2 * gb_rcp(vr1.w + rho2)) * m2 : 0.f;
   }
   const float cf = coef * fac;
   r.ax += cf * drx; r.ay += cf * dry; r.az += cf * drz;
@@ -406,7 +405,7 @@ __device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k,
       float drho;
       if (ddtgen && !(fabsf(t) < 0.05f)) drho = c.rhopzero * powf(1.f + t, 1.f / c.gamma) - c.rhopzero;
       else drho = t * (k.c1 + t * (k.c2 + t * (k.c3 + t * (k.c4 + t * k.c5))));
-      r.delta -= ((vr2.w - vr1.w) - drho) * inv_r2eta * dot3 * inv_rho2;
+      r.delta -= ((rho2 - vr1.w) - drho) * inv_r2eta * dot3 * inv_rho2;
     }
   }
   if (tshift && r.sh0 != FLT_MAX) {
@@ -419,7 +418,7 @@ __device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k,
     r.sh3 -= massrho * dot3;
   }
   if (tvisco != GBSPH_VISCO_ARTIFICIAL) {
-    const float temp = vfac * inv_r2eta * gb_rcp(vr1.w + vr2.w);
+    const float temp = vfac * inv_r2eta * gb_rcp(vr1.w + rho2);
     const float vtemp = m2 * temp * dot3;
     r.ax += vtemp * dvx; r.ay += vtemp * dvy; r.az += vtemp * dvz;
     if (tvisco == GBSPH_VISCO_LAMINARSPS) {
@@ -436,6 +435,73 @@ __device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k,
       dv = dvy * volp2; r.s1 += dv * drx; r.s3 += dv * dry; r.s4 += dv * drz;
       dv = dvz * volp2; r.s2 += dv * drx; r.s4 += dv * dry; r.s5 += dv * drz;
     }
+  }
+}
+
+// Packed sums of the fluid pass of pair_tile2: component x sums the pairs a
+// lane evaluates first in a round, y the second ones (added together after
+// the pass); dsum is the DDT2 sum, subtracted from delta.
+struct PairAcc2 {
+  float2 ax, ay, az, ar, dsum;
+};
+
+// Two pairs of one fluid row against fluid neighbours (A in the x components,
+// B in the y components), the terms of pair_tile for artificial viscosity and
+// no or Fourtakas density diffusion, in packed f32x2 arithmetic: one
+// instruction evaluates an operation for both pairs.  B is a copy of A (and
+// adds nothing) when the lane has one pair only.
+template <int tdensity, bool ddtgen>
+__device__ __forceinline__ void pair_tile2(const gbsph_consts& c, const PairK& k, float2 dx, float2 dy, float2 dz,
+                                           float2 dvx, float2 dvy, float2 dvz, float2 rho2, float2 p2, bool validb,
+                                           float p1press, float rho1, float ninv_rho1, float vfac, PairAcc2& q,
+                                           float& visc) {
+  const float2 rr2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+  const bool reala = rr2.x >= GB_ALMOSTZERO, realb = validb && rr2.y >= GB_ALMOSTZERO;
+  const float2 rinv = make_float2(rsqrtf(rr2.x), rsqrtf(rr2.y));
+  const float2 qq = __fmul2_rn(__fmul2_rn(rr2, rinv), make_float2(k.hinv, k.hinv));
+  const float2 w = __ffma2_rn(qq, make_float2(-0.5f, -0.5f), make_float2(1.f, 1.f));
+  float2 fac = __fmul2_rn(__fmul2_rn(w, w), w);  // gradW / (bwenh r)
+  fac.x = reala ? fac.x : 0.f;
+  fac.y = realb ? fac.y : 0.f;
+  const float2 inv_rho2 = make_float2(gb_rcp(rho2.x), gb_rcp(rho2.y));
+  const float2 r2e = __fadd2_rn(rr2, make_float2(c.eta2, c.eta2));
+  const float2 inv_r2eta = make_float2(gb_rcp(r2e.x), gb_rcp(r2e.y));
+  const float2 dot = __ffma2_rn(dz, dvz, __ffma2_rn(dy, dvy, __fmul2_rn(dx, dvx)));  // r_ij . v_ij
+  const float2 dot_rr2 = __fmul2_rn(dot, inv_r2eta);
+  visc = fmaxf(reala ? dot_rr2.x : 0.f, visc);
+  visc = fmaxf(realb ? dot_rr2.y : 0.f, visc);
+  // momentum: -(p1+p2)/(rho1 rho2), minus the artificial viscosity of approaching pairs
+  float2 coef = __fmul2_rn(__fmul2_rn(__fadd2_rn(make_float2(p1press, p1press), p2),
+                                      make_float2(ninv_rho1, ninv_rho1)), inv_rho2);
+  const float2 rs = __fadd2_rn(make_float2(rho1, rho1), rho2);
+  float2 pv = __fmul2_rn(__fmul2_rn(make_float2(vfac, vfac), dot_rr2), make_float2(gb_rcp(rs.x), gb_rcp(rs.y)));
+  pv.x = dot.x < 0.f ? pv.x : 0.f;
+  pv.y = dot.y < 0.f ? pv.y : 0.f;
+  coef = __ffma2_rn(pv, make_float2(-1.f, -1.f), coef);
+  const float2 cf = __fmul2_rn(coef, fac);
+  q.ax = __ffma2_rn(cf, dx, q.ax);
+  q.ay = __ffma2_rn(cf, dy, q.ay);
+  q.az = __ffma2_rn(cf, dz, q.az);
+  // continuity: v_ij . gradW = fac * dot
+  q.ar = __ffma2_rn(__fmul2_rn(fac, dot), inv_rho2, q.ar);
+  if (tdensity == GBSPH_DDT_DDT2 || tdensity == GBSPH_DDT_DDT2FULL) {
+    const float2 t = __fmul2_rn(make_float2(c.ddtgz, c.ddtgz), dz);
+    float2 drho;
+    if (ddtgen) {
+      drho.x = !(fabsf(t.x) < 0.05f) ? c.rhopzero * powf(1.f + t.x, 1.f / c.gamma) - c.rhopzero
+                                     : t.x * (k.c1 + t.x * (k.c2 + t.x * (k.c3 + t.x * (k.c4 + t.x * k.c5))));
+      drho.y = !(fabsf(t.y) < 0.05f) ? c.rhopzero * powf(1.f + t.y, 1.f / c.gamma) - c.rhopzero
+                                     : t.y * (k.c1 + t.y * (k.c2 + t.y * (k.c3 + t.y * (k.c4 + t.y * k.c5))));
+    } else {
+      float2 u = __ffma2_rn(t, make_float2(k.c5, k.c5), make_float2(k.c4, k.c4));
+      u = __ffma2_rn(t, u, make_float2(k.c3, k.c3));
+      u = __ffma2_rn(t, u, make_float2(k.c2, k.c2));
+      u = __ffma2_rn(t, u, make_float2(k.c1, k.c1));
+      drho = __fmul2_rn(t, u);
+    }
+    // ((rho2 - rho1) - drho) / (r^2 + eta^2) * (r . gradW) / rho2
+    const float2 vd = __ffma2_rn(drho, make_float2(-1.f, -1.f), __fadd2_rn(rho2, make_float2(-rho1, -rho1)));
+    q.dsum = __ffma2_rn(__fmul2_rn(__fmul2_rn(vd, inv_r2eta), __fmul2_rn(fac, rr2)), inv_rho2, q.dsum);
   }
 }
 
@@ -672,22 +738,22 @@ constexpr float kFarAway = 1.0e18f;  // position of an empty ring slot: fails ev
 template <int tvisco, bool tshift, int R>
 struct TileLayout {
   static constexpr bool sps = tvisco == GBSPH_VISCO_LAMINARSPS;
-  // per slot: frame position + pressure (16), velrho (16), negated frame
-  // position as three arrays (12), hit mask (4), [tau a, tau b (24)], [fixed flag (4)]
-  static constexpr size_t per_warp = (size_t)R * 32 * (16 + 16 + 12 + 4 + (sps ? 24 : 0) + (tshift ? 4 : 0));
+  // per slot, as arrays: the negated frame position (12), pressure (4), the
+  // negated velocity (12), density (4), the hit mask (4) [, tau a, tau b (24)]
+  // [, fixed flag (4)]
+  static constexpr size_t per_warp = (size_t)R * 32 * (36 + (sps ? 24 : 0) + (tshift ? 4 : 0));
   static constexpr size_t bytes = per_warp * (kTBlock / 32);
 };
 
 struct TileRing {
-  float4* sa;      // frame position (x, y, z) + pressure, R*32
-  float4* sb;      // velrho, R*32
-  float* nx;       // -x, -y, -z of the frame position, R*32 each
-  float* ny;
-  float* nz;
-  unsigned* sm;    // hit masks [R][32]
-  float4* st;      // SPS tau a
-  float2* stb;     // SPS tau b
-  unsigned* sc;    // 1: fixed boundary particle (NoFixed shifting)
+  float *nx, *ny, *nz;     // -x, -y, -z of the frame position, R*32 each
+  float* pp;               // pressure
+  float *nvx, *nvy, *nvz;  // -vx, -vy, -vz
+  float* rho;              // density
+  unsigned* sm;            // hit masks [R][32]
+  float4* st;              // SPS tau a
+  float2* stb;             // SPS tau b
+  unsigned* sc;            // 1: fixed boundary particle (NoFixed shifting)
 };
 
 // Pending hits of a lane: `cur` holds the unconsumed hits of chunk `cc`;
@@ -711,16 +777,69 @@ __device__ __forceinline__ void tile_round(const gbsph_consts& c, const PairK& k
   if (cur != 0u) {
     const unsigned slot = ((cc & (R - 1)) << 5) | (unsigned)(__ffs(cur) - 1);
     cur &= cur - 1u;
-    const float4 q = ring.sa[slot];
-    const float4 vr2 = ring.sb[slot];
     float4 ta2 = make_float4(0.f, 0.f, 0.f, 0.f);
     float2 tb2 = make_float2(0.f, 0.f);
     if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ta2 = ring.st[slot]; tb2 = ring.stb[slot]; }
     const bool nbfixed = (tshift && boundp2) ? ring.sc[slot] != 0u : false;
-    pair_tile<tvisco, tdensity, boundp2, ddtgen, tshift>(c, k, fx - q.x, fy - q.y, fz - q.z, vr2, q.w, ta2, tb2,
-                                                          nbfixed, vr1, p1press, inv_rho1, ta1, tb1, vfac, massp2, r);
+    pair_tile<tvisco, tdensity, boundp2, ddtgen, tshift>(
+        c, k, fx + ring.nx[slot], fy + ring.ny[slot], fz + ring.nz[slot], vr1.x + ring.nvx[slot],
+        vr1.y + ring.nvy[slot], vr1.z + ring.nvz[slot], ring.rho[slot], ring.pp[slot], ta2, tb2, nbfixed, vr1,
+        p1press, inv_rho1, ta1, tb1, vfac, massp2, r);
     tile_refill<R>(ring, cur, cc, cnext, lane);
   }
+}
+
+// A round of the packed fluid pass: every lane with a pending hit evaluates
+// its next two (the second only when it has one) with pair_tile2.
+template <int tdensity, bool ddtgen, int R>
+__device__ __forceinline__ void tile_round2(const gbsph_consts& c, const PairK& k, const TileRing& ring,
+                                            unsigned& cur, unsigned& cc, unsigned cnext, float fx, float fy,
+                                            float fz, float4 vr1, float p1press, float ninv_rho1, float vfac,
+                                            PairAcc2& q, float& visc, int lane) {
+  if (cur != 0u) {
+    const unsigned sa = ((cc & (R - 1)) << 5) | (unsigned)(__ffs(cur) - 1);
+    cur &= cur - 1u;
+    tile_refill<R>(ring, cur, cc, cnext, lane);
+    const bool hb = cur != 0u;
+    unsigned sb = sa;
+    if (hb) {
+      sb = ((cc & (R - 1)) << 5) | (unsigned)(__ffs(cur) - 1);
+      cur &= cur - 1u;
+      tile_refill<R>(ring, cur, cc, cnext, lane);
+    }
+    pair_tile2<tdensity, ddtgen>(
+        c, k, __fadd2_rn(make_float2(fx, fx), make_float2(ring.nx[sa], ring.nx[sb])),
+        __fadd2_rn(make_float2(fy, fy), make_float2(ring.ny[sa], ring.ny[sb])),
+        __fadd2_rn(make_float2(fz, fz), make_float2(ring.nz[sa], ring.nz[sb])),
+        __fadd2_rn(make_float2(vr1.x, vr1.x), make_float2(ring.nvx[sa], ring.nvx[sb])),
+        __fadd2_rn(make_float2(vr1.y, vr1.y), make_float2(ring.nvy[sa], ring.nvy[sb])),
+        __fadd2_rn(make_float2(vr1.z, vr1.z), make_float2(ring.nvz[sa], ring.nvz[sb])),
+        make_float2(ring.rho[sa], ring.rho[sb]), make_float2(ring.pp[sa], ring.pp[sb]), hb, p1press, vr1.w,
+        ninv_rho1, vfac, q, visc);
+  }
+}
+
+// The fluid pass of these cases evaluates two pairs per lane and round in
+// packed arithmetic (pair_tile2); the other cases one (pair_tile).
+template <int tvisco, int tdensity, bool boundp2, bool tshift>
+struct TilePacked {
+  static constexpr bool value = !boundp2 && !tshift && tvisco == GBSPH_VISCO_ARTIFICIAL &&
+                                (tdensity == GBSPH_DDT_NONE || tdensity == GBSPH_DDT_DDT2 ||
+                                 tdensity == GBSPH_DDT_DDT2FULL);
+};
+
+// One round of whichever kind the case takes.
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, int R>
+__device__ __forceinline__ void tile_step(const gbsph_consts& c, const PairK& k, const TileRing& ring,
+                                          unsigned& cur, unsigned& cc, unsigned cnext, float fx, float fy, float fz,
+                                          float4 vr1, float p1press, float inv_rho1, float4 ta1, float2 tb1,
+                                          float vfac, float massp2, PairAcc& r, PairAcc2& q, int lane) {
+  if constexpr (TilePacked<tvisco, tdensity, boundp2, tshift>::value)
+    tile_round2<tdensity, ddtgen, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, p1press, -inv_rho1, vfac, q,
+                                     r.visc, lane);
+  else
+    tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, p1press,
+                                                             inv_rho1, ta1, tb1, vfac, massp2, r, lane);
 }
 
 // Hit bits of four staged candidates (positions negated, structure of arrays)
@@ -761,7 +880,8 @@ __device__ __forceinline__ void tile_check(const gbsph_consts& c, const PairK& k
                                            unsigned& cur, unsigned& cc, unsigned& cnext, float fx, float fy,
                                            float fz, float2 fxx, float2 fyy, float2 fzz, float ks2, unsigned gmask,
                                            bool ing, unsigned grp, float4 vr1, float p1press, float inv_rho1,
-                                           float4 ta1, float2 tb1, float vfac, float massp2, PairAcc& r, int lane) {
+                                           float4 ta1, float2 tb1, float vfac, float massp2, PairAcc& r,
+                                           PairAcc2& q2, int lane) {
   const unsigned base = (cnext & (R - 1)) << 5;
   unsigned m = 0u;
 #pragma unroll
@@ -777,8 +897,8 @@ __device__ __forceinline__ void tile_check(const gbsph_consts& c, const PairK& k
   cnext++;
   if (cur == 0u) cc = cnext;
   while (__ballot_sync(0xffffffffu, ing && cur != 0u) == grp)
-    tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, p1press,
-                                                             inv_rho1, ta1, tb1, vfac, massp2, r, lane);
+    tile_step<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, p1press,
+                                                            inv_rho1, ta1, tb1, vfac, massp2, r, q2, lane);
 }
 
 // One pass of the warp's fluid rows over the fluid (boundp2=false) or boundary
@@ -800,6 +920,8 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
   const unsigned dcc = c.domcellcode, cmin0 = d.cellmin[0];
   unsigned cnext = 0u, cc = 0u, cur = 0u;
   float fx = 0.f, fy = 0.f, fz = 0.f;
+  PairAcc2 q2 = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
+                 make_float2(0.f, 0.f)};
   unsigned remaining = __ballot_sync(FULL, active);
   while (remaining) {
     // the targets in the row of cells of the lowest remaining lane
@@ -912,16 +1034,19 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
       // and of cnext + 1 - R when the entries run over)
       const unsigned need = fill + nk > 32u ? cnext + 1u : cnext;
       while (__any_sync(FULL, cur != 0u && cc + (unsigned)R <= need))
-        tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, ps1.w,
-                                                                 inv_rho1, ta1, tb1, vfac, massp2, r, lane);
+        tile_step<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, ps1.w,
+                                                                inv_rho1, ta1, tb1, vfac, massp2, r, q2, lane);
       if (keep) {
         const unsigned pos = fill + (unsigned)__popc(kb & ((1u << lane) - 1u));
         const unsigned slot = (((pos < 32u ? cnext : cnext + 1u) & (R - 1)) << 5) | (pos & 31u);
-        ring.sa[slot] = ps2;
-        ring.sb[slot] = vr2;
         ring.nx[slot] = -ps2.x;
         ring.ny[slot] = -ps2.y;
         ring.nz[slot] = -ps2.z;
+        ring.pp[slot] = ps2.w;
+        ring.nvx[slot] = -vr2.x;
+        ring.nvy[slot] = -vr2.y;
+        ring.nvz[slot] = -vr2.z;
+        ring.rho[slot] = vr2.w;
         if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ring.st[slot] = ta2; ring.stb[slot] = tb2; }
         if (tshift && boundp2) ring.sc[slot] = fixed;
       }
@@ -930,7 +1055,7 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
         __syncwarp();
         tile_check<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, fxx, fyy,
                                                                  fzz, ks2, gmask, ing, grp, vr1, ps1.w, inv_rho1,
-                                                                 ta1, tb1, vfac, massp2, r, lane);
+                                                                 ta1, tb1, vfac, massp2, r, q2, lane);
         fill -= 32u;
       }
     }
@@ -944,13 +1069,20 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
       __syncwarp();
       tile_check<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, fxx, fyy, fzz,
                                                                ks2, gmask, ing, grp, vr1, ps1.w, inv_rho1, ta1, tb1,
-                                                               vfac, massp2, r, lane);
+                                                               vfac, massp2, r, q2, lane);
       fill = 0u;
     }
   }
   while (__any_sync(FULL, cur != 0u))
-    tile_round<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, ps1.w,
-                                                             inv_rho1, ta1, tb1, vfac, massp2, r, lane);
+    tile_step<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, vr1, ps1.w,
+                                                            inv_rho1, ta1, tb1, vfac, massp2, r, q2, lane);
+  if constexpr (TilePacked<tvisco, tdensity, boundp2, tshift>::value) {
+    r.ax += q2.ax.x + q2.ax.y;
+    r.ay += q2.ay.x + q2.ay.y;
+    r.az += q2.az.x + q2.az.y;
+    r.ar += q2.ar.x + q2.ar.y;
+    if (tdensity == GBSPH_DDT_DDT2 || tdensity == GBSPH_DDT_DDT2FULL) r.delta -= q2.dsum.x + q2.dsum.y;
+  }
   __syncwarp();  // the next pass reuses the ring
 }
 
@@ -969,12 +1101,15 @@ __global__ void __launch_bounds__(kTBlock, (tvisco == GBSPH_VISCO_LAMINARSPS || 
   if (__all_sync(0xffffffffu, !active)) return;
   char* wbase = (char*)tile_smem + (size_t)warp * L::per_warp;
   TileRing ring;
-  ring.sa = (float4*)wbase;
-  ring.sb = ring.sa + R * 32;
-  ring.nx = (float*)(ring.sb + R * 32);
+  ring.nx = (float*)wbase;
   ring.ny = ring.nx + R * 32;
   ring.nz = ring.ny + R * 32;
-  ring.sm = (unsigned*)(ring.nz + R * 32);
+  ring.pp = ring.nz + R * 32;
+  ring.nvx = ring.pp + R * 32;
+  ring.nvy = ring.nvx + R * 32;
+  ring.nvz = ring.nvy + R * 32;
+  ring.rho = ring.nvz + R * 32;
+  ring.sm = (unsigned*)(ring.rho + R * 32);
   ring.st = L::sps ? (float4*)(ring.sm + R * 32) : nullptr;
   ring.stb = L::sps ? (float2*)(ring.st + R * 32) : nullptr;
   ring.sc = tshift ? (unsigned*)(L::sps ? (void*)(ring.stb + R * 32) : (void*)(ring.sm + R * 32)) : nullptr;

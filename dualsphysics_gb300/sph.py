@@ -248,8 +248,8 @@ class GbSphSingle:
         return ms.value
 
     def set_option(self, key: int, value: int) -> None:
-        """Kernel options: key 1 = fluid-row kernel (3 cell-tiled with a ring of
-        4 chunks, the default; 2 the same with 8; 0 queued rounds; 1 one thread
+        """Kernel options: key 1 = fluid-row kernel (2 cell-tiled with a ring of
+        8 chunks, the default; 3 the same with 4; 0 queued rounds; 1 one thread
         per particle), key 0 = block size of kernel 1, key 2 = sort digit bits."""
         self._check(lib().gbsph_set_option(self.ctx, key, value), "set_option")
 

@@ -361,9 +361,9 @@ unsigned long long gbsph_launch_count(const gbsph_ctx* ctx);
 /* CUDA stream of the context (as void*), for callers that order their own work. */
 void* gbsph_stream(gbsph_ctx* ctx);
 /* Kernel options (autotuner hook).  key 1 = fluid-row kernel of
- * gbsph_forces: 3 (default) cell-tiled: the neighbour cells' particles staged
- * through a shared-memory ring of 4 chunks of 32, distance checks on the
- * staged copies, pair terms in rounds; 2 the same with a ring of 8 chunks;
+ * gbsph_forces: 2 (default) cell-tiled: the neighbour cells' particles staged
+ * through a shared-memory ring of 8 chunks of 32, distance checks on the
+ * staged copies, pair terms in rounds; 3 the same with a ring of 4 chunks;
  * 0 per-lane neighbour queues evaluated in rounds; 1 one thread per particle
  * with no queue.  key 0 = threads per block of the one-thread-per-particle
  * kernel (64, 128 or 256; the other kernels use 128).  The reference fixes
@@ -374,7 +374,7 @@ int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
 int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value);
 
 /* Autotuner (no reference counterpart).  Times each fluid-row kernel
- * configuration -- the cell-tiled kernel with rings of 4 and 8 chunks, the
+ * configuration -- the cell-tiled kernel with rings of 8 and 4 chunks, the
  * queued kernel, and the one-thread-per-particle kernel at 64, 128 and 256
  * threads per block -- over `reps` launches on the context's current state,
  * between steps, and keeps the fastest.  The launches rewrite only the

@@ -96,7 +96,7 @@ def test_autotuner_keeps_the_fastest_candidate():
     r = tune(s, reps=2)
     assert len(r["ms"]) == 6 and all(m > 0 for m in r["ms"])
     assert r["ms"][r["best"]] == min(r["ms"])
-    assert [(v, b) for v, b in zip(r["variant"], r["bsize"])] == [(3, 128), (2, 128), (0, 128), (1, 64), (1, 128),
+    assert [(v, b) for v, b in zip(r["variant"], r["bsize"])] == [(2, 128), (3, 128), (0, 128), (1, 64), (1, 128),
                                                                    (1, 256)]
     # the tuned context steps as one set to the same configuration by hand
     (t,) = _sims(cds[:1])
