@@ -264,6 +264,21 @@ PairK make_pairk(const gbsph_consts& c) {
 // 1/rho, 1/(r^2+eta^2) and 1/rhobar factors of the pair terms.
 __device__ __forceinline__ float gb_rcp(float x) { return __fdividef(1.f, x); }
 
+// Reciprocal and reciprocal square root, one MUFU instruction each, flushing
+// subnormal inputs and results to zero (rcp.approx / rsqrt.approx .ftz: the
+// inputs of the staged kernel's pair terms -- densities, r^2 + eta^2, r^2 of
+// a real pair -- are normal floats, where they equal the forms above).
+__device__ __forceinline__ float gb_rcp_ftz(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float gb_rsqrt_ftz(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 
 // The pair terms of fluid row i and neighbour j, given dr = r_i - r_j, the
 // neighbour's velrho and pressure, its SPS tau/rho^2 (read only for Laminar+SPS
@@ -372,12 +387,12 @@ __device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k,
   const float m2 = boundp2 ? massp2 : 1.f;
   const float rr2 = drx * drx + dry * dry + drz * drz;
   const bool real = rr2 >= GB_ALMOSTZERO;
-  const float rinv = rsqrtf(rr2);
+  const float rinv = gb_rsqrt_ftz(rr2);
   const float qq = rr2 * rinv * k.hinv;
   const float wqq1 = 1.f - 0.5f * qq;
   const float fac = real ? wqq1 * wqq1 * wqq1 : 0.f;  // gradW / (bwenh r)
-  const float inv_rho2 = gb_rcp(rho2);
-  const float inv_r2eta = gb_rcp(rr2 + c.eta2);
+  const float inv_rho2 = gb_rcp_ftz(rho2);
+  const float inv_r2eta = gb_rcp_ftz(rr2 + c.eta2);
   const float dot = drx * dvx + dry * dvy + drz * dvz;  // r_ij . v_ij
   const float dot_rr2 = dot * inv_r2eta;
   r.visc = fmaxf(real ? dot_rr2 : 0.f, r.visc);
@@ -387,7 +402,7 @@ __device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k,
   if (tvisco == GBSPH_VISCO_ARTIFICIAL) {
     // applied for approaching pairs (dot < 0); -alpha*cs0*h*dot_rr2 / rhobar
     // with rhobar = (rho1+rho2)/2 (h and 2 in vfac)
-    coef -= dot < 0 ? (vfac * dot_rr2 * gb_rcp(vr1.w + rho2)) * m2 : 0.f;
+    coef -= dot < 0 ? (vfac * dot_rr2 * gb_rcp_ftz(vr1.w + rho2)) * m2 : 0.f;
   }
   const float cf = coef * fac;
   r.ax += cf * drx; r.ay += cf * dry; r.az += cf * drz;
@@ -418,7 +433,7 @@ __device__ __forceinline__ void pair_tile(const gbsph_consts& c, const PairK& k,
     r.sh3 -= massrho * dot3;
   }
   if (tvisco != GBSPH_VISCO_ARTIFICIAL) {
-    const float temp = vfac * inv_r2eta * gb_rcp(vr1.w + rho2);
+    const float temp = vfac * inv_r2eta * gb_rcp_ftz(vr1.w + rho2);
     const float vtemp = m2 * temp * dot3;
     r.ax += vtemp * dvx; r.ay += vtemp * dvy; r.az += vtemp * dvz;
     if (tvisco == GBSPH_VISCO_LAMINARSPS) {
@@ -457,15 +472,15 @@ __device__ __forceinline__ void pair_tile2(const gbsph_consts& c, const PairK& k
                                            float& visc) {
   const float2 rr2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
   const bool reala = rr2.x >= GB_ALMOSTZERO, realb = validb && rr2.y >= GB_ALMOSTZERO;
-  const float2 rinv = make_float2(rsqrtf(rr2.x), rsqrtf(rr2.y));
+  const float2 rinv = make_float2(gb_rsqrt_ftz(rr2.x), gb_rsqrt_ftz(rr2.y));
   const float2 qq = __fmul2_rn(__fmul2_rn(rr2, rinv), make_float2(k.hinv, k.hinv));
   const float2 w = __ffma2_rn(qq, make_float2(-0.5f, -0.5f), make_float2(1.f, 1.f));
   float2 fac = __fmul2_rn(__fmul2_rn(w, w), w);  // gradW / (bwenh r)
   fac.x = reala ? fac.x : 0.f;
   fac.y = realb ? fac.y : 0.f;
-  const float2 inv_rho2 = make_float2(gb_rcp(rho2.x), gb_rcp(rho2.y));
+  const float2 inv_rho2 = make_float2(gb_rcp_ftz(rho2.x), gb_rcp_ftz(rho2.y));
   const float2 r2e = __fadd2_rn(rr2, make_float2(c.eta2, c.eta2));
-  const float2 inv_r2eta = make_float2(gb_rcp(r2e.x), gb_rcp(r2e.y));
+  const float2 inv_r2eta = make_float2(gb_rcp_ftz(r2e.x), gb_rcp_ftz(r2e.y));
   const float2 dot = __ffma2_rn(dz, dvz, __ffma2_rn(dy, dvy, __fmul2_rn(dx, dvx)));  // r_ij . v_ij
   const float2 dot_rr2 = __fmul2_rn(dot, inv_r2eta);
   visc = fmaxf(reala ? dot_rr2.x : 0.f, visc);
@@ -474,7 +489,7 @@ __device__ __forceinline__ void pair_tile2(const gbsph_consts& c, const PairK& k
   float2 coef = __fmul2_rn(__fmul2_rn(__fadd2_rn(make_float2(p1press, p1press), p2),
                                       make_float2(ninv_rho1, ninv_rho1)), inv_rho2);
   const float2 rs = __fadd2_rn(make_float2(rho1, rho1), rho2);
-  float2 pv = __fmul2_rn(__fmul2_rn(make_float2(vfac, vfac), dot_rr2), make_float2(gb_rcp(rs.x), gb_rcp(rs.y)));
+  float2 pv = __fmul2_rn(__fmul2_rn(make_float2(vfac, vfac), dot_rr2), make_float2(gb_rcp_ftz(rs.x), gb_rcp_ftz(rs.y)));
   pv.x = dot.x < 0.f ? pv.x : 0.f;
   pv.y = dot.y < 0.f ? pv.y : 0.f;
   coef = __ffma2_rn(pv, make_float2(-1.f, -1.f), coef);
@@ -746,15 +761,18 @@ struct TileLayout {
 };
 
 struct TileRing {
-  float *nx, *ny, *nz;     // -x, -y, -z of the frame position, R*32 each
-  float* pp;               // pressure
-  float *nvx, *nvy, *nvz;  // -vx, -vy, -vz
-  float* rho;              // density
-  unsigned* sm;            // hit masks [R][32]
-  float4* st;              // SPS tau a
-  float2* stb;             // SPS tau b
-  unsigned* sc;            // 1: fixed boundary particle (NoFixed shifting)
+  float* f;       // the arrays below, R*32 entries each, from f
+  float4* st;     // SPS tau a
+  float2* stb;    // SPS tau b
+  unsigned* sc;   // 1: fixed boundary particle (NoFixed shifting)
 };
+// arrays of the ring: -x, -y, -z of the frame position, pressure, -vx, -vy,
+// -vz, density, hit masks (unsigned, [R][32])
+enum { TR_NX = 0, TR_NY, TR_NZ, TR_PP, TR_NVX, TR_NVY, TR_NVZ, TR_RHO, TR_SM, TR_N };
+template <int R>
+__device__ __forceinline__ float* tr(const TileRing& r, int k) { return r.f + k * (R * 32); }
+template <int R>
+__device__ __forceinline__ unsigned* tr_sm(const TileRing& r) { return (unsigned*)(r.f + TR_SM * (R * 32)); }
 
 // Pending hits of a lane: `cur` holds the unconsumed hits of chunk `cc`;
 // chunks cc+1 .. cnext-1 have their masks in the ring.  With nothing pending,
@@ -764,7 +782,7 @@ __device__ __forceinline__ void tile_refill(const TileRing& ring, unsigned& cur,
                                             int lane) {
   while (cur == 0u && cc + 1u < cnext) {
     cc++;
-    cur = ring.sm[(cc & (R - 1)) * 32 + lane];
+    cur = tr_sm<R>(ring)[(cc & (R - 1)) * 32 + lane];
   }
   if (cur == 0u) cc = cnext;
 }
@@ -781,10 +799,11 @@ __device__ __forceinline__ void tile_round(const gbsph_consts& c, const PairK& k
     float2 tb2 = make_float2(0.f, 0.f);
     if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ta2 = ring.st[slot]; tb2 = ring.stb[slot]; }
     const bool nbfixed = (tshift && boundp2) ? ring.sc[slot] != 0u : false;
+    const float* e = ring.f + slot;
     pair_tile<tvisco, tdensity, boundp2, ddtgen, tshift>(
-        c, k, fx + ring.nx[slot], fy + ring.ny[slot], fz + ring.nz[slot], vr1.x + ring.nvx[slot],
-        vr1.y + ring.nvy[slot], vr1.z + ring.nvz[slot], ring.rho[slot], ring.pp[slot], ta2, tb2, nbfixed, vr1,
-        p1press, inv_rho1, ta1, tb1, vfac, massp2, r);
+        c, k, fx + e[TR_NX * R * 32], fy + e[TR_NY * R * 32], fz + e[TR_NZ * R * 32], vr1.x + e[TR_NVX * R * 32],
+        vr1.y + e[TR_NVY * R * 32], vr1.z + e[TR_NVZ * R * 32], e[TR_RHO * R * 32], e[TR_PP * R * 32], ta2, tb2,
+        nbfixed, vr1, p1press, inv_rho1, ta1, tb1, vfac, massp2, r);
     tile_refill<R>(ring, cur, cc, cnext, lane);
   }
 }
@@ -807,14 +826,17 @@ __device__ __forceinline__ void tile_round2(const gbsph_consts& c, const PairK& 
       cur &= cur - 1u;
       tile_refill<R>(ring, cur, cc, cnext, lane);
     }
+    const float* ea = ring.f + sa;
+    const float* eb = ring.f + sb;
+    constexpr int S = R * 32;
     pair_tile2<tdensity, ddtgen>(
-        c, k, __fadd2_rn(make_float2(fx, fx), make_float2(ring.nx[sa], ring.nx[sb])),
-        __fadd2_rn(make_float2(fy, fy), make_float2(ring.ny[sa], ring.ny[sb])),
-        __fadd2_rn(make_float2(fz, fz), make_float2(ring.nz[sa], ring.nz[sb])),
-        __fadd2_rn(make_float2(vr1.x, vr1.x), make_float2(ring.nvx[sa], ring.nvx[sb])),
-        __fadd2_rn(make_float2(vr1.y, vr1.y), make_float2(ring.nvy[sa], ring.nvy[sb])),
-        __fadd2_rn(make_float2(vr1.z, vr1.z), make_float2(ring.nvz[sa], ring.nvz[sb])),
-        make_float2(ring.rho[sa], ring.rho[sb]), make_float2(ring.pp[sa], ring.pp[sb]), hb, p1press, vr1.w,
+        c, k, __fadd2_rn(make_float2(fx, fx), make_float2(ea[TR_NX * S], eb[TR_NX * S])),
+        __fadd2_rn(make_float2(fy, fy), make_float2(ea[TR_NY * S], eb[TR_NY * S])),
+        __fadd2_rn(make_float2(fz, fz), make_float2(ea[TR_NZ * S], eb[TR_NZ * S])),
+        __fadd2_rn(make_float2(vr1.x, vr1.x), make_float2(ea[TR_NVX * S], eb[TR_NVX * S])),
+        __fadd2_rn(make_float2(vr1.y, vr1.y), make_float2(ea[TR_NVY * S], eb[TR_NVY * S])),
+        __fadd2_rn(make_float2(vr1.z, vr1.z), make_float2(ea[TR_NVZ * S], eb[TR_NVZ * S])),
+        make_float2(ea[TR_RHO * S], eb[TR_RHO * S]), make_float2(ea[TR_PP * S], eb[TR_PP * S]), hb, p1press, vr1.w,
         ninv_rho1, vfac, q, visc);
   }
 }
@@ -886,13 +908,13 @@ __device__ __forceinline__ void tile_check(const gbsph_consts& c, const PairK& k
   unsigned m = 0u;
 #pragma unroll
   for (int q = 0; q < 32; q += 4) {
-    const float4 xq = *(const float4*)(ring.nx + base + q);
-    const float4 yq = *(const float4*)(ring.ny + base + q);
-    const float4 zq = *(const float4*)(ring.nz + base + q);
+    const float4 xq = *(const float4*)(tr<R>(ring, TR_NX) + base + q);
+    const float4 yq = *(const float4*)(tr<R>(ring, TR_NY) + base + q);
+    const float4 zq = *(const float4*)(tr<R>(ring, TR_NZ) + base + q);
     m |= tile_check4(fxx, fyy, fzz, xq, yq, zq, ks2, q);
   }
   m &= gmask;
-  ring.sm[base + lane] = m;
+  tr_sm<R>(ring)[base + lane] = m;
   if (cc == cnext) cur = m;
   cnext++;
   if (cur == 0u) cc = cnext;
@@ -1039,14 +1061,16 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
       if (keep) {
         const unsigned pos = fill + (unsigned)__popc(kb & ((1u << lane) - 1u));
         const unsigned slot = (((pos < 32u ? cnext : cnext + 1u) & (R - 1)) << 5) | (pos & 31u);
-        ring.nx[slot] = -ps2.x;
-        ring.ny[slot] = -ps2.y;
-        ring.nz[slot] = -ps2.z;
-        ring.pp[slot] = ps2.w;
-        ring.nvx[slot] = -vr2.x;
-        ring.nvy[slot] = -vr2.y;
-        ring.nvz[slot] = -vr2.z;
-        ring.rho[slot] = vr2.w;
+        float* e = ring.f + slot;
+        constexpr int S = R * 32;
+        e[TR_NX * S] = -ps2.x;
+        e[TR_NY * S] = -ps2.y;
+        e[TR_NZ * S] = -ps2.z;
+        e[TR_PP * S] = ps2.w;
+        e[TR_NVX * S] = -vr2.x;
+        e[TR_NVY * S] = -vr2.y;
+        e[TR_NVZ * S] = -vr2.z;
+        e[TR_RHO * S] = vr2.w;
         if (tvisco == GBSPH_VISCO_LAMINARSPS && !boundp2) { ring.st[slot] = ta2; ring.stb[slot] = tb2; }
         if (tshift && boundp2) ring.sc[slot] = fixed;
       }
@@ -1062,9 +1086,9 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
     if (fill) {  // the last chunk of the group: empty slots fail every check
       const unsigned base = (cnext & (R - 1)) << 5;
       if ((unsigned)lane >= fill) {
-        ring.nx[base + lane] = -kFarAway;
-        ring.ny[base + lane] = -kFarAway;
-        ring.nz[base + lane] = -kFarAway;
+        tr<R>(ring, TR_NX)[base + lane] = -kFarAway;
+        tr<R>(ring, TR_NY)[base + lane] = -kFarAway;
+        tr<R>(ring, TR_NZ)[base + lane] = -kFarAway;
       }
       __syncwarp();
       tile_check<tvisco, tdensity, boundp2, ddtgen, tshift, R>(c, k, ring, cur, cc, cnext, fx, fy, fz, fxx, fyy, fzz,
@@ -1101,18 +1125,11 @@ __global__ void __launch_bounds__(kTBlock, (tvisco == GBSPH_VISCO_LAMINARSPS || 
   if (__all_sync(0xffffffffu, !active)) return;
   char* wbase = (char*)tile_smem + (size_t)warp * L::per_warp;
   TileRing ring;
-  ring.nx = (float*)wbase;
-  ring.ny = ring.nx + R * 32;
-  ring.nz = ring.ny + R * 32;
-  ring.pp = ring.nz + R * 32;
-  ring.nvx = ring.pp + R * 32;
-  ring.nvy = ring.nvx + R * 32;
-  ring.nvz = ring.nvy + R * 32;
-  ring.rho = ring.nvz + R * 32;
-  ring.sm = (unsigned*)(ring.rho + R * 32);
-  ring.st = L::sps ? (float4*)(ring.sm + R * 32) : nullptr;
+  ring.f = (float*)wbase;
+  float* const fend = ring.f + TR_N * (R * 32);  // after the hit masks
+  ring.st = L::sps ? (float4*)fend : nullptr;
   ring.stb = L::sps ? (float2*)(ring.st + R * 32) : nullptr;
-  ring.sc = tshift ? (unsigned*)(L::sps ? (void*)(ring.stb + R * 32) : (void*)(ring.sm + R * 32)) : nullptr;
+  ring.sc = tshift ? (unsigned*)(L::sps ? (void*)(ring.stb + R * 32) : (void*)fend) : nullptr;
   float4 ps1 = make_float4(0, 0, 0, 0), vr1 = make_float4(0, 0, 0, 1);
   float4 ta1 = make_float4(0, 0, 0, 0);
   float2 tb1 = make_float2(0, 0);
