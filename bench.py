@@ -2,7 +2,7 @@
 obstacle at dp=0.0025 m (~5.2M fluid + ~1.5M boundary particles).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference] [--dp DP]
-    python bench.py --workload c3|c3err|ensemble|closure   (the other measured workloads)
+    python bench.py --workload c3|c3err|ensemble|closure|closure-judge   (the other measured workloads)
 
 A step is one Symplectic step (predictor + corrector interaction passes, two
 cell divisions, mDBC correction, dt reduction) of the whole particle set.
@@ -364,60 +364,79 @@ def run_ensemble(args, local: int = 0):
 
 
 def run_closure(args, local: int = 0):
-    """Learned closure (--workload closure): paired fine (dp 0.01) / coarse
+    """Learned closure (--workload closure): paired fine (dp 0.005) / coarse
     (dp 0.02) data over seeded column heights, training on the GPU, then on a
     held-out height the probe pressures on the obstacle face and the surge
-    front of the coarse run with and without the closure and of the fine run,
-    each against a finer judge run (dp 0.005), with the wall time of each run."""
+    front of the coarse run with and without the closure and of a plain run
+    at dp 0.01, each against the plain fine run (dp 0.005, the judge), with
+    the wall time of each run.  The target: the learned coarse run as
+    accurate as the plain dp 0.01 run, in a fifth of its time."""
     from dualsphysics_gb300 import closure as cl
     rng = np.random.default_rng(args.clos_seed)
     heights = [float(h) for h in np.sort(rng.uniform(0.2, 0.5, args.clos_heights))]
     held, t_end, dtp = args.clos_held, args.clos_tend, 0.005
+    dpf, ratio = args.clos_dpfine, args.clos_ratio
+    dpc, dpm = dpf * ratio, dpf * ratio / 2
     val = heights[3::8]                                   # 4 of 32 heights validate (early stopping)
     train = [h for h in heights if h not in val]
     t0 = time.perf_counter()
-    xs, ts, meta = cl.paired_samples(train, dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
-    xv, tv, _ = cl.paired_samples(val, dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
+    kw = dict(dp_fine=dpf, ratio=ratio, t_end=t_end, n_snap=args.clos_snaps, device=local)
+    xs, ts, meta = cl.paired_samples(train, **kw)
+    xv, tv, _ = cl.paired_samples(val, **kw)
     t_data = time.perf_counter() - t0
     t1 = time.perf_counter()
     p, w, loss = cl.train_closure(xs, ts, epochs=args.clos_epochs, seed=args.clos_seed, device=local, xv=xv, tv=tv)
     t_train = time.perf_counter() - t1
-    xh, th, _ = cl.paired_samples([held], dp_fine=0.01, t_end=t_end, n_snap=args.clos_snaps, device=local)
+    xh, th, _ = cl.paired_samples([held], **kw)
     ev = cl.Trainer(cl.from_bf16(w), local)     # the deployed BF16 weights
     yh = ev.infer(xh)
     ev.close()
-    coarse = cl._load(cl.spec(0.02, held, "HeldC"))
+    coarse = cl._load(cl.spec(dpc, held, "HeldC"))
     hc = coarse.params.h
-    judge = cl.run_with_probes(cl._load(cl.spec(0.005, held, "HeldJ")), t_end, dtp, device=local, mesh_h=hc)
-    fine = cl.run_with_probes(cl._load(cl.spec(0.01, held, "HeldF")), t_end, dtp, device=local, mesh_h=hc)
+    judge = cl.run_with_probes(cl._load(cl.spec(dpf, held, "HeldJ")), t_end, dtp, device=local, mesh_h=hc)
+    mid = cl.run_with_probes(cl._load(cl.spec(dpm, held, "HeldM")), t_end, dtp, device=local, mesh_h=hc)
     plain = cl.run_with_probes(coarse, t_end, dtp, device=local, mesh_h=hc)
     learned = cl.run_with_probes(coarse, t_end, dtp, w_bf16=w, limit=0.2, device=local, mesh_h=hc)
-    err = {k: cl.probe_error(r, judge) for k, r in (("fine_dp0.01", fine), ("coarse_plain", plain),
-                                                      ("coarse_learned", learned))}
-    werr = {k: cl.probe_error(r, judge, window=0.02) for k, r in (("fine_dp0.01", fine), ("coarse_plain", plain),
-                                                                    ("coarse_learned", learned))}
-    ferr = {k: cl.front_error(r, judge) for k, r in (("fine_dp0.01", fine), ("coarse_plain", plain),
-                                                       ("coarse_learned", learned))}
-    speed = fine["wall_s"] / learned["wall_s"]
-    line = {"metric": "learned vs plain time-to-accuracy (probe pressure on the obstacle face)",
-            "value": speed, "unit": "x (fine dp=0.01 wall time / learned coarse wall time)", "n_gpus": 1,
+    km, kp, kl = f"plain_dp{dpm:g}", f"coarse_plain_dp{dpc:g}", f"coarse_learned_dp{dpc:g}"
+    runs = {km: mid, kp: plain, kl: learned}
+    err = {k: cl.errors(r, judge) for k, r in runs.items()}
+    head = cl.HEADLINE_ERROR
+    speed = mid["wall_s"] / learned["wall_s"]
+    converges = bool(err[km][head] < err[kp][head] and err[km]["front_rmse_m"] < err[kp]["front_rmse_m"])
+    line = {"metric": f"learned vs plain time-to-accuracy ({head}, probes on the obstacle face)",
+            "value": speed, "unit": f"x (plain dp={dpm:g} wall time / learned coarse wall time)", "n_gpus": 1,
             "higher_is_better": True, "data": "synthetic", "dtype": "bf16 weights, f32 accumulate",
             "config": {"workload": f"dam break with box obstacle, mDBC, tank height {cl.TANK_HEIGHT} m; held-out "
-                                   f"column {held} m; {t_end} s; judge dp=0.005",
+                                   f"column {held} m; {t_end} s; fine/judge dp={dpf:g}, coarse dp={dpc:g}",
                        "train_heights": len(train), "validation_heights": len(val),
                        "snapshots_per_height": args.clos_snaps,
                        "samples": int(len(xs)), "epochs": args.clos_epochs},
-            "probe_rmse_pa": err, "probe_rmse_pa_20ms_means": werr, "front_rmse_m": ferr,
-            "wall_s": {"judge_dp0.005": judge["wall_s"], "fine_dp0.01": fine["wall_s"],
-                       "coarse_plain": plain["wall_s"], "coarse_learned": learned["wall_s"]},
-            "particles": {"judge": judge["np"], "fine": fine["np"], "coarse": plain["np"]},
-            "target_met": bool(err["coarse_learned"] <= err["fine_dp0.01"] and speed >= 5.0),
-            "learned_vs_plain_probe_error": err["coarse_learned"] / err["coarse_plain"],
+            "errors": err, "judge_converges": converges,
+            "wall_s": {f"judge_dp{dpf:g}": judge["wall_s"], **{k: r["wall_s"] for k, r in runs.items()}},
+            "ms_per_step": {f"judge_dp{dpf:g}": judge["ms_per_step"], **{k: r["ms_per_step"] for k, r in runs.items()}},
+            "steps": {f"judge_dp{dpf:g}": judge["steps"], **{k: r["steps"] for k, r in runs.items()}},
+            "particles": {"judge": judge["np"], "mid": mid["np"], "coarse": plain["np"]},
+            "target_met": bool(converges and err[kl][head] <= err[km][head] and speed >= 5.0),
+            "learned_vs_plain_error": err[kl][head] / err[kp][head],
             "apriori_heldout_mse": {"plain": float(np.mean(th ** 2)), "learned": float(np.mean((th - yh) ** 2))},
             "train": {"loss_first": float(loss[0]), "loss_last": float(loss[-1]), "data_s": t_data,
                       "train_s": t_train, "fine_steps": meta["fine_steps"]},
             "fallback_rows": learned["fallbacks"]}
     print(json.dumps(line))
+
+
+def run_closure_judge(args, local: int = 0):
+    """Convergence of the closure's error measures (--workload closure-judge):
+    plain runs of the held-out column at the spacings --clos-judge-dps, each
+    judged against the finest."""
+    from dualsphysics_gb300 import closure as cl
+    dps = [float(v) for v in args.clos_judge_dps.split(",")]
+    t0 = time.perf_counter()
+    res = cl.judge_study(args.clos_held, dps, t_end=args.clos_tend, device=local,
+                         log=lambda m: print(m, file=sys.stderr, flush=True))
+    print(json.dumps({"workload": "closure-judge", "column": args.clos_held, "t_end": args.clos_tend,
+                      "reference_dp": min(dps), "by_dp": {f"{k:g}": v for k, v in res.items()},
+                      "total_s": time.perf_counter() - t0}))
 
 
 def main():
@@ -436,7 +455,8 @@ def main():
                     help="fluid-row kernel: 0 queued rounds, 1 one thread per particle, 2/3 cell-tiled staged "
                          "(ring of 8/4 chunks); default: the library's")
     ap.add_argument("--no-tune", action="store_true", help="keep the 8-bit sort digits (no sort autotuning)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c3err", "ensemble", "closure"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c3err", "ensemble", "closure",
+                                                         "closure-judge"],
                     help="c2: the dam break with obstacle (default); c3: the large plain run (dp 0.004, "
                          "~49 M particles); ensemble: the batched cases; closure: the learned closure against "
                          "fine runs")
@@ -446,6 +466,9 @@ def main():
     ap.add_argument("--clos-held", type=float, default=0.3)
     ap.add_argument("--clos-tend", type=float, default=0.3)
     ap.add_argument("--clos-seed", type=int, default=5)
+    ap.add_argument("--clos-dpfine", type=float, default=0.005)
+    ap.add_argument("--clos-ratio", type=int, default=4, choices=[2, 4])
+    ap.add_argument("--clos-judge-dps", default="0.02,0.01,0.005,0.0025")
     ap.add_argument("--ens-cases", type=int, default=64)
     ap.add_argument("--ens-seed", type=int, default=1)
     ap.add_argument("--ens-scale", type=float, default=1.0, help="scales every case's particle count")
@@ -474,9 +497,10 @@ def main():
             dist.destroy_process_group()
         return
 
-    if args.workload in ("ensemble", "closure", "c3err"):
+    if args.workload in ("ensemble", "closure", "c3err", "closure-judge"):
         if rank == 0:
-            {"ensemble": run_ensemble, "closure": run_closure, "c3err": run_c3err}[args.workload](args, local)
+            {"ensemble": run_ensemble, "closure": run_closure, "c3err": run_c3err,
+             "closure-judge": run_closure_judge}[args.workload](args, local)
         if dist:
             dist.destroy_process_group()
         return

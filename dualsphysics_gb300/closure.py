@@ -6,8 +6,9 @@ the method generates itself:
 
 * a fine run (spacing dp) of the dam break with the box obstacle;
 * every fine fluid particle belongs to the coarse particle of its initial
-  lattice block (fine indices 2i..2i+1 per axis; the fine particle at the
-  block's corner starts where the coarse particle starts).  At snapshot
+  lattice block (fine indices ri..ri+r-1 per axis for a spacing ratio r of 2
+  or 4; the fine particle at the block's corner starts where the coarse
+  particle starts).  At snapshot
   times the fine state restricted to the blocks -- the corner particle's
   position, the block's mean velocity and density -- with the coarse case's
   own walls is a coarse state;
@@ -20,7 +21,7 @@ the method generates itself:
 Training, inference and the correction inside the step run in the library's
 own kernels (``gbsph_mlp_*``, ``gbsph_closure_set``); the plain method is the
 fallback (per particle, when the correction exceeds ``limit`` x |ace|) and the
-judge (the fine run's probe pressures).
+judge (the plain fine run's probe pressures and surge front).
 """
 from __future__ import annotations
 
@@ -42,6 +43,8 @@ NHID = 64
 NOUT = 3
 NPARAMS = NHID * NFEAT + NHID + 2 * (NHID * NHID + NHID) + NOUT * NHID + NOUT
 TANK_HEIGHT = 0.6   # room for columns up to 0.5 m
+# the error measure the closure is judged by (a key of errors())
+HEADLINE_ERROR = "probe_rmse_pa_20ms_means"
 
 
 def layer_slices():
@@ -234,29 +237,32 @@ def lattice_key(pos: np.ndarray, dp: float) -> np.ndarray:
 
 
 class Pair:
-    """A fine case and its coarse twin (spacing x2); maps fine fluid ids to
-    coarse fluid rows."""
+    """A fine case and its coarse twin (spacing x ratio, ratio 2 or 4); maps
+    fine fluid ids to coarse fluid rows: the fine lattice point ratio*i of
+    every axis is the coarse lattice point i, and each fine particle belongs
+    to the coarse block floor(i/ratio)."""
 
-    def __init__(self, height: float, dp_fine: float = 0.01, tag: str = "P"):
+    def __init__(self, height: float, dp_fine: float = 0.01, tag: str = "P", ratio: int = 2):
         self.height = height
+        self.ratio = r = int(ratio)
         self.fine = _load(spec(dp_fine, height, f"{tag}F"))
-        self.coarse = _load(spec(2 * dp_fine, height, f"{tag}C"))
+        self.coarse = _load(spec(r * dp_fine, height, f"{tag}C"))
         f, c = self.fine, self.coarse
         fpos = f.pos[f.npb:]
         _, idx = lattice_key(fpos, dp_fine)
-        even = np.all(idx % 2 == 0, axis=1)
-        fkey, _ = lattice_key(fpos[even] / 2.0, dp_fine)
-        ckey, _ = lattice_key(c.pos[c.npb:], 2 * dp_fine)
+        corner = np.all(idx % r == 0, axis=1)
+        fkey, _ = lattice_key(fpos[corner] / float(r), dp_fine)
+        ckey, _ = lattice_key(c.pos[c.npb:], r * dp_fine)
         # coarse fluid row r <- the fine fluid particle with the same lattice point
         order_f = np.argsort(fkey)
         order_c = np.argsort(ckey)
         if len(fkey) != len(ckey) or not np.array_equal(fkey[order_f], ckey[order_c]):
             raise ValueError("fine and coarse lattices do not nest")
-        fine_ids = f.idp[f.npb:][np.nonzero(even)[0]]
+        fine_ids = f.idp[f.npb:][np.nonzero(corner)[0]]
         self.coarse_row_fine_id = np.empty(len(ckey), np.int64)
         self.coarse_row_fine_id[order_c] = fine_ids[order_f]
-        # block of every fine fluid particle: the coarse row of lattice point floor(idx/2)
-        bkey, _ = lattice_key((idx // 2).astype(np.float64), 1.0)
+        # block of every fine fluid particle: the coarse row of lattice point floor(idx/ratio)
+        bkey, _ = lattice_key((idx // r).astype(np.float64), 1.0)
         pos_c = np.searchsorted(ckey[order_c], bkey)
         if (pos_c >= len(ckey)).any() or not np.array_equal(ckey[order_c][pos_c], bkey):
             raise ValueError("a fine particle has no coarse block")
@@ -272,9 +278,12 @@ class Pair:
         ok = (self.fine_id < len(where)) & (rows >= 0)
         nc = self.coarse.np - self.coarse.npb
         v = np.asarray(values, np.float64)[rows[ok]]
-        sums = np.zeros((nc,) + v.shape[1:])
-        np.add.at(sums, self.fine_block[ok], v)
-        cnt = np.bincount(self.fine_block[ok], minlength=nc).astype(np.float64)
+        blk = self.fine_block[ok]
+        cnt = np.bincount(blk, minlength=nc).astype(np.float64)
+        if v.ndim == 1:
+            sums = np.bincount(blk, weights=v, minlength=nc)
+        else:
+            sums = np.stack([np.bincount(blk, weights=v[:, k], minlength=nc) for k in range(v.shape[1])], axis=1)
         return sums / np.maximum(cnt, 1.0).reshape((nc,) + (1,) * (v.ndim - 1)), cnt
 
     def coarse_state(self, fst: dict):
@@ -298,13 +307,14 @@ class Pair:
 
 
 def paired_samples(heights, dp_fine: float = 0.01, t_end: float = 0.3, n_snap: int = 10,
-                   device: int = 0, log=None) -> tuple[np.ndarray, np.ndarray, dict]:
+                   device: int = 0, log=None, ratio: int = 2) -> tuple[np.ndarray, np.ndarray, dict]:
     """Features and targets over fine runs of the given column heights,
-    restricted to the coarse particles at n_snap times in (0, t_end]."""
+    restricted to the coarse particles (spacing ratio*dp_fine) at n_snap
+    times in (0, t_end]."""
     xs, ts, meta = [], [], {"snapshots": 0, "fine_steps": 0, "fine_s": 0.0}
     g = 9.81
     for hk, h in enumerate(heights):
-        pair = Pair(h, dp_fine, tag=f"H{hk}")
+        pair = Pair(h, dp_fine, tag=f"H{hk}", ratio=ratio)
         fine = GbSphSingle(device)
         fine.setup(pair.fine)
         tnext = t_end / n_snap
@@ -350,20 +360,30 @@ def paired_samples(heights, dp_fine: float = 0.01, t_end: float = 0.3, n_snap: i
 
 # ---- evaluation against the fine run ---------------------------------------------
 def probe_mesh(h: float):
-    """Pressure probes on the obstacle's upstream face, 1.5 h off it: 8 points
-    from z = 0.02 to 0.16 m on the face's centre line."""
-    x = cg.OBSTACLE_C2[0] - 1.5 * h
-    y = cg.OBSTACLE_C2[1] + cg.OBSTACLE_C2[3] / 2   # (x0, y0, sx, sy, sz)
-    return dict(ptref=(x, y, 0.02), vec1=(0.0, 0.0, 1.0), vec2=(1.0, 0.0, 0.0), vec3=(0.0, 1.0, 0.0),
-                dis=(0.14, 0.0, 0.0), dispt=(0.02, 0.0, 0.0))
+    """Pressure probes on the obstacle's upstream face, 1.5 h off it: a grid
+    of 10 heights (z = 0.02 to 0.20 m) by 5 positions across the face (from
+    0.01 m inside either edge)."""
+    x0, y0, sx, sy, sz = cg.OBSTACLE_C2
+    return dict(ptref=(x0 - 1.5 * h, y0 + 0.01, 0.02), vec1=(0.0, 0.0, 1.0), vec2=(0.0, 1.0, 0.0),
+                vec3=(1.0, 0.0, 0.0), dis=(0.18, sy - 0.02, 0.0), dispt=(0.02, (sy - 0.02) / 4, 0.0))
+
+
+def probe_pressure(gs, rhop) -> np.ndarray:
+    """Probe pressures (Pa) from a mesh gauge's densities: the Tait pressure
+    where the probe is wet, 0 (the atmosphere) where it is dry.  A dry probe
+    (kernel sum below the gauge's limit) reads the dummy density 0, whose Tait
+    pressure -B would turn a few ms of difference in the arrival of the front
+    into errors of the order of B."""
+    r = np.asarray(rhop, np.float64)
+    return np.where(r > 0, gs.Pressure(r), 0.0)
 
 
 def run_with_probes(cd, t_end: float, dt_probe: float, w_bf16=None, limit: float = 0.2, device: int = 0,
                     mesh_h: float | None = None, chunk: int = 10) -> dict:
     """Runs a case to t_end in graph replays of `chunk` steps, sampling the
     probes and the surge front after the first chunk that passes each
-    multiple of dt_probe; returns them with their times and the wall time of
-    the stepping alone."""
+    multiple of dt_probe; returns them with their times, the wall time of the
+    stepping alone and its steps."""
     from .gauges import GaugeSystem
     s = GbSphSingle(device)
     s.setup(cd)
@@ -374,6 +394,15 @@ def run_with_probes(cd, t_end: float, dt_probe: float, w_bf16=None, limit: float
     gs.AddGaugeMesh("probes", **m)
     times, press, fronts = [], [], []
     tnext, t, wall, nsteps = dt_probe, 0.0, 0.0, 0
+    s.RunSteps(chunk, use_graph=True)       # graph capture and first replay outside the clock
+    s.sync()
+    s.close()
+    s = GbSphSingle(device)
+    s.setup(cd)
+    if w_bf16 is not None:
+        attach(s, w_bf16, limit)
+    gs = GaugeSystem(s)
+    gs.AddGaugeMesh("probes", **m)
     while t < t_end:
         s.sync()
         t0 = time.perf_counter()
@@ -385,10 +414,11 @@ def run_with_probes(cd, t_end: float, dt_probe: float, w_bf16=None, limit: float
             tnext += dt_probe
             gs.CalculeGpu(t)
             times.append(t)
-            press.append(gs.Pressure(gs.GetResult("probes")["rhop"]))
+            press.append(probe_pressure(gs, gs.GetResult("probes")["rhop"]))
             fronts.append(s.fluid_front((1.0, 0.0, 0.0))[0])
     out = {"t": np.array(times), "p": np.array(press), "front": np.array(fronts), "wall_s": wall, "steps": nsteps,
-           "np": cd.np, "fallbacks": fallbacks(s) if w_bf16 is not None else 0}
+           "ms_per_step": 1e3 * wall / max(nsteps, 1), "np": cd.np,
+           "fallbacks": fallbacks(s) if w_bf16 is not None else 0}
     s.close()
     return out
 
@@ -399,6 +429,19 @@ def front_error(run: dict, ref: dict) -> float:
     if n == 0:
         return float("nan")
     return float(np.sqrt(np.mean((run["front"][:n] - np.interp(run["t"][:n], ref["t"], ref["front"])) ** 2)))
+
+
+def _window_means(run: dict, ref: dict, window: float):
+    tmax = min(run["t"][-1], ref["t"][-1])
+    edges = np.arange(0.0, tmax + 1e-12, window)
+    a, b = [], []
+    for lo, hi in zip(edges[:-1], edges[1:]):
+        ma = (run["t"] > lo) & (run["t"] <= hi)
+        mb = (ref["t"] > lo) & (ref["t"] <= hi)
+        if ma.any() and mb.any():
+            a.append(run["p"][ma].mean(axis=0))
+            b.append(ref["p"][mb].mean(axis=0))
+    return np.array(a), np.array(b)
 
 
 def probe_error(run: dict, ref: dict, window: float = 0.0) -> float:
@@ -413,12 +456,44 @@ def probe_error(run: dict, ref: dict, window: float = 0.0) -> float:
     if window <= 0:
         pr = np.stack([np.interp(run["t"][:n], ref["t"], ref["p"][:, k]) for k in range(ref["p"].shape[1])], axis=1)
         return float(np.sqrt(np.mean((run["p"][:n] - pr) ** 2)))
-    tmax = min(run["t"][-1], ref["t"][-1])
-    edges = np.arange(0.0, tmax + 1e-12, window)
-    diffs = []
-    for a, b in zip(edges[:-1], edges[1:]):
-        ma = (run["t"] > a) & (run["t"] <= b)
-        mb = (ref["t"] > a) & (ref["t"] <= b)
-        if ma.any() and mb.any():
-            diffs.append(run["p"][ma].mean(axis=0) - ref["p"][mb].mean(axis=0))
-    return float(np.sqrt(np.mean(np.square(diffs)))) if diffs else float("nan")
+    a, b = _window_means(run, ref, window)
+    return float(np.sqrt(np.mean(np.square(a - b)))) if len(a) else float("nan")
+
+
+def face_error(run: dict, ref: dict, window: float = 0.02) -> float:
+    """RMS difference (Pa) of the mean pressure over the face's probes, in
+    window means, against the reference run."""
+    if min(len(run["t"]), len(ref["t"])) == 0:
+        return float("nan")
+    a, b = _window_means(run, ref, window)
+    return float(np.sqrt(np.mean(np.square(a.mean(axis=1) - b.mean(axis=1))))) if len(a) else float("nan")
+
+
+def errors(run: dict, ref: dict) -> dict:
+    """Every error measure of a run against the reference run."""
+    return {"probe_rmse_pa": probe_error(run, ref), "probe_rmse_pa_20ms_means": probe_error(run, ref, 0.02),
+            "face_rmse_pa_20ms_means": face_error(run, ref, 0.02), "front_rmse_m": front_error(run, ref)}
+
+
+def judge_study(height: float, dps, t_end: float = 0.3, dt_probe: float = 0.005, device: int = 0,
+                mesh_h: float | None = None, log=None) -> dict:
+    """Plain runs of one column height at the spacings `dps`, each judged
+    against the finest: a measure judges the closure only if its error
+    falls as the spacing does."""
+    dps = sorted(dps, reverse=True)
+    mesh_h = mesh_h if mesh_h is not None else _load(spec(dps[0], height, "JS0")).params.h
+    runs = {}
+    for k, dp in enumerate(dps):
+        runs[dp] = run_with_probes(_load(spec(dp, height, f"JS{k}")), t_end, dt_probe, device=device, mesh_h=mesh_h)
+        if log:
+            log(f"dp {dp}: {runs[dp]['np']} particles, {runs[dp]['steps']} steps, {runs[dp]['wall_s']:.1f} s")
+    ref = runs[dps[-1]]
+    out = {}
+    for dp in dps[:-1]:
+        e = errors(runs[dp], ref)
+        e.update(particles=int(runs[dp]["np"]), steps=int(runs[dp]["steps"]), wall_s=runs[dp]["wall_s"],
+                 ms_per_step=runs[dp]["ms_per_step"])
+        out[dp] = e
+    out[dps[-1]] = {"particles": int(ref["np"]), "steps": int(ref["steps"]), "wall_s": ref["wall_s"],
+                    "ms_per_step": ref["ms_per_step"]}
+    return out

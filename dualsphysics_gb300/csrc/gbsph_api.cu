@@ -38,6 +38,7 @@ struct gbsph_ctx {
   int verletstep = 0;
   unsigned long long launches = 0;
   int forces_bsize = 128, forces_variant = 2;
+  int mdbc_variant = 0;   // 0 staged kernel, 1 one thread per boundary row
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_parity = -1;  // pointer-swap parity the graph was captured with
@@ -205,7 +206,7 @@ int enqueue_step(gbsph_ctx* ctx) {
   const gbsph_consts& c = ctx->c;
   double* dtpre = &ctx->a.st->dtpre;
   if (c.tstep == GBSPH_STEP_SYMPLECTIC) {
-    if (c.tboundary == GBSPH_BC_MDBC) gbk::mdbc(c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
+    if (c.tboundary == GBSPH_BC_MDBC) gbk::mdbc(c, ctx->a, ctx->cap, ctx->mdbc_variant, ctx->stream, &ctx->launches);
     if (int rc = do_forces(ctx)) return rc;
     gbk::dtvariable(c, ctx->a, 0, ctx->stream, &ctx->launches);
     gbk::symplectic_pre(c, ctx->a, ctx->cap, dtpre, ctx->stream, &ctx->launches);
@@ -225,7 +226,7 @@ int enqueue_step(gbsph_ctx* ctx) {
                        ctx->cap, ctx->stream, &ctx->launches);
     }
   } else {
-    if (c.tboundary == GBSPH_BC_MDBC) gbk::mdbc(c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
+    if (c.tboundary == GBSPH_BC_MDBC) gbk::mdbc(c, ctx->a, ctx->cap, ctx->mdbc_variant, ctx->stream, &ctx->launches);
     if (int rc = do_forces(ctx)) return rc;
     gbk::dtvariable(c, ctx->a, 2, ctx->stream, &ctx->launches);
     if (ctx->motion) {
@@ -422,7 +423,7 @@ int gbsph_mdbc(gbsph_ctx* ctx, int interstep) {
   if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
   // MdbcCorrector is false for SlipMode=vel0: only the predictor (and Verlet) correct.
   if (ctx->c.tboundary != GBSPH_BC_MDBC || interstep == GBSPH_INTERSTEP_SYMCORRECTOR) return GBSPH_OK;
-  gbk::mdbc(ctx->c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
+  gbk::mdbc(ctx->c, ctx->a, ctx->cap, ctx->mdbc_variant, ctx->stream, &ctx->launches);
   return cuda_check(ctx, cudaGetLastError(), "mdbc");
 }
 
@@ -1065,6 +1066,10 @@ int gbsph_set_option(gbsph_ctx* ctx, int key, int value) {
     if (value != 8 && value != 11) return set_err(ctx, GBSPH_EINVAL, "sort digits of 8 or 11 bits");
     ctx->sort_bits = value;
   }
+  else if (key == 3) {
+    if (value != 0 && value != 1) return set_err(ctx, GBSPH_EINVAL, "mDBC kernel variant %d is not 0 or 1", value);
+    ctx->mdbc_variant = value;
+  }
   else return set_err(ctx, GBSPH_EINVAL, "unknown option %d", key);
   reset_graph(ctx);
   return GBSPH_OK;
@@ -1075,6 +1080,7 @@ int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value) {
   if (key == 0) *value = ctx->forces_bsize;
   else if (key == 1) *value = ctx->forces_variant;
   else if (key == 2) *value = ctx->sort_bits;
+  else if (key == 3) *value = ctx->mdbc_variant;
   else return GBSPH_EINVAL;
   return GBSPH_OK;
 }

@@ -276,7 +276,10 @@ cudaError_t forces_init(const gbsph_consts& c);
 // 2 cell-tiled staged (ring of 8 chunks), 3 cell-tiled staged (ring of 4)
 void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, cudaStream_t s, unsigned long long* nlaunch,
             cudaEvent_t ev_fluid_begin = nullptr, cudaEvent_t ev_fluid_end = nullptr);
-void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch);
+// variant 1: one thread per boundary row (k_mdbc); otherwise the cell-tiled
+// staged kernel (k_mdbc_t)
+void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s,
+          unsigned long long* nlaunch);
 void dtvariable(const gbsph_consts& c, const DevArrays& a, int which, cudaStream_t s, unsigned long long* nlaunch);
 void symplectic_pre(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, cudaStream_t s, unsigned long long* nlaunch);
 void symplectic_cor(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, cudaStream_t s, unsigned long long* nlaunch);

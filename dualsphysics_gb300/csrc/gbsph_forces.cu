@@ -1270,15 +1270,18 @@ __device__ __forceinline__ void gb_kadd(float& hi, float& lo, float x) {
   lo = __fadd_rn(lo, e);
 }
 
-__global__ void __launch_bounds__(128) k_mdbc(gbsph_consts c, DevArrays a) {
-  const DivState& d = *a.div;
-  const unsigned p1 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p1 >= d.npbok) return;
-  const float4 bn = a.boundnor[p1];
-  if (bn.x == 0.f && bn.y == 0.f && bn.z == 0.f) return;
+// The ghost node of boundary row p1 (position + doubled normal, taken back
+// into the domain across periodic faces: UpdatePeriodicPos,
+// JSphCpu_mdbc.cpp:50, JSph.cpp:2079-2101): its cell relative to the trimmed
+// domain (truncated toward zero as int() does, JCellSearch_inline.h:59-61;
+// it may lie outside the domain) and its position relative to that cell.
+struct Ghost {
+  int cx, cy, cz;
+  float lx, ly, lz;
+};
+__device__ __forceinline__ Ghost mdbc_ghost(const gbsph_consts& c, const DevArrays& a, const DivState& d,
+                                            unsigned p1, float4 bn) {
   double gx = a.px[p1] + (double)bn.x, gy = a.py[p1] + (double)bn.y, gz = a.pz[p1] + (double)bn.z;
-  // the ghost node taken back into the domain across periodic faces
-  // (UpdatePeriodicPos, JSphCpu_mdbc.cpp:50, JSph.cpp:2079-2101)
   if (c.peri[0] || c.peri[1] || c.peri[2]) {
     double dx = __dsub_rn(gx, c.maprealposmin[0]), dy = __dsub_rn(gy, c.maprealposmin[1]),
            dz = __dsub_rn(gz, c.maprealposmin[2]);
@@ -1299,74 +1302,84 @@ __global__ void __launch_bounds__(128) k_mdbc(gbsph_consts c, DevArrays a) {
     }
   }
   const double sc = (double)c.scell;
-  // cell of the ghost node, truncated toward zero as int() does (JCellSearch_inline.h:59-61)
   const int gcx = (int)((gx - c.domposmin[0]) / sc), gcy = (int)((gy - c.domposmin[1]) / sc),
             gcz = (int)((gz - c.domposmin[2]) / sc);
-  const float glx = (float)(gx - c.domposmin[0] - (double)gcx * sc);
-  const float gly = (float)(gy - c.domposmin[1] - (double)gcy * sc);
-  const float glz = (float)(gz - c.domposmin[2] - (double)gcz * sc);
-  const CellGrid g = gb_grid(gcx - (int)d.cellmin[0], gcy - (int)d.cellmin[1], gcz - (int)d.cellmin[2],
-                             c.cellmode_div, d);
-  const float scell = c.scell, ks2 = c.kernelsize2, h = c.kernelh;
-  float rhop1 = 0, grx = 0, gry = 0, grz = 0;
-  unsigned nfound = 0;
-  float Ah[4][4], Al[4][4];
+  Ghost g;
+  g.lx = (float)(gx - c.domposmin[0] - (double)gcx * sc);
+  g.ly = (float)(gy - c.domposmin[1] - (double)gcy * sc);
+  g.lz = (float)(gz - c.domposmin[2] - (double)gcz * sc);
+  g.cx = gcx - (int)d.cellmin[0];
+  g.cy = gcy - (int)d.cellmin[1];
+  g.cz = gcz - (int)d.cellmin[2];
+  return g;
+}
+
+// Compensated sums of two entries at once (TwoSum in packed arithmetic:
+// a - b is fma(b, -1, a), rounded once as a subtraction is, so every entry
+// gets the bits the scalar gb_kadd gives it).
+__device__ __forceinline__ void gb_kadd2(float2& hi, float2& lo, float2 x) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  const float2 s = __fadd2_rn(hi, x);
+  const float2 bp = __ffma2_rn(hi, m1, s);
+  const float2 e = __fadd2_rn(__ffma2_rn(__ffma2_rn(bp, m1, s), m1, hi), __ffma2_rn(bp, m1, x));
+  hi = s;
+  lo = __fadd2_rn(lo, e);
+}
+
+// One fluid neighbour of a ghost node at dr = ghost - neighbour: kernel
+// sums and the moment matrix (Wendland WabFac, FunSphKernel.h:235-246).
+// Entries (0,1) and (2,3) of every matrix row, and of b, are summed as pairs.
+struct MdbcAcc {
+  float2 Ah[4][2], Al[4][2];  // the moment matrix A, compensated
+  float2 bh[2], bl[2];        // b = (sum m W, sum m gradW), compensated
+  unsigned nfound;
+};
+__device__ __forceinline__ void mdbc_pair(const gbsph_consts& c, float hinv, float drx, float dry, float drz,
+                                          float rr2, float rhop2, MdbcAcc& m) {
+  m.nfound++;
+  const float rad = sqrtf(rr2);
+  const float qq = rad * hinv;
+  const float wqq1 = 1.f - 0.5f * qq;
+  const float wqq2 = wqq1 * wqq1;
+  const float fac = c.bwenh * wqq2 * wqq1;
+  const float wqq = qq + qq + 1.f;
+  const float wab = c.awen * wqq * wqq2 * wqq2;
+  const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
+  const float massp2 = c.massfluid;
+  const float volp2 = massp2 / rhop2;
+  const float2 mm = make_float2(massp2, massp2);
+  gb_kadd2(m.bh[0], m.bl[0], __fmul2_rn(mm, make_float2(wab, frx)));
+  gb_kadd2(m.bh[1], m.bl[1], __fmul2_rn(mm, make_float2(fry, frz)));
+  const float rowv[4] = {wab * volp2, frx * volp2, fry * volp2, frz * volp2};
+  const float2 d01 = make_float2(1.f, drx), d23 = make_float2(dry, drz);
 #pragma unroll
-  for (int i = 0; i < 4; i++)
-#pragma unroll
-    for (int j = 0; j < 4; j++) Ah[i][j] = Al[i][j] = 0.f;
-  for (int z = g.zini; z < g.zfin; z++) {
-    for (int y = g.yini; y < g.yfin; y++) {
-      const unsigned rowbase = d.boxfluid + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
-      const float by = gly + (float)(g.cy - y) * scell, bz = glz + (float)(g.cz - z) * scell;
-      for (int x = g.xini; x < g.xfin; x++) {
-        const unsigned box = rowbase + (unsigned)x;
-        const unsigned pini = a.begincell[box], pfin = a.begincell[box + 1];
-        const float bx = glx + (float)(g.cx - x) * scell;
-        for (unsigned p2 = pini; p2 < pfin; p2++) {
-          const float4 ps2 = a.pscell[p2];
-          const float drx = bx - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
-          const float rr2 = drx * drx + dry * dry + drz * drz;
-          if (rr2 <= ks2 && (a.code[p2] & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID) {
-            nfound++;
-            // Wendland WabFac (FunSphKernel.h:235-246)
-            const float rad = sqrtf(rr2);
-            const float qq = rad / h;
-            const float wqq1 = 1.f - 0.5f * qq;
-            const float wqq2 = wqq1 * wqq1;
-            const float fac = c.bwenh * wqq2 * wqq1;
-            const float wqq = qq + qq + 1.f;
-            const float wab = c.awen * wqq * wqq2 * wqq2;
-            const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
-            const float rhop2 = a.velrho[p2].w;
-            const float massp2 = c.massfluid;
-            const float volp2 = massp2 / rhop2;
-            rhop1 += massp2 * wab;
-            grx += massp2 * frx; gry += massp2 * fry; grz += massp2 * frz;
-            const float vwab = wab * volp2, vfrx = frx * volp2, vfry = fry * volp2, vfrz = frz * volp2;
-            const float rowv[4] = {vwab, vfrx, vfry, vfrz};
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-              gb_kadd(Ah[i][0], Al[i][0], rowv[i]);
-              gb_kadd(Ah[i][1], Al[i][1], __fmul_rn(drx, rowv[i]));
-              gb_kadd(Ah[i][2], Al[i][2], __fmul_rn(dry, rowv[i]));
-              gb_kadd(Ah[i][3], Al[i][3], __fmul_rn(drz, rowv[i]));
-            }
-          }
-        }
-      }
-    }
+  for (int i = 0; i < 4; i++) {
+    const float2 v = make_float2(rowv[i], rowv[i]);
+    gb_kadd2(m.Ah[i][0], m.Al[i][0], __fmul2_rn(v, d01));
+    gb_kadd2(m.Ah[i][1], m.Al[i][1], __fmul2_rn(v, d23));
   }
+}
+
+// The corrected density of boundary row p1 from its sums, written to velrho.w
+// and its pressure to pscell.w.
+__device__ __forceinline__ void mdbc_final(const gbsph_consts& c, const DevArrays& a, unsigned p1, float4 bn,
+                                           const MdbcAcc& m) {
   float rhofinal = FLT_MAX;
-  if (nfound) {
+  if (m.nfound) {
     // [A | b] with A the moment matrix and b = (rho, grad rho)
     double M[4][5];
 #pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-      for (int j = 0; j < 4; j++) M[i][j] = (double)Ah[i][j] + (double)Al[i][j];
-    M[0][4] = rhop1; M[1][4] = grx; M[2][4] = gry; M[3][4] = grz;
-    const double a00 = M[0][0];
+    for (int i = 0; i < 4; i++) {
+      M[i][0] = (double)m.Ah[i][0].x + (double)m.Al[i][0].x;
+      M[i][1] = (double)m.Ah[i][0].y + (double)m.Al[i][0].y;
+      M[i][2] = (double)m.Ah[i][1].x + (double)m.Al[i][1].x;
+      M[i][3] = (double)m.Ah[i][1].y + (double)m.Al[i][1].y;
+    }
+    M[0][4] = (double)m.bh[0].x + (double)m.bl[0].x;
+    M[1][4] = (double)m.bh[0].y + (double)m.bl[0].y;
+    M[2][4] = (double)m.bh[1].x + (double)m.bl[1].x;
+    M[3][4] = (double)m.bh[1].y + (double)m.bl[1].y;
+    const double a00 = M[0][0], b0 = M[0][4];
     double det = 1.0, rinv[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -1406,7 +1419,7 @@ __global__ void __launch_bounds__(128) k_mdbc(gbsph_consts c, DevArrays a) {
       const float ggx = -(float)xs[1], ggy = -(float)xs[2], ggz = -(float)xs[3];
       rhofinal = rhoghost + ggx * (-bn.x) + ggy * (-bn.y) + ggz * (-bn.z);
     } else if (a00 > 0) {
-      rhofinal = (float)(rhop1 / a00);
+      rhofinal = (float)(b0 / a00);
     }
   }
   rhofinal = (rhofinal != FLT_MAX) ? rhofinal : c.rhopzero;
@@ -1416,6 +1429,281 @@ __global__ void __launch_bounds__(128) k_mdbc(gbsph_consts c, DevArrays a) {
   float4 ps = a.pscell[p1];
   ps.w = gb_press(rhofinal, c.rhopzero, c.cteb, c.gamma);
   a.pscell[p1] = ps;
+}
+
+__device__ __forceinline__ void mdbc_zero(MdbcAcc& m) {
+  const float2 z = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < 4; i++) m.Ah[i][0] = m.Ah[i][1] = m.Al[i][0] = m.Al[i][1] = z;
+  m.bh[0] = m.bh[1] = m.bl[0] = m.bl[1] = z;
+  m.nfound = 0u;
+}
+
+// One thread per boundary row, walking the 27 (or 125) boxes around its ghost
+// node in the reference's order.
+__global__ void __launch_bounds__(128) k_mdbc(gbsph_consts c, DevArrays a) {
+  const DivState& d = *a.div;
+  const unsigned p1 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p1 >= d.npbok) return;
+  const float4 bn = a.boundnor[p1];
+  if (bn.x == 0.f && bn.y == 0.f && bn.z == 0.f) return;
+  const Ghost gh = mdbc_ghost(c, a, d, p1, bn);
+  const CellGrid g = gb_grid(gh.cx, gh.cy, gh.cz, c.cellmode_div, d);
+  const float scell = c.scell, ks2 = c.kernelsize2, hinv = 1.f / c.kernelh;
+  MdbcAcc m;
+  mdbc_zero(m);
+  for (int z = g.zini; z < g.zfin; z++) {
+    for (int y = g.yini; y < g.yfin; y++) {
+      const unsigned rowbase = d.boxfluid + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+      const float by = gh.ly + (float)(g.cy - y) * scell, bz = gh.lz + (float)(g.cz - z) * scell;
+      for (int x = g.xini; x < g.xfin; x++) {
+        const unsigned box = rowbase + (unsigned)x;
+        const unsigned pini = a.begincell[box], pfin = a.begincell[box + 1];
+        const float bx = gh.lx + (float)(g.cx - x) * scell;
+        for (unsigned p2 = pini; p2 < pfin; p2++) {
+          const float4 ps2 = a.pscell[p2];
+          const float drx = bx - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
+          const float rr2 = drx * drx + dry * dry + drz * drz;
+          if (rr2 <= ks2 && (a.code[p2] & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID)
+            mdbc_pair(c, hinv, drx, dry, drz, rr2, a.velrho[p2].w, m);
+        }
+      }
+    }
+  }
+  mdbc_final(c, a, p1, bn, m);
+}
+
+// ---- mDBC, cell-tiled staged kernel -----------------------------------------
+// The fluid-row kernel's scheme with ghost nodes as targets: a warp takes 32
+// consecutive boundary rows; the ghost nodes of one row of cells (y, z) are a
+// group, whose candidates -- the fluid boxes' particles around it, one range
+// per row of boxes -- are staged through a ring of kMdbcR chunks (the negated
+// position in the group's frame and the density), filtered by the box of the
+// group's ghosts widened by 2h and by the fluid type, checked four at a time
+// with packed arithmetic, and consumed in rounds in which every ghost of the
+// group with a pending hit adds one neighbour to its sums.  A ghost whose cell
+// lies outside the domain sees the boxes inside it only, as the per-ghost walk
+// does (gb_grid).  The summation order per ghost is the order of the staged
+// chunks; the moment matrix is summed compensated, as in k_mdbc.
+constexpr int kMdbcR = 8;
+// per slot: -x, -y, -z in the group's frame (the checks), the position
+// relative to the candidate's own cell, its cell offset from the group's
+// reference cell (x as a float, an integer exactly; y and z, within +-sd,
+// as two 8-bit fields), the density, the hit mask
+constexpr int kMdbcArrays = 10;
+constexpr size_t kMdbcWarpBytes = (size_t)kMdbcR * 32 * kMdbcArrays * 4;
+
+__device__ __forceinline__ void mdbc_refill(const float* ring, unsigned& cur, unsigned& cc, unsigned cnext,
+                                            int lane) {
+  const unsigned* sm = (const unsigned*)(ring + 9 * kMdbcR * 32);
+  while (cur == 0u && cc + 1u < cnext) {
+    cc++;
+    cur = sm[(cc & (kMdbcR - 1)) * 32 + lane];
+  }
+  if (cur == 0u) cc = cnext;
+}
+
+// dr = ghost - neighbour formed as the per-row walk forms it, from the
+// ghost's and the neighbour's positions relative to their own cells and the
+// difference of their cells (fox: the ghost's cell offset from the group's
+// reference cell along x; along y and z it is 0 within a group), so that the
+// ill-conditioned solves of ghosts near corners see the same sums.
+__device__ __forceinline__ void mdbc_round(const gbsph_consts& c, float hinv, const float* ring, unsigned& cur,
+                                           unsigned& cc, unsigned cnext, const Ghost& gh, int fox, MdbcAcc& m,
+                                           int lane) {
+  if (cur != 0u) {
+    constexpr int S = kMdbcR * 32;
+    const unsigned slot = ((cc & (kMdbcR - 1)) << 5) | (unsigned)(__ffs(cur) - 1);
+    cur &= cur - 1u;
+    const float* e = ring + slot;
+    const int o = __float_as_int(e[7 * S]);
+    const int dyj = (o << 24) >> 24, dzj = (o << 16) >> 24;
+    const float scell = c.scell;
+    const float drx = (gh.lx + ((float)fox - e[6 * S]) * scell) - e[3 * S];
+    const float dry = (gh.ly + (float)(-dyj) * scell) - e[4 * S];
+    const float drz = (gh.lz + (float)(-dzj) * scell) - e[5 * S];
+    mdbc_pair(c, hinv, drx, dry, drz, drx * drx + dry * dry + drz * drz, e[8 * S], m);
+    mdbc_refill(ring, cur, cc, cnext, lane);
+  }
+}
+
+__global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) {
+  extern __shared__ float4 mdbc_smem[];
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int S = kMdbcR * 32;
+  const DivState& d = *a.div;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned p1 = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned npbok = d.npbok;
+  float4 bn = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (p1 < npbok) bn = a.boundnor[p1];
+  const bool active = p1 < npbok && !(bn.x == 0.f && bn.y == 0.f && bn.z == 0.f);
+  if (__all_sync(FULL, !active)) return;
+  float* ring = (float*)((char*)mdbc_smem + (size_t)warp * kMdbcWarpBytes);
+  unsigned* sm = (unsigned*)(ring + 9 * S);
+  Ghost gh = {0, 0, 0, 0.f, 0.f, 0.f};
+  if (active) gh = mdbc_ghost(c, a, d, p1, bn);
+  const int cx = gh.cx, cy = gh.cy, cz = gh.cz;
+  const float scell = c.scell, ks2 = c.kernelsize2, hinv = 1.f / c.kernelh;
+  const int sd = c.cellmode_div;
+  const int ncx = (int)d.ncx, ncy = (int)d.ncy, ncz = (int)d.ncz;
+  const unsigned dcc = c.domcellcode, cmin0 = d.cellmin[0];
+  MdbcAcc m;
+  mdbc_zero(m);
+  unsigned cnext = 0u, cc = 0u, cur = 0u;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  int fox = 0;
+  unsigned remaining = __ballot_sync(FULL, active);
+  while (remaining) {
+    const int leader = __ffs(remaining) - 1;
+    const int rx = __shfl_sync(FULL, cx, leader), ry = __shfl_sync(FULL, cy, leader),
+              rz = __shfl_sync(FULL, cz, leader);
+    const bool ing = active && cy == ry && cz == rz;
+    const unsigned grp = __ballot_sync(FULL, ing);
+    remaining &= ~grp;
+    const int xmin = __reduce_min_sync(FULL, ing ? cx : 0x7fffffff);
+    const int xmax = __reduce_max_sync(FULL, ing ? cx : (int)0x80000000);
+    const int x0 = max(xmin - sd, 0), x1 = min(xmax + sd, ncx - 1);
+    const int y0 = max(ry - sd, 0), y1 = min(ry + sd, ncy - 1);
+    const int z0 = max(rz - sd, 0), z1 = min(rz + sd, ncz - 1);
+    if (x0 > x1 || y0 > y1 || z0 > z1) continue;  // the ghosts' boxes are all outside the domain
+    const int nyr = y1 - y0 + 1, nrows = nyr * (z1 - z0 + 1);
+    unsigned rb = 0u, rlen = 0u;
+    int rdy = 0, rdz = 0;
+    if (lane < nrows) {
+      const int y = y0 + lane % nyr, z = z0 + lane / nyr;
+      const unsigned rowbase = d.boxfluid + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+      rb = a.begincell[rowbase + (unsigned)x0];
+      rlen = a.begincell[rowbase + (unsigned)x1 + 1u] - rb;
+      rdy = y - ry;
+      rdz = z - rz;
+    }
+    unsigned incl = rlen;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const unsigned total = __shfl_sync(FULL, incl, 31);
+    if (total == 0u) continue;
+    const unsigned rbase = rb - (incl - rlen);
+    if (ing) {
+      fox = cx - rx;
+      fx = gh.lx + (float)fox * scell;
+      fy = gh.ly;
+      fz = gh.lz;
+    }
+    const float2 fxx = make_float2(fx, fx), fyy = make_float2(fy, fy), fzz = make_float2(fz, fz);
+    const unsigned gmask = ing ? FULL : 0u;
+    const float blox = tile_fmin(ing, fx), bloy = tile_fmin(ing, fy), bloz = tile_fmin(ing, fz);
+    const float bhix = tile_fmax(ing, fx), bhiy = tile_fmax(ing, fy), bhiz = tile_fmax(ing, fz);
+    const float ks2m = ks2 * 1.0001f;
+    unsigned fill = 0u;
+    const unsigned nch = (total + 31u) >> 5, plen = nch * kTSeg;
+    unsigned stride = max(1u, (unsigned)__float2uint_rn(0.6180339887f * (float)nch));
+    for (;;) {
+      unsigned u = stride, v = nch;
+      while (v) { const unsigned t = u % v; u = v; v = t; }
+      if (u == 1u) break;
+      stride++;
+    }
+    const unsigned pbase = (unsigned)(lane / kTSeg) * plen + (unsigned)(lane % kTSeg);
+    const unsigned send = min((unsigned)(lane / kTSeg + 1) * plen, total);
+    unsigned ch = 0u;
+    // checks the full chunk cnext and runs rounds while every ghost of the
+    // group has a hit pending
+    auto check = [&]() {
+      const unsigned base = (cnext & (kMdbcR - 1)) << 5;
+      unsigned hm = 0u;
+#pragma unroll
+      for (int q = 0; q < 32; q += 4) {
+        const float4 xq = *(const float4*)(ring + base + q);
+        const float4 yq = *(const float4*)(ring + S + base + q);
+        const float4 zq = *(const float4*)(ring + 2 * S + base + q);
+        hm |= tile_check4(fxx, fyy, fzz, xq, yq, zq, ks2, q);
+      }
+      hm &= gmask;
+      sm[base + lane] = hm;
+      if (cc == cnext) cur = hm;
+      cnext++;
+      if (cur == 0u) cc = cnext;
+      while (__ballot_sync(FULL, ing && cur != 0u) == grp) mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, m, lane);
+    };
+    for (unsigned i = 0; i < nch; i++, ch = (ch + stride >= nch) ? ch + stride - nch : ch + stride) {
+      const unsigned s = pbase + ch * kTSeg;
+      int lo = 0, hi = nrows;
+#pragma unroll
+      for (int it = 0; it < 5; it++) {
+        const int mid = (lo + hi) >> 1;
+        const bool le = __shfl_sync(FULL, incl, mid & 31) <= s;
+        if (lo < hi) {
+          if (le) lo = mid + 1;
+          else hi = mid;
+        }
+      }
+      const bool has = s < send;
+      const int rowc = min(lo, 31);
+      const unsigned jb = __shfl_sync(FULL, rbase, rowc);
+      const int dyj = __shfl_sync(FULL, rdy, rowc), dzj = __shfl_sync(FULL, rdz, rowc);
+      bool keep = false;
+      float qx = 0.f, qy = 0.f, qz = 0.f, qrho = 1.f;
+      float4 ps2 = make_float4(0.f, 0.f, 0.f, 0.f);
+      int dxj = 0;
+      if (has) {
+        const unsigned j = jb + s;
+        if ((a.code[j] & GB_CODE_MASKTYPE) == GB_CODE_TYPE_FLUID) {
+          ps2 = a.pscell[j];
+          qrho = a.velrho[j].w;
+          dxj = (int)(gb_cx(dcc, a.dcell[j]) - cmin0) - rx;
+          qx = ps2.x + (float)dxj * scell;
+          qy = ps2.y + (float)dyj * scell;
+          qz = ps2.z + (float)dzj * scell;
+          const float ex = fmaxf(fmaxf(blox - qx, qx - bhix), 0.f);
+          const float ey = fmaxf(fmaxf(bloy - qy, qy - bhiy), 0.f);
+          const float ez = fmaxf(fmaxf(bloz - qz, qz - bhiz), 0.f);
+          keep = ex * ex + ey * ey + ez * ez <= ks2m;
+        }
+      }
+      const unsigned kb = __ballot_sync(FULL, keep);
+      if (kb == 0u) continue;
+      const unsigned nk = (unsigned)__popc(kb);
+      const unsigned need = fill + nk > 32u ? cnext + 1u : cnext;
+      while (__any_sync(FULL, cur != 0u && cc + (unsigned)kMdbcR <= need))
+        mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, m, lane);
+      if (keep) {
+        const unsigned pos = fill + (unsigned)__popc(kb & ((1u << lane) - 1u));
+        const unsigned slot = (((pos < 32u ? cnext : cnext + 1u) & (kMdbcR - 1)) << 5) | (pos & 31u);
+        ring[slot] = -qx;
+        ring[S + slot] = -qy;
+        ring[2 * S + slot] = -qz;
+        ring[3 * S + slot] = ps2.x;
+        ring[4 * S + slot] = ps2.y;
+        ring[5 * S + slot] = ps2.z;
+        ring[6 * S + slot] = (float)dxj;
+        ring[7 * S + slot] = __int_as_float((dyj & 255) | ((dzj & 255) << 8));
+        ring[8 * S + slot] = qrho;
+      }
+      fill += nk;
+      if (fill >= 32u) {
+        __syncwarp();
+        check();
+        fill -= 32u;
+      }
+    }
+    if (fill) {
+      const unsigned base = (cnext & (kMdbcR - 1)) << 5;
+      if ((unsigned)lane >= fill) {
+        ring[base + lane] = -kFarAway;
+        ring[S + base + lane] = -kFarAway;
+        ring[2 * S + base + lane] = -kFarAway;
+      }
+      __syncwarp();
+      check();
+      fill = 0u;
+    }
+  }
+  while (__any_sync(FULL, cur != 0u)) mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, m, lane);
+  if (active) mdbc_final(c, a, p1, bn, m);
 }
 
 // Particle-interaction count (JDsPips::ComputeGpu / KerInteractionNg,
@@ -1554,7 +1842,9 @@ void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, 
 
 cudaError_t forces_init(const gbsph_consts& c) {
   DevArrays a{};
-  return launch_fluid_v(c, a, 0, 2, 128, true, nullptr);
+  const cudaError_t e = launch_fluid_v(c, a, 0, 2, 128, true, nullptr);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_mdbc_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(4 * kMdbcWarpBytes));
 }
 
 void sps_tau(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch) {
@@ -1567,8 +1857,10 @@ void pips(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t 
   k_pips<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
 }
 
-void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch) {
-  k_mdbc<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s,
+          unsigned long long* nlaunch) {
+  if (variant == 1) k_mdbc<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+  else k_mdbc_t<<<gb_div_up(cap, 128), 128, 4 * kMdbcWarpBytes, s>>>(c, a);
   if (nlaunch) *nlaunch += 1;
 }
 

@@ -368,7 +368,9 @@ void* gbsph_stream(gbsph_ctx* ctx);
  * with no queue.  key 0 = threads per block of the one-thread-per-particle
  * kernel (64, 128 or 256; the other kernels use 128).  The reference fixes
  * 128 threads per block (JSphGpu.cpp, BlockSizes).  key 2 = digit width of
- * the divide's radix sort, 8 (default) or 11 bits. */
+ * the divide's radix sort, 8 (default) or 11 bits.  key 3 = mDBC kernel of
+ * gbsph_mdbc: 0 (default) cell-tiled, the ghost nodes' fluid neighbours
+ * staged through shared memory; 1 one thread per boundary row. */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
 /* The current value of an option of gbsph_set_option (no reference counterpart). */
 int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value);

@@ -119,6 +119,7 @@ _SIG = {
     "orc_sim_time": (C.c_double, [P]),
     "orc_sim_times": (None, [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "orc_set_sampling": (None, [C.c_int, C.c_int]),
+    "orc_sim_mdbc_f64": (None, [C.c_void_p, C.c_void_p]),
 }
 
 _L = None
@@ -331,6 +332,14 @@ def forces_f64(sim: Sim):
                                      _p(shift), _p(absshift))
     return {"ace": ace, "ar": ar, "viscdt": visc.value, "absace": absace, "absar": absar, "shiftpos": shift,
             "absshift": absshift}
+
+
+def mdbc_f64(sim: Sim) -> np.ndarray:
+    """FP64 evaluation of the mDBC corrected densities of the boundary rows
+    (npbok) on the oracle's current state; the state is not changed."""
+    out = np.empty(sim.npbok, np.float64)
+    lib().orc_sim_mdbc_f64(sim.h, _p(out))
+    return out
 
 
 def pips(sim: Sim):

@@ -608,6 +608,89 @@ void orc_mdbc_correction(const orc_ctes* c, const orc_div* d, const unsigned* be
   }
 }
 
+/* The same correction evaluated in double throughout: dr, the kernel and its
+ * gradient, the sums (rho, grad rho) and the moment matrix, the solve.  Writes
+ * the corrected density of every row p1 < n with a normal to rho64[p1] (the
+ * other rows get the state's density); velrho is not changed.  It is the
+ * FP64 reference of the mDBC density criterion. */
+void orc_mdbc_correction_f64(const orc_ctes* c, const orc_div* d, const unsigned* begincell, unsigned n,
+                             const double* pos, const uint16_t* code, const float* boundnor, const float* velrho,
+                             double* rho64, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(guided)
+#endif
+  for (int p1 = 0; p1 < (int)n; p1++) {
+    rho64[p1] = velrho[4 * (size_t)p1 + 3];
+    if (g_sample_stride > 1 && (p1 % g_sample_stride) != g_sample_phase) continue;
+    const float* bn = boundnor + 3 * (size_t)p1;
+    if (bn[0] == 0 && bn[1] == 0 && bn[2] == 0) continue;
+    const double* ps = pos + 3 * (size_t)p1;
+    double gp[3] = {ps[0] + (double)bn[0], ps[1] + (double)bn[1], ps[2] + (double)bn[2]};
+    if (c->peri[0] || c->peri[1] || c->peri[2]) update_periodic_pos(c, gp);
+    double b[4] = {0, 0, 0, 0};
+    double A[4][4];
+    memset(A, 0, sizeof(A));
+    const double h = c->kernelh, bwenh = c->bwenh, awen = c->awen, ks2 = c->kernelsize2;
+    const ngsearch g = ngs_init_pos(c, d, gp, 0);
+    for (int z = g.zini; z < g.zfin; z++)
+      for (int y = g.yini; y < g.yfin; y++) {
+        unsigned pini, pfin;
+        particle_range(d, begincell, y, z, &g, &pini, &pfin);
+        for (unsigned p2 = pini; p2 < pfin; p2++) {
+          const double* q = pos + 3 * (size_t)p2;
+          const double drx = gp[0] - q[0], dry = gp[1] - q[1], drz = gp[2] - q[2];
+          const double rr2 = drx * drx + dry * dry + drz * drz;
+          if (rr2 <= ks2 && codetype(code[p2]) == ORC_CODE_TYPE_FLUID) {
+            const double qq = sqrt(rr2) / h;
+            const double wqq1 = 1. - 0.5 * qq;
+            const double wqq2 = wqq1 * wqq1;
+            const double fac = bwenh * wqq2 * wqq1;
+            const double wab = awen * (qq + qq + 1.) * wqq2 * wqq2;
+            const double fr[3] = {fac * drx, fac * dry, fac * drz};
+            const double massp2 = c->massfluid;
+            const double volp2 = massp2 / (double)velrho[4 * (size_t)p2 + 3];
+            b[0] += massp2 * wab;
+            for (int k = 0; k < 3; k++) b[1 + k] += massp2 * fr[k];
+            const double row[4] = {wab * volp2, fr[0] * volp2, fr[1] * volp2, fr[2] * volp2};
+            for (int r = 0; r < 4; r++) {
+              A[r][0] += row[r];
+              A[r][1] += drx * row[r];
+              A[r][2] += dry * row[r];
+              A[r][3] += drz * row[r];
+            }
+          }
+        }
+      }
+    /* cofactor solve, as mdbc_solve, in double */
+    double C[4][4];
+    for (int i = 0; i < 4; i++)
+      for (int j = 0; j < 4; j++) {
+        double m[9];
+        int k = 0;
+        for (int r = 0; r < 4; r++) {
+          if (r == i) continue;
+          for (int s = 0; s < 4; s++) {
+            if (s == j) continue;
+            m[k++] = A[r][s];
+          }
+        }
+        const double mdet = det3(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]);
+        C[i][j] = ((i + j) & 1) ? -mdet : mdet;
+      }
+    const double det = A[0][0] * C[0][0] + A[0][1] * C[0][1] + A[0][2] * C[0][2] + A[0][3] * C[0][3];
+    double rho = c->rhopzero;
+    if (fabs(det) >= 1e-3) {
+      double x[4];
+      for (int r = 0; r < 4; r++) x[r] = (C[0][r] * b[0] + C[1][r] * b[1] + C[2][r] * b[2] + C[3][r] * b[3]) / det;
+      rho = x[0] - x[1] * -(double)bn[0] - x[2] * -(double)bn[1] - x[3] * -(double)bn[2];
+    } else if (A[0][0] > 0) {
+      rho = b[0] / A[0][0];
+    }
+    rho64[p1] = rho;
+  }
+}
+
 /* Particle-interaction counts (JDsPips.cpp:187-260): out = {checked bound
  * rows, real bound rows, checked fluid rows, real fluid rows}. */
 void orc_pips(const orc_ctes* c, const orc_div* d, const unsigned* begincell, unsigned np, unsigned npb,
@@ -921,6 +1004,11 @@ int orc_sim_run_cell_divide(orc_sim* s) {
 }
 
 /* JSphCpuSingle::MdbcBoundCorrection (JSphCpuSingle.cpp:754-780), vel0. */
+void orc_sim_mdbc_f64(orc_sim* s, double* rho64) {
+  orc_mdbc_correction_f64(&s->c, &s->d, s->begincell, s->npbok, s->pos, s->code, s->boundnor, s->velrho, rho64,
+                          s->nthreads);
+}
+
 int orc_sim_mdbc(orc_sim* s, int corrector) {
   if (s->c.tboundary != ORC_BC_MDBC || corrector) return 0;
   orc_mdbc_correction(&s->c, &s->d, s->begincell, s->npbok, s->pos, s->code, s->boundnor, s->velrho, s->nthreads);

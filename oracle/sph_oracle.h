@@ -182,6 +182,10 @@ unsigned orc_sim_nout(const orc_sim* s);
 double orc_sim_time(const orc_sim* s);
 void orc_sim_times(const orc_sim* s, double* t_inter, double* t_step);
 void orc_set_sampling(int stride, int phase);
+void orc_sim_mdbc_f64(orc_sim* s, double* rho64);
+void orc_mdbc_correction_f64(const orc_ctes* c, const orc_div* d, const unsigned* begincell, unsigned n,
+                             const double* pos, const uint16_t* code, const float* boundnor, const float* velrho,
+                             double* rho64, int nthreads);
 
 #ifdef __cplusplus
 }

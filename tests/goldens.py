@@ -110,3 +110,20 @@ def scaled_err(x, ref, scale):
     if e.ndim == 2:
         e = e.max(axis=1)
     return e / np.maximum(scale, 1e-30)
+
+
+def assert_mdbc_parity(rho, rho_orc32, rho_f64, what="mDBC density"):
+    """mDBC corrected densities, per boundary row, against the FP64 evaluation
+    of the correction (pyoracle.mdbc_f64): the largest relative error is at
+    most twice the largest error of the oracle's own FP32 evaluation (the
+    reference's algorithm: its sums of rho and grad rho are plain float sums
+    in the reference's cell order) plus 1e-7, and the median error at most
+    twice the oracle's median plus 1e-7.  The reference's own densities meet
+    the same bound (tests/test_oracle_golden.py)."""
+    r64 = np.asarray(rho_f64, np.float64)
+    e = np.abs(np.asarray(rho, np.float64) - r64) / np.abs(r64)
+    eo = np.abs(np.asarray(rho_orc32, np.float64) - r64) / np.abs(r64)
+    assert e.max() <= 2.0 * eo.max() + 1e-7, f"{what}: max relative error {e.max():.3e} (oracle FP32 {eo.max():.3e})"
+    assert np.median(e) <= 2.0 * np.median(eo) + 1e-7, \
+        f"{what}: median relative error {np.median(e):.3e} (oracle FP32 {np.median(eo):.3e})"
+    return e.max(), eo.max()

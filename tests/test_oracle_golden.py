@@ -54,9 +54,13 @@ def test_forces_within_fp32_tolerance(name):
     """ace/ar of the oracle and of the reference, both against the FP64 oracle."""
     g = G.golden(name)
     _, _, sim = _sim(name)
+    r64 = po.mdbc_f64(sim)
     sim.mdbc(False)
     rho_b = sim.state()["velrho"][:, 3]
     np.testing.assert_allclose(rho_b, g["s0mdbc_rho"], rtol=2e-6)
+    # the reference's own mDBC densities meet the FP64 criterion of the GPU tests
+    nb = sim.npbok
+    G.assert_mdbc_parity(g["s0mdbc_rho"][:nb], rho_b[:nb], r64, "reference mDBC density")
     f64 = po.forces_f64(sim)
     sim.interaction()
     a32, r32 = sim.forces()
