@@ -57,7 +57,8 @@ FP32_LANES_PER_SM = 128     # FFMA lanes per SM (2 FLOP each per clock)
 # 0.0025 m), from one ncu capture each (dram__bytes_read.sum +
 # dram__bytes_write.sum, --clock-control none), summarised in profiles/:
 # variant -> (kernel, bytes per launch, dp of the capture)
-DRAM_TRAFFIC = {0: ("k_forces_fluid_q", 269218560.0, 0.0025)}
+DRAM_TRAFFIC = {0: ("k_forces_fluid_q", 269218560.0, 0.0025),   # k_forces_fluid_q_c2_dram.md
+                2: ("k_forces_fluid_t", 270835000.0, 0.0025)}   # k_forces_fluid_t_c2_dram.md
 # the fluid-row kernel of each variant (gbsph_set_option key 1)
 KERNEL_NAME = {0: "k_forces_fluid_q", 1: "k_forces_fluid", 2: "k_forces_fluid_t (ring of 8 chunks)",
                3: "k_forces_fluid_t (ring of 4 chunks)"}
@@ -454,6 +455,9 @@ def main():
     ap.add_argument("--variant", type=int, default=None,
                     help="fluid-row kernel: 0 queued rounds, 1 one thread per particle, 2/3 cell-tiled staged "
                          "(ring of 8/4 chunks); default: the library's")
+    ap.add_argument("--split", type=int, default=None, choices=[0, 1, 2, 4],
+                    help="warps per group of 32 fluid rows in the cell-tiled kernel (0 automatic); default: the "
+                         "library's")
     ap.add_argument("--no-tune", action="store_true", help="keep the 8-bit sort digits (no sort autotuning)")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c3err", "ensemble", "closure",
                                                          "closure-judge"],
@@ -520,7 +524,9 @@ def main():
         s._check(_lib.lib().gbsph_tune_sort(s.ctx, 3, C.byref(sort_bits), sort_ms), "gbsph_tune_sort")
     if args.variant is not None:
         s.set_option(1, args.variant)
-    variant = s.get_option(1)
+    if args.split is not None:
+        s.set_option(4, args.split)
+    variant, split = s.get_option(1), s.get_option(5)
     pi = s.pips()
     s.RunSteps(W, use_graph=True)
     s.sync()
@@ -565,6 +571,8 @@ def main():
         e.set_option(2, sort_bits.value)   # the tuned sort width, set as a caller would
         if args.variant is not None:
             e.set_option(1, args.variant)
+        if args.split is not None:
+            e.set_option(4, args.split)
         for _ in range(K):
             e.RunSteps(1, use_graph=True)  # one step, replayed from its captured graph
             e.step_dt()                    # the Run loop reads the step's dt and time back
@@ -601,7 +609,8 @@ def main():
             "dtype": "f32 (f64 positions and integration)", "data": "synthetic",
             "config": {"workload": workload_text(args),
                        "particles": cd.np, "fluid": cd.nfluid, "boundary": cd.npb, "cellmode": args.cellmode,
-                       "sort_digit_bits": sort_bits.value,
+                       "sort_digit_bits": sort_bits.value, "fluid_kernel_variant": variant,
+                       "warps_per_row_group": split,
                        "sort_divide_ms_8_11": [round(float(x), 4) for x in sort_ms] if not args.no_tune else None,
                        "parallelism": "replicas only" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (no flush)"},

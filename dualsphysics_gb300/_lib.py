@@ -105,12 +105,12 @@ MOV_TYPES = {"wait": 1, "mvrect": 2, "mvrectace": 3, "mvrot": 4, "mvrotace": 5, 
              "mvnull": 8}
 
 
-TUNE_CANDIDATES = 6
+TUNE_CANDIDATES = 8
 
 
 class TuneResult(C.Structure):
     _fields_ = [("best", C.c_int), ("variant", C.c_int * TUNE_CANDIDATES), ("bsize", C.c_int * TUNE_CANDIDATES),
-                ("ms", C.c_float * TUNE_CANDIDATES)]
+                ("split", C.c_int * TUNE_CANDIDATES), ("ms", C.c_float * TUNE_CANDIDATES)]
 
 
 class Maxes(C.Structure):

@@ -38,6 +38,9 @@ struct gbsph_ctx {
   int verletstep = 0;
   unsigned long long launches = 0;
   int forces_bsize = 128, forces_variant = 2;
+  int forces_split = 0;   // warps per group of 32 fluid rows in the staged kernel (0: from nfluid)
+  unsigned nfluid = 0;    // fluid rows at the last upload (chooses the automatic split)
+  int nsm = 0;            // SMs of the device
   int mdbc_variant = 0;   // 0 staged kernel, 1 one thread per boundary row
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -71,6 +74,20 @@ struct gbsph_ctx {
 };
 
 namespace {
+
+// Warps per group of 32 fluid rows in the staged kernel: the option, or with
+// 0 the largest of 4, 2, 1 that keeps the launch within about two waves of
+// resident warps (24 a SM), so that a small case runs more warps, each with a
+// shorter chain of chunks, and a large one keeps one warp per group.
+int forces_split(const gbsph_ctx* ctx) {
+  int s = ctx->forces_split;
+  if (!s) {
+    const unsigned long long warps = (ctx->nfluid + 31u) / 32u,
+                             resident = 24ull * (unsigned)(ctx->nsm > 0 ? ctx->nsm : 1);
+    s = warps * 4ull <= 2ull * resident ? 4 : warps * 2ull <= 2ull * resident ? 2 : 1;
+  }
+  return gbk::forces_split_effective(ctx->c, ctx->forces_variant, s);
+}
 
 int set_err(gbsph_ctx* ctx, int code, const char* fmt, ...) {
   if (ctx) {
@@ -182,7 +199,8 @@ int do_forces(gbsph_ctx* ctx) {
     e1 = ctx->prof_ev[2 * ctx->prof_n + 1];
     ctx->prof_n++;
   }
-  gbk::forces(ctx->c, ctx->a, ctx->cap, ctx->forces_bsize, ctx->forces_variant, ctx->stream, &ctx->launches, e0, e1);
+  gbk::forces(ctx->c, ctx->a, ctx->cap, ctx->forces_bsize, ctx->forces_variant, forces_split(ctx), ctx->stream,
+              &ctx->launches, e0, e1);
   if (ctx->c.tvisco == GBSPH_VISCO_LAMINARSPS) gbk::sps_tau(ctx->c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
   if (ctx->clos_on) {  // the learned correction of the fluid accelerations
     gbk::closure_features(ctx->c, ctx->a, ctx->cap, ctx->clos_feat, ctx->stream, &ctx->launches);
@@ -281,7 +299,8 @@ int gbsph_create(const gbsph_consts* c, unsigned capacity, int device, gbsph_ctx
   unsigned bits = 1;
   while ((1ull << bits) < ctx->nctt_cap) bits++;
   ctx->keybits = bits;
-  if (cudaSetDevice(device) != cudaSuccess) {
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
     delete ctx;
     return GBSPH_ECUDA;
   }
@@ -327,6 +346,7 @@ const char* gbsph_last_error(const gbsph_ctx* ctx) { return ctx ? ctx->err.c_str
 
 static int upload_common(gbsph_ctx* ctx, unsigned np, unsigned npb) {
   const gbsph_consts& c = ctx->c;
+  ctx->nfluid = np - npb;
   DivState ds;
   memset(&ds, 0, sizeof(ds));
   ds.np = np;
@@ -1070,6 +1090,11 @@ int gbsph_set_option(gbsph_ctx* ctx, int key, int value) {
     if (value != 0 && value != 1) return set_err(ctx, GBSPH_EINVAL, "mDBC kernel variant %d is not 0 or 1", value);
     ctx->mdbc_variant = value;
   }
+  else if (key == 4) {
+    if (value != 0 && value != 1 && value != 2 && value != 4)
+      return set_err(ctx, GBSPH_EINVAL, "warps per row group %d is not 0 (automatic), 1, 2 or 4", value);
+    ctx->forces_split = value;
+  }
   else return set_err(ctx, GBSPH_EINVAL, "unknown option %d", key);
   reset_graph(ctx);
   return GBSPH_OK;
@@ -1081,6 +1106,8 @@ int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value) {
   else if (key == 1) *value = ctx->forces_variant;
   else if (key == 2) *value = ctx->sort_bits;
   else if (key == 3) *value = ctx->mdbc_variant;
+  else if (key == 4) *value = ctx->forces_split;
+  else if (key == 5) *value = forces_split(ctx);
   else return GBSPH_EINVAL;
   return GBSPH_OK;
 }
@@ -1126,15 +1153,18 @@ int gbsph_tune_sort(gbsph_ctx* ctx, int reps, int* best_bits, float* ms) {
 // ---- autotuner ------------------------------------------------------------
 // Times the fluid-row kernel configurations on the context's current state
 // (between steps) and keeps the fastest: the cell-tiled staged kernel with a
-// ring of 8 and of 4 chunks, the warp-queued rounds kernel, and the
-// one-thread-per-row kernel at 64, 128 and 256 threads per block.  The
+// ring of 8 chunks at 1, 2 and 4 warps per row group and with a ring of 4
+// chunks, the warp-queued rounds kernel, and the one-thread-per-row kernel at
+// 64, 128 and 256 threads per block.  The
 // launches only rewrite the interaction outputs, which the next step
 // recomputes.
 int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
   if (!ctx || !ctx->uploaded) return set_err(ctx, GBSPH_ESTATE, "no particles uploaded");
   if (reps < 1) reps = 1;
   CK(cudaSetDevice(ctx->device), "set device");
-  static const int cand[GBSPH_TUNE_CANDIDATES][2] = {{2, 128}, {3, 128}, {0, 128}, {1, 64}, {1, 128}, {1, 256}};
+  // variant, block size, warps per row group
+  static const int cand[GBSPH_TUNE_CANDIDATES][3] = {{2, 128, 1}, {2, 128, 2}, {2, 128, 4}, {3, 128, 1},
+                                                     {0, 128, 1}, {1, 64, 1},  {1, 128, 1}, {1, 256, 1}};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0), "event");
   CK(cudaEventCreate(&e1), "event");
@@ -1142,10 +1172,11 @@ int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
   float tbest = 0;
   gbsph_tune_result r{};
   for (int k = 0; k < GBSPH_TUNE_CANDIDATES; k++) {
-    const int var = cand[k][0], bs = cand[k][1];
-    gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, ctx->stream, nullptr, nullptr, nullptr);  // warm-up
+    const int var = cand[k][0], bs = cand[k][1], sp = cand[k][2];
+    gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, sp, ctx->stream, nullptr, nullptr, nullptr);  // warm-up
     cudaEventRecord(e0, ctx->stream);
-    for (int i = 0; i < reps; i++) gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, ctx->stream, nullptr, nullptr, nullptr);
+    for (int i = 0; i < reps; i++)
+      gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, sp, ctx->stream, nullptr, nullptr, nullptr);
     cudaEventRecord(e1, ctx->stream);
     cudaError_t e = cudaEventSynchronize(e1);
     float ms = 0;
@@ -1159,6 +1190,7 @@ int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
     r.ms[k] = ms;
     r.variant[k] = var;
     r.bsize[k] = bs;
+    r.split[k] = sp;
     if (k == 0 || ms < tbest) { tbest = ms; best = k; }
   }
   cudaEventDestroy(e0);
@@ -1166,6 +1198,7 @@ int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
   r.best = best;
   ctx->forces_variant = cand[best][0];
   ctx->forces_bsize = cand[best][1];
+  ctx->forces_split = cand[best][2];
   reset_graph(ctx);
   if (out) *out = r;
   return GBSPH_OK;

@@ -94,68 +94,96 @@ __device__ __forceinline__ void mlp_forward(const float* sw, float* act, int lan
 //   9-11   the plain acceleration, / |g|
 //   12     sum over boundary neighbours of V_j W_ij
 //   13-15  0
-__global__ void k_closure_features(gbsph_consts c, DevArrays a, float* __restrict__ feat) {
+//
+// One warp per fluid row: the lanes take the candidates of each of the (2sd+1)^2
+// box rows (contiguous in the sorted order) in turn, and the sums are added
+// across the warp at the end.
+__global__ void __launch_bounds__(128) k_closure_features(gbsph_consts c, DevArrays a, float* __restrict__ feat) {
+  constexpr unsigned FULL = 0xffffffffu;
   const DivState& d = *a.div;
   const unsigned np = d.np, npb = d.npb;
-  const unsigned p1 = npb + blockIdx.x * blockDim.x + threadIdx.x;
-  if (p1 >= np) return;
+  const unsigned p1 = npb + (unsigned)(((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (p1 >= np) return;  // the same for the whole warp
   const float4 ps1 = a.pscell[p1];
   const float4 vr1 = a.velrho[p1];
-  const unsigned dcc = c.domcellcode, cel = a.dcell[p1];
-  const int cx = (int)gb_cx(dcc, cel) - (int)d.cellmin[0], cy = (int)gb_cy(dcc, cel) - (int)d.cellmin[1],
+  const unsigned dcc = c.domcellcode, cel = a.dcell[p1], cmin0 = d.cellmin[0];
+  const int cx = (int)gb_cx(dcc, cel) - (int)cmin0, cy = (int)gb_cy(dcc, cel) - (int)d.cellmin[1],
             cz = (int)gb_cz(dcc, cel) - (int)d.cellmin[2];
   const int sd = c.cellmode_div, ncx = (int)d.ncx, ncy = (int)d.ncy, ncz = (int)d.ncz;
-  const int xini = cx - min(cx, sd), xfin = cx + min(ncx - cx - 1, sd) + 1;
+  const int xini = cx - min(cx, sd), xfin = cx + min(ncx - cx - 1, sd);
   const int yini = cy - min(cy, sd), yfin = cy + min(ncy - cy - 1, sd) + 1;
   const int zini = cz - min(cz, sd), zfin = cz + min(ncz - cz - 1, sd) + 1;
   const float h = c.kernelh, ks2 = c.kernelsize2, scell = c.scell;
-  float shep = c.massfluid / vr1.w * c.awen, sb = 0, dv[3] = {0, 0, 0}, gp[3] = {0, 0, 0}, divr = 0;
+  float shep = 0, sb = 0, dv[3] = {0, 0, 0}, gp[3] = {0, 0, 0}, divr = 0;
   for (int pass = 0; pass < 2; pass++) {
     const unsigned cellinit = pass == 0 ? d.boxfluid : 0u;
     const float mass = pass == 0 ? c.massfluid : c.massbound;
     for (int z = zini; z < zfin; z++)
-      for (int y = yini; y < yfin; y++)
-        for (int x = xini; x < xfin; x++) {
-          const unsigned box = cellinit + (unsigned)x + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
-          const unsigned pini = a.begincell[box], pfin = a.begincell[box + 1];
-          const float bx = ps1.x + (float)(cx - x) * scell;
-          const float by = ps1.y + (float)(cy - y) * scell;
-          const float bz = ps1.z + (float)(cz - z) * scell;
-          for (unsigned p2 = pini; p2 < pfin; p2++) {
-            const float4 ps2 = a.pscell[p2];
-            const float drx = bx - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
-            const float rr2 = drx * drx + dry * dry + drz * drz;
-            if (rr2 > ks2 || rr2 < GB_ALMOSTZERO) continue;
-            const float q = sqrtf(rr2) / h;
-            const float w1 = 1.f - 0.5f * q;
-            const float w = c.awen * (2.f * q + 1.f) * (w1 * w1) * (w1 * w1);
-            const float fac = c.bwenh * w1 * w1 * w1;
-            const float4 vr2 = a.velrho[p2];
-            const float vj = mass / vr2.w;
-            const float vw = vj * w;
-            shep += vw;
-            if (pass == 1) sb += vw;
-            dv[0] += vw * (vr2.x - vr1.x); dv[1] += vw * (vr2.y - vr1.y); dv[2] += vw * (vr2.z - vr1.z);
-            const float dp = vj * (ps2.w - ps1.w) * fac;
-            gp[0] += dp * drx; gp[1] += dp * dry; gp[2] += dp * drz;
-            divr -= vj * fac * rr2;
-          }
+      for (int y = yini; y < yfin; y++) {
+        const unsigned row = cellinit + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+        const unsigned pini = a.begincell[row + (unsigned)xini], pfin = a.begincell[row + (unsigned)xfin + 1u];
+        const float by = ps1.y + (float)(cy - y) * scell;
+        const float bz = ps1.z + (float)(cz - z) * scell;
+        for (unsigned p2 = pini + (unsigned)lane; p2 < pfin; p2 += 32u) {
+          const float4 ps2 = a.pscell[p2];
+          const int x = (int)gb_cx(dcc, a.dcell[p2]) - (int)cmin0;
+          const float drx = (ps1.x + (float)(cx - x) * scell) - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
+          const float rr2 = drx * drx + dry * dry + drz * drz;
+          if (rr2 > ks2 || rr2 < GB_ALMOSTZERO) continue;
+          const float q = sqrtf(rr2) / h;
+          const float w1 = 1.f - 0.5f * q;
+          const float w = c.awen * (2.f * q + 1.f) * (w1 * w1) * (w1 * w1);
+          const float fac = c.bwenh * w1 * w1 * w1;
+          const float4 vr2 = a.velrho[p2];
+          const float vj = mass / vr2.w;
+          const float vw = vj * w;
+          shep += vw;
+          if (pass == 1) sb += vw;
+          dv[0] += vw * (vr2.x - vr1.x); dv[1] += vw * (vr2.y - vr1.y); dv[2] += vw * (vr2.z - vr1.z);
+          const float dp = vj * (ps2.w - ps1.w) * fac;
+          gp[0] += dp * drx; gp[1] += dp * dry; gp[2] += dp * drz;
+          divr -= vj * fac * rr2;
         }
+      }
   }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    shep += __shfl_xor_sync(FULL, shep, o);
+    sb += __shfl_xor_sync(FULL, sb, o);
+    dv[0] += __shfl_xor_sync(FULL, dv[0], o);
+    dv[1] += __shfl_xor_sync(FULL, dv[1], o);
+    dv[2] += __shfl_xor_sync(FULL, dv[2], o);
+    gp[0] += __shfl_xor_sync(FULL, gp[0], o);
+    gp[1] += __shfl_xor_sync(FULL, gp[1], o);
+    gp[2] += __shfl_xor_sync(FULL, gp[2], o);
+    divr += __shfl_xor_sync(FULL, divr, o);
+  }
+  shep += c.massfluid / vr1.w * c.awen;  // the particle's own term
   const float g = sqrtf(c.gravity[0] * c.gravity[0] + c.gravity[1] * c.gravity[1] + c.gravity[2] * c.gravity[2]);
   const float ig = g > 0 ? 1.f / g : 1.f;
   const float iv = 1.f / (0.1f * (float)c.cs0);
   const float ip = ig / c.rhopzero;
   const float4 ac = a.acear[p1];
-  float* f = feat + (size_t)(p1 - npb) * kIn;
-  f[0] = (vr1.w / c.rhopzero - 1.f) * 50.f;
-  f[1] = dv[0] / shep * iv; f[2] = dv[1] / shep * iv; f[3] = dv[2] / shep * iv;
-  f[4] = gp[0] * ip; f[5] = gp[1] * ip; f[6] = gp[2] * ip;
-  f[7] = shep - 1.f;
-  f[8] = divr - 3.f;
-  f[9] = ac.x * ig; f[10] = ac.y * ig; f[11] = ac.z * ig;
-  f[12] = sb;
-  f[13] = f[14] = f[15] = 0.f;
+  // lanes 0..15 write one feature each (a coalesced 64-byte row)
+  float f;
+  switch (lane) {
+    case 0: f = (vr1.w / c.rhopzero - 1.f) * 50.f; break;
+    case 1: f = dv[0] / shep * iv; break;
+    case 2: f = dv[1] / shep * iv; break;
+    case 3: f = dv[2] / shep * iv; break;
+    case 4: f = gp[0] * ip; break;
+    case 5: f = gp[1] * ip; break;
+    case 6: f = gp[2] * ip; break;
+    case 7: f = shep - 1.f; break;
+    case 8: f = divr - 3.f; break;
+    case 9: f = ac.x * ig; break;
+    case 10: f = ac.y * ig; break;
+    case 11: f = ac.z * ig; break;
+    case 12: f = sb; break;
+    default: f = 0.f;
+  }
+  if (lane < kIn) feat[(size_t)(p1 - npb) * kIn + lane] = f;
 }
 
 // The correction inside the step: one warp per fluid row; the correction
@@ -344,7 +372,7 @@ cudaError_t closure_init() {
 
 void closure_features(const gbsph_consts& c, const DevArrays& a, unsigned cap, float* feat, cudaStream_t s,
                       unsigned long long* nlaunch) {
-  k_closure_features<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a, feat);
+  k_closure_features<<<gb_div_up(cap, 4), 128, 0, s>>>(c, a, feat);  // a warp per row
   if (nlaunch) *nlaunch += 1;
 }
 

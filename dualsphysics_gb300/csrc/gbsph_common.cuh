@@ -274,8 +274,12 @@ void sort_noalloc(unsigned char* work, const unsigned* keys, unsigned n, unsigne
 cudaError_t forces_init(const gbsph_consts& c);
 // variant: 0 warp-queued rounds, 1 one thread per row (block size bsize),
 // 2 cell-tiled staged (ring of 8 chunks), 3 cell-tiled staged (ring of 4)
-void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, cudaStream_t s, unsigned long long* nlaunch,
-            cudaEvent_t ev_fluid_begin = nullptr, cudaEvent_t ev_fluid_end = nullptr);
+// split (variant 2): 1, 2 or 4 warps share each group of 32 fluid rows
+// the split a launch of gbk::forces uses: 1 unless the variant is 2 and the
+// case takes the series form of the DDT2 hydrostatic term
+int forces_split_effective(const gbsph_consts& c, int variant, int split);
+void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, int split, cudaStream_t s,
+            unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin = nullptr, cudaEvent_t ev_fluid_end = nullptr);
 // variant 1: one thread per boundary row (k_mdbc); otherwise the cell-tiled
 // staged kernel (k_mdbc_t)
 void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s,

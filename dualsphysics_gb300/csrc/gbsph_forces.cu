@@ -236,10 +236,14 @@ struct PairK {
   // rho0*((1+ddtgz*drz)^(1/gamma)-1), which avoids the cancellation of
   // pow()-1 (truncation below 1e-8 relative for |t| < 0.05)
   float c1, c2, c3, c4, c5;
+  // staged kernel: log2 of the warps that share one group of 32 rows (each
+  // takes every 2^lsplit-th chunk of the rows' candidate stream)
+  unsigned lsplit;
 };
 
-PairK make_pairk(const gbsph_consts& c) {
+PairK make_pairk(const gbsph_consts& c, int split = 1) {
   PairK k;
+  k.lsplit = split >= 4 ? 2u : split >= 2 ? 1u : 0u;
   const float cbar = (float)c.cs0;
   k.hinv = 1.f / c.kernelh;
   k.ddt_kc = c.ddtkh * cbar;
@@ -925,7 +929,7 @@ __device__ __forceinline__ void tile_check(const gbsph_consts& c, const PairK& k
 
 // One pass of the warp's fluid rows over the fluid (boundp2=false) or boundary
 // (boundp2=true) boxes.  cx, cy, cz: the lane's cell in the trimmed domain.
-template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, int R>
+template <int tvisco, int tdensity, bool boundp2, bool ddtgen, bool tshift, int R, bool tsplit>
 __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k, const DevArrays& a,
                                           const DivState& d, const TileRing& ring, bool active, int cx, int cy,
                                           int cz, float4 ps1, float4 vr1, float inv_rho1, float4 ta1, float2 tb1,
@@ -1007,8 +1011,17 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
     }
     const unsigned pbase = (unsigned)(lane / kTSeg) * plen + (unsigned)(lane % kTSeg);
     const unsigned send = min((unsigned)(lane / kTSeg + 1) * plen, total);  // end of this lane's part
-    unsigned ch = 0u;
-    for (unsigned i = 0; i < nch; i++, ch = (ch + stride >= nch) ? ch + stride - nch : ch + stride) {
+    unsigned ch = 0u, mine = nch;
+    if constexpr (tsplit) {
+      // a warp of a split row group takes every 2^lsplit-th chunk of that
+      // order, from its index in the group on (sub * stride and
+      // stride * 2^lsplit mod nch by additions: sub < 4)
+      const unsigned sub = ((unsigned)threadIdx.x >> 5) & ((1u << k.lsplit) - 1u);
+      for (unsigned j = 0; j < sub; j++) ch = (ch + stride >= nch) ? ch + stride - nch : ch + stride;
+      for (unsigned j = 0; j < k.lsplit; j++) stride = (2u * stride >= nch) ? 2u * stride - nch : 2u * stride;
+      mine = nch > sub ? (nch - sub + (1u << k.lsplit) - 1u) >> k.lsplit : 0u;
+    }
+    for (unsigned i = 0; i < mine; i++, ch = (ch + stride >= nch) ? ch + stride - nch : ch + stride) {
       const unsigned s = pbase + ch * kTSeg;
       // the box row holding s: the number of rows whose end is <= s
       int lo = 0, hi = nrows;
@@ -1110,18 +1123,48 @@ __device__ __forceinline__ void tile_pass(const gbsph_consts& c, const PairK& k,
   __syncwarp();  // the next pass reuses the ring
 }
 
-template <int tvisco, int tdensity, bool ddtgen, bool tshift, int R>
+// Adds the partial sums of the other warps of a row group (PairAcc fields
+// in shared memory, field-major) to warp 0's: sums, visc a maximum, and the
+// cancellation markers (delta, sh0 = FLT_MAX) kept if any warp set them.
+template <int tdensity, bool tshift>
+__device__ __forceinline__ void tile_combine(PairAcc& r, const float* part, int lane) {
+  constexpr int S = 32;
+  r.ax += part[0 * S + lane]; r.ay += part[1 * S + lane]; r.az += part[2 * S + lane]; r.ar += part[3 * S + lane];
+  if (tdensity != GBSPH_DDT_NONE) {
+    const float dl = part[4 * S + lane];
+    r.delta = (r.delta == FLT_MAX || dl == FLT_MAX) ? FLT_MAX : r.delta + dl;
+  }
+  r.visc = fmaxf(r.visc, part[5 * S + lane]);
+  r.s0 += part[6 * S + lane]; r.s1 += part[7 * S + lane]; r.s2 += part[8 * S + lane];
+  r.s3 += part[9 * S + lane]; r.s4 += part[10 * S + lane]; r.s5 += part[11 * S + lane];
+  if (tshift) {
+    const float h0 = part[12 * S + lane];
+    r.sh0 = (r.sh0 == FLT_MAX || h0 == FLT_MAX) ? FLT_MAX : r.sh0 + h0;
+    r.sh1 += part[13 * S + lane]; r.sh2 += part[14 * S + lane]; r.sh3 += part[15 * S + lane];
+  }
+}
+
+template <int tvisco, int tdensity, bool ddtgen, bool tshift, int R, bool tsplit>
 // Six blocks of 128 threads per SM leave up to 80 registers a thread; the
 // Laminar+SPS and shifting cases, with more sums per row, take four.
-__global__ void __launch_bounds__(kTBlock, (tvisco == GBSPH_VISCO_LAMINARSPS || tshift) ? 4 : 6)
+// tsplit: 2^k.lsplit consecutive warps (2 or 4) take the same 32 rows, each
+// every 2^lsplit-th chunk of their candidate streams (more warps in flight
+// for cases too small to fill the device), and the first of them adds the
+// others' partial sums (named barrier per row group) and writes the rows.
+// A separate instantiation, so that the one-warp kernel keeps its registers;
+// it runs small cases, far below a full wave, so it takes four blocks a SM
+// (up to 128 registers a thread, no spills).
+__global__ void __launch_bounds__(kTBlock, (tvisco == GBSPH_VISCO_LAMINARSPS || tshift || tsplit) ? 4 : 6)
     k_forces_fluid_t(gbsph_consts c, PairK k, DevArrays a) {
   extern __shared__ float4 tile_smem[];
   using L = TileLayout<tvisco, tshift, R>;
   const DivState& d = *a.div;
   const unsigned np = d.np, npb = d.npb;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const unsigned p1 = npb + blockIdx.x * kTBlock + threadIdx.x;
+  const unsigned p1 = tsplit ? npb + blockIdx.x * (kTBlock >> k.lsplit) + (((unsigned)warp >> k.lsplit) << 5) + (unsigned)lane
+                             : npb + blockIdx.x * kTBlock + threadIdx.x;
   const bool active = p1 < np;
+  // the same for every warp of a row group, so a group leaves together
   if (__all_sync(0xffffffffu, !active)) return;
   char* wbase = (char*)tile_smem + (size_t)warp * L::per_warp;
   TileRing ring;
@@ -1143,10 +1186,9 @@ __global__ void __launch_bounds__(kTBlock, (tvisco == GBSPH_VISCO_LAMINARSPS || 
     cy = (int)gb_cy(dcc, cel) - (int)d.cellmin[1];
     cz = (int)gb_cz(dcc, cel) - (int)d.cellmin[2];
   }
-  (void)lane;
   const float inv_rho1 = gb_rcp(vr1.w);
   PairAcc ff = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  tile_pass<tvisco, tdensity, false, ddtgen, tshift, R>(c, k, a, d, ring, active, cx, cy, cz, ps1, vr1, inv_rho1, ta1,
+  tile_pass<tvisco, tdensity, false, ddtgen, tshift, R, tsplit>(c, k, a, d, ring, active, cx, cy, cz, ps1, vr1, inv_rho1, ta1,
                                                          tb1, ff);
   {  // the fluid-neighbour sums carry neither the mass nor the constant of gradW yet
     const float mf = c.massfluid * c.bwenh;
@@ -1155,8 +1197,29 @@ __global__ void __launch_bounds__(kTBlock, (tvisco == GBSPH_VISCO_LAMINARSPS || 
     ff.s0 *= mf; ff.s1 *= mf; ff.s2 *= mf; ff.s3 *= mf; ff.s4 *= mf; ff.s5 *= mf;
     if (tshift) { ff.sh0 *= mf; ff.sh1 *= mf; ff.sh2 *= mf; ff.sh3 *= mf; }
   }
-  tile_pass<tvisco, tdensity, true, ddtgen, tshift, R>(c, k, a, d, ring, active, cx, cy, cz, ps1, vr1, inv_rho1, ta1,
+  tile_pass<tvisco, tdensity, true, ddtgen, tshift, R, tsplit>(c, k, a, d, ring, active, cx, cy, cz, ps1, vr1, inv_rho1, ta1,
                                                         tb1, ff);
+  if constexpr (tsplit) {
+    // partial sums through the warps' own rings (free after the passes; 2 KB
+    // of the at least 4.6 KB of a ring); the thread index is read anew, which
+    // keeps the warp index out of registers during the passes
+    unsigned tid;
+    asm volatile("mov.u32 %0, %%tid.x;" : "=r"(tid));
+    const unsigned lsplit = k.lsplit, wl = tid >> 5, ln = tid & 31u;
+    const unsigned nthreads = 32u << lsplit, barid = 1u + (wl >> lsplit), sub = wl & ((1u << lsplit) - 1u);
+    if (sub) {
+      float* part = (float*)((char*)tile_smem + (size_t)wl * L::per_warp);
+      const float v[16] = {ff.ax, ff.ay, ff.az, ff.ar, ff.delta, ff.visc, ff.s0, ff.s1,
+                           ff.s2, ff.s3, ff.s4, ff.s5, ff.sh0, ff.sh1, ff.sh2, ff.sh3};
+#pragma unroll
+      for (int f = 0; f < 16; f++) part[f * 32 + ln] = v[f];
+    }
+    asm volatile("bar.sync %0, %1;" ::"r"(barid), "r"(nthreads) : "memory");
+    if (sub) return;
+    for (unsigned w = 1; w < (1u << lsplit); w++)
+      tile_combine<tdensity, tshift>(ff, (const float*)((const char*)tile_smem + (size_t)(wl + w) * L::per_warp),
+                                     (int)ln);
+  }
   ff.ar *= vr1.w;  // the rho1 factor of every continuity term
   float acemax2 = 0, visc = 0, vel2 = 0;
   if (active) {
@@ -1262,13 +1325,6 @@ __global__ void k_sps_tau(gbsph_consts c, DevArrays a) {
 // cofactors: the solutions agree to ~1e-15 relative, and the FP64 work, slow
 // on this part, drops about fourfold.  A ghost node with no fluid neighbour
 // takes rho0 without a solve, as the reference's zero matrix leads it to.
-__device__ __forceinline__ void gb_kadd(float& hi, float& lo, float x) {
-  const float s = __fadd_rn(hi, x);
-  const float bp = __fsub_rn(s, hi);
-  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
-  hi = s;
-  lo = __fadd_rn(lo, e);
-}
 
 // The ghost node of boundary row p1 (position + doubled normal, taken back
 // into the domain across periodic faces: UpdatePeriodicPos,
@@ -1752,38 +1808,53 @@ __global__ void k_pips(gbsph_consts c, DevArrays a) {
 
 // The staged kernel with a ring of R chunks; with prepare set, only raises its
 // dynamic shared-memory limit (done once per context, outside any capture).
-template <int tvisco, int tdensity, bool ddtgen, bool tshift, int R>
+template <int tvisco, int tdensity, bool ddtgen, bool tshift, int R, bool tsplit>
 cudaError_t launch_tiled(const gbsph_consts& c, const PairK& k, const DevArrays& a, unsigned cap, bool prepare,
                          cudaStream_t s) {
   using L = TileLayout<tvisco, tshift, R>;
+  static_assert(L::per_warp >= 16 * 32 * sizeof(float), "a ring holds the partial sums of a split row group");
   if (prepare)
-    return cudaFuncSetAttribute(k_forces_fluid_t<tvisco, tdensity, ddtgen, tshift, R>,
+    return cudaFuncSetAttribute(k_forces_fluid_t<tvisco, tdensity, ddtgen, tshift, R, tsplit>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes);
-  k_forces_fluid_t<tvisco, tdensity, ddtgen, tshift, R><<<gb_div_up(cap, kTBlock), kTBlock, L::bytes, s>>>(c, k, a);
+  const unsigned rows_per_block = (unsigned)kTBlock >> (tsplit ? k.lsplit : 0u);
+  k_forces_fluid_t<tvisco, tdensity, ddtgen, tshift, R, tsplit>
+      <<<gb_div_up(cap, rows_per_block), kTBlock, L::bytes, s>>>(c, k, a);
   return cudaSuccess;
 }
 
 template <int tvisco, int tdensity, bool ddtgen, bool tshift>
 cudaError_t launch_fluid_g(const gbsph_consts& c, const PairK& k, const DevArrays& a, unsigned cap, int variant,
                            bool prepare, cudaStream_t s) {
-  if (variant == 2 || prepare) {
-    const cudaError_t e = launch_tiled<tvisco, tdensity, ddtgen, tshift, 8>(c, k, a, cap, prepare, s);
-    if (variant == 2 || e != cudaSuccess) return e;
+  // the split row groups (k.lsplit > 0) are instantiated for the ring of 8
+  // chunks and the series form of the hydrostatic term; otherwise one warp
+  // takes a row group
+  if (prepare) {
+    cudaError_t e = launch_tiled<tvisco, tdensity, ddtgen, tshift, 8, false>(c, k, a, cap, true, s);
+    if (e == cudaSuccess && !ddtgen) e = launch_tiled<tvisco, tdensity, ddtgen, tshift, 8, true>(c, k, a, cap, true, s);
+    if (e == cudaSuccess) e = launch_tiled<tvisco, tdensity, ddtgen, tshift, 4, false>(c, k, a, cap, true, s);
+    return e;
   }
-  if (variant == 3 || prepare) return launch_tiled<tvisco, tdensity, ddtgen, tshift, 4>(c, k, a, cap, prepare, s);
+  if (variant == 2) {
+    if constexpr (!ddtgen) {
+      if (k.lsplit) return launch_tiled<tvisco, tdensity, ddtgen, tshift, 8, true>(c, k, a, cap, false, s);
+    }
+    return launch_tiled<tvisco, tdensity, ddtgen, tshift, 8, false>(c, k, a, cap, false, s);
+  }
+  if (variant == 3) return launch_tiled<tvisco, tdensity, ddtgen, tshift, 4, false>(c, k, a, cap, false, s);
   k_forces_fluid_q<tvisco, tdensity, ddtgen, tshift><<<gb_div_up(cap, kQBlock), kQBlock, 0, s>>>(c, k, a);
   return cudaSuccess;
 }
 
 template <int tvisco, int tdensity, bool tshift>
-cudaError_t launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, bool prepare,
-                         cudaStream_t s) {
+cudaError_t launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, int split,
+                         bool prepare, cudaStream_t s) {
   if (variant == 1 && !prepare) {  // one thread per row: any block size of 64, 128 or 256
     const unsigned bs = (bsize == 64 || bsize == 256) ? (unsigned)bsize : 128u;
     k_forces_fluid<tvisco, tdensity, tshift><<<gb_div_up(cap, bs), bs, 0, s>>>(c, a);
     return cudaSuccess;
   }
-  const PairK k = make_pairk(c);
+  // split row groups: the staged kernel with a ring of 8 chunks (variant 2)
+  const PairK k = make_pairk(c, variant == 2 ? split : 1);
   if constexpr (tdensity == GBSPH_DDT_DDT2 || tdensity == GBSPH_DDT_DDT2FULL) {
     // the series form of the hydrostatic term holds for |ddtgz*drz| < 0.05 and
     // |drz| <= 2h for every pair; otherwise the general power form is compiled in
@@ -1794,30 +1865,31 @@ cudaError_t launch_fluid(const gbsph_consts& c, const DevArrays& a, unsigned cap
 }
 
 template <int tvisco, int tdensity>
-cudaError_t launch_fluid_s(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize,
+cudaError_t launch_fluid_s(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, int split,
                            bool prepare, cudaStream_t s) {
-  if (c.tshift) return launch_fluid<tvisco, tdensity, true>(c, a, cap, variant, bsize, prepare, s);
-  return launch_fluid<tvisco, tdensity, false>(c, a, cap, variant, bsize, prepare, s);
+  if (c.tshift) return launch_fluid<tvisco, tdensity, true>(c, a, cap, variant, bsize, split, prepare, s);
+  return launch_fluid<tvisco, tdensity, false>(c, a, cap, variant, bsize, split, prepare, s);
 }
 
 template <int tvisco>
-cudaError_t launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize,
+cudaError_t launch_fluid_t(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, int split,
                            bool prepare, cudaStream_t s) {
   switch (c.tdensity) {
-    case GBSPH_DDT_NONE: return launch_fluid_s<tvisco, GBSPH_DDT_NONE>(c, a, cap, variant, bsize, prepare, s);
-    case GBSPH_DDT_DDT: return launch_fluid_s<tvisco, GBSPH_DDT_DDT>(c, a, cap, variant, bsize, prepare, s);
-    case GBSPH_DDT_DDT2: return launch_fluid_s<tvisco, GBSPH_DDT_DDT2>(c, a, cap, variant, bsize, prepare, s);
-    default: return launch_fluid_s<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, variant, bsize, prepare, s);
+    case GBSPH_DDT_NONE: return launch_fluid_s<tvisco, GBSPH_DDT_NONE>(c, a, cap, variant, bsize, split, prepare, s);
+    case GBSPH_DDT_DDT: return launch_fluid_s<tvisco, GBSPH_DDT_DDT>(c, a, cap, variant, bsize, split, prepare, s);
+    case GBSPH_DDT_DDT2: return launch_fluid_s<tvisco, GBSPH_DDT_DDT2>(c, a, cap, variant, bsize, split, prepare, s);
+    default: return launch_fluid_s<tvisco, GBSPH_DDT_DDT2FULL>(c, a, cap, variant, bsize, split, prepare, s);
   }
 }
 
-cudaError_t launch_fluid_v(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize,
+cudaError_t launch_fluid_v(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, int split,
                            bool prepare, cudaStream_t s) {
   switch (c.tvisco) {
     case GBSPH_VISCO_ARTIFICIAL:
-      return launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, variant, bsize, prepare, s);
-    case GBSPH_VISCO_LAMINAR: return launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, variant, bsize, prepare, s);
-    default: return launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, variant, bsize, prepare, s);
+      return launch_fluid_t<GBSPH_VISCO_ARTIFICIAL>(c, a, cap, variant, bsize, split, prepare, s);
+    case GBSPH_VISCO_LAMINAR:
+      return launch_fluid_t<GBSPH_VISCO_LAMINAR>(c, a, cap, variant, bsize, split, prepare, s);
+    default: return launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, variant, bsize, split, prepare, s);
   }
 }
 
@@ -1825,7 +1897,7 @@ cudaError_t launch_fluid_v(const gbsph_consts& c, const DevArrays& a, unsigned c
 
 namespace gbk {
 
-void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, cudaStream_t s,
+void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, int split, cudaStream_t s,
             unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin, cudaEvent_t ev_fluid_end) {
   cudaMemsetAsync(&a.st->acemax2, 0, 3 * sizeof(unsigned), s);
   k_forces_bound<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
@@ -1835,14 +1907,21 @@ void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, 
   if (ev_fluid_begin || ev_fluid_end) cudaStreamIsCapturing(s, &cap_st);
   const unsigned ev_flags = cap_st == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (ev_fluid_begin) cudaEventRecordWithFlags(ev_fluid_begin, s, ev_flags);
-  launch_fluid_v(c, a, cap, variant, bsize, false, s);
+  launch_fluid_v(c, a, cap, variant, bsize, split, false, s);
   if (ev_fluid_end) cudaEventRecordWithFlags(ev_fluid_end, s, ev_flags);
   if (nlaunch) *nlaunch += 2;
 }
 
+int forces_split_effective(const gbsph_consts& c, int variant, int split) {
+  if (variant != 2 || split < 2) return 1;
+  const bool series = !(c.tdensity == GBSPH_DDT_DDT2 || c.tdensity == GBSPH_DDT_DDT2FULL) ||
+                      fabsf(c.ddtgz) * c.kernelsize < 0.049f;
+  return series ? (split >= 4 ? 4 : 2) : 1;
+}
+
 cudaError_t forces_init(const gbsph_consts& c) {
   DevArrays a{};
-  const cudaError_t e = launch_fluid_v(c, a, 0, 2, 128, true, nullptr);
+  const cudaError_t e = launch_fluid_v(c, a, 0, 2, 128, 1, true, nullptr);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_mdbc_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(4 * kMdbcWarpBytes));
 }

@@ -111,5 +111,5 @@ def tune(sim: GbSphSingle, reps: int = 3) -> dict:
     bits = C.c_int()
     ms = (C.c_float * 2)()
     sim._check(lib().gbsph_tune_sort(sim.ctx, reps, C.byref(bits), ms), "gbsph_tune_sort")
-    return {"best": r.best, "variant": list(r.variant), "bsize": list(r.bsize), "ms": list(r.ms),
+    return {"best": r.best, "variant": list(r.variant), "bsize": list(r.bsize), "split": list(r.split), "ms": list(r.ms),
             "sort_bits": bits.value, "sort_ms": list(ms)}

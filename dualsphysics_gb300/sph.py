@@ -250,7 +250,10 @@ class GbSphSingle:
     def set_option(self, key: int, value: int) -> None:
         """Kernel options: key 1 = fluid-row kernel (2 cell-tiled with a ring of
         8 chunks, the default; 3 the same with 4; 0 queued rounds; 1 one thread
-        per particle), key 0 = block size of kernel 1, key 2 = sort digit bits."""
+        per particle), key 0 = block size of kernel 1, key 2 = sort digit bits,
+        key 3 = mDBC kernel (0 cell-tiled, 1 one thread per row), key 4 =
+        warps per group of 32 fluid rows in the cell-tiled kernel (1, 2, 4; 0
+        automatic; get_option(5) reads the value in effect)."""
         self._check(lib().gbsph_set_option(self.ctx, key, value), "set_option")
 
     def get_option(self, key: int) -> int:

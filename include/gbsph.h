@@ -370,24 +370,35 @@ void* gbsph_stream(gbsph_ctx* ctx);
  * 128 threads per block (JSphGpu.cpp, BlockSizes).  key 2 = digit width of
  * the divide's radix sort, 8 (default) or 11 bits.  key 3 = mDBC kernel of
  * gbsph_mdbc: 0 (default) cell-tiled, the ghost nodes' fluid neighbours
- * staged through shared memory; 1 one thread per boundary row. */
+ * staged through shared memory; 1 one thread per boundary row.  key 4 =
+ * warps that share each group of 32 fluid rows in the cell-tiled kernel
+ * with a ring of 8 chunks (each takes every 1st, 2nd or 4th chunk of the
+ * rows' candidates and the first adds the others' sums): 1, 2, 4, or 0
+ * (default) chosen from the fluid rows of the last upload, so that a case
+ * too small to fill the device runs more, shorter warps.  The other kernels,
+ * and cases that need the power form of the DDT2 hydrostatic term, keep one
+ * warp.  The sums' order changes with it, within the FP32 criterion. */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
-/* The current value of an option of gbsph_set_option (no reference counterpart). */
+/* The current value of an option of gbsph_set_option (no reference
+ * counterpart); key 5 reads the warps per row group in effect (key 4
+ * resolved). */
 int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value);
 
 /* Autotuner (no reference counterpart).  Times each fluid-row kernel
- * configuration -- the cell-tiled kernel with rings of 8 and 4 chunks, the
- * queued kernel, and the one-thread-per-particle kernel at 64, 128 and 256
- * threads per block -- over `reps` launches on the context's current state,
+ * configuration -- the cell-tiled kernel with rings of 8 chunks at 1, 2 and
+ * 4 warps per row group and with a ring of 4 chunks, the queued kernel, and
+ * the one-thread-per-particle kernel at 64, 128 and 256 threads per block --
+ * over `reps` launches on the context's current state,
  * between steps, and keeps the fastest.  The launches rewrite only the
  * interaction outputs, which the next step recomputes.  The kernels sum a
  * row's neighbours in different orders: results stay within the FP32
  * criterion of each other, not bit-identical. */
-#define GBSPH_TUNE_CANDIDATES 6
+#define GBSPH_TUNE_CANDIDATES 8
 typedef struct {
   int best;                              /* index of the configuration kept */
   int variant[GBSPH_TUNE_CANDIDATES];    /* gbsph_set_option key 1 */
   int bsize[GBSPH_TUNE_CANDIDATES];      /* gbsph_set_option key 0 */
+  int split[GBSPH_TUNE_CANDIDATES];      /* gbsph_set_option key 4 */
   float ms[GBSPH_TUNE_CANDIDATES];       /* mean time of one fluid-row pass */
 } gbsph_tune_result;
 int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out);

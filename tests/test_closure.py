@@ -73,20 +73,22 @@ def test_standardisation_folds_into_the_first_and_last_layers():
     np.testing.assert_allclose(y_raw, y_std, rtol=2e-5, atol=2e-5 * np.abs(y_std).max())
 
 
-def test_fine_and_coarse_lattices_nest():
-    pair = cl.Pair(0.25, dp_fine=0.04, tag="N")
+@pytest.mark.parametrize("dpf,ratio", [(0.04, 2), (0.02, 4)])
+def test_fine_and_coarse_lattices_nest(dpf, ratio):
+    pair = cl.Pair(0.25, dp_fine=dpf, tag="N", ratio=ratio)
     c = pair.coarse
     assert len(pair.coarse_row_fine_id) == c.np - c.npb
     f = pair.fine
     fp = f.pos[pair.coarse_row_fine_id]
     np.testing.assert_allclose(fp, c.pos[c.npb:], atol=1e-12)
-    # every fine fluid particle in one block of at most 8, whose corner it shares the cell of
+    # every fine fluid particle in one block of at most ratio^3, whose corner it shares the cell of
     cnt = np.bincount(pair.fine_block, minlength=c.np - c.npb)
-    assert cnt.sum() == f.np - f.npb and cnt.min() >= 1 and cnt.max() == 8
+    assert cnt.sum() == f.np - f.npb and cnt.min() >= 1 and cnt.max() == ratio ** 3
     st = {"idp": f.idp, "pos": f.pos, "velrho": f.velrho}
     m, n = pair.block_mean(st, f.pos)
     assert np.array_equal(n, cnt)
-    assert np.abs(m[:, :] - c.pos[c.npb:]).max() <= 0.5 * 0.04 + 1e-12
+    # the block mean lies within the block: at most (ratio - 1) / 2 fine spacings from the corner
+    assert np.abs(m[:, :] - c.pos[c.npb:]).max() <= 0.5 * (ratio - 1) * dpf + 1e-12
 
 
 # ---- GPU ------------------------------------------------------------------

@@ -94,14 +94,16 @@ def test_autotuner_keeps_the_fastest_candidate():
     _, cds = _cases(2, seed=12)
     (s,) = _sims(cds[:1])
     r = tune(s, reps=2)
-    assert len(r["ms"]) == 6 and all(m > 0 for m in r["ms"])
+    assert len(r["ms"]) == 8 and all(m > 0 for m in r["ms"])
     assert r["ms"][r["best"]] == min(r["ms"])
-    assert [(v, b) for v, b in zip(r["variant"], r["bsize"])] == [(2, 128), (3, 128), (0, 128), (1, 64), (1, 128),
-                                                                   (1, 256)]
+    assert list(zip(r["variant"], r["bsize"], r["split"])) == [(2, 128, 1), (2, 128, 2), (2, 128, 4), (3, 128, 1),
+                                                                (0, 128, 1), (1, 64, 1), (1, 128, 1), (1, 256, 1)]
+    assert s.get_option(4) == r["split"][r["best"]]
     # the tuned context steps as one set to the same configuration by hand
     (t,) = _sims(cds[:1])
     t.set_option(1, r["variant"][r["best"]])
     t.set_option(0, r["bsize"][r["best"]])
+    t.set_option(4, r["split"][r["best"]])
     s.RunSteps(5, use_graph=True)
     t.RunSteps(5, use_graph=True)
     _same(s, t, "tuned vs set by hand")

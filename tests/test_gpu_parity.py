@@ -51,6 +51,7 @@ def test_forces_within_tolerance(name):
     g = G.golden(name)
     cd = G.load_generated(name)
     s = _gpu(cd)
+    assert s.get_option(5) == 4  # a small case: four warps per row group by default
     o = _oracle(cd)
     s.MdbcBoundCorrection(_lib.INTERSTEP_SYMPREDICTOR)
     r64 = po.mdbc_f64(o)
@@ -85,13 +86,16 @@ def test_forces_within_tolerance(name):
 
 @pytest.mark.parametrize("name", ["dbc_d04", "vel_d04", "sps_d04", "mdbc_d04", "lam_d04", "ddt2f_d04", "half_d04",
                                   "shift_d04", "shiftnb_d04"])
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
-def test_forces_variants_within_tolerance(name, variant):
+@pytest.mark.parametrize("variant,split", [(0, 1), (1, 1), (2, 1), (2, 2), (2, 4), (3, 1)])
+def test_forces_variants_within_tolerance(name, variant, split):
     """Every fluid-row kernel: queued rounds (0), one thread per particle (1),
-    cell-tiled staged with a ring of 8 (2) or 4 (3) chunks."""
+    cell-tiled staged with a ring of 8 (2) or 4 (3) chunks, with 1, 2 or 4
+    warps per group of 32 rows."""
     cd = G.load_generated(name)
     s = _gpu(cd)
     s.set_option(1, variant)
+    s.set_option(4, split)
+    assert s.get_option(5) == split
     o = _oracle(cd)
     s.MdbcBoundCorrection(_lib.INTERSTEP_SYMPREDICTOR)
     o.mdbc(False)
@@ -324,6 +328,7 @@ def test_c2_full_size_divide_mdbc_and_forces():
     cd = bench.make_case(0.0025)
     assert cd.np == 7093601
     s = _gpu(cd)
+    assert s.get_option(4) == 0 and s.get_option(5) == 1  # large enough for one warp per row group
     o = _oracle(cd)
     gs, os_ = s.download(), o.state()
     for k in ("idp", "dcell", "code"):
@@ -371,6 +376,8 @@ def test_invalid_arguments_are_reported():
     assert rc == -5  # GBSPH_ECAPACITY
     assert b"capacity" in _lib.lib().gbsph_last_error(ctx)
     assert _lib.lib().gbsph_step(ctx) == -7  # GBSPH_ESTATE: nothing uploaded
+    for key, value in ((1, 4), (3, 2), (4, 3), (4, 8), (2, 9), (6, 0)):
+        assert _lib.lib().gbsph_set_option(ctx, key, value) == -1, (key, value)  # GBSPH_EINVAL
     _lib.lib().gbsph_destroy(ctx)
 
 
