@@ -1565,8 +1565,8 @@ __device__ __forceinline__ void mdbc_refill(const float* ring, unsigned& cur, un
 // reference cell along x; along y and z it is 0 within a group), so that the
 // ill-conditioned solves of ghosts near corners see the same sums.
 __device__ __forceinline__ void mdbc_round(const gbsph_consts& c, float hinv, const float* ring, unsigned& cur,
-                                           unsigned& cc, unsigned cnext, const Ghost& gh, int fox, MdbcAcc& m,
-                                           int lane) {
+                                           unsigned& cc, unsigned cnext, const Ghost& gh, int fox, int foy, int foz,
+                                           MdbcAcc& m, int lane) {
   if (cur != 0u) {
     constexpr int S = kMdbcR * 32;
     const unsigned slot = ((cc & (kMdbcR - 1)) << 5) | (unsigned)(__ffs(cur) - 1);
@@ -1576,8 +1576,8 @@ __device__ __forceinline__ void mdbc_round(const gbsph_consts& c, float hinv, co
     const int dyj = (o << 24) >> 24, dzj = (o << 16) >> 24;
     const float scell = c.scell;
     const float drx = (gh.lx + ((float)fox - e[6 * S]) * scell) - e[3 * S];
-    const float dry = (gh.ly + (float)(-dyj) * scell) - e[4 * S];
-    const float drz = (gh.lz + (float)(-dzj) * scell) - e[5 * S];
+    const float dry = (gh.ly + (float)(foy - dyj) * scell) - e[4 * S];
+    const float drz = (gh.lz + (float)(foz - dzj) * scell) - e[5 * S];
     mdbc_pair(c, hinv, drx, dry, drz, drx * drx + dry * dry + drz * drz, e[8 * S], m);
     mdbc_refill(ring, cur, cc, cnext, lane);
   }
@@ -1608,20 +1608,28 @@ __global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) 
   mdbc_zero(m);
   unsigned cnext = 0u, cc = 0u, cur = 0u;
   float fx = 0.f, fy = 0.f, fz = 0.f;
-  int fox = 0;
+  int fox = 0, foy = 0, foz = 0;
+  // A group takes the remaining ghosts whose rows of cells (y, z) lie within
+  // `reach` rows of the leader's: the ghosts of the wall layers of a warp
+  // fall in neighbouring rows, and one stream over the union of their box
+  // rows (at most (2 sd + 1 + 2 reach)^2 <= 25) keeps the warp's lanes in
+  // one set of rounds.
+  const int reach = sd == 1 ? 1 : 0;
   unsigned remaining = __ballot_sync(FULL, active);
   while (remaining) {
     const int leader = __ffs(remaining) - 1;
     const int rx = __shfl_sync(FULL, cx, leader), ry = __shfl_sync(FULL, cy, leader),
               rz = __shfl_sync(FULL, cz, leader);
-    const bool ing = active && cy == ry && cz == rz;
+    const bool ing = ((remaining >> lane) & 1u) && abs(cy - ry) <= reach && abs(cz - rz) <= reach;
     const unsigned grp = __ballot_sync(FULL, ing);
     remaining &= ~grp;
     const int xmin = __reduce_min_sync(FULL, ing ? cx : 0x7fffffff);
     const int xmax = __reduce_max_sync(FULL, ing ? cx : (int)0x80000000);
+    const int gy0 = __reduce_min_sync(FULL, ing ? cy : 0x7fffffff), gy1 = __reduce_max_sync(FULL, ing ? cy : (int)0x80000000);
+    const int gz0 = __reduce_min_sync(FULL, ing ? cz : 0x7fffffff), gz1 = __reduce_max_sync(FULL, ing ? cz : (int)0x80000000);
     const int x0 = max(xmin - sd, 0), x1 = min(xmax + sd, ncx - 1);
-    const int y0 = max(ry - sd, 0), y1 = min(ry + sd, ncy - 1);
-    const int z0 = max(rz - sd, 0), z1 = min(rz + sd, ncz - 1);
+    const int y0 = max(gy0 - sd, 0), y1 = min(gy1 + sd, ncy - 1);
+    const int z0 = max(gz0 - sd, 0), z1 = min(gz1 + sd, ncz - 1);
     if (x0 > x1 || y0 > y1 || z0 > z1) continue;  // the ghosts' boxes are all outside the domain
     const int nyr = y1 - y0 + 1, nrows = nyr * (z1 - z0 + 1);
     unsigned rb = 0u, rlen = 0u;
@@ -1645,9 +1653,11 @@ __global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) 
     const unsigned rbase = rb - (incl - rlen);
     if (ing) {
       fox = cx - rx;
+      foy = cy - ry;
+      foz = cz - rz;
       fx = gh.lx + (float)fox * scell;
-      fy = gh.ly;
-      fz = gh.lz;
+      fy = gh.ly + (float)foy * scell;
+      fz = gh.lz + (float)foz * scell;
     }
     const float2 fxx = make_float2(fx, fx), fyy = make_float2(fy, fy), fzz = make_float2(fz, fz);
     const unsigned gmask = ing ? FULL : 0u;
@@ -1683,7 +1693,7 @@ __global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) 
       if (cc == cnext) cur = hm;
       cnext++;
       if (cur == 0u) cc = cnext;
-      while (__ballot_sync(FULL, ing && cur != 0u) == grp) mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, m, lane);
+      while (__ballot_sync(FULL, ing && cur != 0u) == grp) mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, foy, foz, m, lane);
     };
     for (unsigned i = 0; i < nch; i++, ch = (ch + stride >= nch) ? ch + stride - nch : ch + stride) {
       const unsigned s = pbase + ch * kTSeg;
@@ -1725,7 +1735,7 @@ __global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) 
       const unsigned nk = (unsigned)__popc(kb);
       const unsigned need = fill + nk > 32u ? cnext + 1u : cnext;
       while (__any_sync(FULL, cur != 0u && cc + (unsigned)kMdbcR <= need))
-        mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, m, lane);
+        mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, foy, foz, m, lane);
       if (keep) {
         const unsigned pos = fill + (unsigned)__popc(kb & ((1u << lane) - 1u));
         const unsigned slot = (((pos < 32u ? cnext : cnext + 1u) & (kMdbcR - 1)) << 5) | (pos & 31u);
@@ -1758,7 +1768,7 @@ __global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) 
       fill = 0u;
     }
   }
-  while (__any_sync(FULL, cur != 0u)) mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, m, lane);
+  while (__any_sync(FULL, cur != 0u)) mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, foy, foz, m, lane);
   if (active) mdbc_final(c, a, p1, bn, m);
 }
 
