@@ -352,10 +352,12 @@ def run_ensemble(args, local: int = 0):
             "streams_no_graph": pst / t_streams, "sequential_plain": pst / t_seq,
             "speedup_vs_sequential": t_seq / t_graph,
             "launches_per_replay": ens.launches_per_step(),
-            "tuner": {"choices": [[t["variant"][t["best"]], t["bsize"][t["best"]]] for t in tuned],
+            "tuner": {"choices": [[t["variant"][t["best"]], t["bsize"][t["best"]], t["split"][t["best"]]]
+                                  for t in tuned],
                       "sort_bits": [t["sort_bits"] for t in tuned],
                       "sort_ms_8_11": [[round(x, 4) for x in t["sort_ms"]] for t in tuned],
-                      "candidates": [[v, b] for v, b in zip(tuned[0]["variant"], tuned[0]["bsize"])],
+                      "candidates": [[v, b, sp] for v, b, sp in zip(tuned[0]["variant"], tuned[0]["bsize"],
+                                                                     tuned[0]["split"])],
                       "ms": [[round(x, 4) for x in t["ms"]] for t in tuned]},
             "clocks": clk.summary()}
     ens.close()
@@ -458,6 +460,8 @@ def main():
     ap.add_argument("--split", type=int, default=None, choices=[0, 1, 2, 4],
                     help="warps per group of 32 fluid rows in the cell-tiled kernel (0 automatic); default: the "
                          "library's")
+    ap.add_argument("--bound-lanes", type=int, default=None, choices=[0, 1, 4, 32],
+                    help="lanes a boundary row in the bound-row pass (0 automatic); default: the library's")
     ap.add_argument("--no-tune", action="store_true", help="keep the 8-bit sort digits (no sort autotuning)")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c3err", "ensemble", "closure",
                                                          "closure-judge"],
@@ -526,7 +530,9 @@ def main():
         s.set_option(1, args.variant)
     if args.split is not None:
         s.set_option(4, args.split)
-    variant, split = s.get_option(1), s.get_option(5)
+    if args.bound_lanes is not None:
+        s.set_option(6, args.bound_lanes)
+    variant, split, blanes = s.get_option(1), s.get_option(5), s.get_option(7)
     pi = s.pips()
     s.RunSteps(W, use_graph=True)
     s.sync()
@@ -573,6 +579,8 @@ def main():
             e.set_option(1, args.variant)
         if args.split is not None:
             e.set_option(4, args.split)
+        if args.bound_lanes is not None:
+            e.set_option(6, args.bound_lanes)
         for _ in range(K):
             e.RunSteps(1, use_graph=True)  # one step, replayed from its captured graph
             e.step_dt()                    # the Run loop reads the step's dt and time back
@@ -610,7 +618,7 @@ def main():
             "config": {"workload": workload_text(args),
                        "particles": cd.np, "fluid": cd.nfluid, "boundary": cd.npb, "cellmode": args.cellmode,
                        "sort_digit_bits": sort_bits.value, "fluid_kernel_variant": variant,
-                       "warps_per_row_group": split,
+                       "warps_per_row_group": split, "lanes_per_bound_row": blanes,
                        "sort_divide_ms_8_11": [round(float(x), 4) for x in sort_ms] if not args.no_tune else None,
                        "parallelism": "replicas only" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (no flush)"},

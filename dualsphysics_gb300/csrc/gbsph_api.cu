@@ -39,7 +39,9 @@ struct gbsph_ctx {
   unsigned long long launches = 0;
   int forces_bsize = 128, forces_variant = 2;
   int forces_split = 0;   // warps per group of 32 fluid rows in the staged kernel (0: from nfluid)
+  int bound_lanes = 0;    // lanes a boundary row in the bound-row pass (0: from nbound)
   unsigned nfluid = 0;    // fluid rows at the last upload (chooses the automatic split)
+  unsigned nbound = 0;    // boundary rows at the last upload
   int nsm = 0;            // SMs of the device
   int mdbc_variant = 0;   // 0 staged kernel, 1 one thread per boundary row
   cudaGraph_t graph = nullptr;
@@ -76,17 +78,28 @@ struct gbsph_ctx {
 namespace {
 
 // Warps per group of 32 fluid rows in the staged kernel: the option, or with
-// 0 the largest of 4, 2, 1 that keeps the launch within about two waves of
+// 0 the largest of 4, 2, 1 that keeps the launch within about three waves of
 // resident warps (24 a SM), so that a small case runs more warps, each with a
-// shorter chain of chunks, and a large one keeps one warp per group.
+// shorter chain of chunks, and a large one keeps one warp per group.  On a
+// GB300 (152 SMs) that is 4 up to 87.5 k fluid rows and 2 up to 175 k; one
+// warp a group was 14 % faster at 667 k rows, four 2.9x faster at 11 k.
 int forces_split(const gbsph_ctx* ctx) {
   int s = ctx->forces_split;
   if (!s) {
     const unsigned long long warps = (ctx->nfluid + 31u) / 32u,
                              resident = 24ull * (unsigned)(ctx->nsm > 0 ? ctx->nsm : 1);
-    s = warps * 4ull <= 2ull * resident ? 4 : warps * 2ull <= 2ull * resident ? 2 : 1;
+    s = warps * 4ull <= 3ull * resident ? 4 : warps * 2ull <= 3ull * resident ? 2 : 1;
   }
   return gbk::forces_split_effective(ctx->c, ctx->forces_variant, s);
+}
+
+// Lanes a boundary row in the bound-row pass: the option, or with 0 the
+// largest of 32, 4, 1 that keeps the launch within about three waves of
+// resident threads (2,048 a SM).
+int bound_lanes(const gbsph_ctx* ctx) {
+  if (ctx->bound_lanes) return ctx->bound_lanes;
+  const unsigned long long rows = ctx->nbound, resident = 2048ull * (unsigned)(ctx->nsm > 0 ? ctx->nsm : 1);
+  return rows * 32ull <= 3ull * resident ? 32 : rows * 4ull <= 3ull * resident ? 4 : 1;
 }
 
 int set_err(gbsph_ctx* ctx, int code, const char* fmt, ...) {
@@ -199,8 +212,8 @@ int do_forces(gbsph_ctx* ctx) {
     e1 = ctx->prof_ev[2 * ctx->prof_n + 1];
     ctx->prof_n++;
   }
-  gbk::forces(ctx->c, ctx->a, ctx->cap, ctx->forces_bsize, ctx->forces_variant, forces_split(ctx), ctx->stream,
-              &ctx->launches, e0, e1);
+  gbk::forces(ctx->c, ctx->a, ctx->cap, ctx->forces_bsize, ctx->forces_variant, forces_split(ctx), bound_lanes(ctx),
+              ctx->stream, &ctx->launches, e0, e1);
   if (ctx->c.tvisco == GBSPH_VISCO_LAMINARSPS) gbk::sps_tau(ctx->c, ctx->a, ctx->cap, ctx->stream, &ctx->launches);
   if (ctx->clos_on) {  // the learned correction of the fluid accelerations
     gbk::closure_features(ctx->c, ctx->a, ctx->cap, ctx->clos_feat, ctx->stream, &ctx->launches);
@@ -347,6 +360,7 @@ const char* gbsph_last_error(const gbsph_ctx* ctx) { return ctx ? ctx->err.c_str
 static int upload_common(gbsph_ctx* ctx, unsigned np, unsigned npb) {
   const gbsph_consts& c = ctx->c;
   ctx->nfluid = np - npb;
+  ctx->nbound = npb;
   DivState ds;
   memset(&ds, 0, sizeof(ds));
   ds.np = np;
@@ -1095,6 +1109,11 @@ int gbsph_set_option(gbsph_ctx* ctx, int key, int value) {
       return set_err(ctx, GBSPH_EINVAL, "warps per row group %d is not 0 (automatic), 1, 2 or 4", value);
     ctx->forces_split = value;
   }
+  else if (key == 6) {
+    if (value != 0 && value != 1 && value != 4 && value != 32)
+      return set_err(ctx, GBSPH_EINVAL, "lanes per boundary row %d is not 0 (automatic), 1, 4 or 32", value);
+    ctx->bound_lanes = value;
+  }
   else return set_err(ctx, GBSPH_EINVAL, "unknown option %d", key);
   reset_graph(ctx);
   return GBSPH_OK;
@@ -1108,6 +1127,8 @@ int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value) {
   else if (key == 3) *value = ctx->mdbc_variant;
   else if (key == 4) *value = ctx->forces_split;
   else if (key == 5) *value = forces_split(ctx);
+  else if (key == 6) *value = ctx->bound_lanes;
+  else if (key == 7) *value = bound_lanes(ctx);
   else return GBSPH_EINVAL;
   return GBSPH_OK;
 }
@@ -1173,10 +1194,11 @@ int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
   gbsph_tune_result r{};
   for (int k = 0; k < GBSPH_TUNE_CANDIDATES; k++) {
     const int var = cand[k][0], bs = cand[k][1], sp = cand[k][2];
-    gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, sp, ctx->stream, nullptr, nullptr, nullptr);  // warm-up
+    const int bl = bound_lanes(ctx);
+    gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, sp, bl, ctx->stream, nullptr, nullptr, nullptr);  // warm-up
     cudaEventRecord(e0, ctx->stream);
     for (int i = 0; i < reps; i++)
-      gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, sp, ctx->stream, nullptr, nullptr, nullptr);
+      gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, sp, bl, ctx->stream, nullptr, nullptr, nullptr);
     cudaEventRecord(e1, ctx->stream);
     cudaError_t e = cudaEventSynchronize(e1);
     float ms = 0;

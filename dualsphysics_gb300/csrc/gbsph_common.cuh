@@ -278,8 +278,10 @@ cudaError_t forces_init(const gbsph_consts& c);
 // the split a launch of gbk::forces uses: 1 unless the variant is 2 and the
 // case takes the series form of the DDT2 hydrostatic term
 int forces_split_effective(const gbsph_consts& c, int variant, int split);
-void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, int split, cudaStream_t s,
-            unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin = nullptr, cudaEvent_t ev_fluid_end = nullptr);
+// bound_lanes: lanes a boundary row in the bound-row pass (1, 4 or 32)
+void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, int split,
+            int bound_lanes, cudaStream_t s, unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin = nullptr,
+            cudaEvent_t ev_fluid_end = nullptr);
 // variant 1: one thread per boundary row (k_mdbc); otherwise the cell-tiled
 // staged kernel (k_mdbc_t)
 void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s,

@@ -1291,6 +1291,65 @@ __global__ void __launch_bounds__(128) k_forces_bound(gbsph_consts c, DevArrays 
   gb_warp_maxes(a.st, 0.f, visc, vel2);
 }
 
+// The same bound rows with G lanes a row (G = 4 or 32), for cases too small
+// to fill the device with one thread a row: the lanes of a row take the
+// candidates of each (y, z) box row in turn (a contiguous range of the sorted
+// order, each candidate's x cell from its dcell) and their sums are added
+// across the G lanes (the order of the sum changes, within the FP32
+// criterion).
+template <int G>
+__global__ void __launch_bounds__(128) k_forces_bound_g(gbsph_consts c, DevArrays a) {
+  static_assert(G == 4 || G == 8 || G == 16 || G == 32, "lanes a row");
+  const DivState& d = *a.div;
+  const unsigned npb = d.npb, npbok = d.npbok;
+  const unsigned p1 = (unsigned)(((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) / G);
+  const unsigned sl = threadIdx.x & (G - 1);
+  float visc = 0, vel2 = 0, arp1 = 0;
+  float4 vr1 = make_float4(0.f, 0.f, 0.f, 1.f);
+  if (p1 < npbok) {
+    const float4 ps1 = a.pscell[p1];
+    vr1 = a.velrho[p1];
+    const unsigned dcc = c.domcellcode, cel = a.dcell[p1], cmin0 = d.cellmin[0];
+    const CellGrid g = gb_grid((int)gb_cx(dcc, cel) - (int)cmin0, (int)gb_cy(dcc, cel) - (int)d.cellmin[1],
+                               (int)gb_cz(dcc, cel) - (int)d.cellmin[2], c.cellmode_div, d);
+    const float scell = c.scell, ks2 = c.kernelsize2, h = c.kernelh, bwenh = c.bwenh, eta2 = c.eta2;
+    const float massp2 = c.massfluid;
+    for (int z = g.zini; z < g.zfin; z++) {
+      for (int y = g.yini; y < g.yfin; y++) {
+        const unsigned rowbase = d.boxfluid + (unsigned)y * d.ncx + (unsigned)z * d.nsheet;
+        const float by = ps1.y + (float)(g.cy - y) * scell, bz = ps1.z + (float)(g.cz - z) * scell;
+        const unsigned pini = a.begincell[rowbase + (unsigned)g.xini], pfin = a.begincell[rowbase + (unsigned)g.xfin];
+        for (unsigned p2 = pini + sl; p2 < pfin; p2 += G) {
+          const float4 ps2 = a.pscell[p2];
+          const int x = (int)gb_cx(dcc, a.dcell[p2]) - (int)cmin0;
+          const float drx = (ps1.x + (float)(g.cx - x) * scell) - ps2.x, dry = by - ps2.y, drz = bz - ps2.z;
+          const float rr2 = drx * drx + dry * dry + drz * drz;
+          if (rr2 <= ks2 && rr2 >= GB_ALMOSTZERO) {
+            const float rad = sqrtf(rr2);
+            const float qq = rad / h;
+            const float wqq1 = 1.f - 0.5f * qq;
+            const float fac = bwenh * wqq1 * wqq1 * wqq1;
+            const float frx = fac * drx, fry = fac * dry, frz = fac * drz;
+            const float4 vr2 = a.velrho[p2];
+            const float dvx = vr1.x - vr2.x, dvy = vr1.y - vr2.y, dvz = vr1.z - vr2.z;
+            arp1 += massp2 * (dvx * frx + dvy * fry + dvz * frz) * (vr1.w / vr2.w);
+            const float dot = drx * dvx + dry * dvy + drz * dvz;
+            visc = fmaxf(dot / (rr2 + eta2), visc);
+          }
+        }
+      }
+    }
+    if (c.dtallparticles && sl == 0) vel2 = vr1.x * vr1.x + vr1.y * vr1.y + vr1.z * vr1.z;
+  }
+#pragma unroll
+  for (int o = G / 2; o; o >>= 1) {
+    arp1 += __shfl_xor_sync(0xffffffffu, arp1, o);
+    visc = fmaxf(visc, __shfl_xor_sync(0xffffffffu, visc, o));
+  }
+  if (p1 < npb && sl == 0) a.acear[p1] = make_float4(0.f, 0.f, 0.f, arp1);
+  gb_warp_maxes(a.st, 0.f, visc, vel2);
+}
+
 // JSphCpu::ComputeSpsTau (JSphCpu.cpp:1279-1309) for fluid particles.
 __global__ void k_sps_tau(gbsph_consts c, DevArrays a) {
   const DivState& d = *a.div;
@@ -1907,10 +1966,13 @@ cudaError_t launch_fluid_v(const gbsph_consts& c, const DevArrays& a, unsigned c
 
 namespace gbk {
 
-void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, int split, cudaStream_t s,
-            unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin, cudaEvent_t ev_fluid_end) {
+void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, int split,
+            int bound_lanes, cudaStream_t s, unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin,
+            cudaEvent_t ev_fluid_end) {
   cudaMemsetAsync(&a.st->acemax2, 0, 3 * sizeof(unsigned), s);
-  k_forces_bound<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+  if (bound_lanes == 32) k_forces_bound_g<32><<<gb_div_up(cap, 4), 128, 0, s>>>(c, a);
+  else if (bound_lanes == 4) k_forces_bound_g<4><<<gb_div_up(cap, 32), 128, 0, s>>>(c, a);
+  else k_forces_bound<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
   // inside a stream capture the records must be external nodes so that every
   // replay of the graph records them; outside a capture they are plain records
   cudaStreamCaptureStatus cap_st = cudaStreamCaptureStatusNone;

@@ -253,7 +253,9 @@ class GbSphSingle:
         per particle), key 0 = block size of kernel 1, key 2 = sort digit bits,
         key 3 = mDBC kernel (0 cell-tiled, 1 one thread per row), key 4 =
         warps per group of 32 fluid rows in the cell-tiled kernel (1, 2, 4; 0
-        automatic; get_option(5) reads the value in effect)."""
+        automatic; get_option(5) reads the value in effect), key 6 = lanes a
+        boundary row in the bound-row pass (1, 4, 32; 0 automatic;
+        get_option(7) reads the value in effect)."""
         self._check(lib().gbsph_set_option(self.ctx, key, value), "set_option")
 
     def get_option(self, key: int) -> int:

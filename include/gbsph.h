@@ -377,11 +377,15 @@ void* gbsph_stream(gbsph_ctx* ctx);
  * (default) chosen from the fluid rows of the last upload, so that a case
  * too small to fill the device runs more, shorter warps.  The other kernels,
  * and cases that need the power form of the DDT2 hydrostatic term, keep one
- * warp.  The sums' order changes with it, within the FP32 criterion. */
+ * warp.  The sums' order changes with it, within the FP32 criterion.
+ * key 6 = lanes a boundary row in the bound-row pass of gbsph_forces: 1
+ * (one thread a row, the reference's layout), 4, 32, or 0 (default) chosen
+ * from the boundary rows of the last upload (32 up to 29 k rows and 4 up to
+ * 233 k on 152 SMs); the lanes take a row's candidates in turn. */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
 /* The current value of an option of gbsph_set_option (no reference
  * counterpart); key 5 reads the warps per row group in effect (key 4
- * resolved). */
+ * resolved), key 7 the lanes a boundary row in effect (key 6 resolved). */
 int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value);
 
 /* Autotuner (no reference counterpart).  Times each fluid-row kernel

@@ -51,7 +51,7 @@ def test_forces_within_tolerance(name):
     g = G.golden(name)
     cd = G.load_generated(name)
     s = _gpu(cd)
-    assert s.get_option(5) == 4  # a small case: four warps per row group by default
+    assert s.get_option(5) == 4 and s.get_option(7) == 32  # a small case: split row groups, a warp per bound row
     o = _oracle(cd)
     s.MdbcBoundCorrection(_lib.INTERSTEP_SYMPREDICTOR)
     r64 = po.mdbc_f64(o)
@@ -86,16 +86,18 @@ def test_forces_within_tolerance(name):
 
 @pytest.mark.parametrize("name", ["dbc_d04", "vel_d04", "sps_d04", "mdbc_d04", "lam_d04", "ddt2f_d04", "half_d04",
                                   "shift_d04", "shiftnb_d04"])
-@pytest.mark.parametrize("variant,split", [(0, 1), (1, 1), (2, 1), (2, 2), (2, 4), (3, 1)])
-def test_forces_variants_within_tolerance(name, variant, split):
+@pytest.mark.parametrize("variant,split,blanes", [(0, 1, 1), (1, 1, 4), (2, 1, 1), (2, 2, 4), (2, 4, 32), (3, 1, 32)])
+def test_forces_variants_within_tolerance(name, variant, split, blanes):
     """Every fluid-row kernel: queued rounds (0), one thread per particle (1),
     cell-tiled staged with a ring of 8 (2) or 4 (3) chunks, with 1, 2 or 4
-    warps per group of 32 rows."""
+    warps per group of 32 rows; and the bound-row pass with 1, 4 or 32
+    lanes a row."""
     cd = G.load_generated(name)
     s = _gpu(cd)
     s.set_option(1, variant)
     s.set_option(4, split)
-    assert s.get_option(5) == split
+    s.set_option(6, blanes)
+    assert s.get_option(5) == split and s.get_option(7) == blanes
     o = _oracle(cd)
     s.MdbcBoundCorrection(_lib.INTERSTEP_SYMPREDICTOR)
     o.mdbc(False)
@@ -328,7 +330,7 @@ def test_c2_full_size_divide_mdbc_and_forces():
     cd = bench.make_case(0.0025)
     assert cd.np == 7093601
     s = _gpu(cd)
-    assert s.get_option(4) == 0 and s.get_option(5) == 1  # large enough for one warp per row group
+    assert s.get_option(4) == 0 and s.get_option(5) == 1 and s.get_option(7) == 1  # large: one warp/thread a row
     o = _oracle(cd)
     gs, os_ = s.download(), o.state()
     for k in ("idp", "dcell", "code"):
@@ -376,7 +378,7 @@ def test_invalid_arguments_are_reported():
     assert rc == -5  # GBSPH_ECAPACITY
     assert b"capacity" in _lib.lib().gbsph_last_error(ctx)
     assert _lib.lib().gbsph_step(ctx) == -7  # GBSPH_ESTATE: nothing uploaded
-    for key, value in ((1, 4), (3, 2), (4, 3), (4, 8), (2, 9), (6, 0)):
+    for key, value in ((1, 4), (3, 2), (4, 3), (4, 8), (2, 9), (6, 2), (6, 64), (8, 0)):
         assert _lib.lib().gbsph_set_option(ctx, key, value) == -1, (key, value)  # GBSPH_EINVAL
     _lib.lib().gbsph_destroy(ctx)
 
