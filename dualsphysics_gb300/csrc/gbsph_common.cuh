@@ -283,8 +283,8 @@ void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, 
             int bound_lanes, cudaStream_t s, unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin = nullptr,
             cudaEvent_t ev_fluid_end = nullptr);
 // variant 1: one thread per boundary row (k_mdbc); otherwise the cell-tiled
-// staged kernel (k_mdbc_t)
-void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s,
+// staged kernel (k_mdbc_t) with split (1, 2 or 4) warps per 32 boundary rows
+void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int split, cudaStream_t s,
           unsigned long long* nlaunch);
 void dtvariable(const gbsph_consts& c, const DevArrays& a, int which, cudaStream_t s, unsigned long long* nlaunch);
 void symplectic_pre(const gbsph_consts& c, DevArrays& a, unsigned cap, const double* dtp, cudaStream_t s, unsigned long long* nlaunch);

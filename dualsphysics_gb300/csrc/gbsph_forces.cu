@@ -1642,13 +1642,21 @@ __device__ __forceinline__ void mdbc_round(const gbsph_consts& c, float hinv, co
   }
 }
 
-__global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) {
+// tsplit: 2^lsplit consecutive warps (2 or 4) take the same 32 boundary rows,
+// each every 2^lsplit-th chunk of the candidate stream, for cases whose
+// boundary rows make too few warps to fill the device; the first adds the
+// others' compensated sums (through their rings, after a named barrier per
+// row group) and solves.  A separate instantiation, so that the one-warp
+// kernel keeps its registers.
+template <bool tsplit>
+__global__ void __launch_bounds__(128, tsplit ? 3 : 4) k_mdbc_t(gbsph_consts c, DevArrays a, unsigned lsplit) {
   extern __shared__ float4 mdbc_smem[];
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int S = kMdbcR * 32;
   const DivState& d = *a.div;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const unsigned p1 = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned p1 = tsplit ? blockIdx.x * (128u >> lsplit) + (((unsigned)warp >> lsplit) << 5) + (unsigned)lane
+                             : blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned npbok = d.npbok;
   float4 bn = make_float4(0.f, 0.f, 0.f, 0.f);
   if (p1 < npbok) bn = a.boundnor[p1];
@@ -1734,7 +1742,13 @@ __global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) 
     }
     const unsigned pbase = (unsigned)(lane / kTSeg) * plen + (unsigned)(lane % kTSeg);
     const unsigned send = min((unsigned)(lane / kTSeg + 1) * plen, total);
-    unsigned ch = 0u;
+    unsigned ch = 0u, mine = nch;
+    if constexpr (tsplit) {  // every 2^lsplit-th chunk of the order, from the warp's index in the group on
+      const unsigned sub = (unsigned)warp & ((1u << lsplit) - 1u);
+      for (unsigned j = 0; j < sub; j++) ch = (ch + stride >= nch) ? ch + stride - nch : ch + stride;
+      for (unsigned j = 0; j < lsplit; j++) stride = (2u * stride >= nch) ? 2u * stride - nch : 2u * stride;
+      mine = nch > sub ? (nch - sub + (1u << lsplit) - 1u) >> lsplit : 0u;
+    }
     // checks the full chunk cnext and runs rounds while every ghost of the
     // group has a hit pending
     auto check = [&]() {
@@ -1754,7 +1768,7 @@ __global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) 
       if (cur == 0u) cc = cnext;
       while (__ballot_sync(FULL, ing && cur != 0u) == grp) mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, foy, foz, m, lane);
     };
-    for (unsigned i = 0; i < nch; i++, ch = (ch + stride >= nch) ? ch + stride - nch : ch + stride) {
+    for (unsigned i = 0; i < mine; i++, ch = (ch + stride >= nch) ? ch + stride - nch : ch + stride) {
       const unsigned s = pbase + ch * kTSeg;
       int lo = 0, hi = nrows;
 #pragma unroll
@@ -1828,6 +1842,50 @@ __global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a) 
     }
   }
   while (__any_sync(FULL, cur != 0u)) mdbc_round(c, hinv, ring, cur, cc, cnext, gh, fox, foy, foz, m, lane);
+  if constexpr (tsplit) {
+    // partial sums through the warps' own rings (41 x 32 floats of the 80 x 32)
+    const unsigned sub = (unsigned)warp & ((1u << lsplit) - 1u);
+    const unsigned nthreads = 32u << lsplit, barid = 1u + ((unsigned)warp >> lsplit);
+    __syncwarp();
+    if (sub) {
+      float* part = ring;
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+          const int f = 4 * (2 * i + j);
+          part[(f + 0) * 32 + lane] = m.Ah[i][j].x; part[(f + 1) * 32 + lane] = m.Ah[i][j].y;
+          part[(f + 2) * 32 + lane] = m.Al[i][j].x; part[(f + 3) * 32 + lane] = m.Al[i][j].y;
+        }
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const int f = 32 + 4 * j;
+        part[(f + 0) * 32 + lane] = m.bh[j].x; part[(f + 1) * 32 + lane] = m.bh[j].y;
+        part[(f + 2) * 32 + lane] = m.bl[j].x; part[(f + 3) * 32 + lane] = m.bl[j].y;
+      }
+      part[40 * 32 + lane] = __uint_as_float(m.nfound);
+    }
+    asm volatile("bar.sync %0, %1;" ::"r"(barid), "r"(nthreads) : "memory");
+    if (sub) return;
+    for (unsigned w = 1; w < (1u << lsplit); w++) {
+      const float* part = (const float*)((const char*)mdbc_smem + (size_t)(warp + (int)w) * kMdbcWarpBytes);
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+          const int f = 4 * (2 * i + j);
+          gb_kadd2(m.Ah[i][j], m.Al[i][j], make_float2(part[(f + 0) * 32 + lane], part[(f + 1) * 32 + lane]));
+          m.Al[i][j] = __fadd2_rn(m.Al[i][j], make_float2(part[(f + 2) * 32 + lane], part[(f + 3) * 32 + lane]));
+        }
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const int f = 32 + 4 * j;
+        gb_kadd2(m.bh[j], m.bl[j], make_float2(part[(f + 0) * 32 + lane], part[(f + 1) * 32 + lane]));
+        m.bl[j] = __fadd2_rn(m.bl[j], make_float2(part[(f + 2) * 32 + lane], part[(f + 3) * 32 + lane]));
+      }
+      m.nfound += __float_as_uint(part[40 * 32 + lane]);
+    }
+  }
   if (active) mdbc_final(c, a, p1, bn, m);
 }
 
@@ -1995,7 +2053,10 @@ cudaError_t forces_init(const gbsph_consts& c) {
   DevArrays a{};
   const cudaError_t e = launch_fluid_v(c, a, 0, 2, 128, 1, true, nullptr);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_mdbc_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(4 * kMdbcWarpBytes));
+  const cudaError_t e2 =
+      cudaFuncSetAttribute(k_mdbc_t<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(4 * kMdbcWarpBytes));
+  if (e2 != cudaSuccess) return e2;
+  return cudaFuncSetAttribute(k_mdbc_t<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(4 * kMdbcWarpBytes));
 }
 
 void sps_tau(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t s, unsigned long long* nlaunch) {
@@ -2008,10 +2069,16 @@ void pips(const gbsph_consts& c, const DevArrays& a, unsigned cap, cudaStream_t 
   k_pips<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
 }
 
-void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, cudaStream_t s,
+void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int split, cudaStream_t s,
           unsigned long long* nlaunch) {
+  static_assert(kMdbcArrays * kMdbcR >= 41, "a ring holds the partial sums of a split row group");
   if (variant == 1) k_mdbc<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
-  else k_mdbc_t<<<gb_div_up(cap, 128), 128, 4 * kMdbcWarpBytes, s>>>(c, a);
+  else if (split >= 2) {
+    const unsigned ls = split >= 4 ? 2u : 1u;
+    k_mdbc_t<true><<<gb_div_up(cap, 128u >> ls), 128, 4 * kMdbcWarpBytes, s>>>(c, a, ls);
+  } else {
+    k_mdbc_t<false><<<gb_div_up(cap, 128), 128, 4 * kMdbcWarpBytes, s>>>(c, a, 0u);
+  }
   if (nlaunch) *nlaunch += 1;
 }
 

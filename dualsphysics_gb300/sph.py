@@ -255,7 +255,9 @@ class GbSphSingle:
         warps per group of 32 fluid rows in the cell-tiled kernel (1, 2, 4; 0
         automatic; get_option(5) reads the value in effect), key 6 = lanes a
         boundary row in the bound-row pass (1, 4, 32; 0 automatic;
-        get_option(7) reads the value in effect)."""
+        get_option(7) reads the value in effect), key 8 = warps per group of
+        32 boundary rows in the cell-tiled mDBC kernel (1, 2, 4; 0 automatic;
+        get_option(9) reads the value in effect)."""
         self._check(lib().gbsph_set_option(self.ctx, key, value), "set_option")
 
     def get_option(self, key: int) -> int:

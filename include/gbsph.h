@@ -380,12 +380,17 @@ void* gbsph_stream(gbsph_ctx* ctx);
  * warp.  The sums' order changes with it, within the FP32 criterion.
  * key 6 = lanes a boundary row in the bound-row pass of gbsph_forces: 1
  * (one thread a row, the reference's layout), 4, 32, or 0 (default) chosen
- * from the boundary rows of the last upload (32 up to 29 k rows and 4 up to
- * 233 k on 152 SMs); the lanes take a row's candidates in turn. */
+ * from the boundary rows of the last upload (32 up to 117 k rows and 4 up
+ * to 467 k on 152 SMs); the lanes take a row's candidates in turn.
+ * key 8 = warps that share each group of 32 boundary rows in the cell-tiled
+ * mDBC kernel (each takes every 1st, 2nd or 4th chunk of the ghosts'
+ * candidates, and the first adds the others' compensated sums): 1, 2, 4, or
+ * 0 (default) chosen from the boundary rows of the last upload. */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
 /* The current value of an option of gbsph_set_option (no reference
  * counterpart); key 5 reads the warps per row group in effect (key 4
- * resolved), key 7 the lanes a boundary row in effect (key 6 resolved). */
+ * resolved), key 7 the lanes a boundary row in effect (key 6 resolved),
+ * key 9 the warps per mDBC row group in effect (key 8 resolved). */
 int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value);
 
 /* Autotuner (no reference counterpart).  Times each fluid-row kernel

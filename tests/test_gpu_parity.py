@@ -51,7 +51,8 @@ def test_forces_within_tolerance(name):
     g = G.golden(name)
     cd = G.load_generated(name)
     s = _gpu(cd)
-    assert s.get_option(5) == 4 and s.get_option(7) == 32  # a small case: split row groups, a warp per bound row
+    # a small case: split row groups in the fluid-row and mDBC kernels, a warp per bound row
+    assert s.get_option(5) == 4 and s.get_option(7) == 32 and s.get_option(9) == 4
     o = _oracle(cd)
     s.MdbcBoundCorrection(_lib.INTERSTEP_SYMPREDICTOR)
     r64 = po.mdbc_f64(o)
@@ -119,17 +120,18 @@ def test_forces_variants_within_tolerance(name, variant, split, blanes):
 
 
 @pytest.mark.parametrize("name", ["mdbc_d04", "perim_d04"])
-@pytest.mark.parametrize("variant", [0, 1])
-def test_mdbc_variants_within_tolerance(name, variant):
-    """Both mDBC kernels (0 cell-tiled staged, 1 one thread per boundary row)
-    meet the density criterion against the FP64 correction (both sum the
+@pytest.mark.parametrize("variant,split", [(0, 1), (0, 2), (0, 4), (1, 1)])
+def test_mdbc_variants_within_tolerance(name, variant, split):
+    """Both mDBC kernels (0 cell-tiled staged, with 1, 2 or 4 warps per 32
+    boundary rows; 1 one thread per boundary row) meet the density criterion against the FP64 correction (both sum the
     moment matrix and the right-hand side compensated, so neither reproduces
     the reference's plain-float rounding of ill-conditioned solves); after a
     few steps the two kernels' runs agree to the rounding of their sums."""
     cd = G.load_generated(name)
     s = _gpu(cd)
     s.set_option(3, variant)
-    assert s.get_option(3) == variant
+    s.set_option(8, split)
+    assert s.get_option(3) == variant and s.get_option(9) == split
     o = _oracle(cd)
     s.MdbcBoundCorrection(_lib.INTERSTEP_SYMPREDICTOR)
     r64 = po.mdbc_f64(o)
@@ -330,7 +332,8 @@ def test_c2_full_size_divide_mdbc_and_forces():
     cd = bench.make_case(0.0025)
     assert cd.np == 7093601
     s = _gpu(cd)
-    assert s.get_option(4) == 0 and s.get_option(5) == 1 and s.get_option(7) == 1  # large: one warp/thread a row
+    # large: one warp per row group, one thread per bound row
+    assert s.get_option(4) == 0 and s.get_option(5) == 1 and s.get_option(7) == 1 and s.get_option(9) == 1
     o = _oracle(cd)
     gs, os_ = s.download(), o.state()
     for k in ("idp", "dcell", "code"):
@@ -378,7 +381,7 @@ def test_invalid_arguments_are_reported():
     assert rc == -5  # GBSPH_ECAPACITY
     assert b"capacity" in _lib.lib().gbsph_last_error(ctx)
     assert _lib.lib().gbsph_step(ctx) == -7  # GBSPH_ESTATE: nothing uploaded
-    for key, value in ((1, 4), (3, 2), (4, 3), (4, 8), (2, 9), (6, 2), (6, 64), (8, 0)):
+    for key, value in ((1, 4), (3, 2), (4, 3), (4, 8), (2, 9), (6, 2), (6, 64), (8, 3), (10, 0)):
         assert _lib.lib().gbsph_set_option(ctx, key, value) == -1, (key, value)  # GBSPH_EINVAL
     _lib.lib().gbsph_destroy(ctx)
 
