@@ -110,7 +110,9 @@ TUNE_CANDIDATES = 8
 
 class TuneResult(C.Structure):
     _fields_ = [("best", C.c_int), ("variant", C.c_int * TUNE_CANDIDATES), ("bsize", C.c_int * TUNE_CANDIDATES),
-                ("split", C.c_int * TUNE_CANDIDATES), ("ms", C.c_float * TUNE_CANDIDATES)]
+                ("split", C.c_int * TUNE_CANDIDATES), ("ms", C.c_float * TUNE_CANDIDATES),
+                ("bound_best", C.c_int), ("bound_lanes", C.c_int * 3), ("bound_ms", C.c_float * 3),
+                ("mdbc_best", C.c_int), ("mdbc_split", C.c_int * 3), ("mdbc_ms", C.c_float * 3)]
 
 
 class Maxes(C.Structure):

@@ -109,14 +109,14 @@ int bound_lanes(const gbsph_ctx* ctx) {
 }
 
 // Warps per group of 32 boundary rows in the staged mDBC kernel: the option,
-// or with 0 the largest of 4, 2, 1 that keeps the boundary rows' warps
-// within about three waves of the kernel's 16 resident warps a SM (the rows
-// outside the fluid's domain end at once, so this counts high).
+// or with 0 four.  Only the boundary rows whose ghosts lie in the fluid's
+// domain have work, a fraction of the walls, so the kernel is a latency
+// chain at every size measured: four warps a group gave the shortest steps
+// from 38 k particles (0.364 ms against 0.478 with one) to C2's 7.1 M
+// (21.54 ms against 21.62).
 int mdbc_split(const gbsph_ctx* ctx) {
   if (ctx->mdbc_variant == 1) return 1;
-  if (ctx->mdbc_split) return ctx->mdbc_split;
-  const unsigned long long warps = (ctx->nbound + 31u) / 32u, resident = 16ull * (unsigned)(ctx->nsm > 0 ? ctx->nsm : 1);
-  return warps * 4ull <= 3ull * resident ? 4 : warps * 2ull <= 3ull * resident ? 2 : 1;
+  return ctx->mdbc_split ? ctx->mdbc_split : 4;
 }
 
 int set_err(gbsph_ctx* ctx, int code, const char* fmt, ...) {
@@ -1200,7 +1200,9 @@ int gbsph_tune_sort(gbsph_ctx* ctx, int reps, int* best_bits, float* ms) {
 // (between steps) and keeps the fastest: the cell-tiled staged kernel with a
 // ring of 8 chunks at 1, 2 and 4 warps per row group and with a ring of 4
 // chunks, the warp-queued rounds kernel, and the one-thread-per-row kernel at
-// 64, 128 and 256 threads per block.  The
+// 64, 128 and 256 threads per block.  Then, with that configuration, the
+// lanes a boundary row of the bound-row pass (1, 4, 32) and, for mDBC, the
+// warps per row group of the staged mDBC kernel (1, 2, 4).  The
 // launches only rewrite the interaction outputs, which the next step
 // recomputes.
 int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
@@ -1210,44 +1212,71 @@ int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out) {
   // variant, block size, warps per row group
   static const int cand[GBSPH_TUNE_CANDIDATES][3] = {{2, 128, 1}, {2, 128, 2}, {2, 128, 4}, {3, 128, 1},
                                                      {0, 128, 1}, {1, 64, 1},  {1, 128, 1}, {1, 256, 1}};
+  static const int lanes[3] = {1, 4, 32}, msplits[3] = {1, 2, 4};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0), "event");
   CK(cudaEventCreate(&e1), "event");
-  int best = 0;
-  float tbest = 0;
-  gbsph_tune_result r{};
-  for (int k = 0; k < GBSPH_TUNE_CANDIDATES; k++) {
-    const int var = cand[k][0], bs = cand[k][1], sp = cand[k][2];
-    const int bl = bound_lanes(ctx);
-    gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, sp, bl, ctx->stream, nullptr, nullptr, nullptr);  // warm-up
+  // mean time of `reps` calls of f after one warm-up call
+  auto timed = [&](auto&& f, float* ms) -> int {
+    f();
     cudaEventRecord(e0, ctx->stream);
-    for (int i = 0; i < reps; i++)
-      gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, sp, bl, ctx->stream, nullptr, nullptr, nullptr);
+    for (int i = 0; i < reps; i++) f();
     cudaEventRecord(e1, ctx->stream);
     cudaError_t e = cudaEventSynchronize(e1);
-    float ms = 0;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-    if (e != cudaSuccess) {
-      cudaEventDestroy(e0);
-      cudaEventDestroy(e1);
-      return cuda_check(ctx, e, "tune");
-    }
-    ms /= (float)reps;
-    r.ms[k] = ms;
+    *ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "tune");
+    *ms /= (float)reps;
+    return GBSPH_OK;
+  };
+  int rc = GBSPH_OK;
+  gbsph_tune_result r{};
+  // the fluid-row configuration, with the bound-row lanes of the current choice
+  int best = 0;
+  const int bl0 = bound_lanes(ctx);
+  for (int k = 0; k < GBSPH_TUNE_CANDIDATES && !rc; k++) {
+    const int var = cand[k][0], bs = cand[k][1], sp = cand[k][2];
+    rc = timed([&] { gbk::forces(ctx->c, ctx->a, ctx->cap, bs, var, sp, bl0, ctx->stream, nullptr, nullptr, nullptr); },
+               &r.ms[k]);
     r.variant[k] = var;
     r.bsize[k] = bs;
     r.split[k] = sp;
-    if (k == 0 || ms < tbest) { tbest = ms; best = k; }
+    if (r.ms[k] < r.ms[best]) best = k;
+  }
+  // then the lanes a boundary row, with that fluid-row configuration
+  int bbest = 0;
+  for (int k = 0; k < 3 && !rc; k++) {
+    rc = timed([&] {
+      gbk::forces(ctx->c, ctx->a, ctx->cap, cand[best][1], cand[best][0], cand[best][2], lanes[k], ctx->stream, nullptr,
+                  nullptr, nullptr);
+    }, &r.bound_ms[k]);
+    r.bound_lanes[k] = lanes[k];
+    if (r.bound_ms[k] < r.bound_ms[bbest]) bbest = k;
+  }
+  // and the warps per mDBC row group (the correction rewrites the boundary
+  // densities from the fluid's, the same values every time)
+  int mbest = 0;
+  const bool mdbc = ctx->c.tboundary == GBSPH_BC_MDBC && ctx->mdbc_variant == 0;
+  for (int k = 0; k < 3 && !rc; k++) {
+    r.mdbc_split[k] = msplits[k];
+    if (!mdbc) continue;
+    rc = timed([&] { gbk::mdbc(ctx->c, ctx->a, ctx->cap, 0, msplits[k], ctx->stream, nullptr); }, &r.mdbc_ms[k]);
+    if (r.mdbc_ms[k] < r.mdbc_ms[mbest]) mbest = k;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (rc) return rc;
   r.best = best;
+  r.bound_best = bbest;
+  r.mdbc_best = mdbc ? mbest : -1;
   ctx->forces_variant = cand[best][0];
   ctx->forces_bsize = cand[best][1];
   ctx->forces_split = cand[best][2];
+  ctx->bound_lanes = lanes[bbest];
+  if (mdbc) ctx->mdbc_split = msplits[mbest];
   reset_graph(ctx);
   if (out) *out = r;
-  return GBSPH_OK;
+  return check_device_errors(ctx);
 }
 
 }  // extern "C"

@@ -112,4 +112,6 @@ def tune(sim: GbSphSingle, reps: int = 3) -> dict:
     ms = (C.c_float * 2)()
     sim._check(lib().gbsph_tune_sort(sim.ctx, reps, C.byref(bits), ms), "gbsph_tune_sort")
     return {"best": r.best, "variant": list(r.variant), "bsize": list(r.bsize), "split": list(r.split), "ms": list(r.ms),
+            "bound_best": r.bound_best, "bound_lanes": list(r.bound_lanes), "bound_ms": list(r.bound_ms),
+            "mdbc_best": r.mdbc_best, "mdbc_split": list(r.mdbc_split), "mdbc_ms": list(r.mdbc_ms),
             "sort_bits": bits.value, "sort_ms": list(ms)}

@@ -385,7 +385,7 @@ void* gbsph_stream(gbsph_ctx* ctx);
  * key 8 = warps that share each group of 32 boundary rows in the cell-tiled
  * mDBC kernel (each takes every 1st, 2nd or 4th chunk of the ghosts'
  * candidates, and the first adds the others' compensated sums): 1, 2, 4, or
- * 0 (default) chosen from the boundary rows of the last upload. */
+ * 0 (default: 4, the fastest at every size measured). */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
 /* The current value of an option of gbsph_set_option (no reference
  * counterpart); key 5 reads the warps per row group in effect (key 4
@@ -397,7 +397,9 @@ int gbsph_get_option(const gbsph_ctx* ctx, int key, int* value);
  * configuration -- the cell-tiled kernel with rings of 8 chunks at 1, 2 and
  * 4 warps per row group and with a ring of 4 chunks, the queued kernel, and
  * the one-thread-per-particle kernel at 64, 128 and 256 threads per block --
- * over `reps` launches on the context's current state,
+ * over `reps` launches on the context's current state, then with the
+ * fastest the lanes a boundary row of the bound-row pass and (for mDBC) the
+ * warps per row group of the staged mDBC kernel,
  * between steps, and keeps the fastest.  The launches rewrite only the
  * interaction outputs, which the next step recomputes.  The kernels sum a
  * row's neighbours in different orders: results stay within the FP32
@@ -408,7 +410,13 @@ typedef struct {
   int variant[GBSPH_TUNE_CANDIDATES];    /* gbsph_set_option key 1 */
   int bsize[GBSPH_TUNE_CANDIDATES];      /* gbsph_set_option key 0 */
   int split[GBSPH_TUNE_CANDIDATES];      /* gbsph_set_option key 4 */
-  float ms[GBSPH_TUNE_CANDIDATES];       /* mean time of one fluid-row pass */
+  float ms[GBSPH_TUNE_CANDIDATES];       /* mean time of one interaction pass */
+  int bound_best;                        /* index of the lanes a boundary row kept */
+  int bound_lanes[3];                    /* gbsph_set_option key 6: 1, 4, 32 */
+  float bound_ms[3];                     /* mean time of one interaction pass with each */
+  int mdbc_best;                         /* index of the mDBC split kept (-1: no mDBC) */
+  int mdbc_split[3];                     /* gbsph_set_option key 8: 1, 2, 4 */
+  float mdbc_ms[3];                      /* mean time of one mDBC pass with each */
 } gbsph_tune_result;
 int gbsph_tune_forces(gbsph_ctx* ctx, int reps, gbsph_tune_result* out);
 /* Autotuner of the cell division: times `reps` divisions of the current state

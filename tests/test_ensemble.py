@@ -99,11 +99,20 @@ def test_autotuner_keeps_the_fastest_candidate():
     assert list(zip(r["variant"], r["bsize"], r["split"])) == [(2, 128, 1), (2, 128, 2), (2, 128, 4), (3, 128, 1),
                                                                 (0, 128, 1), (1, 64, 1), (1, 128, 1), (1, 256, 1)]
     assert s.get_option(4) == r["split"][r["best"]]
+    assert r["bound_lanes"] == [1, 4, 32] and all(m > 0 for m in r["bound_ms"])
+    assert r["bound_ms"][r["bound_best"]] == min(r["bound_ms"])
+    assert s.get_option(6) == r["bound_lanes"][r["bound_best"]]
+    if r["mdbc_best"] >= 0:
+        assert r["mdbc_ms"][r["mdbc_best"]] == min(r["mdbc_ms"])
+        assert s.get_option(8) == r["mdbc_split"][r["mdbc_best"]]
     # the tuned context steps as one set to the same configuration by hand
     (t,) = _sims(cds[:1])
     t.set_option(1, r["variant"][r["best"]])
     t.set_option(0, r["bsize"][r["best"]])
     t.set_option(4, r["split"][r["best"]])
+    t.set_option(6, r["bound_lanes"][r["bound_best"]])
+    if r["mdbc_best"] >= 0:
+        t.set_option(8, r["mdbc_split"][r["mdbc_best"]])
     s.RunSteps(5, use_graph=True)
     t.RunSteps(5, use_graph=True)
     _same(s, t, "tuned vs set by hand")
@@ -145,6 +154,30 @@ def test_sort_digit_width_leaves_the_order_unchanged(name):
     _same(a, b, name)
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_autotuner_tunes_the_mdbc_split_on_an_mdbc_case():
+    """On an mDBC case the tuner also times the mDBC kernel at 1, 2 and 4 warps
+    per row group and keeps the fastest; the tuned run equals the run with
+    the same options set by hand."""
+    import goldens as G
+    from dualsphysics_gb300.ensemble import tune
+    cd = G.load_generated("mdbc_d04")
+    (s,) = _sims([cd])
+    r = tune(s, reps=2)
+    assert r["mdbc_split"] == [1, 2, 4] and 0 <= r["mdbc_best"] < 3 and all(m > 0 for m in r["mdbc_ms"])
+    assert r["mdbc_ms"][r["mdbc_best"]] == min(r["mdbc_ms"])
+    assert s.get_option(8) == s.get_option(9) == r["mdbc_split"][r["mdbc_best"]]
+    (t,) = _sims([cd])
+    for key, value in ((1, r["variant"][r["best"]]), (0, r["bsize"][r["best"]]), (4, r["split"][r["best"]]),
+                       (6, r["bound_lanes"][r["bound_best"]]), (8, r["mdbc_split"][r["mdbc_best"]])):
+        t.set_option(key, value)
+    s.RunSteps(4, use_graph=True)
+    t.RunSteps(4, use_graph=True)
+    _same(s, t, "tuned vs set by hand (mDBC)")
+    s.close()
+    t.close()
 
 
 @pytest.mark.gpu

@@ -332,8 +332,8 @@ def test_c2_full_size_divide_mdbc_and_forces():
     cd = bench.make_case(0.0025)
     assert cd.np == 7093601
     s = _gpu(cd)
-    # large: one warp per row group, one thread per bound row
-    assert s.get_option(4) == 0 and s.get_option(5) == 1 and s.get_option(7) == 1 and s.get_option(9) == 1
+    # large: one warp per fluid row group, one thread per bound row, four warps per mDBC row group
+    assert s.get_option(4) == 0 and s.get_option(5) == 1 and s.get_option(7) == 1 and s.get_option(9) == 4
     o = _oracle(cd)
     gs, os_ = s.download(), o.state()
     for k in ("idp", "dcell", "code"):
