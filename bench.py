@@ -383,14 +383,15 @@ def run_closure(args, local: int = 0):
     val = heights[3::8]                                   # 4 of 32 heights validate (early stopping)
     train = [h for h in heights if h not in val]
     t0 = time.perf_counter()
-    kw = dict(dp_fine=dpf, ratio=ratio, t_end=t_end, n_snap=args.clos_snaps, device=local)
+    kw = dict(dp_fine=dpf, ratio=ratio, t_end=t_end, n_snap=args.clos_snaps, device=local,
+              smooth=bool(args.clos_smooth))
     xs, ts, meta = cl.paired_samples(train, **kw)
     xv, tv, _ = cl.paired_samples(val, **kw)
     t_data = time.perf_counter() - t0
     t1 = time.perf_counter()
     p, w, loss = cl.train_closure(xs, ts, epochs=args.clos_epochs, seed=args.clos_seed, device=local, xv=xv, tv=tv)
     t_train = time.perf_counter() - t1
-    xh, th, _ = cl.paired_samples([held], **kw)
+    xh, th, mh = cl.paired_samples([held], **kw)
     ev = cl.Trainer(cl.from_bf16(w), local)     # the deployed BF16 weights
     yh = ev.infer(xh)
     ev.close()
@@ -413,7 +414,8 @@ def run_closure(args, local: int = 0):
                                    f"column {held} m; {t_end} s; fine/judge dp={dpf:g}, coarse dp={dpc:g}",
                        "train_heights": len(train), "validation_heights": len(val),
                        "snapshots_per_height": args.clos_snaps,
-                       "samples": int(len(xs)), "epochs": args.clos_epochs},
+                       "samples": int(len(xs)), "epochs": args.clos_epochs,
+                       "targets": "kernel-smoothed" if args.clos_smooth else "raw"},
             "errors": err, "judge_converges": converges,
             "wall_s": {f"judge_dp{dpf:g}": judge["wall_s"], **{k: r["wall_s"] for k, r in runs.items()}},
             "ms_per_step": {f"judge_dp{dpf:g}": judge["ms_per_step"], **{k: r["ms_per_step"] for k, r in runs.items()}},
@@ -421,7 +423,10 @@ def run_closure(args, local: int = 0):
             "particles": {"judge": judge["np"], "mid": mid["np"], "coarse": plain["np"]},
             "target_met": bool(converges and err[kl][head] <= err[km][head] and speed >= 5.0),
             "learned_vs_plain_error": err[kl][head] / err[kp][head],
-            "apriori_heldout_mse": {"plain": float(np.mean(th ** 2)), "learned": float(np.mean((th - yh) ** 2))},
+            "apriori_heldout_mse": {"plain": float(np.mean(th ** 2)), "learned": float(np.mean((th - yh) ** 2)),
+                                    "targets": "smoothed" if args.clos_smooth else "raw",
+                                    "raw_plain": float(np.mean(mh["raw"] ** 2)),
+                                    "raw_learned": float(np.mean((mh["raw"] - yh) ** 2))},
             "train": {"loss_first": float(loss[0]), "loss_last": float(loss[-1]), "data_s": t_data,
                       "train_s": t_train, "fine_steps": meta["fine_steps"]},
             "fallback_rows": learned["fallbacks"]}
@@ -479,6 +484,8 @@ def main():
     ap.add_argument("--clos-seed", type=int, default=5)
     ap.add_argument("--clos-dpfine", type=float, default=0.005)
     ap.add_argument("--clos-ratio", type=int, default=4, choices=[2, 4])
+    ap.add_argument("--clos-smooth", type=int, default=1, choices=[0, 1],
+                    help="train on kernel-smoothed targets (closure.smooth_targets)")
     ap.add_argument("--clos-judge-dps", default="0.02,0.01,0.005,0.0025")
     ap.add_argument("--ens-cases", type=int, default=64)
     ap.add_argument("--ens-seed", type=int, default=1)

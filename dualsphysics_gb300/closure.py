@@ -306,12 +306,35 @@ class Pair:
         return cd, rows
 
 
+def smooth_targets(pos: np.ndarray, t: np.ndarray, h: float) -> np.ndarray:
+    """Kernel-weighted (Wendland, support 2h) Shepard mean of the targets of
+    each particle's neighbours, itself included: the part of the fine-minus-
+    coarse acceleration that varies over the kernel's scale, without the
+    particle-scale noise no local feature can predict."""
+    from scipy.spatial import cKDTree
+    tree = cKDTree(pos)
+    pairs = tree.query_pairs(2.0 * h, output_type="ndarray")
+    i, j = pairs[:, 0], pairs[:, 1]
+    q = np.linalg.norm(pos[i] - pos[j], axis=1) / h
+    w = (1.0 - 0.5 * q) ** 4 * (2.0 * q + 1.0)
+    n = len(pos)
+    num = np.array(t, np.float64)          # the particle itself, W(0) = 1
+    den = np.ones(n)
+    for k in range(t.shape[1]):
+        num[:, k] += np.bincount(i, weights=w * t[j, k], minlength=n) + np.bincount(j, weights=w * t[i, k], minlength=n)
+    den += np.bincount(i, weights=w, minlength=n) + np.bincount(j, weights=w, minlength=n)
+    return (num / den[:, None]).astype(np.float32)
+
+
 def paired_samples(heights, dp_fine: float = 0.01, t_end: float = 0.3, n_snap: int = 10,
-                   device: int = 0, log=None, ratio: int = 2) -> tuple[np.ndarray, np.ndarray, dict]:
+                   device: int = 0, log=None, ratio: int = 2,
+                   smooth: bool = False) -> tuple[np.ndarray, np.ndarray, dict]:
     """Features and targets over fine runs of the given column heights,
     restricted to the coarse particles (spacing ratio*dp_fine) at n_snap
-    times in (0, t_end]."""
-    xs, ts, meta = [], [], {"snapshots": 0, "fine_steps": 0, "fine_s": 0.0}
+    times in (0, t_end].  With smooth, the targets are replaced by their
+    kernel-weighted neighbourhood means (smooth_targets); meta["raw"] keeps
+    the raw ones."""
+    xs, ts, raw, meta = [], [], [], {"snapshots": 0, "fine_steps": 0, "fine_s": 0.0}
     g = 9.81
     for hk, h in enumerate(heights):
         pair = Pair(h, dp_fine, tag=f"H{hk}", ratio=ratio)
@@ -347,7 +370,12 @@ def paired_samples(heights, dp_fine: float = 0.01, t_end: float = 0.3, n_snap: i
                 tgt = (fmean[crow] - cace[cd.npb:cd.npb + len(crow)]) / g
                 ok = np.isfinite(x).all(axis=1) & np.isfinite(tgt).all(axis=1)
                 xs.append(x[ok])
-                ts.append(tgt[ok].astype(np.float32))
+                raw.append(tgt[ok].astype(np.float32))
+                if smooth:
+                    fpos = cst["pos"][cd.npb:cd.npb + len(crow)].astype(np.float64)
+                    ts.append(smooth_targets(fpos[ok], tgt[ok], float(cd.params.h)))
+                else:
+                    ts.append(tgt[ok].astype(np.float32))
                 meta["snapshots"] += 1
             if t >= t_end - 1e-12:
                 break
@@ -355,6 +383,7 @@ def paired_samples(heights, dp_fine: float = 0.01, t_end: float = 0.3, n_snap: i
         fine.close()
         if log:
             log(f"height {h:.3f}: {sum(len(x) for x in xs)} samples")
+    meta["raw"] = np.concatenate(raw)
     return np.concatenate(xs), np.concatenate(ts), meta
 
 
@@ -380,10 +409,10 @@ def probe_pressure(gs, rhop) -> np.ndarray:
 
 def run_with_probes(cd, t_end: float, dt_probe: float, w_bf16=None, limit: float = 0.2, device: int = 0,
                     mesh_h: float | None = None, chunk: int = 10) -> dict:
-    """Runs a case to t_end in graph replays of `chunk` steps, sampling the
-    probes and the surge front after the first chunk that passes each
-    multiple of dt_probe; returns them with their times, the wall time of the
-    stepping alone and its steps."""
+    """Runs a case to t_end in replays of one graph holding `chunk` steps,
+    sampling the probes and the surge front after the first chunk that passes
+    each multiple of dt_probe; returns them with their times, the wall time of
+    the stepping alone and its steps."""
     from .gauges import GaugeSystem
     s = GbSphSingle(device)
     s.setup(cd)
@@ -394,19 +423,11 @@ def run_with_probes(cd, t_end: float, dt_probe: float, w_bf16=None, limit: float
     gs.AddGaugeMesh("probes", **m)
     times, press, fronts = [], [], []
     tnext, t, wall, nsteps = dt_probe, 0.0, 0.0, 0
-    s.RunSteps(chunk, use_graph=True)       # graph capture and first replay outside the clock
-    s.sync()
-    s.close()
-    s = GbSphSingle(device)
-    s.setup(cd)
-    if w_bf16 is not None:
-        attach(s, w_bf16, limit)
-    gs = GaugeSystem(s)
-    gs.AddGaugeMesh("probes", **m)
+    s.graph_prepare(chunk)                  # one graph of `chunk` steps, captured outside the clock
     while t < t_end:
         s.sync()
         t0 = time.perf_counter()
-        s.RunSteps(chunk, use_graph=True)
+        s.RunSteps(chunk, use_graph=2)
         t = s.step_dt()[2]
         wall += time.perf_counter() - t0
         nsteps += chunk

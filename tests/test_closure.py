@@ -91,6 +91,22 @@ def test_fine_and_coarse_lattices_nest(dpf, ratio):
     assert np.abs(m[:, :] - c.pos[c.npb:]).max() <= 0.5 * (ratio - 1) * dpf + 1e-12
 
 
+def test_smoothed_targets_keep_constant_and_average_noise():
+    """The kernel-weighted neighbourhood mean keeps a constant target field and
+    shrinks particle-scale noise."""
+    rng = np.random.default_rng(2)
+    g = np.stack(np.meshgrid(*[np.arange(20) * 0.02] * 3, indexing="ij"), -1).reshape(-1, 3)
+    c = np.full((len(g), 3), 1.5, np.float32)
+    np.testing.assert_allclose(cl.smooth_targets(g, c, 0.026), c, rtol=1e-6)
+    noise = rng.normal(0.0, 1.0, (len(g), 3)).astype(np.float32)
+    sm = cl.smooth_targets(g, noise, 0.026)
+    assert sm.std() < 0.5 * noise.std()
+    # a field varying over many kernel lengths is kept, away from the edges
+    lin = np.repeat(g[:, :1] * 10.0, 3, axis=1).astype(np.float32)
+    inner = np.all((g > 0.06) & (g < 0.32), axis=1)
+    np.testing.assert_allclose(cl.smooth_targets(g, lin, 0.026)[inner], lin[inner], atol=1e-5)
+
+
 # ---- GPU ------------------------------------------------------------------
 @pytest.mark.gpu
 def test_mlp_forward_and_gradient_match_oracle():
