@@ -1647,9 +1647,11 @@ __device__ __forceinline__ void mdbc_round(const gbsph_consts& c, float hinv, co
 // boundary rows make too few warps to fill the device; the first adds the
 // others' compensated sums (through their rings, after a named barrier per
 // row group) and solves.  A separate instantiation, so that the one-warp
-// kernel keeps its registers.
+// kernel keeps its registers.  Both take four blocks a SM: the split kernel
+// at 128 registers (a few spilled) ran C2 0.9 % faster than at three blocks
+// and 159, and the one-warp kernel was slower at five blocks and 96.
 template <bool tsplit>
-__global__ void __launch_bounds__(128, tsplit ? 3 : 4) k_mdbc_t(gbsph_consts c, DevArrays a, unsigned lsplit) {
+__global__ void __launch_bounds__(128, 4) k_mdbc_t(gbsph_consts c, DevArrays a, unsigned lsplit) {
   extern __shared__ float4 mdbc_smem[];
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int S = kMdbcR * 32;
