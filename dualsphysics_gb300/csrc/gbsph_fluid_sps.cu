@@ -1,0 +1,15 @@
+// gbsph_fluid_sps.cu -- the fluid-row kernels of one viscosity model
+// (GBSPH_VISCO_LAMINARSPS), instantiated apart from the others so that they compile in
+// parallel (gbsph_fluid.cuh).
+#pragma nv_diag_suppress 177
+#include "gbsph_fluid.cuh"
+#pragma nv_diag_default 177
+
+namespace gbk {
+
+cudaError_t fluid_laminarsps(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int bsize, int split,
+                 bool prepare, cudaStream_t s) {
+  return launch_fluid_t<GBSPH_VISCO_LAMINARSPS>(c, a, cap, variant, bsize, split, prepare, s);
+}
+
+}  // namespace gbk
