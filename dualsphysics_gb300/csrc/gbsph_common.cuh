@@ -121,6 +121,9 @@ __device__ __forceinline__ void gb_warp_maxes(StepState* st, float acemax2, floa
   }
 }
 
+__device__ __forceinline__ double gb_f2d(float f);
+__device__ __forceinline__ float gb_d2f(double x);
+
 // Pressure from density: Tait/Monaghan EOS B*((rho/rho0)^gamma-1)
 // (FunSphEos.h:37-39).  (rho/rho0)^gamma is evaluated in double and rounded
 // once to float so it matches a correctly rounded powf.
@@ -128,7 +131,7 @@ __device__ __forceinline__ float gb_press(float rho, float rhopzero, float cteb,
   const float x = rho / rhopzero;
   double xg;
   if (gamma == 7.0f) {
-    const double xd = (double)x;
+    const double xd = gb_f2d(x);
     const double x2 = __dmul_rn(xd, xd);
     const double x3 = __dmul_rn(x2, xd);
     const double x4 = __dmul_rn(x2, x2);
@@ -136,7 +139,7 @@ __device__ __forceinline__ float gb_press(float rho, float rhopzero, float cteb,
   } else {
     xg = pow((double)x, (double)gamma);
   }
-  return cteb * ((float)xg - 1.0f);
+  return cteb * (gb_d2f(xg) - 1.0f);
 }
 
 __host__ __device__ __forceinline__ unsigned gb_div_up(unsigned a, unsigned b) { return (a + b - 1) / b; }
@@ -175,6 +178,17 @@ __device__ __forceinline__ float gb_d2f(double x) {
   const unsigned rem = (unsigned)(m & 0x1fffffffu);
   if (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) r += 1u;
   return __uint_as_float(r | ((unsigned)(b >> 63) << 31));
+}
+
+// (double)u, exactly, for u below 2^31 (cell indices): the bits of 2^52 + u
+// less 2^52 would take an FP64 subtraction, so the exponent and significand
+// are placed directly.
+__device__ __forceinline__ double gb_u2d(unsigned u) {
+  if (u == 0u) return 0.0;
+  const int lz = __clz(u);                 // u = 1.f * 2^(31 - lz)
+  const unsigned long long m = (unsigned long long)u << (lz + 21);  // the leading 1 at bit 52
+  const unsigned long long b = ((unsigned long long)(1023 + 31 - lz) << 52) | (m & 0xfffffffffffffull);
+  return __longlong_as_double((long long)b);
 }
 
 // x < 0 || x >= size || x is NaN, for a finite size > 0 (-0 is not below 0).

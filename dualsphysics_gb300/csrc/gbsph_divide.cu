@@ -412,14 +412,18 @@ __global__ void k_reorder(gbsph_consts c, DevArrays a) {
     a.taub2[p] = a.taub[src];
   }
   if (withnor) a.boundnor2[p] = a.boundnor[src];
-  // position relative to the origin of the particle's cell
+  // position relative to the origin of the particle's cell,
+  // float((pos - DomPosMin) - cell * Scell): cell * Scell (an integer below
+  // 2^24 times a float) is exact in double, so one fused multiply-add rounds
+  // the difference exactly as the subtraction of the rounded product does;
+  // the conversions run on the integer pipe (this part's FP64 rate is low)
   const unsigned dcc = c.domcellcode;
-  const double sc = (double)c.scell;
+  const double sc = gb_f2d(c.scell);
   float4 ps;
   if (cel != 0xffffffffu) {
-    ps.x = (float)__dsub_rn(__dsub_rn(x, c.domposmin[0]), __dmul_rn((double)gb_cx(dcc, cel), sc));
-    ps.y = (float)__dsub_rn(__dsub_rn(y, c.domposmin[1]), __dmul_rn((double)gb_cy(dcc, cel), sc));
-    ps.z = (float)__dsub_rn(__dsub_rn(z, c.domposmin[2]), __dmul_rn((double)gb_cz(dcc, cel), sc));
+    ps.x = gb_d2f(__fma_rn(-gb_u2d(gb_cx(dcc, cel)), sc, __dsub_rn(x, c.domposmin[0])));
+    ps.y = gb_d2f(__fma_rn(-gb_u2d(gb_cy(dcc, cel)), sc, __dsub_rn(y, c.domposmin[1])));
+    ps.z = gb_d2f(__fma_rn(-gb_u2d(gb_cz(dcc, cel)), sc, __dsub_rn(z, c.domposmin[2])));
   } else {
     ps.x = ps.y = ps.z = 0.f;
   }
