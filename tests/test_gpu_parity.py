@@ -68,8 +68,12 @@ def test_forces_within_tolerance(name):
     o.interaction()
     a32, r32 = o.forces()
     npb = o.npb
-    G.assert_fp32_parity(ace[npb:], a32[npb:], f64["ace"][npb:], f64["absace"][npb:], "ace")
-    G.assert_fp32_parity(ar, r32, f64["ar"], f64["absar"], "ar")
+    ea, eoa = G.assert_fp32_parity(ace[npb:], a32[npb:], f64["ace"][npb:], f64["absace"][npb:], "ace")
+    er, eor = G.assert_fp32_parity(ar, r32, f64["ar"], f64["absar"], "ar")
+    # the achieved errors (shown with pytest -s): GPU and oracle FP32 against FP64
+    print(f"\nPARITY {name} ace {ea:.2e} {eoa:.2e} ar {er:.2e} {eor:.2e} "
+          f"median ace {np.median(G.scaled_err(ace[npb:], f64['ace'][npb:], f64['absace'][npb:])):.1e} "
+          f"ar {np.median(G.scaled_err(ar, f64['ar'], f64['absar'])):.1e}")
     # against the reference's own FP32 result (golden fixture), same scale; with
     # mDBC the reference's boundary densities differ in the last bits, which the
     # Tait pressure amplifies, so that comparison is made on the DBC cases only
