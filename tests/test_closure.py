@@ -107,6 +107,26 @@ def test_smoothed_targets_keep_constant_and_average_noise():
     np.testing.assert_allclose(cl.smooth_targets(g, lin, 0.026)[inner], lin[inner], atol=1e-5)
 
 
+def test_judge_error_measures():
+    """The judge's measures on synthetic probe series: a run equal to the
+    reference has no error; a constant offset of the probes is the RMS of the
+    offset in every pressure measure; a shifted front is the shift."""
+    t = np.arange(1, 61) * 0.005
+    p = np.stack([np.sin(40 * t + k) * 1000.0 for k in range(50)], axis=1)
+    ref = {"t": t, "p": p, "front": 0.4 + 2.0 * t}
+    same = cl.errors(ref, ref)
+    assert all(v == 0.0 for v in same.values())
+    off = {"t": t, "p": p + 30.0, "front": ref["front"] + 0.01}
+    e = cl.errors(off, ref)
+    assert abs(e["probe_rmse_pa"] - 30.0) < 1e-9
+    assert abs(e["probe_rmse_pa_20ms_means"] - 30.0) < 1e-9
+    assert abs(e["face_rmse_pa_20ms_means"] - 30.0) < 1e-9
+    assert abs(e["front_rmse_m"] - 0.01) < 1e-12
+    # window means remove what averages out within 20 ms
+    fast = {"t": t, "p": p + 500.0 * np.where(np.arange(60) % 2 == 0, 1.0, -1.0)[:, None], "front": ref["front"]}
+    assert cl.probe_error(fast, ref, 0.02) < 1e-9 < cl.probe_error(fast, ref)
+
+
 # ---- GPU ------------------------------------------------------------------
 @pytest.mark.gpu
 def test_mlp_forward_and_gradient_match_oracle():
