@@ -470,6 +470,8 @@ def main():
     ap.add_argument("--mdbc-split", type=int, default=None, choices=[0, 1, 2, 4],
                     help="warps per group of 32 boundary rows in the cell-tiled mDBC kernel (0 automatic); "
                          "default: the library's")
+    ap.add_argument("--bound-beside", type=int, default=None, choices=[0, 1],
+                    help="the bound-row pass on a side stream beside the fluid-row pass; default: the library's")
     ap.add_argument("--no-tune", action="store_true", help="keep the 8-bit sort digits (no sort autotuning)")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c3err", "ensemble", "closure",
                                                          "closure-judge"],
@@ -544,7 +546,10 @@ def main():
         s.set_option(6, args.bound_lanes)
     if args.mdbc_split is not None:
         s.set_option(8, args.mdbc_split)
+    if args.bound_beside is not None:
+        s.set_option(10, args.bound_beside)
     variant, split, blanes, msplit = s.get_option(1), s.get_option(5), s.get_option(7), s.get_option(9)
+    beside = s.get_option(10)
     pi = s.pips()
     s.RunSteps(W, use_graph=True)
     s.sync()
@@ -595,6 +600,8 @@ def main():
             e.set_option(6, args.bound_lanes)
         if args.mdbc_split is not None:
             e.set_option(8, args.mdbc_split)
+        if args.bound_beside is not None:
+            e.set_option(10, args.bound_beside)
         for _ in range(K):
             e.RunSteps(1, use_graph=True)  # one step, replayed from its captured graph
             e.step_dt()                    # the Run loop reads the step's dt and time back
@@ -633,7 +640,7 @@ def main():
                        "particles": cd.np, "fluid": cd.nfluid, "boundary": cd.npb, "cellmode": args.cellmode,
                        "sort_digit_bits": sort_bits.value, "fluid_kernel_variant": variant,
                        "warps_per_row_group": split, "lanes_per_bound_row": blanes,
-                       "warps_per_mdbc_row_group": msplit,
+                       "warps_per_mdbc_row_group": msplit, "bound_rows_beside_fluid_rows": beside,
                        "sort_divide_ms_8_11": [round(float(x), 4) for x in sort_ms] if not args.no_tune else None,
                        "parallelism": "replicas only" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (no flush)"},

@@ -292,10 +292,18 @@ cudaError_t forces_init(const gbsph_consts& c);
 // the split a launch of gbk::forces uses: 1 unless the variant is 2 and the
 // case takes the series form of the DDT2 hydrostatic term
 int forces_split_effective(const gbsph_consts& c, int variant, int split);
-// bound_lanes: lanes a boundary row in the bound-row pass (1, 4 or 32)
+// A second stream for work that runs beside the main one within a step, with
+// the events that fork it from and join it to the main stream.
+struct StreamFork {
+  cudaStream_t side;
+  cudaEvent_t fork, join;
+};
+// bound_lanes: lanes a boundary row in the bound-row pass (1, 4 or 32); with
+// fork, the bound-row pass runs on fork->side beside the fluid-row pass (they
+// write disjoint rows) and is joined before the call's work ends
 void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, int split,
             int bound_lanes, cudaStream_t s, unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin = nullptr,
-            cudaEvent_t ev_fluid_end = nullptr);
+            cudaEvent_t ev_fluid_end = nullptr, const StreamFork* fork = nullptr);
 // variant 1: one thread per boundary row (k_mdbc); otherwise the cell-tiled
 // staged kernel (k_mdbc_t) with split (1, 2 or 4) warps per 32 boundary rows
 void mdbc(const gbsph_consts& c, const DevArrays& a, unsigned cap, int variant, int split, cudaStream_t s,

@@ -725,11 +725,21 @@ namespace gbk {
 
 void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, int variant, int split,
             int bound_lanes, cudaStream_t s, unsigned long long* nlaunch, cudaEvent_t ev_fluid_begin,
-            cudaEvent_t ev_fluid_end) {
+            cudaEvent_t ev_fluid_end, const StreamFork* fork) {
   cudaMemsetAsync(&a.st->acemax2, 0, 3 * sizeof(unsigned), s);
-  if (bound_lanes == 32) k_forces_bound_g<32><<<gb_div_up(cap, 4), 128, 0, s>>>(c, a);
-  else if (bound_lanes == 4) k_forces_bound_g<4><<<gb_div_up(cap, 32), 128, 0, s>>>(c, a);
-  else k_forces_bound<<<gb_div_up(cap, 128), 128, 0, s>>>(c, a);
+  // the bound rows (p < npb) and the fluid rows write disjoint rows of acear
+  // and meet only in the atomic maxima, so the bound-row pass can run beside
+  // the fluid-row pass and use the issue slots the latter leaves
+  cudaStream_t sb = s;
+  if (fork && fork->side) {
+    cudaEventRecord(fork->fork, s);
+    cudaStreamWaitEvent(fork->side, fork->fork, 0);
+    sb = fork->side;
+  }
+  if (bound_lanes == 32) k_forces_bound_g<32><<<gb_div_up(cap, 4), 128, 0, sb>>>(c, a);
+  else if (bound_lanes == 4) k_forces_bound_g<4><<<gb_div_up(cap, 32), 128, 0, sb>>>(c, a);
+  else k_forces_bound<<<gb_div_up(cap, 128), 128, 0, sb>>>(c, a);
+  if (sb != s) cudaEventRecord(fork->join, sb);
   // inside a stream capture the records must be external nodes so that every
   // replay of the graph records them; outside a capture they are plain records
   cudaStreamCaptureStatus cap_st = cudaStreamCaptureStatusNone;
@@ -738,6 +748,7 @@ void forces(const gbsph_consts& c, const DevArrays& a, unsigned cap, int bsize, 
   if (ev_fluid_begin) cudaEventRecordWithFlags(ev_fluid_begin, s, ev_flags);
   launch_fluid_v(c, a, cap, variant, bsize, split, false, s);
   if (ev_fluid_end) cudaEventRecordWithFlags(ev_fluid_end, s, ev_flags);
+  if (sb != s) cudaStreamWaitEvent(s, fork->join, 0);
   if (nlaunch) *nlaunch += 2;
 }
 

@@ -257,7 +257,8 @@ class GbSphSingle:
         boundary row in the bound-row pass (1, 4, 32; 0 automatic;
         get_option(7) reads the value in effect), key 8 = warps per group of
         32 boundary rows in the cell-tiled mDBC kernel (1, 2, 4; 0 automatic;
-        get_option(9) reads the value in effect)."""
+        get_option(9) reads the value in effect), key 10 = the bound-row pass
+        beside the fluid-row pass on a second stream (1) or before it (0)."""
         self._check(lib().gbsph_set_option(self.ctx, key, value), "set_option")
 
     def get_option(self, key: int) -> int:

@@ -385,7 +385,10 @@ void* gbsph_stream(gbsph_ctx* ctx);
  * key 8 = warps that share each group of 32 boundary rows in the cell-tiled
  * mDBC kernel (each takes every 1st, 2nd or 4th chunk of the ghosts'
  * candidates, and the first adds the others' compensated sums): 1, 2, 4, or
- * 0 (default: 4, the fastest at every size measured). */
+ * 0 (default: 4, the fastest at every size measured).  key 10 = the
+ * bound-row pass of gbsph_forces on a second stream beside the fluid-row
+ * pass (1) or before it on the context's stream (0, the default); the two
+ * write different rows, so the results are the same. */
 int gbsph_set_option(gbsph_ctx* ctx, int key, int value);
 /* The current value of an option of gbsph_set_option (no reference
  * counterpart); key 5 reads the warps per row group in effect (key 4
