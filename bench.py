@@ -20,13 +20,15 @@ cell divisions, mDBC correction, dt reduction) of the whole particle set.
   workload (DRAM_TRAFFIC below, with the capture it comes from).  The kernel is issue-bound, so its HBM
   fraction is small by construction; ``roofline_fp32`` states the same
   launches against the FP32 FLOP model (80 FLOP per real fluid-row pair) and
-  the nominal FFMA rate at the sampled SM clock, and ``gather_gbs`` the
-  neighbour bytes the checks read through L1/L2 (32 B per checked neighbour).
+  the FFMA rate measured in the same run (gbsph_ffma_peak; the nominal rate
+  at the sampled SM clock beside it), and ``gather_gbs`` the neighbour bytes
+  the checks read from the staged copies (32 B per checked neighbour).
 * ``cpu_baseline``: the oracle (CPU restatement of the reference step, OpenMP
   on all host cores), in its timing build, timed over full steps of the same
   state.
 * ``--impl reference``: the same timed oracle on the host cores as the
-  reference arm (the reference's own solver does not build on the GPU host).
+  reference arm (the reference's sources are not on the GPU host, and its
+  x86 build here does not run on the host's Arm cores).
 Inputs (~1.5 GB of particle arrays) are larger than L2 (129 MB).
 """
 from __future__ import annotations
