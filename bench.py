@@ -60,7 +60,7 @@ FP32_LANES_PER_SM = 128     # FFMA lanes per SM (2 FLOP each per clock)
 # dram__bytes_write.sum, --clock-control none), summarised in profiles/:
 # variant -> (kernel, bytes per launch, dp of the capture)
 DRAM_TRAFFIC = {0: ("k_forces_fluid_q", 269218560.0, 0.0025),   # k_forces_fluid_q_c2_dram.md
-                2: ("k_forces_fluid_t", 270835000.0, 0.0025)}   # k_forces_fluid_t_c2_dram.md
+                2: ("k_forces_fluid_t", 271390000.0, 0.0025)}   # k_forces_fluid_t_c2_dram.md
 # the fluid-row kernel of each variant (gbsph_set_option key 1)
 KERNEL_NAME = {0: "k_forces_fluid_q", 1: "k_forces_fluid", 2: "k_forces_fluid_t (ring of 8 chunks)",
                3: "k_forces_fluid_t (ring of 4 chunks)"}
