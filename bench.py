@@ -309,7 +309,8 @@ def run_ensemble(args, local: int = 0):
     case), of the same cases on concurrent streams without a graph, and of the
     cases run one after the other through the plain path (gbsph_run per case),
     wall clock around K steps with the device synchronised on both sides."""
-    from dualsphysics_gb300.ensemble import Ensemble, ensemble_specs, load_ensemble_case, tune
+    from dualsphysics_gb300.ensemble import Ensemble, ensemble_specs, load_ensemble_case, set_case_options, tune, \
+        tune_mix
     from dualsphysics_gb300.sph import GbSphSingle
     specs = ensemble_specs(args.ens_cases, seed=args.ens_seed, scale=args.ens_scale)
     sims, tuned = [], []
@@ -324,6 +325,7 @@ def run_ensemble(args, local: int = 0):
     nps = np.array([s.divinfo()["np"] for s in sims], dtype=np.float64)
     ens = Ensemble(sims)
     K, W = args.steps, args.warmup
+    mix = tune_mix(ens, sims, reps=3)       # the ensemble-level policy (cases step meanwhile)
     ens.run(W, use_graph=True)
     ens.sync()
 
@@ -342,7 +344,14 @@ def run_ensemble(args, local: int = 0):
             for s in sims:
                 s.RunSteps(K, use_graph=True)
                 s.sync()
+        mixed = [{k: s.get_option(k) for k in (1, 0, 4, 6, 8)} for s in sims]
+        for s, o in zip(sims, mix["alone"]):   # the plain path runs each case as tuned alone
+            set_case_options(s, o)
+        for s in sims:
+            s.RunSteps(1, use_graph=True)       # graph capture outside the clock
         t_seq = timed(sequential)
+        for s, o in zip(sims, mixed):
+            set_case_options(s, o)
     pst = float(nps.sum()) * K
     line = {"metric": "aggregate particle-steps/s, batched ensemble", "value": pst / t_graph,
             "unit": "particle-steps/s", "n_gpus": 1, "steps": K, "warmup": W, "higher_is_better": True,
@@ -354,6 +363,8 @@ def run_ensemble(args, local: int = 0):
             "streams_no_graph": pst / t_streams, "sequential_plain": pst / t_seq,
             "speedup_vs_sequential": t_seq / t_graph,
             "launches_per_replay": ens.launches_per_step(),
+            "mix_tuner": {"ms_per_replay": {k: round(v, 4) for k, v in mix["ms_per_replay"].items()},
+                          "kept": mix["kept"]},
             "tuner": {"choices": [[t["variant"][t["best"]], t["bsize"][t["best"]], t["split"][t["best"]]]
                                   for t in tuned],
                       "sort_bits": [t["sort_bits"] for t in tuned],

@@ -115,3 +115,54 @@ def tune(sim: GbSphSingle, reps: int = 3) -> dict:
             "bound_best": r.bound_best, "bound_lanes": list(r.bound_lanes), "bound_ms": list(r.bound_ms),
             "mdbc_best": r.mdbc_best, "mdbc_split": list(r.mdbc_split), "mdbc_ms": list(r.mdbc_ms),
             "sort_bits": bits.value, "sort_ms": list(ms)}
+
+
+# Options of a case that shape its kernels' launches (gbsph_set_option keys):
+# fluid-row kernel, its block size, warps per fluid row group, lanes a
+# boundary row, warps per mDBC row group.
+SHAPE_KEYS = (1, 0, 4, 6, 8)
+
+# Ensemble-level policies, each a function (case options as tuned alone) ->
+# the options the case runs with in the ensemble graph.
+MIX_POLICIES = {
+    "as tuned alone": lambda o: dict(o),
+    "one thread a boundary row": lambda o: {**o, 6: 1},
+    "one warp or thread a row": lambda o: {**o, 4: 1, 6: 1, 8: 1},
+}
+
+
+def case_options(sim: GbSphSingle) -> dict:
+    return {k: sim.get_option(k) for k in SHAPE_KEYS}
+
+
+def set_case_options(sim: GbSphSingle, opts: dict) -> None:
+    for k in SHAPE_KEYS:
+        if sim.get_option(k) != opts[k]:
+            sim.set_option(k, opts[k])
+
+
+def tune_mix(ens: "Ensemble", sims: list, reps: int = 3) -> dict:
+    """The ensemble-level autotuner: each case's autotuner times it alone,
+    where launches that spread a small case over more warps pay off; in the
+    ensemble graph the cases' branches already share the SMs.  This times
+    replays of the whole ensemble under each policy of MIX_POLICIES (one
+    warm-up replay, which captures the graph, then `reps`), applied to the
+    options the cases were tuned to, and keeps the fastest.  The cases step
+    while it runs.  Returns the mean ms of a replay per policy and the
+    policy kept."""
+    import time
+    alone = [case_options(s) for s in sims]
+    ms = {}
+    for name, pol in MIX_POLICIES.items():
+        for s, o in zip(sims, alone):
+            set_case_options(s, pol(o))
+        ens.run(1, use_graph=True)
+        ens.sync()
+        t0 = time.perf_counter()
+        ens.run(reps, use_graph=True)
+        ens.sync()
+        ms[name] = 1e3 * (time.perf_counter() - t0) / reps
+    best = min(ms, key=ms.get)
+    for s, o in zip(sims, alone):
+        set_case_options(s, MIX_POLICIES[best](o))
+    return {"ms_per_replay": ms, "kept": best, "alone": alone}

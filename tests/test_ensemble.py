@@ -157,6 +157,30 @@ def test_sort_digit_width_leaves_the_order_unchanged(name):
 
 
 @pytest.mark.gpu
+def test_ensemble_level_tuner_keeps_the_fastest_policy():
+    """tune_mix times whole ensemble replays under each policy and leaves
+    every case at the kept policy applied to its own tuned options (the
+    ensemble steps each case as the case alone with the same options:
+    test_ensemble_steps_equal_each_case_alone)."""
+    from dualsphysics_gb300.ensemble import MIX_POLICIES, Ensemble, case_options, tune, tune_mix
+    _, cds = _cases(3, seed=5)
+    sims = _sims(cds)
+    for s in sims:
+        tune(s, reps=1)
+    ens = Ensemble(sims)
+    r = tune_mix(ens, sims, reps=1)
+    assert set(r["ms_per_replay"]) == set(MIX_POLICIES) and all(v > 0 for v in r["ms_per_replay"].values())
+    assert r["ms_per_replay"][r["kept"]] == min(r["ms_per_replay"].values())
+    for s, o in zip(sims, r["alone"]):
+        assert case_options(s) == MIX_POLICIES[r["kept"]](o)
+    ens.run(2, use_graph=True)
+    ens.sync()
+    ens.close()
+    for s in sims:
+        s.close()
+
+
+@pytest.mark.gpu
 def test_autotuner_tunes_the_mdbc_split_on_an_mdbc_case():
     """On an mDBC case the tuner also times the mDBC kernel at 1, 2 and 4 warps
     per row group and keeps the fastest; the tuned run equals the run with
