@@ -397,7 +397,7 @@ def run_closure(args, local: int = 0):
     train = [h for h in heights if h not in val]
     t0 = time.perf_counter()
     kw = dict(dp_fine=dpf, ratio=ratio, t_end=t_end, n_snap=args.clos_snaps, device=local,
-              smooth=bool(args.clos_smooth))
+              smooth=bool(args.clos_smooth), avg_steps=args.clos_avg)
     xs, ts, meta = cl.paired_samples(train, **kw)
     xv, tv, _ = cl.paired_samples(val, **kw)
     t_data = time.perf_counter() - t0
@@ -428,7 +428,8 @@ def run_closure(args, local: int = 0):
                        "train_heights": len(train), "validation_heights": len(val),
                        "snapshots_per_height": args.clos_snaps,
                        "samples": int(len(xs)), "epochs": args.clos_epochs,
-                       "targets": "kernel-smoothed" if args.clos_smooth else "raw"},
+                       "targets": ("kernel-smoothed" if args.clos_smooth else "raw") +
+                                  f", fine accelerations averaged over {args.clos_avg} fine steps"},
             "errors": err, "judge_converges": converges,
             "wall_s": {f"judge_dp{dpf:g}": judge["wall_s"], **{k: r["wall_s"] for k, r in runs.items()}},
             "ms_per_step": {f"judge_dp{dpf:g}": judge["ms_per_step"], **{k: r["ms_per_step"] for k, r in runs.items()}},
@@ -501,6 +502,8 @@ def main():
     ap.add_argument("--clos-ratio", type=int, default=4, choices=[2, 4])
     ap.add_argument("--clos-smooth", type=int, default=1, choices=[0, 1],
                     help="train on kernel-smoothed targets (closure.smooth_targets)")
+    ap.add_argument("--clos-avg", type=int, default=8,
+                    help="fine steps the fine block-mean acceleration is averaged over (about one coarse step)")
     ap.add_argument("--clos-judge-dps", default="0.02,0.01,0.005,0.0025")
     ap.add_argument("--ens-cases", type=int, default=64)
     ap.add_argument("--ens-seed", type=int, default=1)

@@ -327,13 +327,17 @@ def smooth_targets(pos: np.ndarray, t: np.ndarray, h: float) -> np.ndarray:
 
 
 def paired_samples(heights, dp_fine: float = 0.01, t_end: float = 0.3, n_snap: int = 10,
-                   device: int = 0, log=None, ratio: int = 2,
-                   smooth: bool = False) -> tuple[np.ndarray, np.ndarray, dict]:
+                   device: int = 0, log=None, ratio: int = 2, smooth: bool = False,
+                   avg_steps: int = 1) -> tuple[np.ndarray, np.ndarray, dict]:
     """Features and targets over fine runs of the given column heights,
     restricted to the coarse particles (spacing ratio*dp_fine) at n_snap
-    times in (0, t_end].  With smooth, the targets are replaced by their
-    kernel-weighted neighbourhood means (smooth_targets); meta["raw"] keeps
-    the raw ones."""
+    times in (0, t_end].  With avg_steps > 1, the fine block-mean
+    acceleration is averaged over that many consecutive fine steps from the
+    snapshot (about one coarse step for avg_steps = 2 * ratio: the mean fine
+    acceleration over the coarse step's interval, without the fine run's
+    acoustic oscillations); the coarse state and features are those of the
+    snapshot.  With smooth, the targets are replaced by their kernel-weighted
+    neighbourhood means (smooth_targets); meta["raw"] keeps the raw ones."""
     xs, ts, raw, meta = [], [], [], {"snapshots": 0, "fine_steps": 0, "fine_s": 0.0}
     g = 9.81
     for hk, h in enumerate(heights):
@@ -367,6 +371,15 @@ def paired_samples(heights, dp_fine: float = 0.01, t_end: float = 0.3, n_snap: i
                 cs.close()
                 crow = cst["idp"][cst["idp"] >= cd.npb] - cd.npb    # coarse fluid row of each feature row
                 fmean, _ = pair.block_mean(fst, face)               # block mean of the fine accelerations
+                for _ in range(1, max(1, avg_steps)):               # averaged over the next fine steps
+                    fine.RunSteps(1, use_graph=True)
+                    meta["fine_steps"] += 1
+                    fine.MdbcBoundCorrection(INTERSTEP_SYMPREDICTOR)
+                    fine.Interaction_Forces(INTERSTEP_SYMPREDICTOR)
+                    fm, _ = pair.block_mean(fine.download(), fine.forces()[0])
+                    fmean = fmean + fm
+                fmean = fmean / max(1, avg_steps)
+                t = fine.step_dt()[2]
                 tgt = (fmean[crow] - cace[cd.npb:cd.npb + len(crow)]) / g
                 ok = np.isfinite(x).all(axis=1) & np.isfinite(tgt).all(axis=1)
                 xs.append(x[ok])
