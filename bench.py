@@ -418,6 +418,18 @@ def run_closure(args, local: int = 0):
     runs = {km: mid, kp: plain, kl: learned}
     err = {k: cl.errors(r, judge) for k, r in runs.items()}
     head = cl.HEADLINE_ERROR
+    # more trainings on the same data with other seeds: the spread of the
+    # learned run's errors (the data generation is the costly part)
+    seeds = []
+    for sd in range(1, max(1, args.clos_seeds)):
+        _, w2, _ = cl.train_closure(xs, ts, epochs=args.clos_epochs, seed=args.clos_seed + sd, device=local,
+                                    xv=xv, tv=tv)
+        ev2 = cl.Trainer(cl.from_bf16(w2), local)
+        yh2 = ev2.infer(xh)
+        ev2.close()
+        l2 = cl.run_with_probes(coarse, t_end, dtp, w_bf16=w2, limit=0.2, device=local, mesh_h=hc)
+        seeds.append({"seed": args.clos_seed + sd, "errors": cl.errors(l2, judge),
+                      "apriori_mse_raw": float(np.mean((mh["raw"] - yh2) ** 2))})
     speed = mid["wall_s"] / learned["wall_s"]
     converges = bool(err[km][head] < err[kp][head] and err[km]["front_rmse_m"] < err[kp]["front_rmse_m"])
     line = {"metric": f"learned vs plain time-to-accuracy ({head}, probes on the obstacle face)",
@@ -444,6 +456,11 @@ def run_closure(args, local: int = 0):
             "train": {"loss_first": float(loss[0]), "loss_last": float(loss[-1]), "data_s": t_data,
                       "train_s": t_train, "fine_steps": meta["fine_steps"]},
             "fallback_rows": learned["fallbacks"]}
+    if seeds:
+        allh = [err[kl][head]] + [sd["errors"][head] for sd in seeds]
+        line["other_seeds"] = seeds
+        line["learned_error_over_seeds"] = {"n": len(allh), "min": min(allh), "max": max(allh),
+                                            "mean": float(np.mean(allh)), "plain": err[kp][head]}
     print(json.dumps(line))
 
 
@@ -502,6 +519,8 @@ def main():
     ap.add_argument("--clos-ratio", type=int, default=4, choices=[2, 4])
     ap.add_argument("--clos-smooth", type=int, default=1, choices=[0, 1],
                     help="train on kernel-smoothed targets (closure.smooth_targets)")
+    ap.add_argument("--clos-seeds", type=int, default=1,
+                    help="trainings (seeds) on the same data; the spread of the learned run's errors")
     ap.add_argument("--clos-avg", type=int, default=8,
                     help="fine steps the fine block-mean acceleration is averaged over (about one coarse step)")
     ap.add_argument("--clos-judge-dps", default="0.02,0.01,0.005,0.0025")
